@@ -1,0 +1,356 @@
+// capi.cu — the C ABI of include/dense2d.h over the sm_103a kernels: device buffers of one
+// block, its stream, the CUDA graph of one time step, status and errors.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+
+extern "C" const char* dense_host_last_error(void);
+
+using dense::KernelTable;
+using dense::Params;
+using dense::Scalars;
+using dense::kB;
+
+struct dense_handle {
+    dense_config_t cfg;
+    const KernelTable* kt = nullptr;
+    cudaStream_t stream = nullptr;
+    int device = 0;
+    double *cons = nullptr, *prim = nullptr, *cons0 = nullptr, *hx = nullptr, *he = nullptr;
+    double *xbot = nullptr, *xtop = nullptr, *yleft = nullptr;
+    Scalars* sc = nullptr;
+    Params prm{};
+    int NIp = 0, NJp = 0, P = 0;
+    bool uploaded = false;
+    int prim_slot = -1;  // stage slot whose max wave speeds match the current state, or -1
+    cudaGraphExec_t step_graph = nullptr;
+    int graph_nodes = 0;
+    long long launches = 0;
+    std::string err;
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+int seterr(dense_handle* h, int code, const std::string& msg) {
+    if (h) h->err = msg; else g_err = msg;
+    return code;
+}
+
+#define CK(h, call)                                                                              \
+    do {                                                                                         \
+        cudaError_t e_ = (call);                                                                 \
+        if (e_ != cudaSuccess)                                                                   \
+            return seterr((h), DENSE_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+__global__ void k_set_loop(Scalars* sc, double t, long long step, double t_end, long long total_step,
+                           int active) {
+    sc->t = t;
+    sc->step = step;
+    sc->t_end = t_end;
+    sc->total_step = total_step;
+    sc->active = active;
+}
+__global__ void k_set_dt(Scalars* sc, double dt) { sc->dt = dt; }
+
+bool valid_split(int s) { return s >= DENSE_SPLIT_LLF && s <= DENSE_SPLIT_SC; }
+bool valid_bench(int b) {
+    return b == 0 || (b >= 1 && b <= 9) || b == DENSE_BENCH_IVC_PERIODIC || b == DENSE_BENCH_RT_REFLECT ||
+           b == DENSE_BENCH_RM_PERIODIC;
+}
+
+int check_config(dense_handle* h, const dense_config_t* c) {
+    if (!c) return seterr(h, DENSE_ERR_ARG, "null config");
+    if (c->ni < 3 || c->nj < 3) return seterr(h, DENSE_ERR_ARG, "ni and nj must be >= 3");
+    if (c->bfsize != kB) return seterr(h, DENSE_ERR_ARG, "bfsize must be 4 (allocate_block(...,4,4,neq))");
+    if (c->neq != 4) return seterr(h, DENSE_ERR_ARG, "neq must be 4");
+    if (c->stages != 3) return seterr(h, DENSE_ERR_ARG, "stages must be 3 (time_rk3_general)");
+    if (!valid_split(c->splitting))
+        return seterr(h, DENSE_ERR_SPLITTING, "No such Selection (flux_splitting.f90:30-32)");
+    if (!valid_bench(c->benchmark))
+        return seterr(h, DENSE_ERR_BENCHMARK, "No such Benchmark index! (boundary_general.f90:26-28)");
+    if (c->dx <= 0.0 || c->dy <= 0.0) return seterr(h, DENSE_ERR_ARG, "dx and dy must be set (dense_init_setup)");
+    return DENSE_OK;
+}
+
+void fill_params(dense_handle* h) {
+    Params& p = h->prm;
+    const dense_config_t& c = h->cfg;
+    p.cons = h->cons; p.prim = h->prim; p.cons0 = h->cons0; p.hx = h->hx; p.he = h->he;
+    p.xbot = h->xbot; p.xtop = h->xtop; p.yleft = h->yleft;
+    p.sc = h->sc;
+    p.ni = c.ni; p.nj = c.nj; p.P = h->P;
+    p.plane = (long long)h->NJp * h->P;
+    p.gamma = c.gamma; p.cfl = c.cfl; p.delta = c.delta; p.dx = c.dx; p.dy = c.dy; p.dt_const = c.dt;
+    p.if_const_dt = c.if_const_dt;
+    // the body force is nonzero only where boundary_rt_general refreshes it (:154-155)
+    p.bodyforce = c.if_bodyforce && (c.benchmark == DENSE_BENCH_RT || c.benchmark == DENSE_BENCH_RT_REFLECT);
+    p.benchmark = c.benchmark; p.splitting = c.splitting; p.recon = c.recon;
+    h->kt = c.strict ? dense::kernels_strict() : dense::kernels_fast();
+}
+
+void drop_graph(dense_handle* h) {
+    if (h->step_graph) cudaGraphExecDestroy(h->step_graph);
+    h->step_graph = nullptr;
+    h->graph_nodes = 0;
+}
+
+int launch_check(dense_handle* h) {
+    CK(h, cudaGetLastError());
+    return DENSE_OK;
+}
+
+// get_primary of the current state into slot `slot`.
+int ensure_prim(dense_handle* h, int slot) {
+    if (h->prim_slot == slot) return DENSE_OK;
+    CK(h, cudaMemsetAsync(&h->sc->maxeig[slot][0], 0, 2 * sizeof(double), h->stream));
+    h->kt->prim(h->prm, slot, h->stream);
+    h->launches += 1;
+    h->prim_slot = slot;
+    return launch_check(h);
+}
+
+// one stage: boundary_general -> flux_splitting_general -> time_rk3_general(irk)
+void enqueue_stage(dense_handle* h, int irk) {
+    h->kt->bc(h->prm, h->stream);
+    h->kt->flux(h->prm, irk, h->stream);
+    h->kt->update(h->prm, irk, h->stream);
+}
+int stage_launches(dense_handle* h) { return 2 + h->kt->flux_launches(h->prm); }
+
+int build_step_graph(dense_handle* h) {
+    if (h->step_graph) return DENSE_OK;
+    cudaGraph_t g = nullptr;
+    CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    h->kt->step_begin(h->prm, h->stream);
+    for (int irk = 1; irk <= 3; ++irk) enqueue_stage(h, irk);
+    h->kt->step_end(h->prm, h->stream);
+    cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+    if (e != cudaSuccess) return seterr(h, DENSE_ERR_CUDA, std::string("stream capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&h->step_graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return seterr(h, DENSE_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    h->graph_nodes = 2 + 3 * stage_launches(h);
+    return DENSE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* dense_last_error(dense_handle_t* h) {
+    if (h) return h->err.c_str();
+    if (!g_err.empty()) return g_err.c_str();
+    return dense_host_last_error();
+}
+
+int dense_create(const dense_config_t* cfg, dense_handle_t** out) {
+    if (!out) return seterr(nullptr, DENSE_ERR_ARG, "null out");
+    *out = nullptr;
+    int rc = check_config(nullptr, cfg);
+    if (rc) return rc;
+    auto* h = new dense_handle();
+    h->cfg = *cfg;
+    h->NIp = cfg->ni + 2 * kB;
+    h->NJp = cfg->nj + 2 * kB;
+    h->P = (h->NIp + 1) & ~1;  // even pitch: rows start on 16-byte boundaries
+    auto cleanup = [&](int code) { dense_destroy(h); return code; };
+    cudaError_t e = cudaGetDevice(&h->device);
+    if (e != cudaSuccess) { g_err = std::string("cudaGetDevice: ") + cudaGetErrorString(e); delete h; return DENSE_ERR_CUDA; }
+    e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { g_err = std::string("cudaStreamCreate: ") + cudaGetErrorString(e); delete h; return DENSE_ERR_CUDA; }
+    const size_t plane = (size_t)h->NJp * h->P;
+    struct A { double** p; size_t n; } allocs[] = {
+        {&h->cons, plane * 4}, {&h->prim, plane * 5}, {&h->cons0, plane * 4},
+        {&h->hx, (size_t)4 * cfg->nj * (cfg->ni + 1)}, {&h->he, (size_t)4 * (cfg->nj + 1) * cfg->ni},
+        {&h->xbot, (size_t)cfg->ni}, {&h->xtop, (size_t)cfg->ni}, {&h->yleft, (size_t)cfg->nj},
+    };
+    for (auto& a : allocs) {
+        e = cudaMalloc((void**)a.p, a.n * sizeof(double));
+        if (e != cudaSuccess) { g_err = std::string("cudaMalloc: ") + cudaGetErrorString(e); return cleanup(DENSE_ERR_NOMEM); }
+        e = cudaMemsetAsync(*a.p, 0, a.n * sizeof(double), h->stream);
+        if (e != cudaSuccess) { g_err = std::string("cudaMemset: ") + cudaGetErrorString(e); return cleanup(DENSE_ERR_CUDA); }
+    }
+    e = cudaMalloc((void**)&h->sc, sizeof(Scalars));
+    if (e != cudaSuccess) { g_err = std::string("cudaMalloc: ") + cudaGetErrorString(e); return cleanup(DENSE_ERR_NOMEM); }
+    Scalars s0{};
+    s0.dt = cfg->dt;
+    s0.t_end = 0.0;
+    e = cudaMemcpyAsync(h->sc, &s0, sizeof(Scalars), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) { g_err = std::string("scalars: ") + cudaGetErrorString(e); return cleanup(DENSE_ERR_CUDA); }
+    fill_params(h);
+    *out = h;
+    return DENSE_OK;
+}
+
+void dense_destroy(dense_handle_t* h) {
+    if (!h) return;
+    drop_graph(h);
+    double* bufs[] = {h->cons, h->prim, h->cons0, h->hx, h->he, h->xbot, h->xtop, h->yleft};
+    for (double* b : bufs) if (b) cudaFree(b);
+    if (h->sc) cudaFree(h->sc);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+int dense_upload(dense_handle_t* h, const double* cons, const double* prim, const double* x, const double* y) {
+    if (!h || !cons) return seterr(h, DENSE_ERR_ARG, "null handle or cons");
+    const dense_config_t& c = h->cfg;
+    const size_t row = (size_t)h->NIp * sizeof(double), pitch = (size_t)h->P * sizeof(double);
+    // Fortran cons(NIp,NJp,4) is a stack of 4*NJp rows of NIp doubles: one pitched copy
+    CK(h, cudaMemcpy2DAsync(h->cons, pitch, cons, row, row, (size_t)h->NJp * 4, cudaMemcpyHostToDevice, h->stream));
+    if (prim) {
+        CK(h, cudaMemcpy2DAsync(h->prim, pitch, prim, row, row, (size_t)h->NJp * 5, cudaMemcpyHostToDevice, h->stream));
+    } else {
+        CK(h, cudaMemsetAsync(h->prim, 0, (size_t)h->NJp * h->P * 5 * sizeof(double), h->stream));
+    }
+    std::vector<double> xb(c.ni, 0.0), xt(c.ni, 0.0), yl(c.nj, 0.0);
+    if (x) for (int i = 0; i < c.ni; ++i) { xb[i] = x[i]; xt[i] = x[(size_t)c.ni * (c.nj - 1) + i]; }
+    if (y) for (int j = 0; j < c.nj; ++j) yl[j] = y[(size_t)c.ni * j];
+    CK(h, cudaMemcpyAsync(h->xbot, xb.data(), c.ni * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaMemcpyAsync(h->xtop, xt.data(), c.ni * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaMemcpyAsync(h->yleft, yl.data(), c.nj * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    h->uploaded = true;
+    h->prim_slot = -1;
+    int rc = ensure_prim(h, 0);
+    if (rc) return rc;
+    CK(h, cudaStreamSynchronize(h->stream));  // the caller's buffers may be reused on return
+    return DENSE_OK;
+}
+
+int dense_stage(dense_handle_t* h, int irk, double current_time, double* dt_inout) {
+    if (!h) return seterr(h, DENSE_ERR_ARG, "null handle");
+    if (irk < 1 || irk > 3) return seterr(h, DENSE_ERR_ARG, "irk must be 1, 2 or 3");
+    if (!h->uploaded) return seterr(h, DENSE_ERR_STATE, "dense_stage before dense_upload");
+    int rc = ensure_prim(h, irk - 1);
+    if (rc) return rc;
+    k_set_loop<<<1, 1, 0, h->stream>>>(h->sc, current_time, 0, 0.0, 0, 1);
+    h->launches += 1;
+    enqueue_stage(h, irk);
+    h->launches += stage_launches(h);
+    rc = launch_check(h);
+    if (rc) return rc;
+    h->prim_slot = irk % 3;
+    double dt = 0.0;
+    CK(h, cudaMemcpyAsync(&dt, &h->sc->dt, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    if (dt_inout) *dt_inout = dt;
+    return DENSE_OK;
+}
+
+int dense_steps(dense_handle_t* h, int nsteps, double t_end, int total_step, double* t_inout,
+                int* step_inout, double* dt_out) {
+    if (!h || !t_inout || !step_inout) return seterr(h, DENSE_ERR_ARG, "null argument");
+    if (nsteps < 0) return seterr(h, DENSE_ERR_ARG, "nsteps < 0");
+    if (!h->uploaded) return seterr(h, DENSE_ERR_STATE, "dense_steps before dense_upload");
+    int rc = ensure_prim(h, 0);
+    if (rc) return rc;
+    rc = build_step_graph(h);
+    if (rc) return rc;
+    k_set_loop<<<1, 1, 0, h->stream>>>(h->sc, *t_inout, *step_inout, t_end, total_step, 0);
+    h->launches += 1;
+    for (int s = 0; s < nsteps; ++s) {
+        CK(h, cudaGraphLaunch(h->step_graph, h->stream));
+        h->launches += h->graph_nodes;
+    }
+    Scalars s{};
+    CK(h, cudaMemcpyAsync(&s, h->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    *t_inout = s.t;
+    *step_inout = (int)s.step;
+    if (dt_out) *dt_out = s.dt;
+    return DENSE_OK;
+}
+
+int dense_download(dense_handle_t* h, double* cons, double* prim) {
+    if (!h) return seterr(h, DENSE_ERR_ARG, "null handle");
+    if (!h->uploaded) return seterr(h, DENSE_ERR_STATE, "dense_download before dense_upload");
+    const size_t row = (size_t)h->NIp * sizeof(double), pitch = (size_t)h->P * sizeof(double);
+    if (cons)
+        CK(h, cudaMemcpy2DAsync(cons, row, h->cons, pitch, row, (size_t)h->NJp * 4, cudaMemcpyDeviceToHost, h->stream));
+    if (prim)
+        CK(h, cudaMemcpy2DAsync(prim, row, h->prim, pitch, row, (size_t)h->NJp * 5, cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    if (prim) {
+        // entropy log(p)-log(rho) of the interior (get_primary.f90:67); ghosts hold 0
+        const size_t P = (size_t)h->NIp * h->NJp;
+        double* s6 = prim + 5 * P;
+        std::memset(s6, 0, P * sizeof(double));
+        for (int J = kB; J < h->NJp - kB; ++J)
+            for (int I = kB; I < h->NIp - kB; ++I) {
+                const size_t o = (size_t)J * h->NIp + I;
+                s6[o] = std::log(prim[3 * P + o]) - std::log(prim[o]);
+            }
+    }
+    return DENSE_OK;
+}
+
+int dense_get_max_eig(dense_handle_t* h, double* mi, double* mj) {
+    if (!h || !mi || !mj) return seterr(h, DENSE_ERR_ARG, "null argument");
+    if (h->prim_slot < 0) return seterr(h, DENSE_ERR_STATE, "no get_primary yet");
+    double m[2];
+    CK(h, cudaMemcpyAsync(m, &h->sc->maxeig[h->prim_slot][0], sizeof(m), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    *mi = m[0];
+    *mj = m[1];
+    return DENSE_OK;
+}
+
+int dense_reconfigure(dense_handle_t* h, const dense_config_t* cfg) {
+    if (!h || !cfg) return seterr(h, DENSE_ERR_ARG, "null argument");
+    if (cfg->ni != h->cfg.ni || cfg->nj != h->cfg.nj || cfg->benchmark != h->cfg.benchmark)
+        return seterr(h, DENSE_ERR_ARG, "grid size and benchmark cannot change on a live handle");
+    int rc = check_config(h, cfg);
+    if (rc) return rc;
+    h->cfg = *cfg;
+    fill_params(h);
+    drop_graph(h);
+    h->prim_slot = -1;  // gamma may have changed: recompute primitives before the next stage
+    k_set_dt<<<1, 1, 0, h->stream>>>(h->sc, cfg->dt);
+    h->launches += 1;
+    return launch_check(h);
+}
+
+int dense_status(dense_handle_t* h, unsigned* flags) {
+    if (!h || !flags) return seterr(h, DENSE_ERR_ARG, "null argument");
+    unsigned f = 0;
+    CK(h, cudaMemcpyAsync(&f, &h->sc->status, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaMemsetAsync(&h->sc->status, 0, sizeof(unsigned), h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    *flags = f;
+    return DENSE_OK;
+}
+
+int dense_get_fluxes(dense_handle_t* h, double* h_xi, double* h_eta) {
+    if (!h) return seterr(h, DENSE_ERR_ARG, "null handle");
+    const int ni = h->cfg.ni, nj = h->cfg.nj;
+    if (h_xi)  // device hx[v][j][f] == Fortran h_xi(f,j,v)
+        CK(h, cudaMemcpyAsync(h_xi, h->hx, (size_t)4 * nj * (ni + 1) * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    std::vector<double> tmp;
+    if (h_eta) {
+        tmp.resize((size_t)4 * (nj + 1) * ni);
+        CK(h, cudaMemcpyAsync(tmp.data(), h->he, tmp.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    }
+    CK(h, cudaStreamSynchronize(h->stream));
+    if (h_eta)  // device he[v][g][i] -> Fortran h_eta(g,i,v)
+        for (int v = 0; v < 4; ++v)
+            for (int g = 0; g <= nj; ++g)
+                for (int i = 0; i < ni; ++i)
+                    h_eta[(size_t)g + (size_t)(nj + 1) * ((size_t)i + (size_t)ni * v)] =
+                        tmp[(size_t)v * (nj + 1) * ni + (size_t)g * ni + i];
+    return DENSE_OK;
+}
+
+long long dense_launch_count(dense_handle_t* h) { return h ? h->launches : -1; }
+
+}  // extern "C"

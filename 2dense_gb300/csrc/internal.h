@@ -1,0 +1,69 @@
+// internal.h — types shared by the kernels (kernels.cu, compiled once per arithmetic variant)
+// and the C ABI layer (capi.cu). Not part of the public interface.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+#include "../../include/dense2d.h"
+
+namespace dense {
+
+constexpr int kB = 4;  // ghost layers per side: allocate_block(...,4,4,neq)
+
+// Device-resident scalars of one block: the module globals of flow_general that the hot path
+// reads and writes (max_eig_i/j, dt, current_time, current_step), plus the loop predicate.
+struct Scalars {
+    double maxeig[3][2];  // slot s = stage (0..2) that reads it: (max_eig_i, max_eig_j)
+    double dt;            // flow_general::dt
+    double dtdx, dtdy;    // dt/dx, dt/dy (time_advance_general.f90:49)
+    double t;             // current_time
+    double elasp;         // elasp_time
+    double t_end;         // loop bound on time (general_main.f90:23)
+    long long step;       // current_step
+    long long total_step; // loop bound on steps
+    int active;           // this step is taken (the while-condition held at its start)
+    unsigned status;      // DENSE_FLAG_* bits
+    int pad[2];
+};
+
+// Everything a kernel needs, passed by value.
+struct Params {
+    double* cons;    // [4][NJp][P] padded conserved variables
+    double* prim;    // [5][NJp][P] padded rho,u,v,p,alpha
+    double* cons0;   // [4][NJp][P] stage-1 copy (cons_temp); interior is read
+    double* hx;      // [4][nj][ni+1] interface fluxes h_xi
+    double* he;      // [4][nj+1][ni] interface fluxes h_eta
+    const double* xbot;   // x(i,1),  i=1..ni  (DMR bottom rule)
+    const double* xtop;   // x(i,nj), i=1..ni  (DMR top rule)
+    const double* yleft;  // y(1,j),  j=1..nj  (SSL inflow rule)
+    Scalars* sc;
+    int ni, nj;
+    int P;           // row pitch of the padded arrays, in doubles
+    long long plane; // doubles per variable plane = NJp * P
+    double gamma, cfl, delta, dx, dy, dt_const;
+    int if_const_dt, bodyforce, benchmark, splitting, recon;
+};
+
+// One arithmetic variant of the kernels (fast or strict), as a table of launchers.
+struct KernelTable {
+    const char* name;
+    // get_primary over the interior; max wave speeds into slot `slot`
+    void (*prim)(const Params&, int slot, void* stream);
+    // boundary_general
+    void (*bc)(const Params&, void* stream);
+    // flux_splitting_general (+ scheme_invis_general): both sweeps, writes hx/he. Also computes
+    // dt (stage 1) and zeroes the next max slot.
+    void (*flux)(const Params&, int irk, void* stream);
+    // time_rk3_general(irk) fused with get_primary of the new state
+    void (*update)(const Params&, int irk, void* stream);
+    // loop bookkeeping: step_begin evaluates the while-condition, step_end advances time
+    void (*step_begin)(const Params&, void* stream);
+    void (*step_end)(const Params&, void* stream);
+    // kernel launches issued by flux() for this configuration
+    int (*flux_launches)(const Params&);
+};
+
+const KernelTable* kernels_fast();
+const KernelTable* kernels_strict();
+
+}  // namespace dense

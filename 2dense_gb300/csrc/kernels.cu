@@ -1,0 +1,815 @@
+// kernels.cu — sm_103a kernels of 2DENSE's per-stage hot path.
+//
+// This file is compiled twice into the same library:
+//   -DDENSE_VARIANT_STRICT=1 -fmad=false : dense::kernels_strict(). Every expression keeps the
+//      reference's evaluation order (left to right as written in the Fortran), no FMA is
+//      contracted and divide/sqrt are IEEE, so results are bit-identical to the reference's
+//      x86-64 arithmetic (except the SSL inflow rule, which calls tanh/cos/exp).
+//   -DDENSE_VARIANT_STRICT=0             : dense::kernels_fast(). FMA contraction and the
+//      algebraic rewrites marked FAST below; agrees with the reference to ~1e-14 per step.
+//
+// All arithmetic is FP64. On GB300 the FP64 pipe, not HBM, bounds every kernel here (about
+// 4-7 kFLOP per cell-update against 256 B of compulsory traffic), so the kernels are built to
+// minimise FP64 instructions: per-cell split fluxes are computed once per tile into shared
+// memory, Roe averages and eigenvectors once per interface for both signs, and loop-invariant
+// scalars (dt/dx, dt/dy, the GLF wave speed) once per stage.
+//
+// Layout in HBM (0-based, padded with 4 ghost layers; I = i + 4, J = j + 4 for interior (i,j)):
+//   cons[v][J][I]  v = 0..3 (rho, rho u, rho v, E)       row pitch P doubles, plane NJp*P
+//   prim[v][J][I]  v = 0..4 (rho, u, v, p, alpha)
+//   hx[v][j][f]    f = 0..ni interface between padded columns f+3 and f+4
+//   he[v][g][i]    g = 0..nj interface between padded rows g+3 and g+4
+#include <cuda_runtime.h>
+
+#include "internal.h"
+
+#ifndef DENSE_VARIANT_STRICT
+#error "DENSE_VARIANT_STRICT must be defined (0 or 1)"
+#endif
+#if DENSE_VARIANT_STRICT
+#define VNS strict_impl
+#define FAST 0
+#else
+#define VNS fast_impl
+#define FAST 1
+#endif
+
+namespace dense {
+namespace VNS {
+
+// ---------------------------------------------------------------------------------------------
+// weno module constants (source/inv_scheme/weno_mod.f90:3-14,37)
+constexpr double a300 = 1.0 / 3.0, a301 = -7.0 / 6.0, a302 = 11.0 / 6.0;
+constexpr double a310 = -1.0 / 6.0, a311 = 5.0 / 6.0, a312 = 1.0 / 3.0;
+constexpr double a320 = 1.0 / 3.0, a321 = 5.0 / 6.0, a322 = -1.0 / 6.0;
+constexpr double c30 = 0.1, c31 = 0.6, c32 = 0.3;
+constexpr double kSS = (double)1.0e-6f;       // ss = 1.0e-6, a default-real literal (:37)
+constexpr double kPFloor = (double)1.0e-6f;   // get_primary.f90:58
+constexpr double kTwoThirdsSP = (double)(2.0f / 3.0f);  // time_advance_general.f90:242
+
+__device__ __forceinline__ double sq(double x) { return x * x; }
+
+// Smoothness indicators of the three 3-point substencils (weno_mod.f90:152-159).
+__device__ __forceinline__ void smoothness(const double lf[5], double& is0, double& is1, double& is2) {
+    is0 = 13.0 * sq(lf[0] - 2.0 * lf[1] + lf[2]) / 12.0 + sq(lf[0] - 4.0 * lf[1] + 3.0 * lf[2]) / 4.0;
+    is1 = 13.0 * sq(lf[1] - 2.0 * lf[2] + lf[3]) / 12.0 + sq(lf[1] - lf[3]) / 4.0;
+    is2 = 13.0 * sq(lf[2] - 2.0 * lf[3] + lf[4]) / 12.0 + sq(3.0 * lf[2] - 4.0 * lf[3] + lf[4]) / 4.0;
+}
+
+// Third-order candidates (weno_mod.f90:57-59).
+__device__ __forceinline__ void candidates(const double lf[5], double& q0, double& q1, double& q2) {
+    q0 = a300 * lf[0] + a301 * lf[1] + a302 * lf[2];
+    q1 = a310 * lf[1] + a311 * lf[2] + a312 * lf[3];
+    q2 = a320 * lf[2] + a321 * lf[3] + a322 * lf[4];
+}
+
+// WENO-JS5 (weno5js_stencil + _omega_only + _alpha, weno_mod.f90:98-165)
+__device__ __forceinline__ double weno5js(const double lf[5]) {
+    double q0, q1, q2, is0, is1, is2;
+    candidates(lf, q0, q1, q2);
+    smoothness(lf, is0, is1, is2);
+    double a0 = c30 / sq(kSS + is0);
+    double a1 = c31 / sq(kSS + is1);
+    double a2 = c32 / sq(kSS + is2);
+    double s = a0 + a1 + a2;
+    double w0 = a0 / s, w1 = a1 / s, w2 = a2 / s;
+    return w0 * q0 + w1 * q1 + w2 * q2;
+}
+
+// WENO-Z alpha (weno5z_stencil_alpha, weno_mod.f90:168-189)
+__device__ __forceinline__ void weno5z_alpha(const double lf[5], double& a0, double& a1, double& a2) {
+    double is0, is1, is2;
+    smoothness(lf, is0, is1, is2);
+    double tau5 = fabs(is2 - is0);
+    a0 = c30 * (1.0 + sq(tau5 / (kSS + is0)));
+    a1 = c31 * (1.0 + sq(tau5 / (kSS + is1)));
+    a2 = c32 * (1.0 + sq(tau5 / (kSS + is2)));
+}
+
+// WENO-Z5 (weno5z_stencil + _omega_only, weno_mod.f90:50-79)
+__device__ __forceinline__ double weno5z(const double lf[5]) {
+    double q0, q1, q2, a0, a1, a2;
+    candidates(lf, q0, q1, q2);
+    weno5z_alpha(lf, a0, a1, a2);
+    double s = a0 + a1 + a2;
+    double w0 = a0 / s, w1 = a1 / s, w2 = a2 / s;
+    return w0 * q0 + w1 * q1 + w2 * q2;
+}
+
+// weno5z_stencil_omega_theta (weno_mod.f90:82-95)
+__device__ __forceinline__ void weno5z_omega_theta(const double lf[5], double& w0, double& w1,
+                                                   double& w2, double& theta) {
+    double a0, a1, a2;
+    weno5z_alpha(lf, a0, a1, a2);
+    double s = a0 + a1 + a2;
+    w0 = a0 / s; w1 = a1 / s; w2 = a2 / s;
+    theta = 1.0 / (1.0 + sq(s - 1.0));
+}
+
+// upwind5 (scheme_upwind5_general.f90:86-90)
+__device__ __forceinline__ double upwind5(const double lf[5]) {
+    return (2.0 * lf[0] - 13.0 * lf[1] + 47.0 * lf[2] + 27.0 * lf[3] - 3.0 * lf[4]) / 60.0;
+}
+
+template <int REC> __device__ __forceinline__ double recon5(const double lf[5]) {
+    if (REC == DENSE_RECON_UPWIND5) return upwind5(lf);
+    if (REC == DENSE_RECON_WENOJS5) return weno5js(lf);
+    return weno5z(lf);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Flux-vector splittings at one cell. DIR 0 = xi (normal velocity u, momentum component 1),
+// DIR 1 = eta (normal velocity v, momentum component 2).
+
+// Lax-Friedrichs family (flux_splitting_LLF.f90:73-81 / :98-106, GLF, CH, SC):
+// F+- = 0.5*((un +- lam)*U + (0, p e_n, u_n p))
+template <int DIR>
+__device__ __forceinline__ void lf_split(const double U[4], double un, double p, double lam,
+                                         double fp[4], double fm[4]) {
+    const double up = un + lam, um = un - lam, upp = un * p;
+    fp[0] = 0.5 * (up * U[0]);
+    fm[0] = 0.5 * (um * U[0]);
+    if (DIR == 0) {
+        fp[1] = 0.5 * (up * U[1] + p); fp[2] = 0.5 * (up * U[2]);
+        fm[1] = 0.5 * (um * U[1] + p); fm[2] = 0.5 * (um * U[2]);
+    } else {
+        fp[1] = 0.5 * (up * U[1]); fp[2] = 0.5 * (up * U[2] + p);
+        fm[1] = 0.5 * (um * U[1]); fm[2] = 0.5 * (um * U[2] + p);
+    }
+    fp[3] = 0.5 * (up * U[3] + upp);
+    fm[3] = 0.5 * (um * U[3] + upp);
+}
+
+// Steger-Warming (flux_splitting_SW.f90:42-91 xi, :110-160 eta)
+template <int DIR>
+__device__ __forceinline__ void sw_split(double rho, double u, double v, double alpha, double gamma,
+                                         double fp[4], double fm[4]) {
+    const double epsl2 = 0.125 * 0.125;
+    const double g1 = gamma - 1.0, two_g1 = 2.0 * (gamma - 1.0), two_g = 2.0 * gamma;
+    const double uu2 = u * u + v * v;
+    const double un = DIR == 0 ? u : v, ut = DIR == 0 ? v : u;
+    const double l1 = un, l2 = un - alpha, l3 = un + alpha;
+    const double s1 = sqrt(l1 * l1 + epsl2), s2 = sqrt(l2 * l2 + epsl2), s3 = sqrt(l3 * l3 + epsl2);
+    const double a2 = alpha * alpha;
+    const double q2 = l2 * l2 + ut * ut, q3 = l3 * l3 + ut * ut;
+#pragma unroll
+    for (int sgn = 0; sgn < 2; ++sgn) {
+        const double lp1 = sgn == 0 ? (l1 + s1) / 2.0 : (l1 - s1) / 2.0;
+        const double lp2 = sgn == 0 ? (l2 + s2) / 2.0 : (l2 - s2) / 2.0;
+        const double lp3 = sgn == 0 ? (l3 + s3) / 2.0 : (l3 - s3) / 2.0;
+        double* f = sgn == 0 ? fp : fm;
+        const double wii = (3.0 - gamma) * (lp2 + lp3) * a2 / two_g1;
+        const double A = lp1 * 2.0 * g1;
+        f[0] = (A + lp2 + lp3) * rho / two_g;
+        const double fn = (A * un + lp2 * l2 + lp3 * l3) * rho / two_g;
+        const double ft = (A * ut + lp2 * ut + lp3 * ut) * rho / two_g;
+        f[1 + DIR] = fn;
+        f[2 - DIR] = ft;
+        f[3] = (lp1 * g1 * uu2 + lp2 * 0.5 * q2 + lp3 * 0.5 * q3 + wii) * rho / two_g;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Roe average (scheme_weno5th_CH.f90:44-62) and eigenvectors (get_l_r_vec_xi/_eta,
+// scheme_weno5th_SC.f90:277-328, 607-658). L[c][k] = l(c+1,k+1): column k is the k-th left
+// eigenvector; R[k][e] = r(k+1,e+1): row k is the k-th right eigenvector.
+struct Eig {
+    double L[4][4];
+    double R[4][4];
+};
+
+__device__ __forceinline__ bool roe_eig(int dir, double gamma, double rhol, double rhor, double ul,
+                                        double ur, double vl, double vr, double pl, double pr, Eig& e) {
+    const double hl = pl / (gamma - 1.0) / rhol + 0.5 * (ul * ul + vl * vl) + pl / rhol;
+    const double hr = pr / (gamma - 1.0) / rhor + 0.5 * (ur * ur + vr * vr) + pr / rhor;
+    const double sr = sqrt(rhor), sl = sqrt(rhol), den = sr + sl;
+    const double u0 = (sr * ur + sl * ul) / den;
+    const double v0 = (sr * vr + sl * vl) / den;
+    const double h0 = (sr * hr + sl * hl) / den;
+    const double c2 = (gamma - 1.0) * (h0 - 0.5 * (u0 * u0 + v0 * v0));
+    const double a0 = sqrt(c2);
+    const double uu0 = 0.5 * (u0 * u0 + v0 * v0);
+    const double hh0 = a0 * a0 / (gamma - 1.0);
+    const double un = dir == 0 ? u0 : v0;
+    e.R[0][0] = 1.0; e.R[1][0] = 1.0; e.R[2][0] = 0.0; e.R[3][0] = 1.0;
+    if (dir == 0) {
+        e.R[0][1] = u0 - a0; e.R[1][1] = u0; e.R[2][1] = 0.0; e.R[3][1] = u0 + a0;
+        e.R[0][2] = v0; e.R[1][2] = v0; e.R[2][2] = 1.0; e.R[3][2] = v0;
+        e.R[0][3] = h0 - a0 * u0; e.R[1][3] = uu0; e.R[2][3] = v0; e.R[3][3] = h0 + a0 * u0;
+    } else {
+        e.R[0][1] = u0; e.R[1][1] = u0; e.R[2][1] = 1.0; e.R[3][1] = u0;
+        e.R[0][2] = v0 - a0; e.R[1][2] = v0; e.R[2][2] = 0.0; e.R[3][2] = v0 + a0;
+        e.R[0][3] = h0 - a0 * v0; e.R[1][3] = uu0; e.R[2][3] = u0; e.R[3][3] = h0 + a0 * v0;
+    }
+    const double hu = 0.5 * uu0 / hh0, nu = 0.5 * un / a0, ia = 0.5 / a0;
+    const double pu = 0.5 * u0 / hh0, pv = 0.5 * v0 / hh0, ih = 0.5 / hh0;
+    if (dir == 0) {
+        e.L[0][0] = hu + nu; e.L[1][0] = -pu - ia; e.L[2][0] = -pv; e.L[3][0] = ih;
+        e.L[0][3] = hu - nu; e.L[1][3] = -pu + ia; e.L[2][3] = -pv; e.L[3][3] = ih;
+        e.L[0][2] = -v0; e.L[1][2] = 0.0; e.L[2][2] = 1.0; e.L[3][2] = 0.0;
+    } else {
+        e.L[0][0] = hu + nu; e.L[1][0] = -pu; e.L[2][0] = -pv - ia; e.L[3][0] = ih;
+        e.L[0][3] = hu - nu; e.L[1][3] = -pu; e.L[2][3] = -pv + ia; e.L[3][3] = ih;
+        e.L[0][2] = -u0; e.L[1][2] = 1.0; e.L[2][2] = 0.0; e.L[3][2] = 0.0;
+    }
+    e.L[0][1] = -uu0 / hh0 + 1.0; e.L[1][1] = u0 / hh0; e.L[2][1] = v0 / hh0; e.L[3][1] = -1.0 / hh0;
+    return !(c2 < 0.0);
+}
+
+// Characteristic-wise WENO-Z at one interface and one sign (scheme_weno5th_CH.f90:66-81).
+// F[m][c]: split flux of component c at stencil point m (m = 0..4 <-> -2..2).
+__device__ __forceinline__ void char_weno(const Eig& e, const double F[5][4], double h[4]) {
+    double cv[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        double lf[5];
+#pragma unroll
+        for (int m = 0; m < 5; ++m)
+            lf[m] = e.L[0][k] * F[m][0] + e.L[1][k] * F[m][1] + e.L[2][k] * F[m][2] + e.L[3][k] * F[m][3];
+        cv[k] = weno5z(lf);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+        h[q] = e.R[0][q] * cv[0] + e.R[1][q] * cv[1] + e.R[2][q] * cv[2] + e.R[3][q] * cv[3];
+}
+
+// ---------------------------------------------------------------------------------------------
+// Index helpers
+__device__ __forceinline__ long long cidx(const Params& p, int I, int J) { return (long long)J * p.P + I; }
+
+// Per-stage scalar work, done by one thread before the sweeps read or the update uses them:
+// the CFL time step (time_advance_general.f90:20-24), dt/dx, dt/dy, and the reset of the max
+// slot that this stage's update fills for the next stage.
+__device__ __forceinline__ void stage_scalars(const Params& p, int irk) {
+    Scalars* sc = p.sc;
+    const int slot = irk - 1;
+    if (irk == 1 && !p.if_const_dt) {
+        const double dt_xi = p.dx / sc->maxeig[slot][0];
+        const double dt_eta = p.dy / sc->maxeig[slot][1];
+        sc->dt = p.cfl * dt_xi * dt_eta / (dt_xi + dt_eta);
+    }
+    sc->dtdx = sc->dt / p.dx;
+    sc->dtdy = sc->dt / p.dy;
+    const int next = irk % 3;
+    sc->maxeig[next][0] = 0.0;
+    sc->maxeig[next][1] = 0.0;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Component-wise flux kernel (splittings 101/102/103 with reconstructions 251/253/255).
+// One thread per interface; the tile's per-cell split fluxes are staged in shared memory.
+// xi tile: TX interfaces x TY rows, cells f0+1 .. f0+TX+5; eta tile: TX columns x TY interfaces.
+template <int DIR, int SPL, int REC, int TX, int TY>
+__global__ void __launch_bounds__(TX* TY) k_flux_cw(Params p, int irk) {
+    if (!p.sc->active) return;
+    constexpr int NL = DIR == 0 ? TY : TY + 5;   // smem rows
+    constexpr int NC = DIR == 0 ? TX + 5 : TX;   // smem columns
+    __shared__ double sF[8][NL][NC];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int slot = irk - 1;
+    if (DIR == 0 && blockIdx.x == 0 && blockIdx.y == 0 && tx == 0 && ty == 0) stage_scalars(p, irk);
+    const double lam_g = p.sc->maxeig[slot][DIR];
+    const int NIp = p.ni + 2 * kB, NJp = p.nj + 2 * kB;
+
+    // phase 1: split fluxes of the tile's cells
+    auto cell = [&](int I, int J, int r, int c) {
+        const long long o = cidx(p, I, J);
+        double U[4], fp[4], fm[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) U[v] = p.cons[v * p.plane + o];
+        if (SPL == 0) {
+            const double un = p.prim[(1 + DIR) * p.plane + o];
+            const double pr = p.prim[3 * p.plane + o];
+            const double lam = p.splitting == DENSE_SPLIT_LLF ? fabs(un) + p.prim[4 * p.plane + o] : lam_g;
+            lf_split<DIR>(U, un, pr, lam, fp, fm);
+        } else {
+            sw_split<DIR>(p.prim[o], p.prim[p.plane + o], p.prim[2 * p.plane + o], p.prim[4 * p.plane + o],
+                          p.gamma, fp, fm);
+        }
+#pragma unroll
+        for (int v = 0; v < 4; ++v) { sF[v][r][c] = fp[v]; sF[4 + v][r][c] = fm[v]; }
+    };
+    if (DIR == 0) {
+        const int f0 = blockIdx.x * TX, j = blockIdx.y * TY + ty;
+        if (j < p.nj)
+            for (int k = tx; k < TX + 5; k += TX) {
+                const int I = f0 + 1 + k;
+                if (I < NIp) cell(I, j + kB, ty, k);
+            }
+    } else {
+        const int g0 = blockIdx.y * TY, i = blockIdx.x * TX + tx;
+        if (i < p.ni)
+            for (int k = ty; k < TY + 5; k += TY) {
+                const int J = g0 + 1 + k;
+                if (J < NJp) cell(i + kB, J, k, tx);
+            }
+    }
+    __syncthreads();
+
+    // phase 2: reconstruction at the interface
+    int line, f;  // line = row j (xi) or column i (eta); f = interface index
+    if (DIR == 0) { line = blockIdx.y * TY + ty; f = blockIdx.x * TX + tx; }
+    else          { line = blockIdx.x * TX + tx; f = blockIdx.y * TY + ty; }
+    const int nline = DIR == 0 ? p.nj : p.ni, nface = DIR == 0 ? p.ni + 1 : p.nj + 1;
+    if (line >= nline || f >= nface) return;
+    const int t = DIR == 0 ? tx : ty;  // position of the interface in the tile
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+        double lp[5], lm[5];
+#pragma unroll
+        for (int m = 0; m < 5; ++m) {
+            // "+": lf(m) = F+(cell f+3+m), smem index t+2+m; "-": lf(m) = F-(cell f+4-m), index t+3-m
+            if (DIR == 0) { lp[m] = sF[v][ty][t + m]; lm[m] = sF[4 + v][ty][t + 5 - m]; }
+            else          { lp[m] = sF[v][t + m][tx]; lm[m] = sF[4 + v][t + 5 - m][tx]; }
+        }
+        const double h = recon5<REC>(lp) + recon5<REC>(lm);
+        if (DIR == 0) p.hx[(long long)v * p.nj * (p.ni + 1) + (long long)line * (p.ni + 1) + f] = h;
+        else          p.he[(long long)v * (p.nj + 1) * p.ni + (long long)f * p.ni + line] = h;
+    }
+}
+
+// Unknown reconstruction index with a component-wise splitting: the reference leaves h_xi and
+// h_eta untouched (scheme_invs_general.f90:4-27); they start at zero (allocate_block).
+__global__ void k_flux_noop(Params p, int irk) {
+    if (!p.sc->active) return;
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        stage_scalars(p, irk);
+        atomicOr(&p.sc->status, DENSE_FLAG_RECON_NOOP);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Characteristic flux kernel: 104 (ADAPT = false) and 105 AdaWENO (ADAPT = true).
+// GLF splitting with the stage's global wave speed, Roe-averaged eigenvectors computed once per
+// interface and shared by the + and - reconstructions (the reference computes them twice).
+template <int DIR, bool ADAPT, int TX, int TY>
+__global__ void __launch_bounds__(TX* TY) k_flux_char(Params p, int irk) {
+    if (!p.sc->active) return;
+    constexpr int NL = DIR == 0 ? TY : TY + 5;
+    constexpr int NC = DIR == 0 ? TX + 5 : TX;
+    __shared__ double sF[8][NL][NC];
+    __shared__ double sQ[4][NL][NC];  // rho, u, v, p
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int slot = irk - 1;
+    if (DIR == 0 && blockIdx.x == 0 && blockIdx.y == 0 && tx == 0 && ty == 0) stage_scalars(p, irk);
+    const double lam = p.sc->maxeig[slot][DIR];
+    const int NIp = p.ni + 2 * kB, NJp = p.nj + 2 * kB;
+
+    auto cell = [&](int I, int J, int r, int c) {
+        const long long o = cidx(p, I, J);
+        double U[4], fp[4], fm[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) U[v] = p.cons[v * p.plane + o];
+        double q[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) q[v] = p.prim[v * p.plane + o];
+        lf_split<DIR>(U, q[1 + DIR], q[3], lam, fp, fm);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) { sF[v][r][c] = fp[v]; sF[4 + v][r][c] = fm[v]; sQ[v][r][c] = q[v]; }
+    };
+    if (DIR == 0) {
+        const int f0 = blockIdx.x * TX, j = blockIdx.y * TY + ty;
+        if (j < p.nj)
+            for (int k = tx; k < TX + 5; k += TX) {
+                const int I = f0 + 1 + k;
+                if (I < NIp) cell(I, j + kB, ty, k);
+            }
+    } else {
+        const int g0 = blockIdx.y * TY, i = blockIdx.x * TX + tx;
+        if (i < p.ni)
+            for (int k = ty; k < TY + 5; k += TY) {
+                const int J = g0 + 1 + k;
+                if (J < NJp) cell(i + kB, J, k, tx);
+            }
+    }
+    __syncthreads();
+
+    int line, f;
+    if (DIR == 0) { line = blockIdx.y * TY + ty; f = blockIdx.x * TX + tx; }
+    else          { line = blockIdx.x * TX + tx; f = blockIdx.y * TY + ty; }
+    const int nline = DIR == 0 ? p.nj : p.ni, nface = DIR == 0 ? p.ni + 1 : p.nj + 1;
+    if (line >= nline || f >= nface) return;
+    const int t = DIR == 0 ? tx : ty;
+    auto SF = [&](int q, int k) -> double { return DIR == 0 ? sF[q][ty][k] : sF[q][k][tx]; };
+    auto SQ = [&](int q, int k) -> double { return DIR == 0 ? sQ[q][ty][k] : sQ[q][k][tx]; };
+
+    // AdaWENO indicator from the scalar surrogate rho + F+-(normal momentum)
+    // (flux_splitting_SC.f90:175-176,206-207; get_theta_*, scheme_weno5th_SC.f90:1-64,330-393)
+    bool smooth[2] = {false, false};
+    double wsur[2][3];
+    if (ADAPT) {
+        double lp[5], lm[5];
+#pragma unroll
+        for (int m = 0; m < 5; ++m) {
+            lp[m] = SQ(0, t + m) + SF(1 + DIR, t + m);
+            lm[m] = SQ(0, t + 5 - m) + SF(4 + 1 + DIR, t + 5 - m);
+        }
+        double th;
+        weno5z_omega_theta(lp, wsur[0][0], wsur[0][1], wsur[0][2], th);
+        smooth[0] = th > p.delta;
+        weno5z_omega_theta(lm, wsur[1][0], wsur[1][1], wsur[1][2], th);
+        smooth[1] = th > p.delta;
+    }
+    Eig e;
+    if (!(ADAPT && smooth[0] && smooth[1])) {
+        // cells f+3 (left) and f+4 (right) of the interface: tile indices t+2, t+3
+        const bool ok = roe_eig(DIR, p.gamma, SQ(0, t + 2), SQ(0, t + 3), SQ(1, t + 2), SQ(1, t + 3),
+                                SQ(2, t + 2), SQ(2, t + 3), SQ(3, t + 2), SQ(3, t + 3), e);
+        if (!ok) atomicOr(&p.sc->status, DENSE_FLAG_ROE_IMAG);
+    }
+    double hsum[4];
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        double F[5][4];
+#pragma unroll
+        for (int m = 0; m < 5; ++m)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) F[m][c] = s == 0 ? SF(c, t + m) : SF(4 + c, t + 5 - m);
+        double h[4];
+        if (ADAPT && smooth[s]) {  // scheme_weno5th_SC.f90:110-124
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                double lf[5], q0, q1, q2;
+#pragma unroll
+                for (int m = 0; m < 5; ++m) lf[m] = F[m][c];
+                candidates(lf, q0, q1, q2);
+                h[c] = wsur[s][0] * q0 + wsur[s][1] * q1 + wsur[s][2] * q2;
+            }
+        } else {
+            char_weno(e, F, h);
+        }
+#pragma unroll
+        for (int c = 0; c < 4; ++c) hsum[c] = s == 0 ? h[c] : hsum[c] + h[c];
+    }
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+        if (DIR == 0) p.hx[(long long)v * p.nj * (p.ni + 1) + (long long)line * (p.ni + 1) + f] = hsum[v];
+        else          p.he[(long long)v * (p.nj + 1) * p.ni + (long long)f * p.ni + line] = hsum[v];
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Max of |u|+alpha, |v|+alpha over a block, then one atomicMax per block on the bit pattern
+// (non-negative doubles order like their bits; a NaN compares above +inf and propagates).
+__device__ __forceinline__ void block_max_atomic(double e1, double e2, double* slot) {
+    unsigned long long a = (unsigned long long)__double_as_longlong(e1);
+    unsigned long long b = (unsigned long long)__double_as_longlong(e2);
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        a = max(a, __shfl_xor_sync(0xffffffffu, a, o));
+        b = max(b, __shfl_xor_sync(0xffffffffu, b, o));
+    }
+    __shared__ unsigned long long red[2][32];
+    const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+    const int nw = (blockDim.x * blockDim.y + 31) / 32;
+    if ((tid & 31) == 0) { red[0][tid >> 5] = a; red[1][tid >> 5] = b; }
+    __syncthreads();
+    if (tid == 0) {
+        for (int w = 1; w < nw; ++w) { a = max(a, red[0][w]); b = max(b, red[1][w]); }
+        atomicMax((unsigned long long*)&slot[0], a);
+        atomicMax((unsigned long long*)&slot[1], b);
+    }
+}
+
+// get_primary at one interior cell (get_primary.f90:53-73); returns the two wave speeds.
+__device__ __forceinline__ void prim_cell(const Params& p, long long o, const double q[4], double& e1,
+                                          double& e2, unsigned& flags) {
+    const double rho = q[0];
+    const double u = q[1] / rho;
+    const double v = q[2] / rho;
+    double pr = (p.gamma - 1.0) * (q[3] - 0.5 * rho * (u * u + v * v));
+    if (pr < 0.0) { pr = kPFloor; flags |= DENSE_FLAG_P_FLOOR; }
+    const double alpha = sqrt(p.gamma * pr / rho);
+    p.prim[o] = rho;
+    p.prim[p.plane + o] = u;
+    p.prim[2 * p.plane + o] = v;
+    p.prim[3 * p.plane + o] = pr;
+    p.prim[4 * p.plane + o] = alpha;
+    e1 = fabs(u) + alpha;
+    e2 = fabs(v) + alpha;
+    if (!(rho > 0.0)) flags |= DENSE_FLAG_NEG_RHO;
+    if (isnan(q[0]) || isnan(q[1]) || isnan(q[2]) || isnan(q[3])) flags |= DENSE_FLAG_NAN;
+}
+
+__global__ void k_prim(Params p, int slot) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    double e1 = 0.0, e2 = 0.0;
+    unsigned flags = 0;
+    if (i < p.ni && j < p.nj) {
+        const long long o = cidx(p, i + kB, j + kB);
+        double q[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) q[v] = p.cons[v * p.plane + o];
+        prim_cell(p, o, q, e1, e2, flags);
+    }
+    if (flags) atomicOr(&p.sc->status, flags);
+    block_max_atomic(e1, e2, p.sc->maxeig[slot]);
+}
+
+// time_rk3_general(irk) (time_advance_general.f90:9-267) fused with get_primary of the updated
+// state for the next stage. Body force of Rayleigh-Taylor: S = (0, 0, rho, rho v) of the stage
+// input (boundary_rt_general.f90:154-155), added after the combine as a separate rounding.
+template <int IRK>
+__global__ void k_update(Params p) {
+    if (!p.sc->active) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    double e1 = 0.0, e2 = 0.0;
+    unsigned flags = 0;
+    if (i < p.ni && j < p.nj) {
+        const Scalars* sc = p.sc;
+        const double dtdx = sc->dtdx, dtdy = sc->dtdy, dt = sc->dt;
+        const long long o = cidx(p, i + kB, j + kB);
+        const long long hxs = (long long)p.nj * (p.ni + 1), hes = (long long)(p.nj + 1) * p.ni;
+        const long long hxo = (long long)j * (p.ni + 1) + i, heo = (long long)j * p.ni + i;
+        const double rho_in = p.cons[o], rv_in = p.cons[2 * p.plane + o];
+        double q[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const double dh_dxi = p.hx[v * hxs + hxo + 1] - p.hx[v * hxs + hxo];
+            const double dh_deta = p.he[v * hes + heo + p.ni] - p.he[v * hes + heo];
+            const double qc = p.cons[v * p.plane + o];
+            double qn;
+            if (IRK == 1) {
+                p.cons0[v * p.plane + o] = qc;
+                qn = qc - dtdx * dh_dxi - dtdy * dh_deta;
+            } else if (IRK == 2) {
+                const double q0 = p.cons0[v * p.plane + o];
+                qn = 3.0 / 4.0 * q0 + 1.0 / 4.0 * qc - 1.0 / 4.0 * (dtdx * dh_dxi + dtdy * dh_deta);
+            } else {
+                const double q0 = p.cons0[v * p.plane + o];
+                qn = 1.0 / 3.0 * q0 + 2.0 / 3.0 * qc - 2.0 / 3.0 * (dtdx * dh_dxi + dtdy * dh_deta);
+            }
+            q[v] = qn;
+        }
+        if (p.bodyforce) {
+            const double f = IRK == 1 ? dt : (IRK == 2 ? 1.0 / 4.0 * dt : kTwoThirdsSP * dt);
+            q[0] = q[0] + f * 0.0;
+            q[1] = q[1] + f * 0.0;
+            q[2] = q[2] + f * rho_in;
+            q[3] = q[3] + f * rv_in;
+        }
+#pragma unroll
+        for (int v = 0; v < 4; ++v) p.cons[v * p.plane + o] = q[v];
+        prim_cell(p, o, q, e1, e2, flags);
+    }
+    if (flags) atomicOr(&p.sc->status, flags);
+    block_max_atomic(e1, e2, p.sc->maxeig[IRK % 3]);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Boundary fill (source/boundary/*.f90). One thread per ghost line: a column of the bottom or
+// top ghost rows, or a row of the left or right ghost columns; the four ghost layers of a line
+// are filled in the reference's order (the extrapolation is recursive outward).
+struct Cell {
+    double c[4];
+    double q[5];
+};
+
+__device__ __forceinline__ void state_from(double gamma, double rho, double u, double v, double pr, Cell& g) {
+    g.c[0] = rho; g.c[1] = rho * u; g.c[2] = rho * v;
+    g.c[3] = pr / (gamma - 1.0) + 0.5 * rho * (u * u + v * v);
+    g.q[0] = rho; g.q[1] = u; g.q[2] = v; g.q[3] = pr; g.q[4] = sqrt(gamma * pr / rho);
+}
+
+__device__ __forceinline__ void load_cell(const Params& p, int I, int J, Cell& g) {
+    const long long o = cidx(p, I, J);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) g.c[v] = p.cons[v * p.plane + o];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) g.q[v] = p.prim[v * p.plane + o];
+}
+__device__ __forceinline__ void store_cell(const Params& p, int I, int J, const Cell& g) {
+    const long long o = cidx(p, I, J);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) p.cons[v * p.plane + o] = g.c[v];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) p.prim[v * p.plane + o] = g.q[v];
+}
+// Copy with the normal velocity negated (reflective wall): comp = 1 (u, x-walls) or 2 (v, y-walls)
+__device__ __forceinline__ void reflect(Cell& g, int comp) { g.c[comp] = -g.c[comp]; g.q[comp] = -g.q[comp]; }
+__device__ __forceinline__ double extrap(double near, double far) { return near * 4.0 / 3.0 - far / 3.0; }
+
+enum Side { kBottom = 0, kTop = 1, kLeft = 2, kRight = 3 };
+enum Rule { kNone, kPeriodic, kExtrap, kReflect, kDirichletRT, kDMRBottom, kDMRTop, kDMRInflow, kSSLInflow };
+
+__device__ __forceinline__ Rule side_rule(int bench, int side) {
+    switch (bench) {
+    case DENSE_BENCH_IVC:  // boundary_ivc_general.f90: y periodic, x extrapolated
+        return side <= kTop ? kPeriodic : kExtrap;
+    case DENSE_BENCH_SEDOV:  // bottom/left reflective, top/right extrapolated
+        return (side == kBottom || side == kLeft) ? kReflect : kExtrap;
+    case DENSE_BENCH_RT:  // Dirichlet bottom/top, periodic sides
+        return side <= kTop ? kDirichletRT : kPeriodic;
+    case DENSE_BENCH_RT_REFLECT:
+        return side <= kTop ? kDirichletRT : kReflect;
+    case DENSE_BENCH_RM: case DENSE_BENCH_SHOCKVORTEX:  // reflective bottom/top, extrapolated sides
+        return side <= kTop ? kReflect : kExtrap;
+    case DENSE_BENCH_DMR:
+        return side == kBottom ? kDMRBottom : side == kTop ? kDMRTop : side == kLeft ? kDMRInflow : kExtrap;
+    case DENSE_BENCH_SSL:  // reflective bottom, top untouched, inflow left, extrapolated right
+        return side == kBottom ? kReflect : side == kTop ? kNone : side == kLeft ? kSSLInflow : kExtrap;
+    case DENSE_BENCH_IVC_PERIODIC: case DENSE_BENCH_RM_PERIODIC:
+        return kPeriodic;
+    default:
+        return kNone;
+    }
+}
+
+__global__ void k_bc(Params p) {
+    if (!p.sc->active) return;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ni = p.ni, nj = p.nj;
+    int side, line;
+    if (tid < ni) { side = kBottom; line = tid; }
+    else if (tid < 2 * ni) { side = kTop; line = tid - ni; }
+    else if (tid < 2 * ni + nj) { side = kLeft; line = tid - 2 * ni; }
+    else if (tid < 2 * ni + 2 * nj) { side = kRight; line = tid - 2 * ni - nj; }
+    else return;
+    const Rule rule = side_rule(p.benchmark, side);
+    if (rule == kNone) return;
+    const double gamma = p.gamma;
+    const bool vert = side <= kTop;  // ghost rows of an interior column
+    const int I = line + kB, J = line + kB;
+    for (int k = 0; k < kB; ++k) {
+        // ghost position and, for copies, its source
+        int gi, gj, si = 0, sj = 0;
+        if (side == kBottom) { gi = I; gj = k; }
+        else if (side == kTop) { gi = I; gj = nj + kB + k; }
+        else if (side == kLeft) { gi = kB - 1 - k; gj = J; }   // extrapolation order: b..1
+        else { gi = ni + kB + k; gj = J; }
+        Cell g;
+        switch (rule) {
+        case kPeriodic:
+            if (side == kBottom) { si = I; sj = nj + k; }
+            else if (side == kTop) { si = I; sj = kB + k; }
+            else if (side == kLeft) { si = ni + gi; sj = J; }
+            else { si = kB + k; sj = J; }
+            load_cell(p, si, sj, g);
+            break;
+        case kReflect:
+            if (side == kBottom) { si = I; sj = 2 * kB - 1 - gj; }
+            else if (side == kTop) { si = I; sj = 2 * nj + 2 * kB - 1 - gj; }
+            else if (side == kLeft) { si = 2 * kB - 1 - gi; sj = J; }
+            else { si = 2 * ni + 2 * kB - 1 - gi; sj = J; }
+            load_cell(p, si, sj, g);
+            reflect(g, vert ? 2 : 1);
+            break;
+        case kExtrap: {
+            Cell a, b2;
+            if (side == kBottom) { load_cell(p, I, gj + 1, a); load_cell(p, I, gj + 2, b2); }
+            else if (side == kTop) { load_cell(p, I, gj - 1, a); load_cell(p, I, gj - 2, b2); }
+            else if (side == kLeft) { load_cell(p, gi + 1, J, a); load_cell(p, gi + 2, J, b2); }
+            else { load_cell(p, gi - 1, J, a); load_cell(p, gi - 2, J, b2); }
+#pragma unroll
+            for (int v = 0; v < 4; ++v) g.c[v] = extrap(a.c[v], b2.c[v]);
+#pragma unroll
+            for (int v = 0; v < 5; ++v) g.q[v] = extrap(a.q[v], b2.q[v]);
+            break;
+        }
+        case kDirichletRT:  // boundary_rt_general.f90:14-57
+            if (side == kBottom) state_from(gamma, 2.0, 0.0, 0.0, 1.0, g);
+            else state_from(gamma, 1.0, 0.0, 0.0, 2.5, g);
+            break;
+        case kDMRBottom: {  // boundary_doublemach_general.f90:14-48
+            const double xx = p.xbot[line];
+            if (xx >= 1.0 / 6.0) {
+                load_cell(p, I, 2 * kB - 1 - gj, g);
+                reflect(g, 2);
+            } else {
+                state_from(gamma, 8.0, (double)8.25f * sqrt(3.0) * 0.5, -(double)8.25f * 0.5, 116.5, g);
+            }
+            break;
+        }
+        case kDMRTop: {  // boundary_doublemach_general.f90:51-76 (time at the start of the step)
+            const double xx = p.xtop[line];
+            if (xx < (1.0 / 6.0 + (1.0 + 20.0 * p.sc->t) / sqrt(3.0)))
+                state_from(gamma, 8.0, (double)8.25f * sqrt(3.0) * 0.5, -(double)8.25f * 0.5, 116.5, g);
+            else
+                state_from(gamma, 1.4, 0.0, 0.0, 1.0, g);
+            break;
+        }
+        case kDMRInflow:  // boundary_doublemach_general.f90:79-99
+            state_from(gamma, 8.0, (double)8.25f * sqrt(3.0) * 0.5, -(double)8.25f * 0.5, 116.5, g);
+            break;
+        case kSSLInflow: {  // boundary_ssl_general.f90:40-66
+            const double yy = p.yleft[line];
+            const double rho = yy >= 0.0 ? 1.6374 : 0.3626, pr = 0.3327;
+            const double pie = 3.141592653589793115997963468544185161590576171875;
+            const double t = p.sc->t;
+            const double u = 2.5 + 0.5 * tanh(2.0 * yy);
+            const double v = 0.05 * cos(2.0 * pie * t / (30.0 / 2.68)) * exp(-(yy * yy) / 10.0)
+                           + 0.05 * cos(2.0 * pie * 2.0 * t / (30.0 / 2.68) + pie / 2.0) * exp(-(yy * yy) / 10.0);
+            state_from(gamma, rho, u, v, pr, g);
+            break;
+        }
+        default:
+            return;
+        }
+        if (rule == kReflect || rule == kDirichletRT || rule == kDMRBottom || rule == kDMRTop ||
+            rule == kDMRInflow || rule == kSSLInflow) {
+            // these rules write rho,u,v,p,alpha of prim and leave the entropy alone
+        }
+        store_cell(p, gi, gj, g);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Step bookkeeping (general_main.f90:23-37): the while-condition at the start of a step and the
+// time/step advance at its end.
+__global__ void k_step_begin(Scalars* sc) {
+    sc->active = (sc->t < sc->t_end) && (sc->step < sc->total_step);
+}
+__global__ void k_step_end(Scalars* sc) {
+    if (sc->active) {
+        sc->step += 1;
+        sc->t = sc->t + sc->dt;
+        sc->elasp = sc->elasp + sc->dt;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Launchers
+constexpr int kXTX = 32, kXTY = 4;   // xi tile
+constexpr int kETX = 32, kETY = 8;   // eta tile
+
+static inline dim3 grid_xi(const Params& p, int tx, int ty) {
+    return dim3((p.ni + 1 + tx - 1) / tx, (p.nj + ty - 1) / ty);
+}
+static inline dim3 grid_eta(const Params& p, int tx, int ty) {
+    return dim3((p.ni + tx - 1) / tx, (p.nj + 1 + ty - 1) / ty);
+}
+
+template <int SPL, int REC>
+static void launch_cw(const Params& p, int irk, cudaStream_t s) {
+    k_flux_cw<0, SPL, REC, kXTX, kXTY><<<grid_xi(p, kXTX, kXTY), dim3(kXTX, kXTY), 0, s>>>(p, irk);
+    k_flux_cw<1, SPL, REC, kETX, kETY><<<grid_eta(p, kETX, kETY), dim3(kETX, kETY), 0, s>>>(p, irk);
+}
+
+static void launch_flux(const Params& p, int irk, void* stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    switch (p.splitting) {
+    case DENSE_SPLIT_LLF: case DENSE_SPLIT_GLF: case DENSE_SPLIT_SW: {
+        const int spl = p.splitting == DENSE_SPLIT_SW ? 1 : 0;
+        if (p.recon == DENSE_RECON_UPWIND5) { spl ? launch_cw<1, 251>(p, irk, s) : launch_cw<0, 251>(p, irk, s); }
+        else if (p.recon == DENSE_RECON_WENOJS5) { spl ? launch_cw<1, 253>(p, irk, s) : launch_cw<0, 253>(p, irk, s); }
+        else if (p.recon == DENSE_RECON_WENOZ5) { spl ? launch_cw<1, 255>(p, irk, s) : launch_cw<0, 255>(p, irk, s); }
+        else k_flux_noop<<<1, 32, 0, s>>>(p, irk);
+        break;
+    }
+    case DENSE_SPLIT_CH:
+        k_flux_char<0, false, kXTX, kXTY><<<grid_xi(p, kXTX, kXTY), dim3(kXTX, kXTY), 0, s>>>(p, irk);
+        k_flux_char<1, false, kETX, kETY><<<grid_eta(p, kETX, kETY), dim3(kETX, kETY), 0, s>>>(p, irk);
+        break;
+    case DENSE_SPLIT_SC:
+        k_flux_char<0, true, kXTX, kXTY><<<grid_xi(p, kXTX, kXTY), dim3(kXTX, kXTY), 0, s>>>(p, irk);
+        k_flux_char<1, true, kETX, kETY><<<grid_eta(p, kETX, kETY), dim3(kETX, kETY), 0, s>>>(p, irk);
+        break;
+    default:
+        break;
+    }
+}
+
+static int flux_launches(const Params& p) {
+    if (p.splitting >= DENSE_SPLIT_LLF && p.splitting <= DENSE_SPLIT_SW &&
+        p.recon != DENSE_RECON_UPWIND5 && p.recon != DENSE_RECON_WENOJS5 && p.recon != DENSE_RECON_WENOZ5)
+        return 1;
+    return 2;
+}
+
+static void launch_prim(const Params& p, int slot, void* stream) {
+    dim3 b(32, 8), g((p.ni + 31) / 32, (p.nj + 7) / 8);
+    k_prim<<<g, b, 0, (cudaStream_t)stream>>>(p, slot);
+}
+static void launch_bc(const Params& p, void* stream) {
+    const int n = 2 * p.ni + 2 * p.nj;
+    k_bc<<<(n + 127) / 128, 128, 0, (cudaStream_t)stream>>>(p);
+}
+static void launch_update(const Params& p, int irk, void* stream) {
+    dim3 b(32, 8), g((p.ni + 31) / 32, (p.nj + 7) / 8);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (irk == 1) k_update<1><<<g, b, 0, s>>>(p);
+    else if (irk == 2) k_update<2><<<g, b, 0, s>>>(p);
+    else k_update<3><<<g, b, 0, s>>>(p);
+}
+static void launch_step_begin(const Params& p, void* stream) { k_step_begin<<<1, 1, 0, (cudaStream_t)stream>>>(p.sc); }
+static void launch_step_end(const Params& p, void* stream) { k_step_end<<<1, 1, 0, (cudaStream_t)stream>>>(p.sc); }
+
+}  // namespace VNS
+
+#if DENSE_VARIANT_STRICT
+const KernelTable* kernels_strict() {
+    static const KernelTable t = {"strict", VNS::launch_prim, VNS::launch_bc, VNS::launch_flux,
+                                  VNS::launch_update, VNS::launch_step_begin, VNS::launch_step_end,
+                                  VNS::flux_launches};
+    return &t;
+}
+#else
+const KernelTable* kernels_fast() {
+    static const KernelTable t = {"fast", VNS::launch_prim, VNS::launch_bc, VNS::launch_flux,
+                                  VNS::launch_update, VNS::launch_step_begin, VNS::launch_step_end,
+                                  VNS::flux_launches};
+    return &t;
+}
+#endif
+
+}  // namespace dense

@@ -1,0 +1,168 @@
+"""Host-side mirror of the reference's per-stage interface, over the C ABI of libdense2d.so.
+
+The reference drives one block through module globals and four argument-less subroutines per
+Runge-Kutta stage (source/utility/general_main.f90:26-31):
+
+    call get_primary; call boundary_general; call flux_splitting_general; call time_rk3_general(irk)
+
+``Solver`` keeps the same vocabulary: ``read_par_namelist`` / ``init_general`` build the block,
+``stage(irk)`` is the four calls, ``steps`` is the loop of general_main.f90:23-38 on the device,
+and the state comes back in the reference's Fortran layout (cons(NIp,NJp,4), prim(NIp,NJp,6)).
+Every call goes to the CUDA library; there is no CPU path. Errors raise ``DenseError`` with the
+library's status code instead of the reference's ``print; stop``.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _abi
+from ._abi import DenseConfig, DenseError
+
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(_dp)
+
+
+def _check(lib, rc: int, h=None):
+    if rc != _abi.DENSE_OK:
+        msg = lib.dense_last_error(h)
+        raise DenseError(rc, msg.decode() if msg else "")
+
+
+def config_default(**overrides) -> DenseConfig:
+    """Module defaults (flow_mod_general.f90:50-179) from the library, plus overrides."""
+    lib = _abi.load_library()
+    c = DenseConfig()
+    _check(lib, lib.dense_config_default(ctypes.byref(c)))
+    for k, v in overrides.items():
+        setattr(c, k, v)
+    return c
+
+
+def read_par_namelist(path: str, cfg: DenseConfig | None = None) -> DenseConfig:
+    """read_par_namelist (flow_mod_general.f90:297-334): entries in the file override cfg."""
+    lib = _abi.load_library()
+    c = config_default() if cfg is None else cfg.copy()
+    _check(lib, lib.dense_read_namelist(path.encode(), ctypes.byref(c)))
+    return c
+
+
+def init_general(cfg: DenseConfig):
+    """init_general (init_general.f90:13-37): returns (cfg, cons, prim, x, y), with cfg.dx/dy
+    (and gamma, if_bodyforce for Rayleigh-Taylor) as the setup leaves them."""
+    lib = _abi.load_library()
+    c = cfg.copy()
+    nip, njp = c.ni + 8, c.nj + 8
+    cons = np.zeros((nip, njp, 4), order="F")
+    prim = np.zeros((nip, njp, 6), order="F")
+    x = np.zeros((c.ni, c.nj), order="F")
+    y = np.zeros((c.ni, c.nj), order="F")
+    _check(lib, lib.dense_init_setup(ctypes.byref(c), _ptr(cons), _ptr(prim), _ptr(x), _ptr(y)))
+    return c, cons, prim, x, y
+
+
+class Solver:
+    """One block of the solver resident on the GPU."""
+
+    def __init__(self, cfg: DenseConfig):
+        self.lib = _abi.load_library()
+        self.cfg = cfg.copy()
+        h = ctypes.c_void_p()
+        _check(self.lib, self.lib.dense_create(ctypes.byref(self.cfg), ctypes.byref(h)))
+        self.h = h
+        self.current_time = 0.0
+        self.current_step = 0
+        self.dt = cfg.dt
+
+    @classmethod
+    def from_setup(cls, cfg: DenseConfig) -> "Solver":
+        """init_general + upload: the block as the reference's start-up leaves it."""
+        c, cons, prim, x, y = init_general(cfg)
+        s = cls(c)
+        s.upload(cons, prim, x, y)
+        return s
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.dense_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _chk(self, rc):
+        _check(self.lib, rc, self.h)
+
+    # -- state -------------------------------------------------------------------------
+    def upload(self, cons, prim=None, x=None, y=None):
+        arrs = [None if a is None else np.asfortranarray(a, dtype=np.float64)
+                for a in (cons, prim, x, y)]
+        self._chk(self.lib.dense_upload(self.h, *[_ptr(a) for a in arrs]))
+
+    def download(self, with_prim: bool = True):
+        nip, njp = self.cfg.ni + 8, self.cfg.nj + 8
+        cons = np.zeros((nip, njp, 4), order="F")
+        prim = np.zeros((nip, njp, 6), order="F") if with_prim else None
+        self._chk(self.lib.dense_download(self.h, _ptr(cons), _ptr(prim)))
+        return (cons, prim) if with_prim else cons
+
+    def fluxes(self):
+        ni, nj = self.cfg.ni, self.cfg.nj
+        hx = np.zeros((ni + 1, nj, 4), order="F")
+        he = np.zeros((nj + 1, ni, 4), order="F")
+        self._chk(self.lib.dense_get_fluxes(self.h, _ptr(hx), _ptr(he)))
+        return hx, he
+
+    def max_eig(self):
+        a, b = ctypes.c_double(), ctypes.c_double()
+        self._chk(self.lib.dense_get_max_eig(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def status(self) -> int:
+        f = ctypes.c_uint()
+        self._chk(self.lib.dense_status(self.h, ctypes.byref(f)))
+        return f.value
+
+    def reconfigure(self, cfg: DenseConfig):
+        self._chk(self.lib.dense_reconfigure(self.h, ctypes.byref(cfg)))
+        self.cfg = cfg.copy()
+
+    def launch_count(self) -> int:
+        return int(self.lib.dense_launch_count(self.h))
+
+    # -- the hot path ---------------------------------------------------------------------
+    def stage(self, irk: int) -> float:
+        """get_primary, boundary_general, flux_splitting_general, time_rk3_general(irk)."""
+        dt = ctypes.c_double(self.dt)
+        self._chk(self.lib.dense_stage(self.h, irk, self.current_time, ctypes.byref(dt)))
+        self.dt = dt.value
+        return self.dt
+
+    def step(self):
+        """One time step of general_main.f90:26-37 through three dense_stage calls."""
+        for irk in range(1, self.cfg.stages + 1):
+            self.stage(irk)
+        self.current_step += 1
+        self.current_time = self.current_time + self.dt
+
+    def steps(self, n: int, t_end: float = float("inf"), total_step: int = 2**31 - 1):
+        """Up to n steps on the device while current_time < t_end and current_step < total_step."""
+        t = ctypes.c_double(self.current_time)
+        s = ctypes.c_int(self.current_step)
+        dt = ctypes.c_double(self.dt)
+        self._chk(self.lib.dense_steps(self.h, n, t_end, total_step, ctypes.byref(t),
+                                       ctypes.byref(s), ctypes.byref(dt)))
+        self.current_time, self.current_step, self.dt = t.value, s.value, dt.value

@@ -1,0 +1,199 @@
+/*
+ * dense2d.h — C ABI of the GB300 (sm_103a) implementation of 2DENSE's per-stage hot path:
+ * primitive recovery, boundary (ghost) fill, flux-vector splitting, WENO reconstruction and
+ * the TVD-RK3 stage update.
+ *
+ * The reference has no FFI. Its seam is the four argument-less subroutines that the Fortran
+ * driver calls once per Runge-Kutta stage (source/utility/general_main.f90:27-30):
+ *     call get_primary; call boundary_general; call flux_splitting_general; call time_rk3_general(irk)
+ * and the module globals they share (source/utility/flow_mod_general.f90:47-183).
+ * dense_stage() replaces those four calls; dense_steps() replaces the whole stage loop of
+ * general_main.f90:23-38. Each declaration below names the reference code it stands in for.
+ *
+ * Conventions
+ *  - Every entry point returns an int status (DENSE_OK == 0) and never exits the process;
+ *    the reference instead prints and stops (flux_splitting.f90:30-32, boundary_general.f90:26-28).
+ *  - Host arrays use the reference's Fortran layout: column-major, i fastest, padded with
+ *    `bfsize` ghost layers on every side: cons(ni+2b, nj+2b, 4), prim(ni+2b, nj+2b, 6),
+ *    x(ni, nj), y(ni, nj) (source/utility/flow_mod_general.f90:205-206,251-252).
+ *  - Host arrays stay owned by the caller; the handle owns its device buffers and stream.
+ *    One handle per host thread; calls are ordered on the handle's stream.
+ *  - All arithmetic is IEEE binary64.
+ */
+#ifndef DENSE2D_H
+#define DENSE2D_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------------------- */
+#define DENSE_OK              0
+#define DENSE_ERR_ARG         1  /* null pointer, bad size or bad index argument              */
+#define DENSE_ERR_SPLITTING   2  /* unknown scheme_splitting_index (flux_splitting.f90:30-32) */
+#define DENSE_ERR_BENCHMARK   3  /* unknown benchmark_index (boundary_general.f90:26-28,
+                                    init_general.f90:34-36)                                  */
+#define DENSE_ERR_CUDA        4  /* a CUDA runtime call failed; see dense_last_error()        */
+#define DENSE_ERR_NUMERIC     5  /* the device status word holds a numeric fault flag         */
+#define DENSE_ERR_TIMEOUT     6  /* a bounded device-side wait gave up                        */
+#define DENSE_ERR_IO          7  /* file could not be opened, read or written                 */
+#define DENSE_ERR_STATE       8  /* call out of order, e.g. dense_stage() before dense_upload() */
+#define DENSE_ERR_NOMEM       9  /* device allocation failed                                  */
+#define DENSE_ERR_LIMIT      10  /* a size exceeds a documented maximum                       */
+
+/* ---- device status-word bits (dense_status) -------------------------------------------- */
+#define DENSE_FLAG_NAN          0x01u /* a NaN appeared in the updated state                 */
+#define DENSE_FLAG_NEG_RHO      0x02u /* density <= 0 in an updated cell                      */
+#define DENSE_FLAG_P_FLOOR      0x04u /* the p<0 -> 1.0e-6 floor fired (get_primary.f90:57-59) */
+#define DENSE_FLAG_ROE_IMAG     0x08u /* Roe sound speed squared < 0 (sqrt of a negative)    */
+#define DENSE_FLAG_RECON_NOOP   0x10u /* unknown scheme_inv_index: h stays zero, as in the
+                                         reference's silent no-op (scheme_invs_general.f90:4-27) */
+#define DENSE_FLAG_TIMEOUT      0x20u /* a bounded device wait gave up                        */
+
+/* ---- scheme and benchmark indices (the reference's namelist values) --------------------- */
+#define DENSE_SPLIT_LLF   101  /* local Lax-Friedrichs       flux_splitting_LLF.f90:13-77    */
+#define DENSE_SPLIT_GLF   102  /* global Lax-Friedrichs      flux_splitting_GLF.f90:13-70    */
+#define DENSE_SPLIT_SW    103  /* Steger-Warming             flux_splitting_SW.f90:14-168    */
+#define DENSE_SPLIT_CH    104  /* characteristic WENO-Z, Roe + GLF  flux_splitting_CH.f90   */
+#define DENSE_SPLIT_SC    105  /* AdaWENO (adaptive characteristic) flux_splitting_SC.f90   */
+#define DENSE_RECON_UPWIND5  251 /* scheme_upwind5_general.f90 */
+#define DENSE_RECON_WENOJS5  253 /* scheme_weno5js_general.f90 */
+#define DENSE_RECON_WENOZ5   255 /* scheme_weno5z_general.f90  */
+
+#define DENSE_BENCH_USER          0  /* nothing initialised, no ghost fill (init_general.f90:32-33) */
+#define DENSE_BENCH_IVC           1  /* isentropic vortex, reference setup                        */
+#define DENSE_BENCH_SEDOV         2
+#define DENSE_BENCH_RT            3  /* Rayleigh-Taylor, periodic sides, body force               */
+#define DENSE_BENCH_RM            4  /* Richtmyer-Meshkov                                         */
+#define DENSE_BENCH_DMR           5  /* double Mach reflection                                    */
+#define DENSE_BENCH_SSL           6  /* shock / shear layer                                       */
+#define DENSE_BENCH_SHOCKVORTEX   9
+/* Variants that the reference does not ship (its commented-out code paths and the published
+ * test problems' standard forms). They keep the reference's formulas where it has them. */
+#define DENSE_BENCH_IVC_PERIODIC 11  /* translating vortex: freestream (1,1,1,1), strength var_eps,
+                                        centre (var_xc,var_yc), periodic in x and y             */
+#define DENSE_BENCH_RT_REFLECT   13  /* RT with reflective side walls (boundary_rt_general.f90:59-127,
+                                        commented out in the reference)                         */
+#define DENSE_BENCH_RM_PERIODIC  14  /* Mach 1.2 shock into a density-3 sinusoidal interface of
+                                        amplitude var_amp, periodic in x and y                   */
+
+/* ---- configuration: the six namelists of input.in (flow_mod_general.f90:50-179) ---------- */
+typedef struct dense_config_t {
+    /* grid_pars */
+    int ni, nj;               /* single_ni, single_nj                                       */
+    int bfsize;               /* ghost layers per side; the reference always uses 4          */
+    int neq;                  /* number of equations, 4                                      */
+    /* model_pars */
+    int benchmark;            /* benchmark_index                                             */
+    int if_bodyforce, if_source, if_viscous;
+    /* scheme_pars */
+    int splitting;            /* scheme_splitting_index                                      */
+    int recon;                /* scheme_inv_index                                            */
+    double delta;             /* AdaWENO switch threshold on theta                           */
+    /* time_step_pars */
+    int stages;               /* 3                                                           */
+    int if_const_dt;
+    double cfl, dt;
+    double total_time, dt_save;
+    int total_step, save_step;
+    int if_save_binary, if_save_tec, if_save_theta;
+    /* gas_pars */
+    double gamma;
+    /* block geometry, written by dense_init_setup() (init_*_general.f90) */
+    double dx, dy;
+    /* parameters of the variant benchmarks 11, 13, 14 */
+    double var_eps, var_xc, var_yc, var_amp;
+    /* remaining namelist entries, carried so an input.in round-trips */
+    int omp_thread_num, if_curve_grid, if_read_from_file, scheme_vis_index;
+    double mach_inf, reynolds;
+    /* kernel variant: 0 = fast (FMA contraction and algebraic rewrites, agrees with the
+       reference to <= 1e-12 relative after one step); 1 = strict (the reference's evaluation
+       order, no FMA contraction, IEEE divide and sqrt: bit-identical on the reference's
+       x86-64 arithmetic except where a boundary rule calls a transcendental function) */
+    int strict;
+    int reserved[7];
+} dense_config_t;
+
+typedef struct dense_handle dense_handle_t;
+
+/* ---- configuration and initial setup (host side, one-time) ----------------------------- */
+
+/* Module defaults of flow_mod_general.f90:50-179 (e.g. splitting 101, recon 201, cfl 0.5). */
+int dense_config_default(dense_config_t* cfg);
+
+/* read_par_namelist (flow_mod_general.f90:297-334): parse the six namelists of an input.in.
+   Entries absent from the file keep the values already in *cfg. */
+int dense_read_namelist(const char* path, dense_config_t* cfg);
+
+/* init_general (init_general.f90:13-37): fill the interior of cons and prim and the cell
+   centres x, y for cfg->benchmark; set cfg->dx, cfg->dy (and, for Rayleigh-Taylor, gamma=5/3
+   and if_bodyforce=1 as init_RT_general.f90:9-10 does). Ghost cells are zeroed, like
+   allocate_block (flow_mod_general.f90:207-208), except where the setup writes them. */
+int dense_init_setup(dense_config_t* cfg, double* cons, double* prim, double* x, double* y);
+
+/* Bytes of the host arrays for cfg: cons, prim, x (== y). */
+int dense_array_sizes(const dense_config_t* cfg, long long* cons_count, long long* prim_count,
+                      long long* xy_count);
+
+/* ---- solver handle --------------------------------------------------------------------- */
+
+/* allocate_block (flow_mod_general.f90:190-295) on the device: state, stage copy, interface
+   fluxes, scratch. Picks device 0 unless CUDA_VISIBLE_DEVICES says otherwise. */
+int dense_create(const dense_config_t* cfg, dense_handle_t** out);
+
+/* Copy the caller's state to the device (block_grid(1)%cons / %prim / %x / %y). prim may be
+   NULL: interior primitives are then recomputed on the device (get_primary) and ghost
+   primitives are zero. x and y are needed only by boundary rules that read them
+   (DMR, SSL); they may be NULL otherwise. */
+int dense_upload(dense_handle_t* h, const double* cons, const double* prim,
+                 const double* x, const double* y);
+
+/* One Runge-Kutta stage: get_primary -> boundary_general -> flux_splitting_general ->
+   time_rk3_general(irk) (general_main.f90:27-30). current_time is the driver's time at the
+   start of the step (boundary rules read it). On irk == 1 without if_const_dt the CFL time
+   step is computed on the device (time_advance_general.f90:20-24) and returned in *dt_inout;
+   otherwise *dt_inout is the dt used. Synchronises the stream to return dt. */
+int dense_stage(dense_handle_t* h, int irk, double current_time, double* dt_inout);
+
+/* The device-resident step loop of general_main.f90:23-38: up to nsteps steps of `stages`
+   stages, each taken only while (*t_inout < t_end && *step_inout < total_step), advancing
+   time and step on the device; no host synchronisation between steps. On return *t_inout,
+   *step_inout and *dt_out hold the driver's current_time, current_step and dt. */
+int dense_steps(dense_handle_t* h, int nsteps, double t_end, int total_step,
+                double* t_inout, int* step_inout, double* dt_out);
+
+/* Copy the state back (Fortran layout). prim may be NULL; when given, the interior is
+   recomputed exactly as get_primary does (rho,u,v,p,alpha and entropy log(p)-log(rho)) and
+   the ghosts hold what the last boundary fill wrote. */
+int dense_download(dense_handle_t* h, double* cons, double* prim);
+
+/* max_eig_i / max_eig_j of the most recent get_primary (get_primary.f90:69-73). */
+int dense_get_max_eig(dense_handle_t* h, double* max_eig_i, double* max_eig_j);
+
+/* The namelist re-read at every save (general_main.f90:53) changes gamma, cfl, dt, flags
+   and scheme indices mid-run; apply such a change to a live handle. Grid sizes and the
+   benchmark must not change (DENSE_ERR_ARG). */
+int dense_reconfigure(dense_handle_t* h, const dense_config_t* cfg);
+
+/* Read (and clear) the device status word: DENSE_FLAG_* bits. Synchronises. */
+int dense_status(dense_handle_t* h, unsigned* flags);
+
+/* Text of the last error on this handle (or of the last handle-less call when h is NULL). */
+const char* dense_last_error(dense_handle_t* h);
+
+void dense_destroy(dense_handle_t* h);
+
+/* ---- inspection (tests and tooling) ---------------------------------------------------- */
+
+/* Interface fluxes of the last stage, in the reference's layout:
+   h_xi(ni+1, nj, 4) and h_eta(nj+1, ni, 4) (flow_mod_general.f90:236-237). */
+int dense_get_fluxes(dense_handle_t* h, double* h_xi, double* h_eta);
+
+/* Number of kernel launches this handle has issued (including those inside CUDA graphs,
+   counted once per graph launch per node). */
+long long dense_launch_count(dense_handle_t* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DENSE2D_H */
