@@ -167,6 +167,12 @@ def load_library(path: str | None = None):
         "dense_launch_count": (ctypes.c_longlong, [vp]),
         "dense_config_size": (_c_int, []),
         "dense_measure_fp64": (_c_int, [_c_int, dp]),
+        "dense_get_stream": (_c_int, [vp, ctypes.POINTER(vp)]),
+        "dense_steps_async": (_c_int, [vp, _c_int, _c_double, _c_int]),
+        "dense_set_time": (_c_int, [vp, _c_double, _c_int]),
+        "dense_get_time": (_c_int, [vp, dp, ctypes.POINTER(_c_int), dp]),
+        "dense_sync": (_c_int, [vp]),
+        "dense_profile_stage": (_c_int, [vp, _c_int, ctypes.POINTER(ctypes.c_float)]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)

@@ -61,6 +61,15 @@ __global__ void k_set_loop(Scalars* sc, double t, long long step, double t_end, 
     sc->active = active;
 }
 __global__ void k_set_dt(Scalars* sc, double dt) { sc->dt = dt; }
+__global__ void k_set_bounds(Scalars* sc, double t_end, long long total_step) {
+    sc->t_end = t_end;
+    sc->total_step = total_step;
+}
+__global__ void k_set_time(Scalars* sc, double t, long long step) {
+    sc->t = t;
+    sc->step = step;
+}
+__global__ void k_set_active(Scalars* sc) { sc->active = 1; }
 
 bool valid_split(int s) { return s >= DENSE_SPLIT_LLF && s <= DENSE_SPLIT_SC; }
 bool valid_bench(int b) {
@@ -122,10 +131,13 @@ int ensure_prim(dense_handle* h, int slot) {
 // one stage: boundary_general -> flux_splitting_general -> time_rk3_general(irk)
 void enqueue_stage(dense_handle* h, int irk) {
     h->kt->bc(h->prm, h->stream);
-    h->kt->flux(h->prm, irk, h->stream);
+    h->kt->flux(h->prm, irk, 0, h->stream);
+    h->kt->flux(h->prm, irk, 1, h->stream);
     h->kt->update(h->prm, irk, h->stream);
 }
-int stage_launches(dense_handle* h) { return 2 + h->kt->flux_launches(h->prm); }
+int stage_launches(dense_handle* h) {
+    return 2 + h->kt->flux_launches(h->prm, 0) + h->kt->flux_launches(h->prm, 1);
+}
 
 int build_step_graph(dense_handle* h) {
     if (h->step_graph) return DENSE_OK;
@@ -352,5 +364,78 @@ int dense_get_fluxes(dense_handle_t* h, double* h_xi, double* h_eta) {
 }
 
 long long dense_launch_count(dense_handle_t* h) { return h ? h->launches : -1; }
+
+int dense_get_stream(dense_handle_t* h, void** stream) {
+    if (!h || !stream) return seterr(h, DENSE_ERR_ARG, "null argument");
+    *stream = (void*)h->stream;
+    return DENSE_OK;
+}
+
+int dense_steps_async(dense_handle_t* h, int nsteps, double t_end, int total_step) {
+    if (!h) return seterr(h, DENSE_ERR_ARG, "null handle");
+    if (nsteps < 0) return seterr(h, DENSE_ERR_ARG, "nsteps < 0");
+    if (!h->uploaded) return seterr(h, DENSE_ERR_STATE, "dense_steps_async before dense_upload");
+    int rc = ensure_prim(h, 0);
+    if (rc) return rc;
+    rc = build_step_graph(h);
+    if (rc) return rc;
+    k_set_bounds<<<1, 1, 0, h->stream>>>(h->sc, t_end, total_step);
+    h->launches += 1;
+    for (int s = 0; s < nsteps; ++s) {
+        CK(h, cudaGraphLaunch(h->step_graph, h->stream));
+        h->launches += h->graph_nodes;
+    }
+    return DENSE_OK;
+}
+
+int dense_get_time(dense_handle_t* h, double* t, int* step, double* dt) {
+    if (!h) return seterr(h, DENSE_ERR_ARG, "null handle");
+    Scalars s{};
+    CK(h, cudaMemcpyAsync(&s, h->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    if (t) *t = s.t;
+    if (step) *step = (int)s.step;
+    if (dt) *dt = s.dt;
+    return DENSE_OK;
+}
+
+int dense_set_time(dense_handle_t* h, double t, int step) {
+    if (!h) return seterr(h, DENSE_ERR_ARG, "null handle");
+    k_set_time<<<1, 1, 0, h->stream>>>(h->sc, t, step);
+    h->launches += 1;
+    return launch_check(h);
+}
+
+int dense_sync(dense_handle_t* h) {
+    if (!h) return seterr(h, DENSE_ERR_ARG, "null handle");
+    CK(h, cudaStreamSynchronize(h->stream));
+    return DENSE_OK;
+}
+
+int dense_profile_stage(dense_handle_t* h, int irk, float* ms) {
+    if (!h || !ms) return seterr(h, DENSE_ERR_ARG, "null argument");
+    if (irk < 1 || irk > 3) return seterr(h, DENSE_ERR_ARG, "irk must be 1, 2 or 3");
+    if (!h->uploaded) return seterr(h, DENSE_ERR_STATE, "dense_profile_stage before dense_upload");
+    int rc = ensure_prim(h, irk - 1);
+    if (rc) return rc;
+    k_set_active<<<1, 1, 0, h->stream>>>(h->sc);
+    cudaEvent_t ev[5];
+    for (auto& e : ev) CK(h, cudaEventCreate(&e));
+    CK(h, cudaEventRecord(ev[0], h->stream));
+    h->kt->bc(h->prm, h->stream);
+    CK(h, cudaEventRecord(ev[1], h->stream));
+    h->kt->flux(h->prm, irk, 0, h->stream);
+    CK(h, cudaEventRecord(ev[2], h->stream));
+    h->kt->flux(h->prm, irk, 1, h->stream);
+    CK(h, cudaEventRecord(ev[3], h->stream));
+    h->kt->update(h->prm, irk, h->stream);
+    CK(h, cudaEventRecord(ev[4], h->stream));
+    h->launches += 1 + stage_launches(h);
+    CK(h, cudaEventSynchronize(ev[4]));
+    for (int k = 0; k < 4; ++k) CK(h, cudaEventElapsedTime(&ms[k], ev[k], ev[k + 1]));
+    for (auto& e : ev) cudaEventDestroy(e);
+    h->prim_slot = irk % 3;
+    return launch_check(h);
+}
 
 }  // extern "C"

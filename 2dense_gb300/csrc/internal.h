@@ -51,16 +51,16 @@ struct KernelTable {
     void (*prim)(const Params&, int slot, void* stream);
     // boundary_general
     void (*bc)(const Params&, void* stream);
-    // flux_splitting_general (+ scheme_invis_general): both sweeps, writes hx/he. Also computes
-    // dt (stage 1) and zeroes the next max slot.
-    void (*flux)(const Params&, int irk, void* stream);
+    // flux_splitting_general (+ scheme_invis_general) in one direction: dir 0 writes hx (and
+    // computes dt on stage 1, dt/dx, dt/dy, and zeroes the next max slot), dir 1 writes he.
+    void (*flux)(const Params&, int irk, int dir, void* stream);
     // time_rk3_general(irk) fused with get_primary of the new state
     void (*update)(const Params&, int irk, void* stream);
     // loop bookkeeping: step_begin evaluates the while-condition, step_end advances time
     void (*step_begin)(const Params&, void* stream);
     void (*step_end)(const Params&, void* stream);
-    // kernel launches issued by flux() for this configuration
-    int (*flux_launches)(const Params&);
+    // kernel launches issued by flux(dir) for this configuration
+    int (*flux_launches)(const Params&, int dir);
 };
 
 const KernelTable* kernels_fast();

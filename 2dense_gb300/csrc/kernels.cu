@@ -740,40 +740,43 @@ static inline dim3 grid_eta(const Params& p, int tx, int ty) {
 }
 
 template <int SPL, int REC>
-static void launch_cw(const Params& p, int irk, cudaStream_t s) {
-    k_flux_cw<0, SPL, REC, kXTX, kXTY><<<grid_xi(p, kXTX, kXTY), dim3(kXTX, kXTY), 0, s>>>(p, irk);
-    k_flux_cw<1, SPL, REC, kETX, kETY><<<grid_eta(p, kETX, kETY), dim3(kETX, kETY), 0, s>>>(p, irk);
+static void launch_cw(const Params& p, int irk, int dir, cudaStream_t s) {
+    if (dir == 0) k_flux_cw<0, SPL, REC, kXTX, kXTY><<<grid_xi(p, kXTX, kXTY), dim3(kXTX, kXTY), 0, s>>>(p, irk);
+    else          k_flux_cw<1, SPL, REC, kETX, kETY><<<grid_eta(p, kETX, kETY), dim3(kETX, kETY), 0, s>>>(p, irk);
 }
 
-static void launch_flux(const Params& p, int irk, void* stream) {
+static bool recon_known(int r) {
+    return r == DENSE_RECON_UPWIND5 || r == DENSE_RECON_WENOJS5 || r == DENSE_RECON_WENOZ5;
+}
+
+static void launch_flux(const Params& p, int irk, int dir, void* stream) {
     cudaStream_t s = (cudaStream_t)stream;
     switch (p.splitting) {
     case DENSE_SPLIT_LLF: case DENSE_SPLIT_GLF: case DENSE_SPLIT_SW: {
         const int spl = p.splitting == DENSE_SPLIT_SW ? 1 : 0;
-        if (p.recon == DENSE_RECON_UPWIND5) { spl ? launch_cw<1, 251>(p, irk, s) : launch_cw<0, 251>(p, irk, s); }
-        else if (p.recon == DENSE_RECON_WENOJS5) { spl ? launch_cw<1, 253>(p, irk, s) : launch_cw<0, 253>(p, irk, s); }
-        else if (p.recon == DENSE_RECON_WENOZ5) { spl ? launch_cw<1, 255>(p, irk, s) : launch_cw<0, 255>(p, irk, s); }
-        else k_flux_noop<<<1, 32, 0, s>>>(p, irk);
+        if (p.recon == DENSE_RECON_UPWIND5) { spl ? launch_cw<1, 251>(p, irk, dir, s) : launch_cw<0, 251>(p, irk, dir, s); }
+        else if (p.recon == DENSE_RECON_WENOJS5) { spl ? launch_cw<1, 253>(p, irk, dir, s) : launch_cw<0, 253>(p, irk, dir, s); }
+        else if (p.recon == DENSE_RECON_WENOZ5) { spl ? launch_cw<1, 255>(p, irk, dir, s) : launch_cw<0, 255>(p, irk, dir, s); }
+        else if (dir == 0) k_flux_noop<<<1, 32, 0, s>>>(p, irk);
         break;
     }
     case DENSE_SPLIT_CH:
-        k_flux_char<0, false, kXTX, kXTY><<<grid_xi(p, kXTX, kXTY), dim3(kXTX, kXTY), 0, s>>>(p, irk);
-        k_flux_char<1, false, kETX, kETY><<<grid_eta(p, kETX, kETY), dim3(kETX, kETY), 0, s>>>(p, irk);
+        if (dir == 0) k_flux_char<0, false, kXTX, kXTY><<<grid_xi(p, kXTX, kXTY), dim3(kXTX, kXTY), 0, s>>>(p, irk);
+        else          k_flux_char<1, false, kETX, kETY><<<grid_eta(p, kETX, kETY), dim3(kETX, kETY), 0, s>>>(p, irk);
         break;
     case DENSE_SPLIT_SC:
-        k_flux_char<0, true, kXTX, kXTY><<<grid_xi(p, kXTX, kXTY), dim3(kXTX, kXTY), 0, s>>>(p, irk);
-        k_flux_char<1, true, kETX, kETY><<<grid_eta(p, kETX, kETY), dim3(kETX, kETY), 0, s>>>(p, irk);
+        if (dir == 0) k_flux_char<0, true, kXTX, kXTY><<<grid_xi(p, kXTX, kXTY), dim3(kXTX, kXTY), 0, s>>>(p, irk);
+        else          k_flux_char<1, true, kETX, kETY><<<grid_eta(p, kETX, kETY), dim3(kETX, kETY), 0, s>>>(p, irk);
         break;
     default:
         break;
     }
 }
 
-static int flux_launches(const Params& p) {
-    if (p.splitting >= DENSE_SPLIT_LLF && p.splitting <= DENSE_SPLIT_SW &&
-        p.recon != DENSE_RECON_UPWIND5 && p.recon != DENSE_RECON_WENOJS5 && p.recon != DENSE_RECON_WENOZ5)
-        return 1;
-    return 2;
+static int flux_launches(const Params& p, int dir) {
+    if (p.splitting >= DENSE_SPLIT_LLF && p.splitting <= DENSE_SPLIT_SW && !recon_known(p.recon))
+        return dir == 0 ? 1 : 0;
+    return 1;
 }
 
 static void launch_prim(const Params& p, int slot, void* stream) {

@@ -1,0 +1,322 @@
+"""Benchmark of the 2DENSE hot path on GB300: FP64 WENO5-RK3 cell-updates per second.
+
+Workload (default): double Mach reflection, 1920x480 cells, characteristic-wise AdaWENO with
+Roe eigenvectors and GLF splitting (scheme 105, delta 0.5), TVD-RK3 at CFL 0.5, FP64 -- the
+configuration the headline metric is quoted on. A "step" is one full TVD-RK3 time step (three
+right-hand-side evaluations and stage updates) of the whole grid; one cell-update is one interior
+cell advanced one step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload ...]
+
+Reported on one JSON line (rank 0):
+  value        cell-updates/s with the state resident in HBM, each timed step bracketed by CUDA
+               events on the solver's own stream, L2 flushed (256 MiB write) between steps;
+  e2e          the same metric through the C ABI with host buffers: every step uploads the state
+               from pinned host memory (dense_upload), advances one step (dense_steps) and reads
+               the state back (dense_download);
+  roofline     the dominant kernel (the xi-direction flux sweep) against the FP64 peak measured
+               live on this GPU (dense_measure_fp64, an FMA-throughput probe): achieved = the
+               reference algorithm's FLOPs for that sweep per launch / its mean CUDA-event time;
+  cpu_baseline the CPU oracle (a line-faithful C++ restatement of the reference, OpenMP) on
+               this host's cores, on a bounded sample of the same workload.
+With --impl reference the CPU restatement of the reference (the Fortran itself cannot be built
+without a Fortran compiler) is timed on all host threads instead, on the same workload.
+N > 1 (torchrun) runs independent replicas, one per GPU: the path has no exchange step.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: (benchmark, splitting, recon, ni, nj, description, flop key)
+    "dmr": (5, 105, 0, 1920, 480, "double Mach reflection 1920x480, AdaWENO (105), CFL 0.5",
+            "C2 DMR 1920x480 AdaWENO"),
+    "ivc": (11, 101, 253, 200, 200, "isentropic vortex 200x200 periodic, LLF + WENO-JS5, CFL 0.5",
+            "C1 IVC 200x200 LLF+WENO-JS5"),
+    "rt": (13, 104, 0, 256, 1024, "Rayleigh-Taylor 256x1024 reflective sides, characteristic "
+           "WENO-Z + GLF (104), CFL 0.5", "C3 RT 256x1024 CH"),
+}
+METRIC = "FP64 WENO5-RK3 cell-updates/s"
+UNIT = "cell-updates/s"
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def load_flops(key):
+    with open(os.path.join(ROOT, "tests", "golden", "flop_counts.json")) as f:
+        return json.load(f)["bench"][key]
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clock and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.out = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.out = self.proc.communicate(timeout=5)[0]
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out = self.proc.communicate()[0]
+
+    def summary(self):
+        if not self.out:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.out.strip().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        busy = [s for s in sm if smax and s > 0.5 * smax] or sm
+        return {"sm_mhz": statistics.median(busy) if busy else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(cfg_tuple, steps: int, reference_arm: bool = False):
+    """Time the CPU oracle (OpenMP, all host threads) on the workload; returns a dict."""
+    from oracle import oracle as orc
+    bench, split, recon, ni, nj, desc, _ = cfg_tuple
+    cfg = orc.default_config(ni=ni, nj=nj, benchmark=bench, splitting=split, recon=recon, cfl=0.5,
+                             var_eps=5.0, var_xc=5.0, var_yc=5.0)
+    o = orc.OracleSolver(cfg, timed=True)
+    o.steps(1)  # warm-up
+    t0 = time.perf_counter()
+    o.steps(steps)
+    el = time.perf_counter() - t0
+    threads = orc.load(True).oracle_threads()
+    return {"value": ni * nj * steps / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{desc}: {steps} step(s) of the C++ restatement of the reference "
+                      f"(OpenMP, {threads} threads, gcc -O2), after 1 warm-up step",
+            "seconds": el}
+
+
+def run_reference_arm(args, wl):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    steps = max(1, args.steps)
+    # each step a bounded sample: full-size oracle steps take ~0.1-1 s on 16 cores
+    cb = cpu_baseline(wl, steps=min(steps, 10), reference_arm=True)
+    bench, split, recon, ni, nj, desc, _ = wl
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT,
+            "n_gpus": args.gpus, "steps": min(steps, 10), "warmup": 1,
+            "ms_per_step": 1e3 * cb["seconds"] / min(steps, 10), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": desc, "benchmark": bench, "splitting": split, "recon": recon,
+                       "ni": ni, "nj": nj, "l2": "not applicable (CPU)"},
+            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "the reference is Fortran; no Fortran compiler exists on this image or the GPU "
+                    "box, so the reference arm times its line-faithful C++ restatement"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="dmr", choices=sorted(WORKLOADS))
+    ap.add_argument("--strict", type=int, default=0)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--cpu-steps", type=int, default=20)
+    ap.add_argument("--ni", type=int, default=0, help="override the grid (smaller profiling cases)")
+    ap.add_argument("--nj", type=int, default=0)
+    args = ap.parse_args()
+    wl = WORKLOADS[args.workload]
+    if args.ni and args.nj:
+        wl = wl[:3] + (args.ni, args.nj, wl[5].split(" ")[0] + f" {args.ni}x{args.nj} (reduced) "
+                       + " ".join(wl[5].split(" ")[2:]), wl[6])
+    if args.impl == "reference":
+        return run_reference_arm(args, wl)
+
+    import torch
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    dense = importlib.import_module("2dense_gb300")
+    lib = dense.load_library()
+
+    bench, split, recon, ni, nj, desc, fkey = wl
+    cfg = dense.config_default(ni=ni, nj=nj, benchmark=bench, splitting=split, recon=recon,
+                               cfl=0.5, strict=args.strict)
+    c, cons, prim, x, y = dense.init_general(cfg)
+    cells = ni * nj
+    s = dense.Solver(c)
+    s.upload(cons, prim, x, y)
+    sp = ctypes.c_void_p()
+    lib.dense_get_stream(s.h, ctypes.byref(sp))
+    stream = torch.cuda.ExternalStream(sp.value)
+
+    # warm-up (also builds the step graph)
+    s.steps(args.warmup)
+    lib.dense_set_time(s.h, s.current_time, s.current_step)
+
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    launches0 = s.launch_count()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    wall0 = time.perf_counter()
+    with Clocks(local) as clk:
+        for k in range(args.steps):
+            stream.synchronize()
+            flush.fill_(float(k))  # L2 flush between timed steps (outside the events)
+            torch.cuda.current_stream().synchronize()
+            evs[k][0].record(stream)
+            rc = lib.dense_steps_async(s.h, 1, float("inf"), 2**31 - 1)
+            if rc:
+                raise RuntimeError(lib.dense_last_error(s.h))
+            evs[k][1].record(stream)
+        torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    launches = s.launch_count() - launches0
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = cells * args.steps * world / (total_ms * 1e-3)
+    status = s.status()
+
+    # per-kernel times of the stage, for the roofline of the dominant kernel
+    prof = np.zeros((3, 4))
+    reps = 5
+    for r in range(reps):
+        for irk in (1, 2, 3):
+            ms = (ctypes.c_float * 4)()
+            if lib.dense_profile_stage(s.h, irk, ms):
+                raise RuntimeError(lib.dense_last_error(s.h))
+            prof[irk - 1] += np.array(list(ms)) / reps
+    fl = load_flops(fkey)
+    peak = ctypes.c_double()
+    lib.dense_measure_fp64(0, ctypes.byref(peak))
+    div_rate = ctypes.c_double()
+    lib.dense_measure_fp64(1, ctypes.byref(div_rate))
+    xi_ms = prof[:, 1].mean()
+    eta_ms = prof[:, 2].mean()
+    stage_ms = prof.sum(axis=1).mean()
+    # reference-algorithm FLOPs of one xi sweep (splitting + reconstruction of one stage)
+    xi_flops = fl["flux_xi_per_cell_update"] / 3.0 * cells
+    achieved = xi_flops / (xi_ms * 1e-3) / 1e12
+    step_flops = fl["flops_per_cell_update"] * cells
+    roofline = {"bound": "fp64", "kernel": "xi flux sweep (k_flux_char<0,true>)",
+                "achieved": achieved, "peak": peak.value / 1e12, "unit": "TFLOP/s",
+                "frac": achieved * 1e12 / peak.value,
+                "peak_source": "measured live: dense_measure_fp64 FMA-throughput probe on this GPU "
+                               "(MEASURED_PEAKS.json has no FP64 figure)",
+                "traffic": None,
+                "whole_step": {"achieved_tflops": step_flops * value / cells / world / 1e12,
+                               "frac": step_flops * value / cells / world / peak.value,
+                               "flops_per_cell_update": fl["flops_per_cell_update"]},
+                "kernel_ms": {"bc": prof[:, 0].mean(), "flux_xi": xi_ms, "flux_eta": eta_ms,
+                              "update": prof[:, 3].mean()},
+                "kernel_share": {"bc": prof[:, 0].mean() / stage_ms, "flux_xi": xi_ms / stage_ms,
+                                 "flux_eta": eta_ms / stage_ms, "update": prof[:, 3].mean() / stage_ms},
+                "hbm": {"algorithmic_bytes_per_cell_update": 256,
+                        "achieved_gbs": 256 * value / world / 1e9},
+                "fp64_div_per_s": div_rate.value}
+
+    # end to end through the C ABI with pinned host buffers
+    e2e_steps = max(3, min(args.steps, 20))
+    nip, njp = ni + 8, nj + 8
+    pin = torch.empty(nip * njp * 4, dtype=torch.float64, pin_memory=True)
+    host = pin.numpy().reshape((nip, njp, 4), order="F")
+    host[...] = cons
+    xs, ys = np.asfortranarray(x), np.asfortranarray(y)
+    dp = ctypes.POINTER(ctypes.c_double)
+    hp = host.ctypes.data_as(dp)
+    with dense.Solver(c) as s2:
+        s2.upload(host, None, xs, ys)
+        s2.steps(1)
+        tcur, scur = ctypes.c_double(s2.current_time), ctypes.c_int(s2.current_step)
+        t0 = time.perf_counter()
+        for k in range(e2e_steps):
+            rc = lib.dense_upload(s2.h, hp, None, xs.ctypes.data_as(dp), ys.ctypes.data_as(dp))
+            rc = rc or lib.dense_steps(s2.h, 1, float("inf"), 2**31 - 1, ctypes.byref(tcur),
+                                       ctypes.byref(scur), None)
+            rc = rc or lib.dense_download(s2.h, hp, None)
+            if rc:
+                raise RuntimeError(lib.dense_last_error(s2.h))
+        e2e_s = time.perf_counter() - t0
+    e2e = {"value": cells * e2e_steps * world / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": nip * njp * 4 * 8 + (2 * ni + nj) * 8,
+           "d2h_bytes_per_step": nip * njp * 4 * 8,
+           "steps": e2e_steps,
+           "api": "dense_upload(cons from pinned host) + dense_steps(1) + dense_download(cons)"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(wl, args.cpu_steps)
+        cpu.pop("seconds", None)
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": desc, "benchmark": bench, "splitting": split, "recon": recon,
+                       "ni": ni, "nj": nj, "cells": cells, "strict": args.strict,
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                       "l2": "flushed between timed steps (256 MiB write)"},
+            "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
+            "clocks": clk.summary(), "status_flags": status, "wall_s_timed_region": wall}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    s.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -193,6 +193,30 @@ int dense_get_fluxes(dense_handle_t* h, double* h_xi, double* h_eta);
    counted once per graph launch per node). */
 long long dense_launch_count(dense_handle_t* h);
 
+/* ---- asynchronous loop and timing (callers that own the clock: benchmarks, PyTorch) ---- */
+
+/* The handle's CUDA stream (cudaStream_t), so a caller can order its own work and events. */
+int dense_get_stream(dense_handle_t* h, void** stream);
+
+/* dense_steps without host synchronisation: continue from the device-resident time and step
+   (set by dense_set_time or a previous dense_steps) and enqueue nsteps step graphs. */
+int dense_steps_async(dense_handle_t* h, int nsteps, double t_end, int total_step);
+
+/* Set / read the device-resident current_time and current_step (dense_get_time syncs). */
+int dense_set_time(dense_handle_t* h, double t, int step);
+int dense_get_time(dense_handle_t* h, double* t, int* step, double* dt);
+
+/* Wait for all work on the handle's stream. */
+int dense_sync(dense_handle_t* h);
+
+/* Run one stage with CUDA events between its kernels; ms[0..3] = boundary fill, xi flux,
+   eta flux, update (+ get_primary). Advances the state like dense_stage. */
+int dense_profile_stage(dense_handle_t* h, int irk, float* ms);
+
+/* Throughput probe of the FP64 pipe on the current device: kind 0 = FMA (FLOP/s, one FMA
+   counted as two), kind 1 = IEEE double divides per second. */
+int dense_measure_fp64(int kind, double* result);
+
 #ifdef __cplusplus
 }
 #endif

@@ -186,6 +186,8 @@ template <class T> struct Solver {
     std::vector<T> theta_xip, theta_xin, theta_etap, theta_etan;
     std::vector<double> x, y;
 
+    static long long ops_now() { return g_ops.add + g_ops.mul + g_ops.div + g_ops.sqrt; }
+
     explicit Solver(const dense_config_t& c) : cfg(c) {
         ni = c.ni; nj = c.nj; b = 4; NIp = ni + 2 * b; NJp = nj + 2 * b;
         gamma = c.gamma; cfl = c.cfl; delta = c.delta; dt = c.dt;
@@ -529,6 +531,10 @@ template <class T> struct Solver {
         }
     }
     void split_sw() {
+        in_dir(0, [&] { split_sw_xi(); });
+        in_dir(1, [&] { split_sw_eta(); });
+    }
+    void split_sw_xi() {
         OMP_FOR
         for (int j = 1; j <= nj; ++j)
             for (int i = 1; i <= NIp; ++i) {
@@ -536,6 +542,8 @@ template <class T> struct Solver {
                 sw_cell(Pm(i, j + b, 1), Pm(i, j + b, 2), Pm(i, j + b, 3), Pm(i, j + b, 5), true, fp, fm);
                 for (int v = 1; v <= 4; ++v) { FXP(i, j, v) = fp[v - 1]; FXN(i, j, v) = fm[v - 1]; }
             }
+    }
+    void split_sw_eta() {
         OMP_FOR
         for (int i = 1; i <= ni; ++i)
             for (int j = 1; j <= NJp; ++j) {
@@ -552,7 +560,19 @@ template <class T> struct Solver {
         if (R == 253) return weno5js(lf);
         return weno5z(lf);
     }
+    long long dir_ops[2] = {0, 0};  // counted operations attributed to the xi / eta sweep
+    template <class F> void in_dir(int d, F&& f) {
+        long long t0 = ops_now();
+        f();
+        dir_ops[d] += ops_now() - t0;
+    }
     template <int R> void recon_all() {
+        in_dir(0, [&] { recon_xi<R>(); });
+        in_dir(1, [&] { recon_eta<R>(); });
+        in_dir(0, [&] { for (size_t k = 0; k < h_xi.size(); ++k) h_xi[k] = h_xip[k] + h_xin[k]; });
+        in_dir(1, [&] { for (size_t k = 0; k < h_eta.size(); ++k) h_eta[k] = h_etap[k] + h_etan[k]; });
+    }
+    template <int R> void recon_xi() {
         // xi+: lf(m)=flux_xip(i+m+b-1,j,eq); xi-: lf(m)=flux_xin(i-m+b,j,eq)
         for (int v = 1; v <= 4; ++v) {
             OMP_FOR
@@ -570,6 +590,8 @@ template <class T> struct Solver {
                     HXN(i, j, v) = recon<R>(lf);
                 }
         }
+    }
+    template <int R> void recon_eta() {
         for (int v = 1; v <= 4; ++v) {
             OMP_FOR
             for (int i = 1; i <= ni; ++i)
@@ -586,11 +608,10 @@ template <class T> struct Solver {
                     HEN(j, i, v) = recon<R>(lf);
                 }
         }
-        sum_fields();
     }
     void sum_fields() {  // sum_field (field_op.f90:1-21)
-        for (size_t k = 0; k < h_xi.size(); ++k) h_xi[k] = h_xip[k] + h_xin[k];
-        for (size_t k = 0; k < h_eta.size(); ++k) h_eta[k] = h_etap[k] + h_etan[k];
+        in_dir(0, [&] { for (size_t k = 0; k < h_xi.size(); ++k) h_xi[k] = h_xip[k] + h_xin[k]; });
+        in_dir(1, [&] { for (size_t k = 0; k < h_eta.size(); ++k) h_eta[k] = h_etap[k] + h_etan[k]; });
     }
 
     // =========================================================================================
@@ -746,7 +767,10 @@ template <class T> struct Solver {
         switch (cfg.splitting) {
         case 101: case 102: case 103:
             if (cfg.splitting == 103) split_sw();
-            else { split_lf_xi(cfg.splitting == 101 ? 0 : 1, false); split_lf_eta(cfg.splitting == 101 ? 0 : 1, false); }
+            else {
+                in_dir(0, [&] { split_lf_xi(cfg.splitting == 101 ? 0 : 1, false); });
+                in_dir(1, [&] { split_lf_eta(cfg.splitting == 101 ? 0 : 1, false); });
+            }
             // scheme_invis_general (scheme_invs_general.f90:1-28)
             if (cfg.recon == 251) recon_all<251>();
             else if (cfg.recon == 253) recon_all<253>();
@@ -754,19 +778,21 @@ template <class T> struct Solver {
             else recon_noop = true;  // silent no-op: h_xi/h_eta keep their values
             return DENSE_OK;
         case 104:  // flux_splitting_CH_block (flux_splitting_CH.f90:24-110)
-            split_lf_xi(1, false);
-            char_xi(+1, false); char_xi(-1, false);
-            split_lf_eta(1, false);
-            char_eta(+1, false); char_eta(-1, false);
+            in_dir(0, [&] { split_lf_xi(1, false); char_xi(+1, false); char_xi(-1, false); });
+            in_dir(1, [&] { split_lf_eta(1, false); char_eta(+1, false); char_eta(-1, false); });
             sum_fields();
             return DENSE_OK;
         case 105:  // flux_splitting_SC_block (flux_splitting_SC.f90:141-237)
-            split_lf_xi(1, true);
-            get_theta_xi(+1); char_xi(+1, true);
-            get_theta_xi(-1); char_xi(-1, true);
-            split_lf_eta(1, true);
-            get_theta_eta(+1); char_eta(+1, true);
-            get_theta_eta(-1); char_eta(-1, true);
+            in_dir(0, [&] {
+                split_lf_xi(1, true);
+                get_theta_xi(+1); char_xi(+1, true);
+                get_theta_xi(-1); char_xi(-1, true);
+            });
+            in_dir(1, [&] {
+                split_lf_eta(1, true);
+                get_theta_eta(+1); char_eta(+1, true);
+                get_theta_eta(-1); char_eta(-1, true);
+            });
             sum_fields();
             return DENSE_OK;
         default:
@@ -818,14 +844,22 @@ template <class T> struct Solver {
         }
     }
 
-    // general_main.f90:26-31
+    // general_main.f90:26-31. phase_ops[k] receives the operation count of each phase when
+    // counting (k = 0 get_primary, 1 boundary_general, 2 flux_splitting_general, 3 time_rk3).
+    long long phase_ops[4] = {0, 0, 0, 0};
     int stage(int irk) {
+        long long t0 = ops_now();
         get_primary();
+        long long t1 = ops_now();
         int rc = boundary_general();
         if (rc) return rc;
+        long long t2 = ops_now();
         rc = flux_splitting_general();
         if (rc) return rc;
+        long long t3 = ops_now();
         time_rk3(irk);
+        long long t4 = ops_now();
+        phase_ops[0] += t1 - t0; phase_ops[1] += t2 - t1; phase_ops[2] += t3 - t2; phase_ops[3] += t4 - t3;
         return DENSE_OK;
     }
     // general_main.f90:23-38, without the save block
@@ -1085,7 +1119,9 @@ int oracle_threads(void) {
 
 // Count the floating-point operations of one full step (all stages) on field values, starting
 // from the given padded state (or the benchmark's setup when cons is NULL).
-// out: [add, mul, div, sqrt, transcendental, interior cells]
+// out: [add, mul, div, sqrt, transcendental, interior cells,
+//       get_primary, boundary_general, flux_splitting_general, time_rk3 (add+mul+div+sqrt each),
+//       flux xi sweep, flux eta sweep]
 int oracle_count_step(const dense_config_t* cfg, const double* cons, long long* out) {
     Solver<Counted> s(*cfg);
     if (cons) {
@@ -1102,6 +1138,45 @@ int oracle_count_step(const dense_config_t* cfg, const double* cons, long long* 
     }
     out[0] = oracle::g_ops.add; out[1] = oracle::g_ops.mul; out[2] = oracle::g_ops.div;
     out[3] = oracle::g_ops.sqrt; out[4] = oracle::g_ops.transc; out[5] = (long long)s.ni * s.nj;
+    for (int k = 0; k < 4; ++k) out[6 + k] = s.phase_ops[k];
+    out[10] = s.dir_ops[0];
+    out[11] = s.dir_ops[1];
+    return 0;
+}
+
+// Known-answer hooks: one reconstruction of a 5-point stencil. kind 251/253/255 returns h in
+// out[0]; kind 1 returns WENO-JS weights (w0,w1,w2), kind 2 WENO-Z (w0,w1,w2,theta).
+int oracle_recon(int kind, const double* lf, double* out) {
+    double a0, a1, a2;
+    switch (kind) {
+    case 251: out[0] = oracle::upwind5(lf); return 0;
+    case 253: out[0] = oracle::weno5js(lf); return 0;
+    case 255: out[0] = oracle::weno5z(lf); return 0;
+    case 1: {
+        oracle::weno5js_alpha(lf, a0, a1, a2);
+        double s = a0 + a1 + a2;
+        out[0] = a0 / s; out[1] = a1 / s; out[2] = a2 / s;
+        return 0;
+    }
+    case 2: oracle::weno5z_omega_theta(lf, out[0], out[1], out[2], out[3]); return 0;
+    default: return 1;
+    }
+}
+
+// Roe average of two states and the left/right eigenvector matrices of get_l_r_vec_xi/_eta.
+// L[c*4+k] = l(c+1,k+1), R[k*4+e] = r(k+1,e+1); roe_out = (u0, v0, h0, alpha0).
+int oracle_roe_lr(int dir, double gamma, const double* left, const double* right, double* roe_out,
+                  double* L, double* R) {
+    dense_config_t c;
+    std::memset(&c, 0, sizeof(c));
+    c.ni = 3; c.nj = 3; c.gamma = gamma;
+    Solver<double> s(c);
+    double u0, v0, h0, a0, Lm[4][4], Rm[4][4];
+    s.roe(left[0], right[0], left[1], right[1], left[2], right[2], left[3], right[3], u0, v0, h0, a0);
+    s.lr_vec(dir == 0, u0, v0, h0, a0, Lm, Rm);
+    roe_out[0] = u0; roe_out[1] = v0; roe_out[2] = h0; roe_out[3] = a0;
+    for (int a = 0; a < 4; ++a)
+        for (int b = 0; b < 4; ++b) { L[a * 4 + b] = Lm[a][b]; R[a * 4 + b] = Rm[a][b]; }
     return 0;
 }
 

@@ -57,6 +57,8 @@ def load(timed: bool = False) -> ctypes.CDLL:
         "oracle_steps": (i, [vp, i, ctypes.c_double, i]),
         "oracle_threads": (i, []),
         "oracle_count_step": (i, [cfgp, dp, ctypes.POINTER(ctypes.c_longlong)]),
+        "oracle_recon": (i, [i, dp, dp]),
+        "oracle_roe_lr": (i, [i, ctypes.c_double, dp, dp, dp, dp, dp]),
     }
     for fname, (res, args) in sigs.items():
         fn = getattr(lib, fname)
@@ -174,15 +176,41 @@ def count_step_flops(cfg: DenseConfig, cons: np.ndarray | None = None) -> dict:
     """Floating-point operations of one full step of the reference on field values
     (add/sub, mul, div, sqrt each counted as one; transcendental calls counted apart)."""
     lib = load(False)
-    out = (ctypes.c_longlong * 6)()
+    out = (ctypes.c_longlong * 12)()
     c = None if cons is None else np.asfortranarray(cons, dtype=np.float64)
     rc = lib.oracle_count_step(ctypes.byref(cfg), None if c is None else _dp(c), out)
     if rc:
         raise RuntimeError(f"count_step: {rc}")
-    add, mul, div, sqrt, transc, cells = list(out)
+    add, mul, div, sqrt, transc, cells, p_prim, p_bc, p_flux, p_rk, d_xi, d_eta = list(out)
     flops = add + mul + div + sqrt
     return {"add": add, "mul": mul, "div": div, "sqrt": sqrt, "transcendental": transc,
-            "cells": cells, "flops": flops, "flops_per_cell_update": flops / cells}
+            "cells": cells, "flops": flops, "flops_per_cell_update": flops / cells,
+            "phase": {"get_primary": p_prim, "boundary": p_bc, "flux": p_flux, "time_rk3": p_rk},
+            "flux_dir": {"xi": d_xi, "eta": d_eta}}
+
+
+def recon(kind: int, lf) -> np.ndarray:
+    """One stencil evaluation: kind 251/253/255 -> [h]; 1 -> WENO-JS weights; 2 -> WENO-Z
+    weights and theta."""
+    lib = load(False)
+    a = np.ascontiguousarray(lf, dtype=np.float64)
+    out = np.zeros(4)
+    if lib.oracle_recon(kind, _dp(a), _dp(out)):
+        raise ValueError(kind)
+    return out[:1] if kind > 200 else out[:3 if kind == 1 else 4]
+
+
+def roe_lr(direction: int, gamma: float, left, right):
+    """Roe average (u0,v0,h0,alpha0) of two primitive states (rho,u,v,p) and the eigenvector
+    matrices L[c,k] = l(c+1,k+1), R[k,e] = r(k+1,e+1)."""
+    lib = load(False)
+    le = np.ascontiguousarray(left, dtype=np.float64)
+    ri = np.ascontiguousarray(right, dtype=np.float64)
+    roe = np.zeros(4)
+    L = np.zeros(16)
+    R = np.zeros(16)
+    lib.oracle_roe_lr(direction, gamma, _dp(le), _dp(ri), _dp(roe), _dp(L), _dp(R))
+    return roe, L.reshape(4, 4), R.reshape(4, 4)
 
 
 def threads() -> int:
