@@ -173,6 +173,7 @@ def load_library(path: str | None = None):
         "dense_get_time": (_c_int, [vp, dp, ctypes.POINTER(_c_int), dp]),
         "dense_sync": (_c_int, [vp]),
         "dense_profile_stage": (_c_int, [vp, _c_int, ctypes.POINTER(ctypes.c_float)]),
+        "dense_fastmath_check": (_c_int, [dp, dp, _c_int]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)

@@ -41,6 +41,9 @@ struct Params {
     int P;           // row pitch of the padded arrays, in doubles
     long long plane; // doubles per variable plane = NJp * P
     double gamma, cfl, delta, dx, dy, dt_const;
+    // AdaWENO switch theta > delta written without a divide (fast kernels):
+    // theta_k1 * D > theta_k2 * (N - D) with theta_k1 = sqrt(1-delta), theta_k2 = sqrt(delta)
+    double theta_k1, theta_k2;
     int if_const_dt, bodyforce, benchmark, splitting, recon;
 };
 

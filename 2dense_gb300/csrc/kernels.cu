@@ -111,10 +111,109 @@ __device__ __forceinline__ double upwind5(const double lf[5]) {
     return (2.0 * lf[0] - 13.0 * lf[1] + 47.0 * lf[2] + 27.0 * lf[3] - 3.0 * lf[4]) / 60.0;
 }
 
+// ---------------------------------------------------------------------------------------------
+// FAST arithmetic. On GB300 an IEEE double divide costs about ten FMA slots of the FP64 pipe,
+// and the reference's WENO weights spend seven divides per stencil. The fast variant
+//  * takes reciprocals and inverse square roots from the hardware seeds (rcp.approx.ftz.f64,
+//    rsqrt.approx.ftz.f64) refined by two Newton-Raphson steps each (Newton's iteration for
+//    1/d: r <- r + r(1 - d r); for 1/sqrt(x): y <- y + y(1 - x y^2)/2), which lands within
+//    an ulp of the correctly rounded result for the positive normal arguments used here;
+//  * writes the WENO weights over a common denominator: with d_k = ss + beta_k,
+//    P_k = prod_{j != k} d_j^2 and D = prod_j d_j^2,
+//      WENO-JS: alpha_k D = c_k P_k,   WENO-Z: alpha_k D = c_k (D + tau^2 P_k),
+//    so h = sum(alpha_k D q_k) / sum(alpha_k D) costs one reciprocal instead of six divides,
+//    and the AdaWENO test theta > delta becomes sqrt(1-delta) D > sqrt(delta) (N - D) with
+//    N = sum alpha_k D (theta = 1/(1+(sum alpha - 1)^2)), which needs no divide at all.
+// Products of squared d_k stay far inside the double range for d_k in [1e-6, 1e40].
+__device__ __forceinline__ double rcp_nr(double d) {
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(d));
+    double e = fma(-d, r, 1.0);
+    r = fma(r, e, r);
+    e = fma(-d, r, 1.0);
+    return fma(r, e, r);
+}
+__device__ __forceinline__ double rsqrt_nr(double x) {
+    double y;
+    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    double e = fma(-x * y, y, 1.0);
+    y = fma(0.5 * y, e, y);
+    e = fma(-x * y, y, 1.0);
+    return fma(0.5 * y, e, y);
+}
+
+constexpr double k1312 = 13.0 / 12.0;
+
+// d_k = ss + beta_k and tau = |beta_2 - beta_0| with beta_k = 13/12 a_k^2 + 1/4 b_k^2.
+__device__ __forceinline__ void betas_fast(const double lf[5], double& d0, double& d1, double& d2,
+                                           double& tau) {
+    const double a0 = fma(-2.0, lf[1], lf[0]) + lf[2];
+    const double b0 = fma(3.0, lf[2], fma(-4.0, lf[1], lf[0]));
+    const double a1 = fma(-2.0, lf[2], lf[1]) + lf[3];
+    const double b1 = lf[1] - lf[3];
+    const double a2 = fma(-2.0, lf[3], lf[2]) + lf[4];
+    const double b2 = fma(3.0, lf[2], fma(-4.0, lf[3], lf[4]));
+    const double be0 = fma(k1312 * a0, a0, (0.25 * b0) * b0);
+    const double be1 = fma(k1312 * a1, a1, (0.25 * b1) * b1);
+    const double be2 = fma(k1312 * a2, a2, (0.25 * b2) * b2);
+    tau = fabs(be2 - be0);
+    d0 = kSS + be0;
+    d1 = kSS + be1;
+    d2 = kSS + be2;
+}
+
+// Weight numerators n_k = alpha_k D and their sum N = (sum alpha) D.
+template <bool Z>
+__device__ __forceinline__ void weno_num_fast(const double lf[5], double& n0, double& n1, double& n2,
+                                              double& N, double& D) {
+    double d0, d1, d2, tau;
+    betas_fast(lf, d0, d1, d2, tau);
+    const double e0 = d0 * d0, e1 = d1 * d1, e2 = d2 * d2;
+    const double P0 = e1 * e2, P1 = e0 * e2, P2 = e0 * e1;
+    D = e0 * P0;
+    if (Z) {
+        const double T = tau * tau;
+        n0 = c30 * fma(T, P0, D);
+        n1 = c31 * fma(T, P1, D);
+        n2 = c32 * fma(T, P2, D);
+    } else {
+        n0 = c30 * P0;
+        n1 = c31 * P1;
+        n2 = c32 * P2;
+    }
+    N = n0 + n1 + n2;
+}
+
+__device__ __forceinline__ void candidates_fast(const double lf[5], double& q0, double& q1, double& q2) {
+    q0 = fma(a302, lf[2], fma(a301, lf[1], a300 * lf[0]));
+    q1 = fma(a312, lf[3], fma(a311, lf[2], a310 * lf[1]));
+    q2 = fma(a322, lf[4], fma(a321, lf[3], a320 * lf[2]));
+}
+
+template <bool Z> __device__ __forceinline__ double weno_fast(const double lf[5]) {
+    double q0, q1, q2, n0, n1, n2, N, D;
+    candidates_fast(lf, q0, q1, q2);
+    weno_num_fast<Z>(lf, n0, n1, n2, N, D);
+    return fma(n2, q2, fma(n1, q1, n0 * q0)) * rcp_nr(N);
+}
+
+// The five coefficients of h = sum_k w_k q_k as one 5-point stencil: W[m] lf[m].
+__device__ __forceinline__ void stencil_from_weights(double w0, double w1, double w2, double W[5]) {
+    W[0] = w0 * a300;
+    W[1] = fma(w1, a310, w0 * a301);
+    W[2] = fma(w2, a320, fma(w1, a311, w0 * a302));
+    W[3] = fma(w2, a321, w1 * a312);
+    W[4] = w2 * a322;
+}
+
 template <int REC> __device__ __forceinline__ double recon5(const double lf[5]) {
     if (REC == DENSE_RECON_UPWIND5) return upwind5(lf);
+#if FAST
+    return weno_fast<REC == DENSE_RECON_WENOZ5>(lf);
+#else
     if (REC == DENSE_RECON_WENOJS5) return weno5js(lf);
     return weno5z(lf);
+#endif
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -233,6 +332,74 @@ __device__ __forceinline__ void char_weno(const Eig& e, const double F[5][4], do
         h[q] = e.R[0][q] * cv[0] + e.R[1][q] * cv[1] + e.R[2][q] * cv[2] + e.R[3][q] * cv[3];
 }
 
+// FAST characteristic machinery. The Roe state of the two cells next to an interface from
+// their sqrt(rho) and total enthalpy H = gamma/(gamma-1) p/rho + |u|^2/2 (staged once per cell),
+// with one reciprocal for the three weighted means and one inverse square root giving both
+// alpha0 and 1/alpha0; 1/hh0 = (gamma-1)/alpha0^2. The eigenvector products use the zero and
+// unit entries of the matrices of get_l_r_vec_xi/_eta (scheme_weno5th_SC.f90:277-328, 607-658):
+// the tangential-shear characteristic is F_t - u_t0 F_0, and the back-projection is
+//   h_0 = c0 + c1 + c3,  h_n = u_n0 h_0 + a0 (c3 - c0),  h_t = u_t0 h_0 + c2,
+//   h_3 = H0 (c0 + c3) + a0 u_n0 (c3 - c0) + uu0 c1 + u_t0 c2,
+// with n the normal and t the tangential momentum component.
+struct EigFast {
+    double un0, ut0, a0, h0, uu0, a0un0;
+    double l00, l10, l20, l30;  // column 0 (acoustic, u_n - a)
+    double l01, l11, l21, l31;  // column 1 (entropy)
+    double l03, l13, l23;       // column 3 (acoustic, u_n + a); l33 == l30
+};
+
+template <int DIR>
+__device__ __forceinline__ bool roe_eig_fast(double g1, double sl, double sr, double ul, double ur,
+                                             double vl, double vr, double hl, double hr, EigFast& e) {
+    const double r = rcp_nr(sl + sr);
+    const double u0 = fma(sr, ur, sl * ul) * r;
+    const double v0 = fma(sr, vr, sl * vl) * r;
+    const double h0 = fma(sr, hr, sl * hl) * r;
+    const double uu0 = 0.5 * fma(u0, u0, v0 * v0);
+    const double c2 = g1 * (h0 - uu0);
+    const double ia = rsqrt_nr(c2);
+    const double a0 = c2 * ia;
+    const double ihh = g1 * ia * ia;
+    const double un0 = DIR == 0 ? u0 : v0, ut0 = DIR == 0 ? v0 : u0;
+    e.un0 = un0; e.ut0 = ut0; e.a0 = a0; e.h0 = h0; e.uu0 = uu0; e.a0un0 = a0 * un0;
+    const double hu = 0.5 * uu0 * ihh, nu = 0.5 * un0 * ia, ia5 = 0.5 * ia;
+    const double pn = 0.5 * un0 * ihh, pt = 0.5 * ut0 * ihh, ih = 0.5 * ihh;
+    // rows of the normal (n) and tangential (t) momentum components
+    const double ln0 = -pn - ia5, ln3 = -pn + ia5;
+    if (DIR == 0) {
+        e.l00 = hu + nu; e.l10 = ln0; e.l20 = -pt;
+        e.l03 = hu - nu; e.l13 = ln3; e.l23 = -pt;
+    } else {
+        e.l00 = hu + nu; e.l10 = -pt; e.l20 = ln0;
+        e.l03 = hu - nu; e.l13 = -pt; e.l23 = ln3;
+    }
+    e.l30 = ih;
+    e.l01 = fma(-uu0, ihh, 1.0); e.l11 = u0 * ihh; e.l21 = v0 * ihh; e.l31 = -ihh;
+    return c2 > 0.0;
+}
+
+template <int DIR>
+__device__ __forceinline__ void char_weno_fast(const EigFast& e, const double F[5][4], double h[4]) {
+    double l0[5], l1[5], l2[5], l3[5];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+        const double f0 = F[m][0], f1 = F[m][1], f2 = F[m][2], f3 = F[m][3];
+        l0[m] = fma(e.l00, f0, fma(e.l10, f1, fma(e.l20, f2, e.l30 * f3)));
+        l1[m] = fma(e.l01, f0, fma(e.l11, f1, fma(e.l21, f2, e.l31 * f3)));
+        l2[m] = fma(-e.ut0, f0, DIR == 0 ? f2 : f1);
+        l3[m] = fma(e.l03, f0, fma(e.l13, f1, fma(e.l23, f2, e.l30 * f3)));
+    }
+    const double c0 = weno_fast<true>(l0), c1 = weno_fast<true>(l1);
+    const double c2 = weno_fast<true>(l2), c3 = weno_fast<true>(l3);
+    const double s = c0 + c1 + c3, d = c3 - c0;
+    const double hn = fma(e.un0, s, e.a0 * d);
+    const double ht = fma(e.ut0, s, c2);
+    h[0] = s;
+    h[1 + DIR] = hn;
+    h[2 - DIR] = ht;
+    h[3] = fma(e.h0, c0 + c3, fma(e.a0un0, d, fma(e.uu0, c1, e.ut0 * c2)));
+}
+
 // ---------------------------------------------------------------------------------------------
 // Index helpers
 __device__ __forceinline__ long long cidx(const Params& p, int I, int J) { return (long long)J * p.P + I; }
@@ -348,7 +515,12 @@ __global__ void __launch_bounds__(TX* TY) k_flux_char(Params p, int irk) {
     constexpr int NL = DIR == 0 ? TY : TY + 5;
     constexpr int NC = DIR == 0 ? TX + 5 : TX;
     __shared__ double sF[8][NL][NC];
-    __shared__ double sQ[4][NL][NC];  // rho, u, v, p
+    // strict: rho, u, v, p; fast: rho, u, v, total enthalpy H, and sqrt(rho) in sS
+    __shared__ double sQ[4][NL][NC];
+#if FAST
+    __shared__ double sS[NL][NC];
+    const double g1 = p.gamma - 1.0, kg = p.gamma / (p.gamma - 1.0);
+#endif
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int slot = irk - 1;
     if (DIR == 0 && blockIdx.x == 0 && blockIdx.y == 0 && tx == 0 && ty == 0) stage_scalars(p, irk);
@@ -364,6 +536,11 @@ __global__ void __launch_bounds__(TX* TY) k_flux_char(Params p, int irk) {
 #pragma unroll
         for (int v = 0; v < 4; ++v) q[v] = p.prim[v * p.plane + o];
         lf_split<DIR>(U, q[1 + DIR], q[3], lam, fp, fm);
+#if FAST
+        const double ir = rcp_nr(q[0]);
+        q[3] = fma(kg * q[3], ir, 0.5 * fma(q[1], q[1], q[2] * q[2]));
+        sS[r][c] = q[0] * rsqrt_nr(q[0]);
+#endif
 #pragma unroll
         for (int v = 0; v < 4; ++v) { sF[v][r][c] = fp[v]; sF[4 + v][r][c] = fm[v]; sQ[v][r][c] = q[v]; }
     };
@@ -392,6 +569,9 @@ __global__ void __launch_bounds__(TX* TY) k_flux_char(Params p, int irk) {
     const int t = DIR == 0 ? tx : ty;
     auto SF = [&](int q, int k) -> double { return DIR == 0 ? sF[q][ty][k] : sF[q][k][tx]; };
     auto SQ = [&](int q, int k) -> double { return DIR == 0 ? sQ[q][ty][k] : sQ[q][k][tx]; };
+#if FAST
+    auto sS_at = [&](int k) -> double { return DIR == 0 ? sS[ty][k] : sS[k][tx]; };
+#endif
 
     // AdaWENO indicator from the scalar surrogate rho + F+-(normal momentum)
     // (flux_splitting_SC.f90:175-176,206-207; get_theta_*, scheme_weno5th_SC.f90:1-64,330-393)
@@ -404,12 +584,31 @@ __global__ void __launch_bounds__(TX* TY) k_flux_char(Params p, int irk) {
             lp[m] = SQ(0, t + m) + SF(1 + DIR, t + m);
             lm[m] = SQ(0, t + 5 - m) + SF(4 + 1 + DIR, t + 5 - m);
         }
+#if FAST
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+            double n0, n1, n2, N, D;
+            weno_num_fast<true>(s == 0 ? lp : lm, n0, n1, n2, N, D);
+            smooth[s] = p.theta_k1 * D > p.theta_k2 * (N - D);
+            const double r = rcp_nr(N);
+            wsur[s][0] = n0 * r; wsur[s][1] = n1 * r; wsur[s][2] = n2 * r;
+        }
+#else
         double th;
         weno5z_omega_theta(lp, wsur[0][0], wsur[0][1], wsur[0][2], th);
         smooth[0] = th > p.delta;
         weno5z_omega_theta(lm, wsur[1][0], wsur[1][1], wsur[1][2], th);
         smooth[1] = th > p.delta;
+#endif
     }
+#if FAST
+    EigFast e;
+    if (!(ADAPT && smooth[0] && smooth[1])) {
+        const bool ok = roe_eig_fast<DIR>(g1, sS_at(t + 2), sS_at(t + 3), SQ(1, t + 2), SQ(1, t + 3),
+                                          SQ(2, t + 2), SQ(2, t + 3), SQ(3, t + 2), SQ(3, t + 3), e);
+        if (!ok) atomicOr(&p.sc->status, DENSE_FLAG_ROE_IMAG);
+    }
+#else
     Eig e;
     if (!(ADAPT && smooth[0] && smooth[1])) {
         // cells f+3 (left) and f+4 (right) of the interface: tile indices t+2, t+3
@@ -417,6 +616,7 @@ __global__ void __launch_bounds__(TX* TY) k_flux_char(Params p, int irk) {
                                 SQ(2, t + 2), SQ(2, t + 3), SQ(3, t + 2), SQ(3, t + 3), e);
         if (!ok) atomicOr(&p.sc->status, DENSE_FLAG_ROE_IMAG);
     }
+#endif
     double hsum[4];
 #pragma unroll
     for (int s = 0; s < 2; ++s) {
@@ -427,6 +627,13 @@ __global__ void __launch_bounds__(TX* TY) k_flux_char(Params p, int irk) {
             for (int c = 0; c < 4; ++c) F[m][c] = s == 0 ? SF(c, t + m) : SF(4 + c, t + 5 - m);
         double h[4];
         if (ADAPT && smooth[s]) {  // scheme_weno5th_SC.f90:110-124
+#if FAST
+            double W[5];
+            stencil_from_weights(wsur[s][0], wsur[s][1], wsur[s][2], W);
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+                h[c] = fma(W[4], F[4][c], fma(W[3], F[3][c], fma(W[2], F[2][c], fma(W[1], F[1][c], W[0] * F[0][c]))));
+#else
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
                 double lf[5], q0, q1, q2;
@@ -435,8 +642,13 @@ __global__ void __launch_bounds__(TX* TY) k_flux_char(Params p, int irk) {
                 candidates(lf, q0, q1, q2);
                 h[c] = wsur[s][0] * q0 + wsur[s][1] * q1 + wsur[s][2] * q2;
             }
+#endif
         } else {
+#if FAST
+            char_weno_fast<DIR>(e, F, h);
+#else
             char_weno(e, F, h);
+#endif
         }
 #pragma unroll
         for (int c = 0; c < 4; ++c) hsum[c] = s == 0 ? h[c] : hsum[c] + h[c];
@@ -475,11 +687,21 @@ __device__ __forceinline__ void block_max_atomic(double e1, double e2, double* s
 __device__ __forceinline__ void prim_cell(const Params& p, long long o, const double q[4], double& e1,
                                           double& e2, unsigned& flags) {
     const double rho = q[0];
+#if FAST
+    const double ir = rcp_nr(rho);
+    const double u = q[1] * ir;
+    const double v = q[2] * ir;
+#else
     const double u = q[1] / rho;
     const double v = q[2] / rho;
+#endif
     double pr = (p.gamma - 1.0) * (q[3] - 0.5 * rho * (u * u + v * v));
     if (pr < 0.0) { pr = kPFloor; flags |= DENSE_FLAG_P_FLOOR; }
+#if FAST
+    const double alpha = sqrt(p.gamma * pr * ir);
+#else
     const double alpha = sqrt(p.gamma * pr / rho);
+#endif
     p.prim[o] = rho;
     p.prim[p.plane + o] = u;
     p.prim[2 * p.plane + o] = v;
@@ -816,3 +1038,35 @@ const KernelTable* kernels_fast() {
 #endif
 
 }  // namespace dense
+
+#if !DENSE_VARIANT_STRICT
+// Accuracy check of the fast reciprocal and inverse square root against CUDA's IEEE divide and
+// square root: out[4k..4k+3] = (rcp_nr(x), 1/x, rsqrt_nr(x), 1/sqrt(x)) for each x[k].
+namespace {
+__global__ void k_fastmath(const double* x, double* out, int n) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const double v = x[k];
+    out[4 * k + 0] = dense::fast_impl::rcp_nr(v);
+    out[4 * k + 1] = 1.0 / v;
+    out[4 * k + 2] = dense::fast_impl::rsqrt_nr(v);
+    out[4 * k + 3] = 1.0 / sqrt(v);
+}
+}  // namespace
+
+extern "C" int dense_fastmath_check(const double* x, double* out, int n) {
+    if (!x || !out || n <= 0) return DENSE_ERR_ARG;
+    double *dx = nullptr, *dout = nullptr;
+    if (cudaMalloc(&dx, n * sizeof(double)) != cudaSuccess) return DENSE_ERR_NOMEM;
+    if (cudaMalloc(&dout, 4 * (size_t)n * sizeof(double)) != cudaSuccess) { cudaFree(dx); return DENSE_ERR_NOMEM; }
+    cudaError_t e = cudaMemcpy(dx, x, n * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        k_fastmath<<<(n + 255) / 256, 256>>>(dx, dout, n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(out, dout, 4 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost);
+    cudaFree(dx);
+    cudaFree(dout);
+    return e == cudaSuccess ? DENSE_OK : DENSE_ERR_CUDA;
+}
+#endif

@@ -217,6 +217,10 @@ int dense_profile_stage(dense_handle_t* h, int irk, float* ms);
    counted as two), kind 1 = IEEE double divides per second. */
 int dense_measure_fp64(int kind, double* result);
 
+/* Accuracy check of the fast kernels' Newton-refined reciprocal and inverse square root:
+   out[4k..4k+3] = (fast 1/x[k], IEEE 1/x[k], fast 1/sqrt(x[k]), IEEE 1/sqrt(x[k])). */
+int dense_fastmath_check(const double* x, double* out, int n);
+
 #ifdef __cplusplus
 }
 #endif

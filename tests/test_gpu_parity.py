@@ -54,6 +54,9 @@ def run_pair(dense, orc, cfg, nsteps):
         g_dt = s.dt
         g_t = s.current_time
         flags = s.status()
+    # the reference's prim is that of the last stage's input until get_primary runs again
+    # (general_main.f90:46 calls it before every output); the device keeps it current
+    o.get_primary()
     o_cons, o_prim = o.get_state()
     return g_cons, g_prim, o_cons, o_prim, g_dt, g_t, o.scalars(), flags
 
