@@ -62,6 +62,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
                            "-c", os.path.join(CSRC, "kernels.cu")],
         "capi": [nvcc, *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, "capi.cu")],
         "probe": [nvcc, *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, "probe.cu")],
+        "noalloc": [nvcc, *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, "noalloc.cu")],
         "host_setup": ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-c",
                        os.path.join(CSRC, "host_setup.cpp")],
     }

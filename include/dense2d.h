@@ -221,6 +221,28 @@ int dense_measure_fp64(int kind, double* result);
    out[4k..4k+3] = (fast 1/x[k], IEEE 1/x[k], fast 1/sqrt(x[k]), IEEE 1/sqrt(x[k])). */
 int dense_fastmath_check(const double* x, double* out, int n);
 
+/* ---- one stage without any device allocation ------------------------------------------- */
+
+/* No counterpart in the reference: an addition for callers that cannot let the library
+   allocate device memory -- host codes that manage every device byte through their own pool or
+   a fixed budget (for example a Fortran driver that allocates all block arrays itself), for
+   which dense_create's cudaMalloc calls are not allowed.
+   One stage (get_primary, boundary_general, flux_splitting_general, time_rk3_general(irk)) on
+   the caller's device arrays cons[4][NJp][P], prim[5][NJp][P], cons0[4][NJp][P] (P = ni+8
+   rounded up to even; all in/out), with xbot = x(:,1), xtop = x(:,nj), yleft = y(1,:) on the
+   device (needed by the double Mach reflection and shock / shear layer rules, else NULL).
+   *dt_inout gives dt for irk 2 and 3 and constant-dt runs and returns the dt used. Work is
+   queued on `stream` (a cudaStream_t, 0 for the default stream) and the call waits for it.
+   The scratch (interface fluxes, per-stage scalars) is a fixed 8 MiB device array inside the
+   library, held by every GPU that loads it until exit: grids needing more than 2^20 doubles of
+   fluxes (4 nj (ni+1) + 4 (nj+1) ni, about 360 x 360 cells) fail with DENSE_ERR_LIMIT. All calls
+   share that array, so calls whose GPU work overlaps race and must be serialised. The first
+   call on a device resolves the array's device address; make it before any stream capture. The
+   call allocates nothing and calls no allocating routine. */
+int dense_stage_noalloc(const dense_config_t* cfg, int irk, double current_time, double* cons,
+                        double* prim, double* cons0, const double* xbot, const double* xtop,
+                        const double* yleft, double* dt_inout, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
