@@ -174,6 +174,8 @@ def load_library(path: str | None = None):
         "dense_sync": (_c_int, [vp]),
         "dense_profile_stage": (_c_int, [vp, _c_int, ctypes.POINTER(ctypes.c_float)]),
         "dense_fastmath_check": (_c_int, [dp, dp, _c_int]),
+        "dense_count_branches": (_c_int, [vp, _c_int]),
+        "dense_get_branch_counts": (_c_int, [vp, ctypes.POINTER(ctypes.c_ulonglong)]),
         "dense_stage_noalloc": (_c_int, [cfgp, _c_int, _c_double, vp, vp, vp, vp, vp, vp, dp, vp]),
     }
     for name, (res, args) in sigs.items():

@@ -33,6 +33,7 @@ struct dense_handle {
     cudaGraphExec_t step_graph = nullptr;
     int graph_nodes = 0;
     long long launches = 0;
+    int count_branches = 0;
     std::string err;
 };
 
@@ -109,6 +110,7 @@ void fill_params(dense_handle* h) {
     // the body force is nonzero only where boundary_rt_general refreshes it (:154-155)
     p.bodyforce = c.if_bodyforce && (c.benchmark == DENSE_BENCH_RT || c.benchmark == DENSE_BENCH_RT_REFLECT);
     p.benchmark = c.benchmark; p.splitting = c.splitting; p.recon = c.recon;
+    p.count_branches = h->count_branches;
     h->kt = c.strict ? dense::kernels_strict() : dense::kernels_fast();
 }
 
@@ -413,6 +415,23 @@ int dense_set_time(dense_handle_t* h, double t, int step) {
 
 int dense_sync(dense_handle_t* h) {
     if (!h) return seterr(h, DENSE_ERR_ARG, "null handle");
+    CK(h, cudaStreamSynchronize(h->stream));
+    return DENSE_OK;
+}
+
+int dense_count_branches(dense_handle_t* h, int enable) {
+    if (!h) return seterr(h, DENSE_ERR_ARG, "null handle");
+    h->count_branches = enable ? 1 : 0;
+    fill_params(h);
+    drop_graph(h);
+    CK(h, cudaMemsetAsync(h->sc->branch_count, 0, sizeof(h->sc->branch_count), h->stream));
+    return DENSE_OK;
+}
+
+int dense_get_branch_counts(dense_handle_t* h, unsigned long long* counts) {
+    if (!h || !counts) return seterr(h, DENSE_ERR_ARG, "null argument");
+    CK(h, cudaMemcpyAsync(counts, h->sc->branch_count, sizeof(h->sc->branch_count),
+                          cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
     return DENSE_OK;
 }

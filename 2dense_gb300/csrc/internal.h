@@ -24,6 +24,10 @@ struct Scalars {
     int active;           // this step is taken (the while-condition held at its start)
     unsigned status;      // DENSE_FLAG_* bits
     int pad[2];
+    // AdaWENO branch counts over (interface, sign) pairs while Params::count_branches is set,
+    // per sweep direction d (xi 0, eta 1) at [4d + k]: k = 0 smooth branch, 1 characteristic
+    // branch, 2 warps, 3 warps with a characteristic lane
+    unsigned long long branch_count[8];
 };
 
 // Everything a kernel needs, passed by value.
@@ -45,6 +49,7 @@ struct Params {
     // theta_k1 * D > theta_k2 * (N - D) with theta_k1 = sqrt(1-delta), theta_k2 = sqrt(delta)
     double theta_k1, theta_k2;
     int if_const_dt, bodyforce, benchmark, splitting, recon;
+    int count_branches;  // accumulate Scalars::branch_count in the AdaWENO sweeps
 };
 
 // One arithmetic variant of the kernels (fast or strict), as a table of launchers.

@@ -601,6 +601,19 @@ __global__ void __launch_bounds__(TX* TY) k_flux_char(Params p, int irk) {
         smooth[1] = th > p.delta;
 #endif
     }
+    if (ADAPT && p.count_branches) {
+        const unsigned act = __activemask();
+        const int ns = (int)smooth[0] + (int)smooth[1];
+        const unsigned tot_s = __reduce_add_sync(act, (unsigned)ns);
+        const unsigned tot_c = __reduce_add_sync(act, (unsigned)(2 - ns));
+        const bool any_c = __any_sync(act, ns < 2);
+        if ((threadIdx.x + threadIdx.y * blockDim.x) % 32 == __ffs(act) - 1) {
+            atomicAdd(&p.sc->branch_count[4 * DIR + 0], (unsigned long long)tot_s);
+            atomicAdd(&p.sc->branch_count[4 * DIR + 1], (unsigned long long)tot_c);
+            atomicAdd(&p.sc->branch_count[4 * DIR + 2], 1ull);
+            if (any_c) atomicAdd(&p.sc->branch_count[4 * DIR + 3], 1ull);
+        }
+    }
 #if FAST
     EigFast e;
     if (!(ADAPT && smooth[0] && smooth[1])) {

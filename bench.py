@@ -118,13 +118,29 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(cfg_tuple, steps: int, reference_arm: bool = False):
-    """Time the CPU oracle (OpenMP, all host threads) on the workload; returns a dict."""
+def wl_t_start(args) -> float:
+    """Start time of the timed steps: the midpoint (t = 0.1) of the reference's double Mach
+    reflection run to t = 0.2 for the AdaWENO workload, whose cost depends on the flow; t = 0
+    for the others, whose cost does not."""
+    if args.t_start >= 0:
+        return args.t_start
+    return 0.1 if args.workload == "dmr" else 0.0
+
+
+def cpu_baseline(cfg_tuple, steps: int, state=None, t_start: float = 0.0):
+    """Time the CPU oracle (OpenMP, all host threads) on the workload, from `state`
+    (cons, prim, t, step, dt) when given, else from the setup advanced to t_start."""
     from oracle import oracle as orc
     bench, split, recon, ni, nj, desc, _ = cfg_tuple
     cfg = orc.default_config(ni=ni, nj=nj, benchmark=bench, splitting=split, recon=recon, cfl=0.5,
                              var_eps=5.0, var_xc=5.0, var_yc=5.0)
     o = orc.OracleSolver(cfg, timed=True)
+    if state is not None:
+        cons, prim, t, step, dt = state
+        o.set_state(cons, prim)
+        o.set_time(t, step, dt)
+    elif t_start > 0:
+        o.steps(10 ** 7, t_end=t_start)
     o.steps(1)  # warm-up
     t0 = time.perf_counter()
     o.steps(steps)
@@ -141,15 +157,16 @@ def run_reference_arm(args, wl):
     if rank != 0:
         return
     steps = max(1, args.steps)
-    # each step a bounded sample: full-size oracle steps take ~0.1-1 s on 16 cores
-    cb = cpu_baseline(wl, steps=min(steps, 10), reference_arm=True)
+    # each step a bounded sample: full-size oracle steps take ~0.05-1 s on 16 cores; the oracle
+    # first advances itself (untimed) to the start time of the GPU arm's timed steps
+    cb = cpu_baseline(wl, steps=min(steps, 10), t_start=wl_t_start(args))
     bench, split, recon, ni, nj, desc, _ = wl
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT,
             "n_gpus": args.gpus, "steps": min(steps, 10), "warmup": 1,
             "ms_per_step": 1e3 * cb["seconds"] / min(steps, 10), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": desc, "benchmark": bench, "splitting": split, "recon": recon,
-                       "ni": ni, "nj": nj, "l2": "not applicable (CPU)"},
+                       "ni": ni, "nj": nj, "t_start": wl_t_start(args), "l2": "not applicable (CPU)"},
             "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
             "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "the reference is Fortran; no Fortran compiler exists on this image or the GPU "
@@ -169,6 +186,8 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=20)
     ap.add_argument("--ni", type=int, default=0, help="override the grid (smaller profiling cases)")
     ap.add_argument("--nj", type=int, default=0)
+    ap.add_argument("--t-start", type=float, default=-1.0,
+                    help="flow time the timed steps start from (default: 0.1 for dmr, 0 otherwise)")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     if args.ni and args.nj:
@@ -197,9 +216,17 @@ def main():
     lib.dense_get_stream(s.h, ctypes.byref(sp))
     stream = torch.cuda.ExternalStream(sp.value)
 
+    # The timed steps start from a developed state at t_start, produced by this solver before the
+    # warm-up (AdaWENO's cost depends on how much of the flow is non-smooth).
+    t_start = wl_t_start(args)
+    while s.current_time < t_start:
+        s.steps(200, t_end=t_start)
     # warm-up (also builds the step graph)
     s.steps(args.warmup)
     lib.dense_set_time(s.h, s.current_time, s.current_step)
+    # the state the timed steps start from, replayed below to count the work they did
+    snap_cons, snap_prim = s.download()
+    snap_t, snap_step, snap_dt = s.current_time, s.current_step, s.dt
 
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     launches0 = s.launch_count()
@@ -248,11 +275,36 @@ def main():
     xi_ms = prof[:, 1].mean()
     eta_ms = prof[:, 2].mean()
     stage_ms = prof.sum(axis=1).mean()
-    # reference-algorithm FLOPs of one xi sweep (splitting + reconstruction of one stage)
-    xi_flops = fl["flux_xi_per_cell_update"] / 3.0 * cells
+    # Reference-algorithm FLOPs of the timed steps. AdaWENO's work depends on the data only
+    # through the branch each (interface, sign) takes: replay the timed steps from the same
+    # state with the branch counters on and price each branch with the oracle's counts.
+    branches = None
+    if split == 105:
+        ada = fl["adaweno"]
+        s.upload(snap_cons, snap_prim, x, y)
+        lib.dense_set_time(s.h, snap_t, snap_step)
+        lib.dense_count_branches(s.h, 1)
+        lib.dense_steps_async(s.h, args.steps, float("inf"), 2**31 - 1)
+        cnt = (ctypes.c_ulonglong * 8)()
+        lib.dense_get_branch_counts(s.h, cnt)
+        lib.dense_count_branches(s.h, 0)
+        cnt = [int(v) for v in cnt]
+        S, C = ada["smooth_branch_flops"], ada["char_branch_flops"]
+        nsteps = args.steps
+        step_flops = (ada["base_per_cell_update"] * cells
+                      + (S * (cnt[0] + cnt[4]) + C * (cnt[1] + cnt[5])) / nsteps)
+        xi_flops = ada["base_xi_per_cell_update"] / 3.0 * cells + (S * cnt[0] + C * cnt[1]) / (3 * nsteps)
+        branches = {"smooth": cnt[0] + cnt[4], "char": cnt[1] + cnt[5],
+                    "char_fraction": (cnt[1] + cnt[5]) / max(1, sum(cnt[0:2]) + sum(cnt[4:6])),
+                    "warps_with_char_fraction": (cnt[3] + cnt[7]) / max(1, cnt[2] + cnt[6]),
+                    "smooth_branch_flops": S, "char_branch_flops": C,
+                    "base_flops_per_cell_update": ada["base_per_cell_update"]}
+    else:
+        step_flops = fl["flops_per_cell_update"] * cells
+        xi_flops = fl["flux_xi_per_cell_update"] / 3.0 * cells
     achieved = xi_flops / (xi_ms * 1e-3) / 1e12
-    step_flops = fl["flops_per_cell_update"] * cells
-    roofline = {"bound": "fp64", "kernel": "xi flux sweep (k_flux_char<0,true>)",
+    kname = {104: "k_flux_char<0,false>", 105: "k_flux_char<0,true>"}.get(split, "k_flux_cw<0,...>")
+    roofline = {"bound": "fp64", "kernel": f"xi flux sweep ({kname})",
                 "achieved": achieved, "peak": peak.value / 1e12, "unit": "TFLOP/s",
                 "frac": achieved * 1e12 / peak.value,
                 "peak_source": "measured live: dense_measure_fp64 FMA-throughput probe on this GPU "
@@ -260,7 +312,9 @@ def main():
                 "traffic": None,
                 "whole_step": {"achieved_tflops": step_flops * value / cells / world / 1e12,
                                "frac": step_flops * value / cells / world / peak.value,
-                               "flops_per_cell_update": fl["flops_per_cell_update"]},
+                               "flops_per_cell_update": step_flops / cells},
+                "flops_per_xi_launch": xi_flops,
+                "adaweno_branches": branches,
                 "kernel_ms": {"bc": prof[:, 0].mean(), "flux_xi": xi_ms, "flux_eta": eta_ms,
                               "update": prof[:, 3].mean()},
                 "kernel_share": {"bc": prof[:, 0].mean() / stage_ms, "flux_xi": xi_ms / stage_ms,
@@ -274,12 +328,13 @@ def main():
     nip, njp = ni + 8, nj + 8
     pin = torch.empty(nip * njp * 4, dtype=torch.float64, pin_memory=True)
     host = pin.numpy().reshape((nip, njp, 4), order="F")
-    host[...] = cons
+    host[...] = snap_cons
     xs, ys = np.asfortranarray(x), np.asfortranarray(y)
     dp = ctypes.POINTER(ctypes.c_double)
     hp = host.ctypes.data_as(dp)
     with dense.Solver(c) as s2:
-        s2.upload(host, None, xs, ys)
+        s2.upload(host, snap_prim, xs, ys)
+        s2.current_time, s2.current_step = snap_t, snap_step
         s2.steps(1)
         tcur, scur = ctypes.c_double(s2.current_time), ctypes.c_int(s2.current_step)
         t0 = time.perf_counter()
@@ -299,7 +354,7 @@ def main():
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_baseline(wl, args.cpu_steps)
+        cpu = cpu_baseline(wl, args.cpu_steps, state=(snap_cons, snap_prim, snap_t, snap_step, snap_dt))
         cpu.pop("seconds", None)
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -307,6 +362,8 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": desc, "benchmark": bench, "splitting": split, "recon": recon,
                        "ni": ni, "nj": nj, "cells": cells, "strict": args.strict,
+                       "t_start": snap_t, "start": "state at t_start produced by this solver "
+                                                   "before the warm-up (0 = the initial setup)",
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                        "l2": "flushed between timed steps (256 MiB write)"},
             "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,

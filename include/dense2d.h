@@ -213,6 +213,14 @@ int dense_sync(dense_handle_t* h);
    eta flux, update (+ get_primary). Advances the state like dense_stage. */
 int dense_profile_stage(dense_handle_t* h, int irk, float* ms);
 
+/* Branch mix of the AdaWENO sweeps (scheme 105), for counting the algorithmic work of the
+   steps actually run: while enabled, the sweeps of direction d (xi 0, eta 1) add to counts8[4d+k]:
+   k = 0 (interface, sign) pairs that took the smooth branch, 1 pairs that took the characteristic
+   branch, 2 warps, 3 warps with at least one characteristic lane. Enabling or disabling zeroes
+   the counters. */
+int dense_count_branches(dense_handle_t* h, int enable);
+int dense_get_branch_counts(dense_handle_t* h, unsigned long long* counts8);
+
 /* Throughput probe of the FP64 pipe on the current device: kind 0 = FMA (FLOP/s, one FMA
    counted as two), kind 1 = IEEE double divides per second. */
 int dense_measure_fp64(int kind, double* result);

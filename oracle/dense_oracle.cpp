@@ -561,6 +561,7 @@ template <class T> struct Solver {
         return weno5z(lf);
     }
     long long dir_ops[2] = {0, 0};  // counted operations attributed to the xi / eta sweep
+    long long n_smooth[2] = {0, 0}, n_char[2] = {0, 0};  // AdaWENO branch decisions per direction (interface x sign)
     template <class F> void in_dir(int d, F&& f) {
         long long t0 = ops_now();
         f();
@@ -682,6 +683,7 @@ template <class T> struct Solver {
                 if (adaptive) {
                     T* th = &TH[(size_t)4 * ((size_t)(i - 1) + (size_t)(ni + 1) * (j - 1))];
                     if (th[0] > T(delta)) {  // scheme_weno5th_SC.f90:110-124
+                        n_smooth[0]++;
                         T w0 = th[1], w1 = th[2], w2 = th[3];
                         for (int v = 1; v <= 4; ++v) {
                             T lf[5], q30, q31, q32;
@@ -692,6 +694,7 @@ template <class T> struct Solver {
                         continue;
                     }
                 }
+                if (adaptive) n_char[0]++;
                 T u0, v0, h0, a0, L[4][4], R[4][4], Fs[5][4], h[4];
                 roe(Pm(i + b - 1, j + b, 1), Pm(i + b, j + b, 1), Pm(i + b - 1, j + b, 2), Pm(i + b, j + b, 2),
                     Pm(i + b - 1, j + b, 3), Pm(i + b, j + b, 3), Pm(i + b - 1, j + b, 4), Pm(i + b, j + b, 4),
@@ -715,6 +718,7 @@ template <class T> struct Solver {
                 if (adaptive) {
                     T* th = &TH[(size_t)4 * ((size_t)(j - 1) + (size_t)(nj + 1) * (i - 1))];
                     if (th[0] > T(delta)) {  // scheme_weno5th_SC.f90:439-454
+                        n_smooth[1]++;
                         T w0 = th[1], w1 = th[2], w2 = th[3];
                         for (int v = 1; v <= 4; ++v) {
                             T lf[5], q30, q31, q32;
@@ -725,6 +729,7 @@ template <class T> struct Solver {
                         continue;
                     }
                 }
+                if (adaptive) n_char[1]++;
                 T u0, v0, h0, a0, L[4][4], R[4][4], Fs[5][4], h[4];
                 roe(Pm(i + b, j + b - 1, 1), Pm(i + b, j + b, 1), Pm(i + b, j + b - 1, 2), Pm(i + b, j + b, 2),
                     Pm(i + b, j + b - 1, 3), Pm(i + b, j + b, 3), Pm(i + b, j + b - 1, 4), Pm(i + b, j + b, 4),
@@ -1141,6 +1146,37 @@ int oracle_count_step(const dense_config_t* cfg, const double* cons, long long* 
     for (int k = 0; k < 4; ++k) out[6 + k] = s.phase_ops[k];
     out[10] = s.dir_ops[0];
     out[11] = s.dir_ops[1];
+    out[12] = s.n_smooth[0]; out[14] = s.n_smooth[1];
+    out[13] = s.n_char[0]; out[15] = s.n_char[1];
+    return 0;
+}
+
+// Operations of one AdaWENO branch at one interface and sign, the same for any data:
+// out[0] = the smooth branch (component-wise with the surrogate's weights, SC.f90:110-124),
+// out[1] = the characteristic branch (Roe average, eigenvectors, projection, 4 WENO-Z, back-
+// projection; SC.f90:126-163, the same work as one sign of scheme 104).
+int oracle_branch_costs(double gamma, long long* out) {
+    dense_config_t c;
+    std::memset(&c, 0, sizeof(c));
+    c.ni = 3; c.nj = 3; c.gamma = gamma;
+    Solver<Counted> s(c);
+    Counted F[5][4], L[4][4], R[4][4], h[4], u0, v0, h0, a0;
+    for (int m = 0; m < 5; ++m)
+        for (int k = 0; k < 4; ++k) F[m][k] = Counted(1.0 + 0.1 * m + 0.01 * k * m * m);
+    oracle::g_ops = oracle::OpCount();
+    for (int v = 0; v < 4; ++v) {
+        Counted lf[5], q30, q31, q32, w0 = 0.2, w1 = 0.5, w2 = 0.3;
+        for (int m = 0; m < 5; ++m) lf[m] = F[m][v];
+        oracle::candidates(lf, q30, q31, q32);
+        h[v] = w0 * q30 + w1 * q31 + w2 * q32;
+    }
+    out[0] = Solver<Counted>::ops_now();
+    oracle::g_ops = oracle::OpCount();
+    s.roe(Counted(1.0), Counted(1.2), Counted(0.1), Counted(0.2), Counted(0.0), Counted(0.1),
+          Counted(1.0), Counted(1.1), u0, v0, h0, a0);
+    s.lr_vec(true, u0, v0, h0, a0, L, R);
+    s.char_weno(L, R, F, h);
+    out[1] = Solver<Counted>::ops_now();
     return 0;
 }
 

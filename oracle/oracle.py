@@ -59,6 +59,7 @@ def load(timed: bool = False) -> ctypes.CDLL:
         "oracle_count_step": (i, [cfgp, dp, ctypes.POINTER(ctypes.c_longlong)]),
         "oracle_recon": (i, [i, dp, dp]),
         "oracle_roe_lr": (i, [i, ctypes.c_double, dp, dp, dp, dp, dp]),
+        "oracle_branch_costs": (i, [ctypes.c_double, ctypes.POINTER(ctypes.c_longlong)]),
     }
     for fname, (res, args) in sigs.items():
         fn = getattr(lib, fname)
@@ -176,17 +177,29 @@ def count_step_flops(cfg: DenseConfig, cons: np.ndarray | None = None) -> dict:
     """Floating-point operations of one full step of the reference on field values
     (add/sub, mul, div, sqrt each counted as one; transcendental calls counted apart)."""
     lib = load(False)
-    out = (ctypes.c_longlong * 12)()
+    out = (ctypes.c_longlong * 16)()
     c = None if cons is None else np.asfortranarray(cons, dtype=np.float64)
     rc = lib.oracle_count_step(ctypes.byref(cfg), None if c is None else _dp(c), out)
     if rc:
         raise RuntimeError(f"count_step: {rc}")
-    add, mul, div, sqrt, transc, cells, p_prim, p_bc, p_flux, p_rk, d_xi, d_eta = list(out)
+    (add, mul, div, sqrt, transc, cells, p_prim, p_bc, p_flux, p_rk, d_xi, d_eta, n_sm, n_ch,
+     n_sm1, n_ch1) = list(out)
     flops = add + mul + div + sqrt
     return {"add": add, "mul": mul, "div": div, "sqrt": sqrt, "transcendental": transc,
             "cells": cells, "flops": flops, "flops_per_cell_update": flops / cells,
             "phase": {"get_primary": p_prim, "boundary": p_bc, "flux": p_flux, "time_rk3": p_rk},
-            "flux_dir": {"xi": d_xi, "eta": d_eta}}
+            "flux_dir": {"xi": d_xi, "eta": d_eta},
+            "adaweno_branches": {"smooth": n_sm + n_sm1, "char": n_ch + n_ch1,
+                                 "smooth_xi": n_sm, "char_xi": n_ch, "smooth_eta": n_sm1, "char_eta": n_ch1}}
+
+
+def branch_costs(gamma: float = 1.4) -> dict:
+    """Operations of one AdaWENO smooth branch and one characteristic branch (one interface,
+    one sign); both are independent of the data."""
+    lib = load(False)
+    out = (ctypes.c_longlong * 2)()
+    lib.oracle_branch_costs(gamma, out)
+    return {"smooth": out[0], "char": out[1]}
 
 
 def recon(kind: int, lf) -> np.ndarray:

@@ -93,6 +93,21 @@ def main(ref: str) -> None:
                              "div_per_cell_update": c["div"] / c["cells"],
                              "sqrt_per_cell_update": c["sqrt"] / c["cells"],
                              "phase_per_cell_update": {k: v / c["cells"] for k, v in c["phase"].items()}}
+        if s == 105:
+            # AdaWENO's work depends on the data only through the branch taken at each
+            # (interface, sign): record the price of each branch and the rest as a base
+            bc = orc.branch_costs(cfg.gamma)
+            br = c["adaweno_branches"]
+            e = counts[key][name]
+            e["adaweno"] = {
+                "smooth_branch_flops": bc["smooth"], "char_branch_flops": bc["char"],
+                "base_per_cell_update": (c["flops"] - bc["smooth"] * br["smooth"]
+                                         - bc["char"] * br["char"]) / c["cells"],
+                "base_xi_per_cell_update": (c["flux_dir"]["xi"] - bc["smooth"] * br["smooth_xi"]
+                                            - bc["char"] * br["char_xi"]) / c["cells"],
+                "base_eta_per_cell_update": (c["flux_dir"]["eta"] - bc["smooth"] * br["smooth_eta"]
+                                             - bc["char"] * br["char_eta"]) / c["cells"],
+                "branches_at_setup": br}
         print(name, round(c["flops_per_cell_update"], 1))
     with open(os.path.join(HERE, "flop_counts.json"), "w") as f:
         json.dump(counts, f, indent=1)
