@@ -507,40 +507,49 @@ __global__ void k_flux_noop(Params p, int irk) {
 
 // ---------------------------------------------------------------------------------------------
 // Characteristic flux kernel: 104 (ADAPT = false) and 105 AdaWENO (ADAPT = true).
-// GLF splitting with the stage's global wave speed, Roe-averaged eigenvectors computed once per
-// interface and shared by the + and - reconstructions (the reference computes them twice).
+// GLF splitting with the stage's global wave speed; Roe averages and eigenvectors once per
+// interface for both signs (104; the reference computes them twice) or once per characteristic
+// work item (105). AdaWENO takes its cheap smooth branch at most interfaces and the
+// characteristic branch at a few percent of them, clustered near shocks. Run per thread, that
+// branch would hold whole warps for the sake of one or two lanes; instead each thread does its
+// smooth signs and queues its characteristic (interface, sign) items in shared memory, and the
+// whole block then works through the queue on full warps.
 template <int DIR, bool ADAPT, int TX, int TY>
 __global__ void __launch_bounds__(TX* TY) k_flux_char(Params p, int irk) {
     if (!p.sc->active) return;
     constexpr int NL = DIR == 0 ? TY : TY + 5;
     constexpr int NC = DIR == 0 ? TX + 5 : TX;
+    constexpr int NT = TX * TY;
+    constexpr bool kStageHS = FAST && !ADAPT;  // per-cell enthalpy and sqrt(rho) in shared memory
     __shared__ double sF[8][NL][NC];
-    // strict: rho, u, v, p; fast: rho, u, v, total enthalpy H, and sqrt(rho) in sS
-    __shared__ double sQ[4][NL][NC];
-#if FAST
-    __shared__ double sS[NL][NC];
-    const double g1 = p.gamma - 1.0, kg = p.gamma / (p.gamma - 1.0);
-#endif
-    const int tx = threadIdx.x, ty = threadIdx.y;
+    __shared__ double sQ[4][NL][NC];  // rho, u, v, and p (H when kStageHS)
+    __shared__ double sS[kStageHS ? NL : 1][kStageHS ? NC : 1];
+    __shared__ double hbuf[ADAPT ? 2 : 1][4][ADAPT ? NT : 1];
+    __shared__ int queue[ADAPT ? 2 * NT : 1];
+    __shared__ int qn;
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + ty * TX;
     const int slot = irk - 1;
-    if (DIR == 0 && blockIdx.x == 0 && blockIdx.y == 0 && tx == 0 && ty == 0) stage_scalars(p, irk);
+    if (DIR == 0 && blockIdx.x == 0 && blockIdx.y == 0 && tid == 0) stage_scalars(p, irk);
     const double lam = p.sc->maxeig[slot][DIR];
     const int NIp = p.ni + 2 * kB, NJp = p.nj + 2 * kB;
+    const double g1 = p.gamma - 1.0, kg = p.gamma / (p.gamma - 1.0);
+    if (ADAPT && tid == 0) qn = 0;
+    (void)g1; (void)kg;
 
+    // phase 1: split fluxes (and primitives) of the tile's cells
     auto cell = [&](int I, int J, int r, int c) {
         const long long o = cidx(p, I, J);
-        double U[4], fp[4], fm[4];
+        double U[4], fp[4], fm[4], q[4];
 #pragma unroll
         for (int v = 0; v < 4; ++v) U[v] = p.cons[v * p.plane + o];
-        double q[4];
 #pragma unroll
         for (int v = 0; v < 4; ++v) q[v] = p.prim[v * p.plane + o];
         lf_split<DIR>(U, q[1 + DIR], q[3], lam, fp, fm);
-#if FAST
-        const double ir = rcp_nr(q[0]);
-        q[3] = fma(kg * q[3], ir, 0.5 * fma(q[1], q[1], q[2] * q[2]));
-        sS[r][c] = q[0] * rsqrt_nr(q[0]);
-#endif
+        if constexpr (kStageHS) {
+            const double ir = rcp_nr(q[0]);
+            q[3] = fma(kg * q[3], ir, 0.5 * fma(q[1], q[1], q[2] * q[2]));
+            sS[r][c] = q[0] * rsqrt_nr(q[0]);
+        }
 #pragma unroll
         for (int v = 0; v < 4; ++v) { sF[v][r][c] = fp[v]; sF[4 + v][r][c] = fm[v]; sQ[v][r][c] = q[v]; }
     };
@@ -565,111 +574,177 @@ __global__ void __launch_bounds__(TX* TY) k_flux_char(Params p, int irk) {
     if (DIR == 0) { line = blockIdx.y * TY + ty; f = blockIdx.x * TX + tx; }
     else          { line = blockIdx.x * TX + tx; f = blockIdx.y * TY + ty; }
     const int nline = DIR == 0 ? p.nj : p.ni, nface = DIR == 0 ? p.ni + 1 : p.nj + 1;
-    if (line >= nline || f >= nface) return;
-    const int t = DIR == 0 ? tx : ty;
-    auto SF = [&](int q, int k) -> double { return DIR == 0 ? sF[q][ty][k] : sF[q][k][tx]; };
-    auto SQ = [&](int q, int k) -> double { return DIR == 0 ? sQ[q][ty][k] : sQ[q][k][tx]; };
+    const bool valid = line < nline && f < nface;
+    // tile accessors for the interface at tile position (ox, oy); k runs along the sweep
+    auto SF = [&](int q, int k, int ox, int oy) -> double { return DIR == 0 ? sF[q][oy][k] : sF[q][k][ox]; };
+    auto SQ = [&](int q, int k, int ox, int oy) -> double { return DIR == 0 ? sQ[q][oy][k] : sQ[q][k][ox]; };
 #if FAST
-    auto sS_at = [&](int k) -> double { return DIR == 0 ? sS[ty][k] : sS[k][tx]; };
-#endif
-
-    // AdaWENO indicator from the scalar surrogate rho + F+-(normal momentum)
-    // (flux_splitting_SC.f90:175-176,206-207; get_theta_*, scheme_weno5th_SC.f90:1-64,330-393)
-    bool smooth[2] = {false, false};
-    double wsur[2][3];
-    if (ADAPT) {
-        double lp[5], lm[5];
-#pragma unroll
-        for (int m = 0; m < 5; ++m) {
-            lp[m] = SQ(0, t + m) + SF(1 + DIR, t + m);
-            lm[m] = SQ(0, t + 5 - m) + SF(4 + 1 + DIR, t + 5 - m);
-        }
-#if FAST
-#pragma unroll
-        for (int s = 0; s < 2; ++s) {
-            double n0, n1, n2, N, D;
-            weno_num_fast<true>(s == 0 ? lp : lm, n0, n1, n2, N, D);
-            smooth[s] = p.theta_k1 * D > p.theta_k2 * (N - D);
-            const double r = rcp_nr(N);
-            wsur[s][0] = n0 * r; wsur[s][1] = n1 * r; wsur[s][2] = n2 * r;
-        }
+    using EigT = EigFast;
 #else
-        double th;
-        weno5z_omega_theta(lp, wsur[0][0], wsur[0][1], wsur[0][2], th);
-        smooth[0] = th > p.delta;
-        weno5z_omega_theta(lm, wsur[1][0], wsur[1][1], wsur[1][2], th);
-        smooth[1] = th > p.delta;
+    using EigT = Eig;
 #endif
-    }
-    if (ADAPT && p.count_branches) {
-        const unsigned act = __activemask();
-        const int ns = (int)smooth[0] + (int)smooth[1];
-        const unsigned tot_s = __reduce_add_sync(act, (unsigned)ns);
-        const unsigned tot_c = __reduce_add_sync(act, (unsigned)(2 - ns));
-        const bool any_c = __any_sync(act, ns < 2);
-        if ((threadIdx.x + threadIdx.y * blockDim.x) % 32 == __ffs(act) - 1) {
-            atomicAdd(&p.sc->branch_count[4 * DIR + 0], (unsigned long long)tot_s);
-            atomicAdd(&p.sc->branch_count[4 * DIR + 1], (unsigned long long)tot_c);
-            atomicAdd(&p.sc->branch_count[4 * DIR + 2], 1ull);
-            if (any_c) atomicAdd(&p.sc->branch_count[4 * DIR + 3], 1ull);
-        }
-    }
+    // Roe average and eigenvectors of the interface at (ox, oy): cells at tile offsets +2, +3
+    auto eig_at = [&](int ox, int oy, EigT& e) {
+        const int kl = (DIR == 0 ? ox : oy) + 2, kr = kl + 1;
 #if FAST
-    EigFast e;
-    if (!(ADAPT && smooth[0] && smooth[1])) {
-        const bool ok = roe_eig_fast<DIR>(g1, sS_at(t + 2), sS_at(t + 3), SQ(1, t + 2), SQ(1, t + 3),
-                                          SQ(2, t + 2), SQ(2, t + 3), SQ(3, t + 2), SQ(3, t + 3), e);
-        if (!ok) atomicOr(&p.sc->status, DENSE_FLAG_ROE_IMAG);
-    }
+        double sl, sr, hl, hr;
+        if constexpr (kStageHS) {
+            sl = DIR == 0 ? sS[oy][kl] : sS[kl][ox];
+            sr = DIR == 0 ? sS[oy][kr] : sS[kr][ox];
+            hl = SQ(3, kl, ox, oy);
+            hr = SQ(3, kr, ox, oy);
+        } else {
+            const double rl = SQ(0, kl, ox, oy), rr = SQ(0, kr, ox, oy);
+            const double ul = SQ(1, kl, ox, oy), ur = SQ(1, kr, ox, oy);
+            const double vl = SQ(2, kl, ox, oy), vr = SQ(2, kr, ox, oy);
+            hl = fma(kg * SQ(3, kl, ox, oy), rcp_nr(rl), 0.5 * fma(ul, ul, vl * vl));
+            hr = fma(kg * SQ(3, kr, ox, oy), rcp_nr(rr), 0.5 * fma(ur, ur, vr * vr));
+            sl = rl * rsqrt_nr(rl);
+            sr = rr * rsqrt_nr(rr);
+        }
+        const bool ok = roe_eig_fast<DIR>(g1, sl, sr, SQ(1, kl, ox, oy), SQ(1, kr, ox, oy),
+                                          SQ(2, kl, ox, oy), SQ(2, kr, ox, oy), hl, hr, e);
 #else
-    Eig e;
-    if (!(ADAPT && smooth[0] && smooth[1])) {
-        // cells f+3 (left) and f+4 (right) of the interface: tile indices t+2, t+3
-        const bool ok = roe_eig(DIR, p.gamma, SQ(0, t + 2), SQ(0, t + 3), SQ(1, t + 2), SQ(1, t + 3),
-                                SQ(2, t + 2), SQ(2, t + 3), SQ(3, t + 2), SQ(3, t + 3), e);
-        if (!ok) atomicOr(&p.sc->status, DENSE_FLAG_ROE_IMAG);
-    }
+        const bool ok = roe_eig(DIR, p.gamma, SQ(0, kl, ox, oy), SQ(0, kr, ox, oy), SQ(1, kl, ox, oy),
+                                SQ(1, kr, ox, oy), SQ(2, kl, ox, oy), SQ(2, kr, ox, oy), SQ(3, kl, ox, oy),
+                                SQ(3, kr, ox, oy), e);
 #endif
-    double hsum[4];
-#pragma unroll
-    for (int s = 0; s < 2; ++s) {
-        double F[5][4];
+        if (!ok) atomicOr(&p.sc->status, DENSE_FLAG_ROE_IMAG);
+    };
+    // stencil of sign s: "+" lf(m) = F+(cell f+3+m), tile index t+m; "-" lf(m) = F-(cell f+4-m),
+    // tile index t+5-m (m = 0..4 <-> -2..2)
+    auto stencil = [&](int ox, int oy, int s, double F[5][4]) {
+        const int t0 = DIR == 0 ? ox : oy;
 #pragma unroll
         for (int m = 0; m < 5; ++m)
 #pragma unroll
-            for (int c = 0; c < 4; ++c) F[m][c] = s == 0 ? SF(c, t + m) : SF(4 + c, t + 5 - m);
-        double h[4];
-        if (ADAPT && smooth[s]) {  // scheme_weno5th_SC.f90:110-124
+            for (int c = 0; c < 4; ++c) F[m][c] = s == 0 ? SF(c, t0 + m, ox, oy) : SF(4 + c, t0 + 5 - m, ox, oy);
+    };
+    auto char_recon = [&](const EigT& e, const double F[5][4], double h[4]) {
 #if FAST
-            double W[5];
-            stencil_from_weights(wsur[s][0], wsur[s][1], wsur[s][2], W);
-#pragma unroll
-            for (int c = 0; c < 4; ++c)
-                h[c] = fma(W[4], F[4][c], fma(W[3], F[3][c], fma(W[2], F[2][c], fma(W[1], F[1][c], W[0] * F[0][c]))));
+        char_weno_fast<DIR>(e, F, h);
 #else
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                double lf[5], q0, q1, q2;
-#pragma unroll
-                for (int m = 0; m < 5; ++m) lf[m] = F[m][c];
-                candidates(lf, q0, q1, q2);
-                h[c] = wsur[s][0] * q0 + wsur[s][1] * q1 + wsur[s][2] * q2;
-            }
+        char_weno(e, F, h);
 #endif
-        } else {
+    };
+    auto store = [&](const double hsum[4]) {
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            if (DIR == 0) p.hx[(long long)v * p.nj * (p.ni + 1) + (long long)line * (p.ni + 1) + f] = hsum[v];
+            else          p.he[(long long)v * (p.nj + 1) * p.ni + (long long)f * p.ni + line] = hsum[v];
+        }
+    };
+
+    if constexpr (!ADAPT) {
+        // 104: every interface takes the characteristic branch for both signs
+        if (!valid) return;
+        EigT e;
+        eig_at(tx, ty, e);
+        double hsum[4];
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+            double F[5][4], h[4];
+            stencil(tx, ty, s, F);
+            char_recon(e, F, h);
+#pragma unroll
+            for (int c = 0; c < 4; ++c) hsum[c] = s == 0 ? h[c] : hsum[c] + h[c];
+        }
+        store(hsum);
+    } else {
+        // 105, phase 2a: the AdaWENO indicator from the scalar surrogate rho + F+-(normal
+        // momentum) (flux_splitting_SC.f90:175-176,206-207; get_theta_*, scheme_weno5th_SC.f90:
+        // 1-64,330-393), the smooth branch (SC.f90:110-124), and the queue of the rest
+        const int t = DIR == 0 ? tx : ty;
+        bool smooth[2] = {true, true};
+        double wsur[2][3];
+        if (valid) {
+            double lp[5], lm[5];
+#pragma unroll
+            for (int m = 0; m < 5; ++m) {
+                lp[m] = SQ(0, t + m, tx, ty) + SF(1 + DIR, t + m, tx, ty);
+                lm[m] = SQ(0, t + 5 - m, tx, ty) + SF(5 + DIR, t + 5 - m, tx, ty);
+            }
 #if FAST
-            char_weno_fast<DIR>(e, F, h);
+#pragma unroll
+            for (int s = 0; s < 2; ++s) {
+                double n0, n1, n2, N, D;
+                weno_num_fast<true>(s == 0 ? lp : lm, n0, n1, n2, N, D);
+                smooth[s] = p.theta_k1 * D > p.theta_k2 * (N - D);
+                const double r = rcp_nr(N);
+                wsur[s][0] = n0 * r; wsur[s][1] = n1 * r; wsur[s][2] = n2 * r;
+            }
 #else
-            char_weno(e, F, h);
+            double th;
+            weno5z_omega_theta(lp, wsur[0][0], wsur[0][1], wsur[0][2], th);
+            smooth[0] = th > p.delta;
+            weno5z_omega_theta(lm, wsur[1][0], wsur[1][1], wsur[1][2], th);
+            smooth[1] = th > p.delta;
 #endif
         }
+        if (p.count_branches) {
+            const int ns = valid ? (int)smooth[0] + (int)smooth[1] : 0;
+            const int nc = valid ? 2 - ns : 0;
+            const unsigned tot_s = __reduce_add_sync(0xffffffffu, (unsigned)ns);
+            const unsigned tot_c = __reduce_add_sync(0xffffffffu, (unsigned)nc);
+            const bool any_valid = __any_sync(0xffffffffu, valid);
+            const bool any_c = __any_sync(0xffffffffu, nc > 0);
+            if ((tid & 31) == 0 && any_valid) {
+                atomicAdd(&p.sc->branch_count[4 * DIR + 0], (unsigned long long)tot_s);
+                atomicAdd(&p.sc->branch_count[4 * DIR + 1], (unsigned long long)tot_c);
+                atomicAdd(&p.sc->branch_count[4 * DIR + 2], 1ull);
+                if (any_c) atomicAdd(&p.sc->branch_count[4 * DIR + 3], 1ull);
+            }
+        }
 #pragma unroll
-        for (int c = 0; c < 4; ++c) hsum[c] = s == 0 ? h[c] : hsum[c] + h[c];
-    }
+        for (int s = 0; s < 2; ++s) {
+            if (!valid) continue;
+            if (smooth[s]) {
+                double F[5][4], h[4];
+                stencil(tx, ty, s, F);
+#if FAST
+                double W[5];
+                stencil_from_weights(wsur[s][0], wsur[s][1], wsur[s][2], W);
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {
-        if (DIR == 0) p.hx[(long long)v * p.nj * (p.ni + 1) + (long long)line * (p.ni + 1) + f] = hsum[v];
-        else          p.he[(long long)v * (p.nj + 1) * p.ni + (long long)f * p.ni + line] = hsum[v];
+                for (int c = 0; c < 4; ++c)
+                    h[c] = fma(W[4], F[4][c], fma(W[3], F[3][c], fma(W[2], F[2][c], fma(W[1], F[1][c], W[0] * F[0][c]))));
+#else
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    double lf[5], q0, q1, q2;
+#pragma unroll
+                    for (int m = 0; m < 5; ++m) lf[m] = F[m][c];
+                    candidates(lf, q0, q1, q2);
+                    h[c] = wsur[s][0] * q0 + wsur[s][1] * q1 + wsur[s][2] * q2;
+                }
+#endif
+#pragma unroll
+                for (int c = 0; c < 4; ++c) hbuf[s][c][tid] = h[c];
+            } else {
+                queue[atomicAdd(&qn, 1)] = 2 * tid + s;
+            }
+        }
+        __syncthreads();
+        // phase 2b: the block works through the characteristic items (SC.f90:126-163)
+        const int nq = qn;
+        for (int it = tid; it < nq; it += NT) {
+            const int item = queue[it], owner = item >> 1, s = item & 1;
+            const int ox = owner % TX, oy = owner / TX;
+            EigT e;
+            eig_at(ox, oy, e);
+            double F[5][4], h[4];
+            stencil(ox, oy, s, F);
+            char_recon(e, F, h);
+#pragma unroll
+            for (int c = 0; c < 4; ++c) hbuf[s][c][owner] = h[c];
+        }
+        __syncthreads();
+        // phase 2c: h = h+ + h- (sum_field, field_op.f90:1-21)
+        if (valid) {
+            double hsum[4];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) hsum[c] = hbuf[0][c][tid] + hbuf[1][c][tid];
+            store(hsum);
+        }
     }
 }
 
@@ -966,6 +1041,7 @@ __global__ void k_step_end(Scalars* sc) {
 // Launchers
 constexpr int kXTX = 32, kXTY = 4;   // xi tile
 constexpr int kETX = 32, kETY = 8;   // eta tile
+constexpr int kETY_ADAPT = 6;        // AdaWENO eta tile: its work queue must fit the 48 KB static smem
 
 static inline dim3 grid_xi(const Params& p, int tx, int ty) {
     return dim3((p.ni + 1 + tx - 1) / tx, (p.nj + ty - 1) / ty);
@@ -1001,7 +1077,7 @@ static void launch_flux(const Params& p, int irk, int dir, void* stream) {
         break;
     case DENSE_SPLIT_SC:
         if (dir == 0) k_flux_char<0, true, kXTX, kXTY><<<grid_xi(p, kXTX, kXTY), dim3(kXTX, kXTY), 0, s>>>(p, irk);
-        else          k_flux_char<1, true, kETX, kETY><<<grid_eta(p, kETX, kETY), dim3(kETX, kETY), 0, s>>>(p, irk);
+        else          k_flux_char<1, true, kETX, kETY_ADAPT><<<grid_eta(p, kETX, kETY_ADAPT), dim3(kETX, kETY_ADAPT), 0, s>>>(p, irk);
         break;
     default:
         break;
