@@ -786,7 +786,8 @@ __device__ __forceinline__ void prim_cell(const Params& p, long long o, const do
     double pr = (p.gamma - 1.0) * (q[3] - 0.5 * rho * (u * u + v * v));
     if (pr < 0.0) { pr = kPFloor; flags |= DENSE_FLAG_P_FLOOR; }
 #if FAST
-    const double alpha = sqrt(p.gamma * pr * ir);
+    const double a2 = p.gamma * pr * ir;
+    const double alpha = a2 > 0.0 ? a2 * rsqrt_nr(a2) : sqrt(a2);
 #else
     const double alpha = sqrt(p.gamma * pr / rho);
 #endif
@@ -797,8 +798,15 @@ __device__ __forceinline__ void prim_cell(const Params& p, long long o, const do
     p.prim[4 * p.plane + o] = alpha;
     e1 = fabs(u) + alpha;
     e2 = fabs(v) + alpha;
-    if (!(rho > 0.0)) flags |= DENSE_FLAG_NEG_RHO;
-    if (isnan(q[0]) || isnan(q[1]) || isnan(q[2]) || isnan(q[3])) flags |= DENSE_FLAG_NAN;
+    // numeric checks on the bit patterns (integer pipe): rho <= 0 or NaN, and any NaN
+    const long long rb = __double_as_longlong(rho);
+    if (rb <= 0 || rb > 0x7ff0000000000000LL) flags |= DENSE_FLAG_NEG_RHO;
+    const unsigned long long kAbs = 0x7fffffffffffffffULL, kInf = 0x7ff0000000000000ULL;
+    if (((unsigned long long)__double_as_longlong(q[0]) & kAbs) > kInf ||
+        ((unsigned long long)__double_as_longlong(q[1]) & kAbs) > kInf ||
+        ((unsigned long long)__double_as_longlong(q[2]) & kAbs) > kInf ||
+        ((unsigned long long)__double_as_longlong(q[3]) & kAbs) > kInf)
+        flags |= DENSE_FLAG_NAN;
 }
 
 __global__ void k_prim(Params p, int slot) {
@@ -940,68 +948,98 @@ __global__ void k_bc(Params p) {
     const double gamma = p.gamma;
     const bool vert = side <= kTop;  // ghost rows of an interior column
     const int I = line + kB, J = line + kB;
-    for (int k = 0; k < kB; ++k) {
-        // ghost position and, for copies, its source
-        int gi, gj, si = 0, sj = 0;
-        if (side == kBottom) { gi = I; gj = k; }
+    // ghost layer k (0 = next to the interior) of this line
+    auto ghost = [&](int k, int& gi, int& gj) {
+        if (side == kBottom) { gi = I; gj = kB - 1 - k; }
         else if (side == kTop) { gi = I; gj = nj + kB + k; }
-        else if (side == kLeft) { gi = kB - 1 - k; gj = J; }   // extrapolation order: b..1
+        else if (side == kLeft) { gi = kB - 1 - k; gj = J; }
         else { gi = ni + kB + k; gj = J; }
-        Cell g;
-        switch (rule) {
-        case kPeriodic:
-            if (side == kBottom) { si = I; sj = nj + k; }
-            else if (side == kTop) { si = I; sj = kB + k; }
-            else if (side == kLeft) { si = ni + gi; sj = J; }
-            else { si = kB + k; sj = J; }
-            load_cell(p, si, sj, g);
-            break;
-        case kReflect:
-            if (side == kBottom) { si = I; sj = 2 * kB - 1 - gj; }
-            else if (side == kTop) { si = I; sj = 2 * nj + 2 * kB - 1 - gj; }
-            else if (side == kLeft) { si = 2 * kB - 1 - gi; sj = J; }
-            else { si = 2 * ni + 2 * kB - 1 - gi; sj = J; }
-            load_cell(p, si, sj, g);
-            reflect(g, vert ? 2 : 1);
-            break;
-        case kExtrap: {
-            Cell a, b2;
-            if (side == kBottom) { load_cell(p, I, gj + 1, a); load_cell(p, I, gj + 2, b2); }
-            else if (side == kTop) { load_cell(p, I, gj - 1, a); load_cell(p, I, gj - 2, b2); }
-            else if (side == kLeft) { load_cell(p, gi + 1, J, a); load_cell(p, gi + 2, J, b2); }
-            else { load_cell(p, gi - 1, J, a); load_cell(p, gi - 2, J, b2); }
+    };
+    // interior cell at distance d (1 = adjacent) from the boundary of this line
+    auto inner = [&](int d, int& si, int& sj) {
+        if (side == kBottom) { si = I; sj = kB - 1 + d; }
+        else if (side == kTop) { si = I; sj = nj + kB - d; }
+        else if (side == kLeft) { si = kB - 1 + d; sj = J; }
+        else { si = ni + kB - d; sj = J; }
+    };
+    int gi, gj, si, sj;
+    switch (rule) {
+    case kPeriodic:
+    case kReflect: {
+        // periodic: ghost k copies the interior cell k+1 in from the opposite side
+        // reflect:  ghost k mirrors the interior cell k+1 in from the same side, normal velocity negated
 #pragma unroll
-            for (int v = 0; v < 4; ++v) g.c[v] = extrap(a.c[v], b2.c[v]);
-#pragma unroll
-            for (int v = 0; v < 5; ++v) g.q[v] = extrap(a.q[v], b2.q[v]);
-            break;
-        }
-        case kDirichletRT:  // boundary_rt_general.f90:14-57
-            if (side == kBottom) state_from(gamma, 2.0, 0.0, 0.0, 1.0, g);
-            else state_from(gamma, 1.0, 0.0, 0.0, 2.5, g);
-            break;
-        case kDMRBottom: {  // boundary_doublemach_general.f90:14-48
-            const double xx = p.xbot[line];
-            if (xx >= 1.0 / 6.0) {
-                load_cell(p, I, 2 * kB - 1 - gj, g);
-                reflect(g, 2);
+        for (int k = 0; k < kB; ++k) {
+            ghost(k, gi, gj);
+            if (rule == kPeriodic) {
+                if (side == kBottom) { si = I; sj = nj + gj; }
+                else if (side == kTop) { si = I; sj = gj - nj; }
+                else if (side == kLeft) { si = ni + gi; sj = J; }
+                else { si = gi - ni; sj = J; }
             } else {
-                state_from(gamma, 8.0, (double)8.25f * sqrt(3.0) * 0.5, -(double)8.25f * 0.5, 116.5, g);
+                inner(k + 1, si, sj);
+            }
+            Cell g;
+            load_cell(p, si, sj, g);
+            if (rule == kReflect) reflect(g, vert ? 2 : 1);
+            store_cell(p, gi, gj, g);
+        }
+        break;
+    }
+    case kExtrap: {
+        // recursive outward: g = near*4/3 - far/3 with (near, far) = (g_{k-1}, g_{k-2})
+        Cell a, b;
+        inner(1, si, sj);
+        load_cell(p, si, sj, a);
+        inner(2, si, sj);
+        load_cell(p, si, sj, b);
+#pragma unroll
+        for (int k = 0; k < kB; ++k) {
+            Cell g;
+#pragma unroll
+            for (int v = 0; v < 4; ++v) g.c[v] = extrap(a.c[v], b.c[v]);
+#pragma unroll
+            for (int v = 0; v < 5; ++v) g.q[v] = extrap(a.q[v], b.q[v]);
+            ghost(k, gi, gj);
+            store_cell(p, gi, gj, g);
+            b = a;
+            a = g;
+        }
+        break;
+    }
+    case kDMRBottom: {  // boundary_doublemach_general.f90:14-48
+        if (p.xbot[line] >= 1.0 / 6.0) {
+#pragma unroll
+            for (int k = 0; k < kB; ++k) {
+                Cell g;
+                inner(k + 1, si, sj);
+                load_cell(p, si, sj, g);
+                reflect(g, 2);
+                ghost(k, gi, gj);
+                store_cell(p, gi, gj, g);
             }
             break;
         }
-        case kDMRTop: {  // boundary_doublemach_general.f90:51-76 (time at the start of the step)
-            const double xx = p.xtop[line];
-            if (xx < (1.0 / 6.0 + (1.0 + 20.0 * p.sc->t) / sqrt(3.0)))
+        Cell g;
+        state_from(gamma, 8.0, (double)8.25f * sqrt(3.0) * 0.5, -(double)8.25f * 0.5, 116.5, g);
+#pragma unroll
+        for (int k = 0; k < kB; ++k) { ghost(k, gi, gj); store_cell(p, gi, gj, g); }
+        break;
+    }
+    default: {
+        // Dirichlet states: the same state in all four layers
+        Cell g;
+        if (rule == kDirichletRT) {  // boundary_rt_general.f90:14-57
+            if (side == kBottom) state_from(gamma, 2.0, 0.0, 0.0, 1.0, g);
+            else state_from(gamma, 1.0, 0.0, 0.0, 2.5, g);
+        } else if (rule == kDMRTop) {  // boundary_doublemach_general.f90:51-76, time at the step's start
+            if (p.xtop[line] < (1.0 / 6.0 + (1.0 + 20.0 * p.sc->t) / sqrt(3.0)))
                 state_from(gamma, 8.0, (double)8.25f * sqrt(3.0) * 0.5, -(double)8.25f * 0.5, 116.5, g);
             else
                 state_from(gamma, 1.4, 0.0, 0.0, 1.0, g);
-            break;
-        }
-        case kDMRInflow:  // boundary_doublemach_general.f90:79-99
+        } else if (rule == kDMRInflow) {  // boundary_doublemach_general.f90:79-99
             state_from(gamma, 8.0, (double)8.25f * sqrt(3.0) * 0.5, -(double)8.25f * 0.5, 116.5, g);
-            break;
-        case kSSLInflow: {  // boundary_ssl_general.f90:40-66
+        } else if (rule == kSSLInflow) {  // boundary_ssl_general.f90:40-66
             const double yy = p.yleft[line];
             const double rho = yy >= 0.0 ? 1.6374 : 0.3626, pr = 0.3327;
             const double pie = 3.141592653589793115997963468544185161590576171875;
@@ -1010,16 +1048,13 @@ __global__ void k_bc(Params p) {
             const double v = 0.05 * cos(2.0 * pie * t / (30.0 / 2.68)) * exp(-(yy * yy) / 10.0)
                            + 0.05 * cos(2.0 * pie * 2.0 * t / (30.0 / 2.68) + pie / 2.0) * exp(-(yy * yy) / 10.0);
             state_from(gamma, rho, u, v, pr, g);
-            break;
-        }
-        default:
+        } else {
             return;
         }
-        if (rule == kReflect || rule == kDirichletRT || rule == kDMRBottom || rule == kDMRTop ||
-            rule == kDMRInflow || rule == kSSLInflow) {
-            // these rules write rho,u,v,p,alpha of prim and leave the entropy alone
-        }
-        store_cell(p, gi, gj, g);
+#pragma unroll
+        for (int k = 0; k < kB; ++k) { ghost(k, gi, gj); store_cell(p, gi, gj, g); }
+        break;
+    }
     }
 }
 

@@ -188,6 +188,8 @@ def main():
     ap.add_argument("--nj", type=int, default=0)
     ap.add_argument("--t-start", type=float, default=-1.0,
                     help="flow time the timed steps start from (default: 0.1 for dmr, 0 otherwise)")
+    ap.add_argument("--save-state", default="", help="write the start state (npz) before warm-up")
+    ap.add_argument("--load-state", default="", help="start from a state written by --save-state")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     if args.ni and args.nj:
@@ -219,8 +221,16 @@ def main():
     # The timed steps start from a developed state at t_start, produced by this solver before the
     # warm-up (AdaWENO's cost depends on how much of the flow is non-smooth).
     t_start = wl_t_start(args)
+    if args.load_state:
+        z = np.load(args.load_state)
+        s.upload(z["cons"], z["prim"], x, y)
+        s.current_time, s.current_step = float(z["t"]), int(z["step"])
+        t_start = s.current_time
     while s.current_time < t_start:
         s.steps(200, t_end=t_start)
+    if args.save_state:
+        sc_, sp_ = s.download()
+        np.savez(args.save_state, cons=sc_, prim=sp_, t=s.current_time, step=s.current_step)
     # warm-up (also builds the step graph)
     s.steps(args.warmup)
     lib.dense_set_time(s.h, s.current_time, s.current_step)
