@@ -697,17 +697,30 @@ __global__ void __launch_bounds__(TX* TY) k_flux_char(Params p, int irk) {
         }
 #pragma unroll
         for (int s = 0; s < 2; ++s) {
-            if (!valid) continue;
-            if (smooth[s]) {
-                double F[5][4], h[4];
-                stencil(tx, ty, s, F);
 #if FAST
-                double W[5];
+            // the smooth result is computed by every lane (uniform, no divergence) and kept
+            // only where the smooth branch is taken
+            {
+                double F[5][4], h[4], W[5];
+                stencil(tx, ty, s, F);
                 stencil_from_weights(wsur[s][0], wsur[s][1], wsur[s][2], W);
 #pragma unroll
                 for (int c = 0; c < 4; ++c)
                     h[c] = fma(W[4], F[4][c], fma(W[3], F[3][c], fma(W[2], F[2][c], fma(W[1], F[1][c], W[0] * F[0][c]))));
-#else
+                if (valid && smooth[s]) {
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) hbuf[s][c][tid] = h[c];
+                } else if (valid) {
+                    queue[atomicAdd(&qn, 1)] = 2 * tid + s;
+                }
+            }
+            continue;
+#endif
+            if (!valid) continue;
+            if (smooth[s]) {
+                double F[5][4], h[4];
+                stencil(tx, ty, s, F);
+#if !FAST
 #pragma unroll
                 for (int c = 0; c < 4; ++c) {
                     double lf[5], q0, q1, q2;
@@ -905,7 +918,16 @@ __device__ __forceinline__ void store_cell(const Params& p, int I, int J, const 
 }
 // Copy with the normal velocity negated (reflective wall): comp = 1 (u, x-walls) or 2 (v, y-walls)
 __device__ __forceinline__ void reflect(Cell& g, int comp) { g.c[comp] = -g.c[comp]; g.q[comp] = -g.q[comp]; }
-__device__ __forceinline__ double extrap(double near, double far) { return near * 4.0 / 3.0 - far / 3.0; }
+// Recursive 4/3, -1/3 extrapolation (boundary_ivc_general.f90:101-119). Strict: the reference's
+// two divides; fast: multiplies by the rounded constants (within an ulp, and no serial divides
+// in the boundary kernel's dependent chain).
+__device__ __forceinline__ double extrap(double near, double far) {
+#if FAST
+    return fma(near, 4.0 / 3.0, -(far * (1.0 / 3.0)));
+#else
+    return near * 4.0 / 3.0 - far / 3.0;
+#endif
+}
 
 enum Side { kBottom = 0, kTop = 1, kLeft = 2, kRight = 3 };
 enum Rule { kNone, kPeriodic, kExtrap, kReflect, kDirichletRT, kDMRBottom, kDMRTop, kDMRInflow, kSSLInflow };
