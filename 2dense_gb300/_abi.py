@@ -174,6 +174,20 @@ def load_library(path: str | None = None):
         "dense_sync": (_c_int, [vp]),
         "dense_profile_stage": (_c_int, [vp, _c_int, ctypes.POINTER(ctypes.c_float)]),
         "dense_fastmath_check": (_c_int, [dp, dp, _c_int]),
+        "dense_batch_create": (_c_int, [_c_int, cfgp, ctypes.POINTER(vp)]),
+        "dense_batch_destroy": (None, [vp]),
+        "dense_batch_upload": (_c_int, [vp, _c_int, dp, dp, dp, dp]),
+        "dense_batch_download": (_c_int, [vp, _c_int, dp, dp]),
+        "dense_batch_set_time": (_c_int, [vp, _c_int, _c_double, _c_int]),
+        "dense_batch_get_time": (_c_int, [vp, _c_int, dp, ctypes.POINTER(_c_int), dp]),
+        "dense_batch_steps": (_c_int, [vp, _c_int, _c_double, _c_int]),
+        "dense_batch_steps_async": (_c_int, [vp, _c_int, _c_double, _c_int]),
+        "dense_batch_set_schedule": (_c_int, [vp, _c_int, _c_int, _c_int]),
+        "dense_batch_get_stream": (_c_int, [vp, ctypes.POINTER(vp)]),
+        "dense_batch_status": (_c_int, [vp, ctypes.POINTER(ctypes.c_uint)]),
+        "dense_batch_launch_count": (ctypes.c_longlong, [vp]),
+        "dense_batch_cells": (ctypes.c_longlong, [vp]),
+        "dense_batch_last_error": (ctypes.c_char_p, [vp]),
         "dense_count_branches": (_c_int, [vp, _c_int]),
         "dense_get_branch_counts": (_c_int, [vp, ctypes.POINTER(ctypes.c_ulonglong)]),
         "dense_stage_noalloc": (_c_int, [cfgp, _c_int, _c_double, vp, vp, vp, vp, vp, vp, dp, vp]),

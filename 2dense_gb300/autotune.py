@@ -1,0 +1,115 @@
+"""Autotuner of the batched form's launch schedule.
+
+A schedule is (xi tile variant, eta tile variant, block order): the thread-block shape of each
+direction sweep (``batch_tile_shape`` in csrc/kernels.cu) and the order in which the instances'
+blocks are laid out in each launch (instance-major, largest instance first, or round-robin).
+None of them changes any result -- every interface's arithmetic is the same -- so the tuner is
+free to pick whichever is fastest for the batch at hand.
+
+The search is a coordinate descent (order, then xi tile, then eta tile), each candidate timed on a
+scratch copy of the batch (same configurations, same initial states) so the caller's solution is
+untouched. The winner is cached in a JSON file keyed by device, scheme and the histogram of
+instance sizes, so a second batch of the same shape reuses it without timing.
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import time
+
+from .solver import BatchSolver, init_general
+
+CACHE = os.environ.get("DENSE2D_AUTOTUNE_CACHE",
+                       os.path.join(os.path.expanduser("~"), ".cache", "dense2d_gb300", "autotune.json"))
+N_VARIANTS = 3
+ORDERS = 3
+
+
+def _device_key() -> str:
+    try:
+        import torch
+        p = torch.cuda.get_device_properties(torch.cuda.current_device())
+        return f"{p.name}|{p.multi_processor_count}"
+    except Exception:  # no torch: the key still separates schemes and shapes
+        return "cuda"
+
+
+def batch_key(cfgs) -> str:
+    sizes = sorted((c.ni, c.nj) for c in cfgs)
+    h = hashlib.sha1(json.dumps(sizes).encode()).hexdigest()[:16]
+    c0 = cfgs[0]
+    return f"{_device_key()}|{c0.splitting}|{c0.recon}|{c0.strict}|n{len(cfgs)}|{h}"
+
+
+def _load_cache() -> dict:
+    try:
+        with open(CACHE) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def _store_cache(d: dict) -> None:
+    try:
+        os.makedirs(os.path.dirname(CACHE), exist_ok=True)
+        tmp = CACHE + ".tmp"
+        with open(tmp, "w") as f:
+            json.dump(d, f, indent=1, sort_keys=True)
+        os.replace(tmp, CACHE)
+    except OSError:
+        pass
+
+
+def _time_schedule(b: BatchSolver, sched, steps: int, reps: int) -> float:
+    b.set_schedule(*sched)
+    b.steps(1)  # warm-up: builds the graph for this schedule
+    best = float("inf")
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        b.steps(steps)
+        best = min(best, time.perf_counter() - t0)
+    return best
+
+
+def tune(cfgs, setups=None, steps: int = 2, reps: int = 2, use_cache: bool = True):
+    """Best (xi_variant, eta_variant, order) for this batch, and the timings tried.
+
+    ``setups`` is the list of (cfg, cons, prim, x, y) the batch starts from (init_general of each
+    configuration when omitted)."""
+    key = batch_key(cfgs)
+    cache = _load_cache() if use_cache else {}
+    if key in cache:
+        e = cache[key]
+        return tuple(e["schedule"]), {"cached": True, "key": key, "trials": e.get("trials", {})}
+    if setups is None:
+        setups = [init_general(c) for c in cfgs]
+    trials = {}
+    scratch = BatchSolver([s[0] for s in setups])
+    try:
+        for i, (c, cons, prim, x, y) in enumerate(setups):
+            scratch.upload(i, cons, prim, x, y)
+        best = (0, 0, 0)
+
+        def run(sched):
+            if sched not in trials:
+                trials[sched] = _time_schedule(scratch, sched, steps, reps)
+            return trials[sched]
+
+        for o in range(ORDERS):
+            if run((best[0], best[1], o)) < run(best):
+                best = (best[0], best[1], o)
+        for v in range(N_VARIANTS):
+            if run((v, best[1], best[2])) < run(best):
+                best = (v, best[1], best[2])
+        for v in range(N_VARIANTS):
+            if run((best[0], v, best[2])) < run(best):
+                best = (best[0], v, best[2])
+    finally:
+        scratch.close()
+    named = {f"{k[0]},{k[1]},{k[2]}": v for k, v in trials.items()}
+    if use_cache:
+        cache = _load_cache()
+        cache[key] = {"schedule": list(best), "trials": named}
+        _store_cache(cache)
+    return best, {"cached": False, "key": key, "trials": named}

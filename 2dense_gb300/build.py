@@ -63,6 +63,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         "capi": [nvcc, *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, "capi.cu")],
         "probe": [nvcc, *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, "probe.cu")],
         "noalloc": [nvcc, *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, "noalloc.cu")],
+        "batch": [nvcc, *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, "batch.cu")],
         "host_setup": ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-c",
                        os.path.join(CSRC, "host_setup.cpp")],
     }

@@ -74,4 +74,34 @@ struct KernelTable {
 const KernelTable* kernels_fast();
 const KernelTable* kernels_strict();
 
+// ---- batched form: many independent blocks of uneven size advanced by one launch per phase
+struct int3_ { int x, y, z; };  // host mirror of CUDA's int3 (instance, block x, block y)
+
+// Tile shapes (threads x, threads y) the batched flux sweeps can run with; an autotuner picks
+// one per direction. Variant 0 is the single-instance shape.
+constexpr int kTileVariants = 3;
+void batch_tile_shape(int splitting, int dir, int variant, int* tx, int* ty);
+
+struct BatchLaunch {
+    const Params* tab;  // device array: one Params per instance
+    int n;              // instances
+    const void* map_cells; int nb_cells;  // 32 x 8 blocks over each instance's interior cells
+    const void* map_bc;    int nb_bc;     // 128-thread blocks over each instance's ghost lines
+    const void* map_xi;    int nb_xi;     // xi-sweep tiles
+    const void* map_eta;   int nb_eta;    // eta-sweep tiles
+    int xi_variant, eta_variant;
+    int splitting, recon;  // common to the batch
+};
+
+struct BatchKernelTable {
+    void (*prim)(const BatchLaunch&, int slot, void* stream);
+    void (*bc)(const BatchLaunch&, void* stream);
+    void (*flux)(const BatchLaunch&, int irk, int dir, void* stream);
+    void (*update)(const BatchLaunch&, int irk, void* stream);
+    void (*step_begin)(const BatchLaunch&, void* stream);
+    void (*step_end)(const BatchLaunch&, void* stream);
+};
+const BatchKernelTable* batch_kernels_fast();
+const BatchKernelTable* batch_kernels_strict();
+
 }  // namespace dense

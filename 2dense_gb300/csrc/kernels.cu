@@ -427,14 +427,14 @@ __device__ __forceinline__ void stage_scalars(const Params& p, int irk) {
 // One thread per interface; the tile's per-cell split fluxes are staged in shared memory.
 // xi tile: TX interfaces x TY rows, cells f0+1 .. f0+TX+5; eta tile: TX columns x TY interfaces.
 template <int DIR, int SPL, int REC, int TX, int TY>
-__global__ void __launch_bounds__(TX* TY) k_flux_cw(Params p, int irk) {
+__device__ __forceinline__ void flux_cw_block(const Params& p, int irk, int bx, int by) {
     if (!p.sc->active) return;
     constexpr int NL = DIR == 0 ? TY : TY + 5;   // smem rows
     constexpr int NC = DIR == 0 ? TX + 5 : TX;   // smem columns
     __shared__ double sF[8][NL][NC];
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int slot = irk - 1;
-    if (DIR == 0 && blockIdx.x == 0 && blockIdx.y == 0 && tx == 0 && ty == 0) stage_scalars(p, irk);
+    if (DIR == 0 && bx == 0 && by == 0 && tx == 0 && ty == 0) stage_scalars(p, irk);
     const double lam_g = p.sc->maxeig[slot][DIR];
     const int NIp = p.ni + 2 * kB, NJp = p.nj + 2 * kB;
 
@@ -457,14 +457,14 @@ __global__ void __launch_bounds__(TX* TY) k_flux_cw(Params p, int irk) {
         for (int v = 0; v < 4; ++v) { sF[v][r][c] = fp[v]; sF[4 + v][r][c] = fm[v]; }
     };
     if (DIR == 0) {
-        const int f0 = blockIdx.x * TX, j = blockIdx.y * TY + ty;
+        const int f0 = bx * TX, j = by * TY + ty;
         if (j < p.nj)
             for (int k = tx; k < TX + 5; k += TX) {
                 const int I = f0 + 1 + k;
                 if (I < NIp) cell(I, j + kB, ty, k);
             }
     } else {
-        const int g0 = blockIdx.y * TY, i = blockIdx.x * TX + tx;
+        const int g0 = by * TY, i = bx * TX + tx;
         if (i < p.ni)
             for (int k = ty; k < TY + 5; k += TY) {
                 const int J = g0 + 1 + k;
@@ -475,8 +475,8 @@ __global__ void __launch_bounds__(TX* TY) k_flux_cw(Params p, int irk) {
 
     // phase 2: reconstruction at the interface
     int line, f;  // line = row j (xi) or column i (eta); f = interface index
-    if (DIR == 0) { line = blockIdx.y * TY + ty; f = blockIdx.x * TX + tx; }
-    else          { line = blockIdx.x * TX + tx; f = blockIdx.y * TY + ty; }
+    if (DIR == 0) { line = by * TY + ty; f = bx * TX + tx; }
+    else          { line = bx * TX + tx; f = by * TY + ty; }
     const int nline = DIR == 0 ? p.nj : p.ni, nface = DIR == 0 ? p.ni + 1 : p.nj + 1;
     if (line >= nline || f >= nface) return;
     const int t = DIR == 0 ? tx : ty;  // position of the interface in the tile
@@ -515,7 +515,7 @@ __global__ void k_flux_noop(Params p, int irk) {
 // smooth signs and queues its characteristic (interface, sign) items in shared memory, and the
 // whole block then works through the queue on full warps.
 template <int DIR, bool ADAPT, int TX, int TY>
-__global__ void __launch_bounds__(TX* TY) k_flux_char(Params p, int irk) {
+__device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx, int by) {
     if (!p.sc->active) return;
     constexpr int NL = DIR == 0 ? TY : TY + 5;
     constexpr int NC = DIR == 0 ? TX + 5 : TX;
@@ -529,7 +529,7 @@ __global__ void __launch_bounds__(TX* TY) k_flux_char(Params p, int irk) {
     __shared__ int qn;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + ty * TX;
     const int slot = irk - 1;
-    if (DIR == 0 && blockIdx.x == 0 && blockIdx.y == 0 && tid == 0) stage_scalars(p, irk);
+    if (DIR == 0 && bx == 0 && by == 0 && tid == 0) stage_scalars(p, irk);
     const double lam = p.sc->maxeig[slot][DIR];
     const int NIp = p.ni + 2 * kB, NJp = p.nj + 2 * kB;
     const double g1 = p.gamma - 1.0, kg = p.gamma / (p.gamma - 1.0);
@@ -554,14 +554,14 @@ __global__ void __launch_bounds__(TX* TY) k_flux_char(Params p, int irk) {
         for (int v = 0; v < 4; ++v) { sF[v][r][c] = fp[v]; sF[4 + v][r][c] = fm[v]; sQ[v][r][c] = q[v]; }
     };
     if (DIR == 0) {
-        const int f0 = blockIdx.x * TX, j = blockIdx.y * TY + ty;
+        const int f0 = bx * TX, j = by * TY + ty;
         if (j < p.nj)
             for (int k = tx; k < TX + 5; k += TX) {
                 const int I = f0 + 1 + k;
                 if (I < NIp) cell(I, j + kB, ty, k);
             }
     } else {
-        const int g0 = blockIdx.y * TY, i = blockIdx.x * TX + tx;
+        const int g0 = by * TY, i = bx * TX + tx;
         if (i < p.ni)
             for (int k = ty; k < TY + 5; k += TY) {
                 const int J = g0 + 1 + k;
@@ -571,8 +571,8 @@ __global__ void __launch_bounds__(TX* TY) k_flux_char(Params p, int irk) {
     __syncthreads();
 
     int line, f;
-    if (DIR == 0) { line = blockIdx.y * TY + ty; f = blockIdx.x * TX + tx; }
-    else          { line = blockIdx.x * TX + tx; f = blockIdx.y * TY + ty; }
+    if (DIR == 0) { line = by * TY + ty; f = bx * TX + tx; }
+    else          { line = bx * TX + tx; f = by * TY + ty; }
     const int nline = DIR == 0 ? p.nj : p.ni, nface = DIR == 0 ? p.ni + 1 : p.nj + 1;
     const bool valid = line < nline && f < nface;
     // tile accessors for the interface at tile position (ox, oy); k runs along the sweep
@@ -822,8 +822,8 @@ __device__ __forceinline__ void prim_cell(const Params& p, long long o, const do
         flags |= DENSE_FLAG_NAN;
 }
 
-__global__ void k_prim(Params p, int slot) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+__device__ __forceinline__ void prim_block(const Params& p, int slot, int bx, int by) {
+    const int i = bx * blockDim.x + threadIdx.x, j = by * blockDim.y + threadIdx.y;
     double e1 = 0.0, e2 = 0.0;
     unsigned flags = 0;
     if (i < p.ni && j < p.nj) {
@@ -841,9 +841,9 @@ __global__ void k_prim(Params p, int slot) {
 // state for the next stage. Body force of Rayleigh-Taylor: S = (0, 0, rho, rho v) of the stage
 // input (boundary_rt_general.f90:154-155), added after the combine as a separate rounding.
 template <int IRK>
-__global__ void k_update(Params p) {
+__device__ __forceinline__ void update_block(const Params& p, int bx, int by) {
     if (!p.sc->active) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int i = bx * blockDim.x + threadIdx.x, j = by * blockDim.y + threadIdx.y;
     double e1 = 0.0, e2 = 0.0;
     unsigned flags = 0;
     if (i < p.ni && j < p.nj) {
@@ -955,9 +955,9 @@ __device__ __forceinline__ Rule side_rule(int bench, int side) {
     }
 }
 
-__global__ void k_bc(Params p) {
+__device__ __forceinline__ void bc_block(const Params& p, int bx) {
     if (!p.sc->active) return;
-    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int tid = bx * blockDim.x + threadIdx.x;
     const int ni = p.ni, nj = p.nj;
     int side, line;
     if (tid < ni) { side = kBottom; line = tid; }
@@ -1081,18 +1081,70 @@ __global__ void k_bc(Params p) {
 }
 
 // ---------------------------------------------------------------------------------------------
+// Kernels of one block (instance) of the solver: block coordinates are the launch's own.
+template <int DIR, int SPL, int REC, int TX, int TY>
+__global__ void __launch_bounds__(TX* TY) k_flux_cw(Params p, int irk) {
+    flux_cw_block<DIR, SPL, REC, TX, TY>(p, irk, blockIdx.x, blockIdx.y);
+}
+template <int DIR, bool ADAPT, int TX, int TY>
+__global__ void __launch_bounds__(TX* TY) k_flux_char(Params p, int irk) {
+    flux_char_block<DIR, ADAPT, TX, TY>(p, irk, blockIdx.x, blockIdx.y);
+}
+__global__ void k_prim(Params p, int slot) { prim_block(p, slot, blockIdx.x, blockIdx.y); }
+template <int IRK>
+__global__ void k_update(Params p) { update_block<IRK>(p, blockIdx.x, blockIdx.y); }
+__global__ void k_bc(Params p) { bc_block(p, blockIdx.x); }
+
+// Batched kernels: one launch covers every instance of a batch. Block b works on instance
+// map[b].x at block coordinates (map[b].y, map[b].z) of that instance's own grid, with the
+// instance's parameters staged in shared memory; the per-block code is the single-instance
+// code, so each instance's arithmetic -- and result -- is the same as a plain solve's.
+#define DENSE_BATCH_PROLOGUE                                                 \
+    __shared__ Params sp;                                                    \
+    const int3 m = map[blockIdx.x];                                          \
+    if (threadIdx.x == 0 && threadIdx.y == 0) sp = tab[m.x];                 \
+    __syncthreads();
+
+template <int DIR, int SPL, int REC, int TX, int TY>
+__global__ void __launch_bounds__(TX* TY) kb_flux_cw(const Params* tab, const int3* map, int irk) {
+    DENSE_BATCH_PROLOGUE
+    flux_cw_block<DIR, SPL, REC, TX, TY>(sp, irk, m.y, m.z);
+}
+template <int DIR, bool ADAPT, int TX, int TY>
+__global__ void __launch_bounds__(TX* TY) kb_flux_char(const Params* tab, const int3* map, int irk) {
+    DENSE_BATCH_PROLOGUE
+    flux_char_block<DIR, ADAPT, TX, TY>(sp, irk, m.y, m.z);
+}
+__global__ void kb_prim(const Params* tab, const int3* map, int slot) {
+    DENSE_BATCH_PROLOGUE
+    prim_block(sp, slot, m.y, m.z);
+}
+template <int IRK>
+__global__ void kb_update(const Params* tab, const int3* map) {
+    DENSE_BATCH_PROLOGUE
+    update_block<IRK>(sp, m.y, m.z);
+}
+__global__ void kb_bc(const Params* tab, const int3* map) {
+    DENSE_BATCH_PROLOGUE
+    bc_block(sp, m.y);
+}
+#undef DENSE_BATCH_PROLOGUE
+
+// ---------------------------------------------------------------------------------------------
 // Step bookkeeping (general_main.f90:23-37): the while-condition at the start of a step and the
 // time/step advance at its end.
-__global__ void k_step_begin(Scalars* sc) {
+__device__ __forceinline__ void k_step_begin_body(Scalars* sc) {
     sc->active = (sc->t < sc->t_end) && (sc->step < sc->total_step);
 }
-__global__ void k_step_end(Scalars* sc) {
+__device__ __forceinline__ void k_step_end_body(Scalars* sc) {
     if (sc->active) {
         sc->step += 1;
         sc->t = sc->t + sc->dt;
         sc->elasp = sc->elasp + sc->dt;
     }
 }
+__global__ void k_step_begin(Scalars* sc) { k_step_begin_body(sc); }
+__global__ void k_step_end(Scalars* sc) { k_step_end_body(sc); }
 
 // ---------------------------------------------------------------------------------------------
 // Launchers
@@ -1165,7 +1217,108 @@ static void launch_update(const Params& p, int irk, void* stream) {
 static void launch_step_begin(const Params& p, void* stream) { k_step_begin<<<1, 1, 0, (cudaStream_t)stream>>>(p.sc); }
 static void launch_step_end(const Params& p, void* stream) { k_step_end<<<1, 1, 0, (cudaStream_t)stream>>>(p.sc); }
 
+// ---------------------------------------------------------------------------------------------
+// Batched launchers
+__global__ void kb_step_begin(const Params* tab, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) k_step_begin_body(tab[i].sc);
+}
+__global__ void kb_step_end(const Params* tab, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) k_step_end_body(tab[i].sc);
+}
+
+static inline const int3* as_map(const void* m) { return (const int3*)m; }
+
+template <int SPL, int REC, int XTX, int XTY, int ETX, int ETY>
+static void batch_cw(const BatchLaunch& b, int irk, int dir, cudaStream_t s) {
+    if (dir == 0) kb_flux_cw<0, SPL, REC, XTX, XTY><<<b.nb_xi, dim3(XTX, XTY), 0, s>>>(b.tab, as_map(b.map_xi), irk);
+    else          kb_flux_cw<1, SPL, REC, ETX, ETY><<<b.nb_eta, dim3(ETX, ETY), 0, s>>>(b.tab, as_map(b.map_eta), irk);
+}
+// xi tiles: (32,4) (64,2) (32,8); eta tiles: (32,8) (32,4) (64,4)
+template <int SPL, int REC>
+static void batch_cw_variant(const BatchLaunch& b, int irk, int dir, cudaStream_t s) {
+    const int v = dir == 0 ? b.xi_variant : b.eta_variant;
+    if (dir == 0) {
+        if (v == 1) batch_cw<SPL, REC, 64, 2, 32, 8>(b, irk, 0, s);
+        else if (v == 2) batch_cw<SPL, REC, 32, 8, 32, 8>(b, irk, 0, s);
+        else batch_cw<SPL, REC, 32, 4, 32, 8>(b, irk, 0, s);
+    } else {
+        if (v == 1) batch_cw<SPL, REC, 32, 4, 32, 4>(b, irk, 1, s);
+        else if (v == 2) batch_cw<SPL, REC, 32, 4, 64, 4>(b, irk, 1, s);
+        else batch_cw<SPL, REC, 32, 4, 32, 8>(b, irk, 1, s);
+    }
+}
+
+static void batch_flux(const BatchLaunch& b, int irk, int dir, void* stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    switch (b.splitting) {
+    case DENSE_SPLIT_LLF: case DENSE_SPLIT_GLF: case DENSE_SPLIT_SW: {
+        const int spl = b.splitting == DENSE_SPLIT_SW ? 1 : 0;
+        if (b.recon == DENSE_RECON_UPWIND5) { spl ? batch_cw_variant<1, 251>(b, irk, dir, s) : batch_cw_variant<0, 251>(b, irk, dir, s); }
+        else if (b.recon == DENSE_RECON_WENOJS5) { spl ? batch_cw_variant<1, 253>(b, irk, dir, s) : batch_cw_variant<0, 253>(b, irk, dir, s); }
+        else if (b.recon == DENSE_RECON_WENOZ5) { spl ? batch_cw_variant<1, 255>(b, irk, dir, s) : batch_cw_variant<0, 255>(b, irk, dir, s); }
+        break;  // unknown reconstruction: rejected when the batch is created
+    }
+    case DENSE_SPLIT_CH:
+        if (dir == 0) kb_flux_char<0, false, kXTX, kXTY><<<b.nb_xi, dim3(kXTX, kXTY), 0, s>>>(b.tab, as_map(b.map_xi), irk);
+        else          kb_flux_char<1, false, kETX, kETY><<<b.nb_eta, dim3(kETX, kETY), 0, s>>>(b.tab, as_map(b.map_eta), irk);
+        break;
+    case DENSE_SPLIT_SC:
+        if (dir == 0) kb_flux_char<0, true, kXTX, kXTY><<<b.nb_xi, dim3(kXTX, kXTY), 0, s>>>(b.tab, as_map(b.map_xi), irk);
+        else          kb_flux_char<1, true, kETX, kETY_ADAPT><<<b.nb_eta, dim3(kETX, kETY_ADAPT), 0, s>>>(b.tab, as_map(b.map_eta), irk);
+        break;
+    default:
+        break;
+    }
+}
+static void batch_prim(const BatchLaunch& b, int slot, void* stream) {
+    kb_prim<<<b.nb_cells, dim3(32, 8), 0, (cudaStream_t)stream>>>(b.tab, as_map(b.map_cells), slot);
+}
+static void batch_bc(const BatchLaunch& b, void* stream) {
+    kb_bc<<<b.nb_bc, 128, 0, (cudaStream_t)stream>>>(b.tab, as_map(b.map_bc));
+}
+static void batch_update(const BatchLaunch& b, int irk, void* stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    if (irk == 1) kb_update<1><<<b.nb_cells, dim3(32, 8), 0, s>>>(b.tab, as_map(b.map_cells));
+    else if (irk == 2) kb_update<2><<<b.nb_cells, dim3(32, 8), 0, s>>>(b.tab, as_map(b.map_cells));
+    else kb_update<3><<<b.nb_cells, dim3(32, 8), 0, s>>>(b.tab, as_map(b.map_cells));
+}
+static void batch_step_begin(const BatchLaunch& b, void* stream) {
+    kb_step_begin<<<(b.n + 127) / 128, 128, 0, (cudaStream_t)stream>>>(b.tab, b.n);
+}
+static void batch_step_end(const BatchLaunch& b, void* stream) {
+    kb_step_end<<<(b.n + 127) / 128, 128, 0, (cudaStream_t)stream>>>(b.tab, b.n);
+}
+
 }  // namespace VNS
+
+#if DENSE_VARIANT_STRICT
+const BatchKernelTable* batch_kernels_strict() {
+    static const BatchKernelTable t = {VNS::batch_prim, VNS::batch_bc, VNS::batch_flux, VNS::batch_update,
+                                       VNS::batch_step_begin, VNS::batch_step_end};
+    return &t;
+}
+#else
+const BatchKernelTable* batch_kernels_fast() {
+    static const BatchKernelTable t = {VNS::batch_prim, VNS::batch_bc, VNS::batch_flux, VNS::batch_update,
+                                       VNS::batch_step_begin, VNS::batch_step_end};
+    return &t;
+}
+// Tile shapes of the batched sweeps (the shapes instantiated above).
+void batch_tile_shape(int splitting, int dir, int variant, int* tx, int* ty) {
+    if (splitting == DENSE_SPLIT_CH || splitting == DENSE_SPLIT_SC) {
+        *tx = 32;
+        *ty = dir == 0 ? 4 : (splitting == DENSE_SPLIT_SC ? 6 : 8);
+        return;
+    }
+    static const int xi[kTileVariants][2] = {{32, 4}, {64, 2}, {32, 8}};
+    static const int eta[kTileVariants][2] = {{32, 8}, {32, 4}, {64, 4}};
+    const int v = variant < 0 || variant >= kTileVariants ? 0 : variant;
+    *tx = dir == 0 ? xi[v][0] : eta[v][0];
+    *ty = dir == 0 ? xi[v][1] : eta[v][1];
+}
+#endif
 
 #if DENSE_VARIANT_STRICT
 const KernelTable* kernels_strict() {

@@ -159,10 +159,102 @@ class Solver:
         self.current_time = self.current_time + self.dt
 
     def steps(self, n: int, t_end: float = float("inf"), total_step: int = 2**31 - 1):
-        """Up to n steps on the device while current_time < t_end and current_step < total_step."""
+        """Up to n steps on the device while current_time < t_end and current_step < total_step.
+        Rejects nothing the reference would accept; stops like general_main.f90:23."""
         t = ctypes.c_double(self.current_time)
         s = ctypes.c_int(self.current_step)
         dt = ctypes.c_double(self.dt)
         self._chk(self.lib.dense_steps(self.h, n, t_end, total_step, ctypes.byref(t),
                                        ctypes.byref(s), ctypes.byref(dt)))
         self.current_time, self.current_step, self.dt = t.value, s.value, dt.value
+
+
+class BatchSolver:
+    """Many independent blocks of uneven size advanced together (the batched form).
+
+    Every instance has its own configuration, CFL time step, time and step count; all share the
+    splitting, reconstruction and kernel variant. One launch per phase covers the whole batch and
+    one CUDA graph covers a step; each instance's results equal a plain ``Solver`` run's."""
+
+    def __init__(self, cfgs):
+        self.lib = _abi.load_library()
+        self.cfgs = [c.copy() for c in cfgs]
+        arr = (DenseConfig * len(cfgs))(*self.cfgs)
+        h = ctypes.c_void_p()
+        rc = self.lib.dense_batch_create(len(cfgs), arr, ctypes.byref(h))
+        if rc:
+            raise DenseError(rc, self.lib.dense_batch_last_error(None).decode())
+        self.h = h
+        self.n = len(cfgs)
+
+    def _chk(self, rc):
+        if rc:
+            raise DenseError(rc, self.lib.dense_batch_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.dense_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def upload(self, i: int, cons, prim=None, x=None, y=None):
+        arrs = [None if a is None else np.asfortranarray(a, dtype=np.float64) for a in (cons, prim, x, y)]
+        self._chk(self.lib.dense_batch_upload(self.h, i, *[_ptr(a) for a in arrs]))
+
+    def download(self, i: int, with_prim: bool = False):
+        c = self.cfgs[i]
+        cons = np.zeros((c.ni + 8, c.nj + 8, 4), order="F")
+        prim = np.zeros((c.ni + 8, c.nj + 8, 6), order="F") if with_prim else None
+        self._chk(self.lib.dense_batch_download(self.h, i, _ptr(cons), _ptr(prim)))
+        return (cons, prim) if with_prim else cons
+
+    def set_time(self, i: int, t: float, step: int = 0):
+        self._chk(self.lib.dense_batch_set_time(self.h, i, t, step))
+
+    def time(self, i: int):
+        t, s, dt = ctypes.c_double(), ctypes.c_int(), ctypes.c_double()
+        self._chk(self.lib.dense_batch_get_time(self.h, i, ctypes.byref(t), ctypes.byref(s), ctypes.byref(dt)))
+        return t.value, s.value, dt.value
+
+    def steps(self, n: int, t_end: float = float("inf"), total_step: int = 2**31 - 1, wait: bool = True):
+        fn = self.lib.dense_batch_steps if wait else self.lib.dense_batch_steps_async
+        self._chk(fn(self.h, n, t_end, total_step))
+
+    def set_schedule(self, xi_variant: int, eta_variant: int, order: int):
+        self._chk(self.lib.dense_batch_set_schedule(self.h, xi_variant, eta_variant, order))
+
+    def stream(self) -> int:
+        s = ctypes.c_void_p()
+        self._chk(self.lib.dense_batch_get_stream(self.h, ctypes.byref(s)))
+        return s.value or 0
+
+    def status(self) -> int:
+        f = ctypes.c_uint()
+        self._chk(self.lib.dense_batch_status(self.h, ctypes.byref(f)))
+        return f.value
+
+    def cells(self) -> int:
+        return int(self.lib.dense_batch_cells(self.h))
+
+    def launch_count(self) -> int:
+        return int(self.lib.dense_batch_launch_count(self.h))
+
+    @classmethod
+    def from_setups(cls, cfgs) -> "BatchSolver":
+        """init_general for every instance, then upload: the batch as the setups leave it."""
+        setups = [init_general(c) for c in cfgs]
+        b = cls([s[0] for s in setups])
+        for i, (c, cons, prim, x, y) in enumerate(setups):
+            b.upload(i, cons, prim, x, y)
+        return b

@@ -174,13 +174,118 @@ def run_reference_arm(args, wl):
     print(json.dumps(line), flush=True)
 
 
+def batched_configs(dense, n: int = 512, seed: int = 2024):
+    """The batched workload: n square periodic instances, N drawn uniformly from
+    {64, 96, ..., 512}; even instances a translating vortex with strength U[1,5] and centre
+    offset U[-1,1]^2, odd ones a Mach 1.2 shock into a density-3 interface of amplitude
+    U[0.01,0.05]; LLF + WENO-Z5, CFL 0.5, each with its own CFL time step."""
+    rng = np.random.default_rng(seed)
+    sizes = list(range(64, 513, 32))
+    cfgs = []
+    for k in range(n):
+        N = int(rng.choice(sizes))
+        if k % 2 == 0:
+            cfgs.append(dense.config_default(ni=N, nj=N, benchmark=11, splitting=101, recon=255, cfl=0.5,
+                                             var_eps=float(rng.uniform(1, 5)),
+                                             var_xc=5 + float(rng.uniform(-1, 1)),
+                                             var_yc=5 + float(rng.uniform(-1, 1))))
+        else:
+            cfgs.append(dense.config_default(ni=N, nj=N, benchmark=14, splitting=101, recon=255, cfl=0.5,
+                                             var_amp=float(rng.uniform(0.01, 0.05))))
+    return cfgs
+
+
+def run_batched(args, dense, lib):
+    """Batched form vs looped plain solves of the same instances on the same GPU."""
+    import torch
+    at = importlib.import_module("2dense_gb300.autotune")
+    n = args.batch
+    cfgs = batched_configs(dense, n, seed=args.seed)
+    setups = [dense.init_general(c) for c in cfgs]
+    cfgs = [s[0] for s in setups]
+    cells = sum(c.ni * c.nj for c in cfgs)
+    sched, info = at.tune(cfgs, setups=setups, steps=2, reps=2)
+    b = dense.BatchSolver(cfgs)
+    for i, (c, cons, prim, x, y) in enumerate(setups):
+        b.upload(i, cons, prim, x, y)
+    b.set_schedule(*sched)
+    b.steps(args.warmup)
+    stream = torch.cuda.ExternalStream(b.stream())
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = b.launch_count()
+    torch.cuda.synchronize()
+    wall0 = time.perf_counter()
+    with Clocks(0) as clk:
+        ev0.record(stream)
+        b.steps(args.steps, wait=False)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    ms = ev0.elapsed_time(ev1)
+    launches = b.launch_count() - launches0
+    value = cells * args.steps / (ms * 1e-3)
+    # identical results: sampled instances against plain solves of the same total steps
+    total = args.warmup + args.steps
+    picks = sorted(set([0, 1, n // 2, n - 1]))
+    same = 0
+    for i in picks:
+        c, cons, prim, x, y = setups[i]
+        with dense.Solver(c) as s:
+            s.upload(cons, prim, x, y)
+            s.steps(total)
+            if np.array_equal(s.download(False), b.download(i)):
+                same += 1
+    status = b.status()
+    b.close()
+    # looped plain solves: one handle per instance, each advanced in turn
+    loop_steps = max(1, min(args.steps, args.loop_steps))
+    solvers = []
+    for (c, cons, prim, x, y) in setups:
+        s = dense.Solver(c)
+        s.upload(cons, prim, x, y)
+        s.steps(1)
+        solvers.append(s)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s in solvers:
+        s.steps(loop_steps)
+    loop_s = time.perf_counter() - t0
+    for s in solvers:
+        s.close()
+    looped = cells * loop_steps / loop_s
+    fl = json.load(open(os.path.join(ROOT, "tests", "golden", "flop_counts.json")))["schemes"]["LLF+WENO-Z5"]
+    peak = ctypes.c_double()
+    lib.dense_measure_fp64(0, ctypes.byref(peak))
+    sizes = sorted(c.ni for c in cfgs)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"batched: {n} periodic instances, N in 64..512 (seed {args.seed}), "
+                                   "vortex / Richtmyer-Meshkov, LLF + WENO-Z5, CFL 0.5",
+                       "instances": n, "cells": cells, "n_min": sizes[0], "n_max": sizes[-1],
+                       "l2": "inputs larger than L2 (about 1.7 GB per state copy)"},
+            "batched": {"schedule": {"xi_variant": sched[0], "eta_variant": sched[1], "order": sched[2]},
+                        "autotune": {"cached": info["cached"], "trials_s": info["trials"]}},
+            "looped_plain": {"value": looped, "unit": UNIT, "steps_per_instance": loop_steps,
+                             "api": "one dense_create handle per instance, dense_steps in turn"},
+            "speedup_vs_looped": value / looped,
+            "identical_results": {"checked": len(picks), "bitwise_equal": same},
+            "gpu_launches": launches,
+            "roofline": {"bound": "fp64", "achieved": fl["flops_per_cell_update"] * value / 1e12,
+                         "peak": peak.value / 1e12, "unit": "TFLOP/s",
+                         "frac": fl["flops_per_cell_update"] * value / peak.value,
+                         "flops_per_cell_update": fl["flops_per_cell_update"], "traffic": None},
+            "clocks": clk.summary(), "status_flags": status, "wall_s_timed_region": wall}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="dmr", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="dmr", choices=sorted(WORKLOADS) + ["batched"])
     ap.add_argument("--strict", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--cpu-steps", type=int, default=20)
@@ -190,7 +295,21 @@ def main():
                     help="flow time the timed steps start from (default: 0.1 for dmr, 0 otherwise)")
     ap.add_argument("--save-state", default="", help="write the start state (npz) before warm-up")
     ap.add_argument("--load-state", default="", help="start from a state written by --save-state")
+    ap.add_argument("--batch", type=int, default=512, help="instances of the batched workload")
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--loop-steps", type=int, default=10, help="steps per instance of the looped plain solves")
     args = ap.parse_args()
+    if args.workload == "batched":
+        if args.impl == "reference":
+            rank, _, _ = dist_info()
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "the reference advances one block per "
+                                  "process; it has no batched form to time"}))
+            return
+        import torch
+        torch.cuda.set_device(0)
+        dense = importlib.import_module("2dense_gb300")
+        return run_batched(args, dense, dense.load_library())
     wl = WORKLOADS[args.workload]
     if args.ni and args.nj:
         wl = wl[:3] + (args.ni, args.nj, wl[5].split(" ")[0] + f" {args.ni}x{args.nj} (reduced) "

@@ -229,6 +229,35 @@ int dense_measure_fp64(int kind, double* result);
    out[4k..4k+3] = (fast 1/x[k], IEEE 1/x[k], fast 1/sqrt(x[k]), IEEE 1/sqrt(x[k])). */
 int dense_fastmath_check(const double* x, double* out, int n);
 
+/* ---- batched form: many independent blocks of uneven size in one launch per phase ------- */
+
+/* The reference advances one block per process (num_block = 1, init_*_general.f90); the batched
+   form runs n independent blocks -- each its own dense_config_t (grid size, benchmark, gamma,
+   cfl) with its own CFL time step, time and step count -- through one launch per phase and one
+   CUDA graph per step. All instances share splitting, recon and strict. Each instance's results
+   are bit-identical to a plain dense_create/dense_steps solve of the same configuration. */
+typedef struct dense_batch dense_batch_t;
+int dense_batch_create(int n, const dense_config_t* cfgs, dense_batch_t** out);
+void dense_batch_destroy(dense_batch_t* b);
+/* instance i's state in the layout of dense_upload / dense_download */
+int dense_batch_upload(dense_batch_t* b, int i, const double* cons, const double* prim,
+                       const double* x, const double* y);
+int dense_batch_download(dense_batch_t* b, int i, double* cons, double* prim);
+int dense_batch_set_time(dense_batch_t* b, int i, double t, int step);
+int dense_batch_get_time(dense_batch_t* b, int i, double* t, int* step, double* dt);
+/* up to nsteps steps of every instance, each while its t < t_end and step < total_step;
+   the _async form does not wait */
+int dense_batch_steps(dense_batch_t* b, int nsteps, double t_end, int total_step);
+int dense_batch_steps_async(dense_batch_t* b, int nsteps, double t_end, int total_step);
+/* launch schedule (picked by the autotuner): tile shape variants of the xi and eta sweeps
+   (0..2) and the block order (0 instance-major, 1 largest instance first, 2 round-robin) */
+int dense_batch_set_schedule(dense_batch_t* b, int xi_variant, int eta_variant, int order);
+int dense_batch_get_stream(dense_batch_t* b, void** stream);
+int dense_batch_status(dense_batch_t* b, unsigned* flags);
+long long dense_batch_launch_count(dense_batch_t* b);
+long long dense_batch_cells(dense_batch_t* b);
+const char* dense_batch_last_error(dense_batch_t* b);
+
 /* ---- one stage without any device allocation ------------------------------------------- */
 
 /* No counterpart in the reference: an addition for callers that cannot let the library

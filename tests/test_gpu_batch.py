@@ -1,0 +1,96 @@
+"""The batched form against plain solves: every instance of a batch -- uneven sizes, different
+benchmarks, vortex strengths and interface amplitudes, each with its own CFL time step -- must
+equal the single-instance solve of the same configuration bit for bit, for every launch
+schedule the autotuner can pick."""
+import importlib
+
+import numpy as np
+import pytest
+
+from conftest import interior
+
+pytestmark = pytest.mark.gpu
+
+
+def batch_cfgs(dense, split, recon, sizes, seed=5, strict=0):
+    rng = np.random.default_rng(seed)
+    cfgs = []
+    for k, (ni, nj) in enumerate(sizes):
+        if k % 2 == 0:  # translating vortex, strength and centre drawn per instance
+            cfgs.append(dense.config_default(ni=ni, nj=nj, benchmark=11, splitting=split, recon=recon,
+                                             cfl=0.5, strict=strict, var_eps=rng.uniform(1, 5),
+                                             var_xc=5 + rng.uniform(-1, 1), var_yc=5 + rng.uniform(-1, 1)))
+        else:  # periodic Richtmyer-Meshkov, interface amplitude drawn per instance
+            cfgs.append(dense.config_default(ni=ni, nj=nj, benchmark=14, splitting=split, recon=recon,
+                                             cfl=0.5, strict=strict, var_amp=rng.uniform(0.01, 0.05)))
+    return cfgs
+
+
+SIZES = [(40, 40), (24, 36), (64, 64), (17, 29), (33, 33), (48, 20)]
+
+
+def plain(dense, cfg, nsteps, t_end=float("inf")):
+    c, cons, prim, x, y = dense.init_general(cfg)
+    with dense.Solver(c) as s:
+        s.upload(cons, prim, x, y)
+        s.steps(nsteps, t_end=t_end)
+        return s.download(False), s.current_time, s.current_step, s.dt
+
+
+@pytest.mark.parametrize("split,recon", [(101, 255), (101, 253), (103, 251), (104, 0), (105, 0)])
+def test_batch_equals_plain_solves(dense, split, recon):
+    cfgs = batch_cfgs(dense, split, recon, SIZES)
+    with dense.BatchSolver.from_setups(cfgs) as b:
+        b.steps(3)
+        for i, cfg in enumerate(cfgs):
+            ref, t, step, dt = plain(dense, cfg, 3)
+            got = b.download(i)
+            np.testing.assert_array_equal(interior(got), interior(ref), err_msg=f"instance {i}")
+            bt, bs, bdt = b.time(i)
+            assert (bt, bs, bdt) == (t, step, dt)
+
+
+def test_every_schedule_gives_the_same_bits(dense):
+    cfgs = batch_cfgs(dense, 101, 255, SIZES, seed=9)
+    ref = None
+    for sched in [(0, 0, 0), (1, 2, 1), (2, 1, 2), (1, 1, 0), (2, 2, 1)]:
+        with dense.BatchSolver.from_setups(cfgs) as b:
+            b.set_schedule(*sched)
+            b.steps(2)
+            out = [b.download(i) for i in range(len(cfgs))]
+        if ref is None:
+            ref = out
+        for i in range(len(cfgs)):
+            np.testing.assert_array_equal(out[i], ref[i], err_msg=f"schedule {sched} instance {i}")
+
+
+def test_per_instance_time_bounds(dense):
+    """Each instance stops at its own step count: the loop bound is per instance, its dt its own."""
+    cfgs = batch_cfgs(dense, 101, 255, SIZES[:4], seed=2)
+    t_end = 0.05
+    with dense.BatchSolver.from_setups(cfgs) as b:
+        b.steps(500, t_end=t_end)
+        for i, cfg in enumerate(cfgs):
+            ref, t, step, dt = plain(dense, cfg, 500, t_end=t_end)
+            np.testing.assert_array_equal(interior(b.download(i)), interior(ref))
+            assert b.time(i)[:2] == (t, step)
+
+
+def test_strict_batch_matches_oracle(dense, orc):
+    cfgs = batch_cfgs(dense, 101, 255, SIZES[:3], seed=4, strict=1)
+    with dense.BatchSolver.from_setups(cfgs) as b:
+        b.steps(2)
+        for i, cfg in enumerate(cfgs):
+            o = orc.OracleSolver(cfg)
+            o.steps(2)
+            np.testing.assert_array_equal(interior(b.download(i)), interior(o.get_state()[0]))
+
+
+def test_autotuner_picks_a_valid_schedule(dense, tmp_path, monkeypatch):
+    monkeypatch.setenv("DENSE2D_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    at = importlib.reload(importlib.import_module("2dense_gb300.autotune"))
+    cfgs = batch_cfgs(dense, 101, 255, SIZES, seed=1)
+    best, info = at.tune(cfgs, steps=1, reps=1)
+    assert len(best) == 3 and not info["cached"] and len(info["trials"]) >= 3
+    best2, info2 = at.tune(cfgs)
+    assert best2 == best and info2["cached"]
