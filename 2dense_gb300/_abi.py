@@ -191,6 +191,15 @@ def load_library(path: str | None = None):
         "dense_count_branches": (_c_int, [vp, _c_int]),
         "dense_get_branch_counts": (_c_int, [vp, ctypes.POINTER(ctypes.c_ulonglong)]),
         "dense_stage_noalloc": (_c_int, [cfgp, _c_int, _c_double, vp, vp, vp, vp, vp, vp, dp, vp]),
+        "dense_adjoint_create": (_c_int, [cfgp, _c_int, ctypes.POINTER(vp)]),
+        "dense_adjoint_destroy": (None, [vp]),
+        "dense_adjoint_forward": (_c_int, [vp, vp, _c_int, vp, vp]),
+        "dense_adjoint_backward": (_c_int, [vp, vp, vp, vp]),
+        "dense_adjoint_rhs_vjp": (_c_int, [vp, vp, vp, vp, dp, vp]),
+        "dense_adjoint_get_dts": (_c_int, [vp, dp, _c_int]),
+        "dense_adjoint_get_argmax": (_c_int, [vp, ctypes.POINTER(_c_int), _c_int]),
+        "dense_adjoint_launch_count": (ctypes.c_longlong, [vp]),
+        "dense_adjoint_last_error": (ctypes.c_char_p, [vp]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)

@@ -4,6 +4,9 @@ Translation units, compiled in parallel:
   kernels.cu  twice: -DDENSE_VARIANT_STRICT=0 (fast: FMA contraction) and
               -DDENSE_VARIANT_STRICT=1 -fmad=false (strict: the reference's rounding)
   capi.cu     the C ABI (handles, graphs, copies)
+  batch.cu    the batched form (many blocks per launch)
+  adjoint.cu  the discrete adjoint of the time step
+  noalloc.cu, probe.cu  the allocation-free stage and the FP64 throughput probes
   host_setup.cpp  namelist reader and initial setups, g++ -ffp-contract=off so the initial
               state rounds exactly like the reference's gfortran -O2 build on x86-64
 The ptxas resource report of each kernel (registers, spills, shared memory) is written to
@@ -64,6 +67,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         "probe": [nvcc, *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, "probe.cu")],
         "noalloc": [nvcc, *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, "noalloc.cu")],
         "batch": [nvcc, *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, "batch.cu")],
+        "adjoint": [nvcc, *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, "adjoint.cu")],
         "host_setup": ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-c",
                        os.path.join(CSRC, "host_setup.cpp")],
     }

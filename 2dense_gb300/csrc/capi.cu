@@ -9,7 +9,7 @@
 #include <string>
 #include <vector>
 
-#include "internal.h"
+#include "handle.h"
 
 extern "C" const char* dense_host_last_error(void);
 
@@ -17,25 +17,6 @@ using dense::KernelTable;
 using dense::Params;
 using dense::Scalars;
 using dense::kB;
-
-struct dense_handle {
-    dense_config_t cfg;
-    const KernelTable* kt = nullptr;
-    cudaStream_t stream = nullptr;
-    int device = 0;
-    double *cons = nullptr, *prim = nullptr, *cons0 = nullptr, *hx = nullptr, *he = nullptr;
-    double *xbot = nullptr, *xtop = nullptr, *yleft = nullptr;
-    Scalars* sc = nullptr;
-    Params prm{};
-    int NIp = 0, NJp = 0, P = 0;
-    bool uploaded = false;
-    int prim_slot = -1;  // stage slot whose max wave speeds match the current state, or -1
-    cudaGraphExec_t step_graph = nullptr;
-    int graph_nodes = 0;
-    long long launches = 0;
-    int count_branches = 0;
-    std::string err;
-};
 
 namespace {
 
@@ -163,6 +144,10 @@ int build_step_graph(dense_handle* h) {
 }
 
 }  // namespace
+
+int dense::handle_ensure_prim(dense_handle* h, int slot) { return ensure_prim(h, slot); }
+int dense::handle_step_graph(dense_handle* h) { return build_step_graph(h); }
+int dense::handle_stage_launches(dense_handle* h) { return stage_launches(h); }
 
 extern "C" {
 

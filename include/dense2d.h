@@ -258,6 +258,38 @@ long long dense_batch_launch_count(dense_batch_t* b);
 long long dense_batch_cells(dense_batch_t* b);
 const char* dense_batch_last_error(dense_batch_t* b);
 
+/* ---- discrete adjoint of the time step -------------------------------------------------- */
+
+/* No counterpart in the reference (it has no derivatives): the reverse mode of n steps of the
+   plain solver, for the LLF splitting (101) with upwind5, WENO-JS5 or WENO-Z5 (251/253/255) on
+   grids periodic in x and y (benchmarks 11 and 14), CFL or constant dt. States and gradients
+   are device arrays of the interior, u[4][nj][ni] (conserved variables, i fastest). The
+   forward runs the plain solver's kernels and keeps the state every `checkpoint_every` steps;
+   the reverse recomputes each segment from its checkpoint, storing the three stage states of
+   each step, and runs the adjoint kernels back through it. The time step's dependence on the
+   state (dt from the max wave speeds) is differentiated: its gradient goes to the cells where
+   the maxima are attained. `stream` is the caller's cudaStream_t (0 for the default stream):
+   each call starts after the work queued there and makes it wait for the call's work; the
+   call itself does not block the host. */
+typedef struct dense_adjoint dense_adjoint_t;
+int dense_adjoint_create(const dense_config_t* cfg, int checkpoint_every, dense_adjoint_t** out);
+void dense_adjoint_destroy(dense_adjoint_t* a);
+/* uT = the state after nsteps steps from u0; keeps the checkpoints for dense_adjoint_backward */
+int dense_adjoint_forward(dense_adjoint_t* a, const double* u0, int nsteps, double* uT, void* stream);
+/* g0 = (d uT / d u0)^T gT for the last forward */
+int dense_adjoint_backward(dense_adjoint_t* a, const double* gT, double* g0, void* stream);
+/* one right-hand side L(u) = -(dh_xi/dx + dh_eta/dy) (the operator each stage applies):
+   out = (dL/du)^T v at the state u; *vdotl = v . L(u) (host, the call waits) */
+int dense_adjoint_rhs_vjp(dense_adjoint_t* a, const double* u, const double* v, double* out,
+                          double* vdotl, void* stream);
+/* the time steps of the last forward, on the host (the call waits) */
+int dense_adjoint_get_dts(dense_adjoint_t* a, double* dts, int n);
+/* after dense_adjoint_backward: per step k, the interior cells j*ni+i where max(|u|+alpha) and
+   max(|v|+alpha) were attained (idx[2k], idx[2k+1]); -1 for constant dt (the call waits) */
+int dense_adjoint_get_argmax(dense_adjoint_t* a, int* idx, int n);
+long long dense_adjoint_launch_count(dense_adjoint_t* a);
+const char* dense_adjoint_last_error(dense_adjoint_t* a);
+
 /* ---- one stage without any device allocation ------------------------------------------- */
 
 /* No counterpart in the reference: an addition for callers that cannot let the library

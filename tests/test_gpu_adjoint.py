@@ -1,0 +1,119 @@
+"""The discrete adjoint against autograd through the pure-PyTorch reference step and against
+central finite differences of the CUDA forward."""
+import importlib
+
+import numpy as np
+import pytest
+import torch
+
+import torch_step
+from test_torch_step import to_state, vortex_cfg
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def adjoint(dense):
+    return importlib.import_module("2dense_gb300.adjoint")
+
+
+def rel(a, b):
+    return float((a - b).abs().max() / b.abs().max())
+
+
+def perturbed_state(dense, cfg, seed=0, amp=1e-3):
+    c, cons, prim, x, y = dense.init_general(cfg)
+    U = torch.from_numpy(to_state(cons)).cuda()
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    U[0] += amp * torch.randn(U.shape[1:], generator=g, dtype=torch.float64).cuda()
+    return c, U.contiguous()
+
+
+@pytest.mark.parametrize("recon", [251, 253, 255])
+def test_rhs_vjp_matches_autograd(dense, adjoint, recon):
+    cfg = vortex_cfg(dense, recon, ni=24, nj=20, var_eps=4.0, var_xc=4.6, var_yc=5.3)
+    c, U = perturbed_state(dense, cfg)
+    v = torch.randn(U.shape, generator=torch.Generator().manual_seed(1), dtype=torch.float64).cuda()
+    with adjoint.Adjoint(c) as adj:
+        out, vdotl = adj.rhs_vjp(U, v)
+    Ut = U.clone().requires_grad_(True)
+    L = torch_step.rhs(Ut, c.gamma, c.dx, c.dy, recon)
+    (ref,) = torch.autograd.grad(L, Ut, v)
+    L = L.detach()
+    # two evaluation orders of derivatives whose WENO weights scale like 1/(1e-6 + beta)^3
+    assert rel(out, ref) < 1e-10
+    assert abs(vdotl - float((v * L).sum())) < 1e-12 * float((v * L).abs().sum())
+
+
+@pytest.mark.parametrize("recon,const_dt", [(253, 0), (255, 0), (251, 0), (253, 1)])
+def test_steps_gradient_matches_autograd(dense, adjoint, recon, const_dt):
+    """7 steps with checkpoints every 3: two full segments and a partial one."""
+    cfg = vortex_cfg(dense, recon, ni=24, nj=20, var_eps=4.0, var_xc=4.6, var_yc=5.3,
+                     if_const_dt=const_dt, dt=0.02)
+    c, U = perturbed_state(dense, cfg)
+    gT = torch.randn(U.shape, generator=torch.Generator().manual_seed(2), dtype=torch.float64).cuda()
+    with adjoint.Adjoint(c, checkpoint_every=3) as adj:
+        uT = adj.forward(U, 7)
+        g0 = adj.backward(gT)
+        dts = adj.dts()
+    Ut = U.clone().requires_grad_(True)
+    ref_T = torch_step.run(Ut, 7, c.gamma, c.dx, c.dy, recon, c.cfl, c.dt if const_dt else None)
+    assert rel(uT, ref_T.detach()) < 1e-12
+    (ref,) = torch.autograd.grad(ref_T, Ut, gT)
+    assert rel(g0, ref) < 1e-10
+    assert np.all(dts > 0) and (not const_dt or np.all(dts == c.dt))
+
+
+def test_backward_is_deterministic_and_repeatable(dense, adjoint):
+    cfg = vortex_cfg(dense, 253, ni=40, nj=32)
+    c, U = perturbed_state(dense, cfg)
+    gT = torch.ones_like(U)
+    with adjoint.Adjoint(c, checkpoint_every=4) as adj:
+        adj.forward(U, 9)
+        a = adj.backward(gT)
+        b = adj.backward(gT)
+    assert torch.equal(a, b)
+
+
+def test_autograd_function_in_a_graph(dense, adjoint):
+    """Loss 1/2 ||rho(T) - rho_target||^2 of a vortex built from (eps, xc, yc) by torch ops:
+    autograd chains the vortex's derivatives with the adjoint; checked against central
+    differences of the CUDA forward, which must not change the cells of the wave-speed maxima
+    (the time step is not differentiable where they switch)."""
+    cfg = vortex_cfg(dense, 253, ni=48, nj=48, cfl=0.4)
+    c = dense.init_general(cfg)[0]
+    n, h = 30, 1e-6
+    with adjoint.Adjoint(c, checkpoint_every=8) as adj:
+        target = adj.forward(adjoint.vortex_state(c, 5.0, 5.0, 5.0), n)[0].clone()
+        theta = torch.tensor([4.8, 5.1, 4.9], dtype=torch.float64, device="cuda", requires_grad=True)
+
+        def loss_of(th):
+            uT = adjoint.AdjointStep.apply(adjoint.vortex_state(c, th[0], th[1], th[2]), adj, n)
+            return 0.5 * ((uT[0] - target) ** 2).sum()
+
+        loss = loss_of(theta)
+        loss.backward()
+        grad = theta.grad.detach().cpu().numpy()
+        am0 = adj.argmax().copy()
+        for k in range(3):
+            vals, traces = [], []
+            for s in (1, -1):
+                th = theta.detach().clone()
+                th[k] += s * h
+                th.requires_grad_(True)
+                lk = loss_of(th)
+                lk.backward()
+                vals.append(float(lk.detach()))
+                traces.append(adj.argmax().copy())
+            assert np.array_equal(traces[0], traces[1]) and np.array_equal(traces[0], am0)
+            fd = (vals[0] - vals[1]) / (2 * h)
+            assert abs(fd - grad[k]) <= 1e-6 * abs(grad[k]), (k, fd, grad[k])
+
+
+def test_rejects_unsupported_configurations(dense, adjoint):
+    for kw in (dict(splitting=104), dict(recon=0, splitting=105), dict(benchmark=5), dict(ni=6)):
+        cfg = dense.init_general(vortex_cfg(dense, 253))[0]
+        for k, v in kw.items():
+            setattr(cfg, k, v)
+        with pytest.raises(dense.DenseError):
+            adjoint.Adjoint(cfg)

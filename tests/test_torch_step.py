@@ -1,0 +1,53 @@
+"""The pure-PyTorch reference step (the autograd check of the adjoint) pinned on the CPU: its
+states against the oracle, its initial state against dense_init_setup, and its own autograd
+against finite differences."""
+import importlib
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import interior
+import torch_step
+
+
+def to_state(cons):
+    """Fortran cons(NIp, NJp, 4) -> interior (4, nj, ni)."""
+    return np.ascontiguousarray(interior(cons).transpose(2, 1, 0))
+
+
+def vortex_cfg(dense, recon, ni=24, nj=20, **kw):
+    base = dict(ni=ni, nj=nj, benchmark=11, splitting=101, recon=recon, cfl=0.4, var_eps=5.0,
+                var_xc=5.0, var_yc=5.0)
+    base.update(kw)
+    return dense.config_default(**base)
+
+
+@pytest.mark.parametrize("recon", [251, 253, 255])
+def test_torch_step_matches_oracle(dense, orc, recon):
+    cfg = vortex_cfg(dense, recon, var_eps=4.0, var_xc=4.6, var_yc=5.3)
+    c, cons, prim, x, y = dense.init_general(cfg)
+    o = orc.OracleSolver(c)
+    o.steps(3)
+    ref = to_state(o.get_state()[0])
+    U = torch.from_numpy(to_state(cons))
+    got = torch_step.run(U, 3, c.gamma, c.dx, c.dy, recon, c.cfl).numpy()
+    scale = np.abs(ref).max(axis=(1, 2), keepdims=True)
+    assert (np.abs(got - ref) / scale).max() < 1e-12
+
+
+def test_vortex_state_matches_setup(dense):
+    adjoint = importlib.import_module("2dense_gb300.adjoint")
+    cfg = vortex_cfg(dense, 253, var_eps=3.5, var_xc=4.2, var_yc=5.9)
+    c, cons, prim, x, y = dense.init_general(cfg)
+    got = adjoint.vortex_state(c, 3.5, 4.2, 5.9, device="cpu").numpy()
+    np.testing.assert_allclose(got, to_state(cons), rtol=1e-14, atol=1e-14)
+
+
+@pytest.mark.parametrize("recon", [253, 255])
+def test_torch_step_autograd_matches_finite_differences(dense, recon):
+    cfg = vortex_cfg(dense, recon, ni=8, nj=8)
+    c, cons, prim, x, y = dense.init_general(cfg)
+    U = torch.from_numpy(to_state(cons)).requires_grad_(True)
+    f = lambda U: torch_step.run(U, 2, c.gamma, c.dx, c.dy, recon, c.cfl)
+    assert torch.autograd.gradcheck(f, (U,), eps=1e-6, atol=1e-6, rtol=1e-5, fast_mode=True)

@@ -1,0 +1,89 @@
+"""Pure-PyTorch float64 reference of the time step on x- and y-periodic grids, for checking the
+adjoint kernels against autograd (test infrastructure; never used by the library).
+
+Same scheme as the plain solver: get_primary (get_primary.f90:53-60), LLF splitting with
+lambda = |u_n| + alpha per cell (flux_splitting_LLF.f90:67-81), upwind5 / WENO-JS5 / WENO-Z5
+reconstruction of F+ and F- at each face (scheme_*_general.f90, weno_mod.f90), the flux
+difference, and TVD-RK3 (time_advance_general.f90:9-267) with dt = cfl/(max(|u|+alpha)/dx +
+max(|v|+alpha)/dy) of the step's input (or a constant dt). States are (4, nj, ni) tensors of the
+interior; periodic neighbours come from torch.roll.
+"""
+from __future__ import annotations
+
+import torch
+
+SS = float(torch.tensor(1.0e-6, dtype=torch.float32))  # weno_mod.f90:37, a default-real literal
+C = (0.1, 0.6, 0.3)
+
+
+def _recon(f, rec):
+    f0, f1, f2, f3, f4 = f
+    if rec == 251:
+        return (2.0 * f0 - 13.0 * f1 + 47.0 * f2 + 27.0 * f3 - 3.0 * f4) / 60.0
+    q0 = 1.0 / 3.0 * f0 - 7.0 / 6.0 * f1 + 11.0 / 6.0 * f2
+    q1 = -1.0 / 6.0 * f1 + 5.0 / 6.0 * f2 + 1.0 / 3.0 * f3
+    q2 = 1.0 / 3.0 * f2 + 5.0 / 6.0 * f3 - 1.0 / 6.0 * f4
+    b0 = 13.0 * (f0 - 2.0 * f1 + f2) ** 2 / 12.0 + (f0 - 4.0 * f1 + 3.0 * f2) ** 2 / 4.0
+    b1 = 13.0 * (f1 - 2.0 * f2 + f3) ** 2 / 12.0 + (f1 - f3) ** 2 / 4.0
+    b2 = 13.0 * (f2 - 2.0 * f3 + f4) ** 2 / 12.0 + (3.0 * f2 - 4.0 * f3 + f4) ** 2 / 4.0
+    if rec == 253:
+        a0, a1, a2 = C[0] / (SS + b0) ** 2, C[1] / (SS + b1) ** 2, C[2] / (SS + b2) ** 2
+    elif rec == 255:
+        tau = (b2 - b0).abs()
+        a0 = C[0] * (1.0 + (tau / (SS + b0)) ** 2)
+        a1 = C[1] * (1.0 + (tau / (SS + b1)) ** 2)
+        a2 = C[2] * (1.0 + (tau / (SS + b2)) ** 2)
+    else:
+        raise ValueError(rec)
+    s = a0 + a1 + a2
+    return a0 / s * q0 + a1 / s * q1 + a2 / s * q2
+
+
+def primitives(U, gamma):
+    rho = U[0]
+    u = U[1] / rho
+    v = U[2] / rho
+    p = (gamma - 1.0) * (U[3] - 0.5 * rho * (u * u + v * v))
+    a = torch.sqrt(gamma * p / rho)
+    return rho, u, v, p, a
+
+
+def rhs(U, gamma, dx, dy, rec):
+    """L(U) = -(h_{i+1/2} - h_{i-1/2})/dx - (g_{j+1/2} - g_{j-1/2})/dy."""
+    rho, u, v, p, a = primitives(U, gamma)
+    out = torch.zeros_like(U)
+    for d, (un, h, axis) in enumerate(((u, dx, 2), (v, dy, 1))):
+        lam = un.abs() + a
+        P = torch.stack([torch.zeros_like(p), p if d == 0 else torch.zeros_like(p),
+                         p if d == 1 else torch.zeros_like(p), un * p])
+        Fp = 0.5 * ((un + lam) * U + P)
+        Fm = 0.5 * ((un - lam) * U + P)
+        sh = lambda F, k: torch.roll(F, shifts=-k, dims=axis)  # element f holds F[f + k]
+        # face f (left of cell f): F+ of cells f-3..f+1, F- of cells f+2..f-2
+        hp = _recon([sh(Fp, k) for k in (-3, -2, -1, 0, 1)], rec)
+        hm = _recon([sh(Fm, k) for k in (2, 1, 0, -1, -2)], rec)
+        hf = hp + hm
+        out = out - (sh(hf, 1) - hf) / h
+    return out
+
+
+def time_step(U, gamma, dx, dy, rec, cfl, dt_const=None):
+    """One TVD-RK3 step; returns (U_next, dt)."""
+    if dt_const is None:
+        _, u, v, _, a = primitives(U, gamma)
+        mx = (u.abs() + a).max()
+        my = (v.abs() + a).max()
+        dt_x, dt_y = dx / mx, dy / my
+        dt = cfl * dt_x * dt_y / (dt_x + dt_y)
+    else:
+        dt = torch.tensor(dt_const, dtype=U.dtype, device=U.device)
+    u1 = U + dt * rhs(U, gamma, dx, dy, rec)
+    u2 = 3.0 / 4.0 * U + 1.0 / 4.0 * u1 + 1.0 / 4.0 * dt * rhs(u1, gamma, dx, dy, rec)
+    u3 = 1.0 / 3.0 * U + 2.0 / 3.0 * u2 + 2.0 / 3.0 * dt * rhs(u2, gamma, dx, dy, rec)
+    return u3, dt
+
+
+def run(U, n, gamma, dx, dy, rec, cfl, dt_const=None):
+    for _ in range(n):
+        U, _ = time_step(U, gamma, dx, dy, rec, cfl, dt_const)
+    return U
