@@ -198,6 +198,7 @@ def load_library(path: str | None = None):
         "dense_adjoint_rhs_vjp": (_c_int, [vp, vp, vp, vp, dp, vp]),
         "dense_adjoint_get_dts": (_c_int, [vp, dp, _c_int]),
         "dense_adjoint_get_argmax": (_c_int, [vp, ctypes.POINTER(_c_int), _c_int]),
+        "dense_adjoint_get_solver": (_c_int, [vp, ctypes.POINTER(vp)]),
         "dense_adjoint_launch_count": (ctypes.c_longlong, [vp]),
         "dense_adjoint_last_error": (ctypes.c_char_p, [vp]),
     }

@@ -125,6 +125,22 @@ class Adjoint:
     def launch_count(self) -> int:
         return int(self.lib.dense_adjoint_launch_count(self.h))
 
+    def solver_state(self):
+        """The forward solver's current conserved variables, padded Fortran layout (ni+8, nj+8, 4),
+        and its interface fluxes (h_xi, h_eta) of the last stage it ran."""
+        hs = ctypes.c_void_p()
+        self._chk(self.lib.dense_adjoint_get_solver(self.h, ctypes.byref(hs)))
+        c = self.cfg
+        dp = ctypes.POINTER(ctypes.c_double)
+        cons = np.zeros((c.ni + 8, c.nj + 8, 4), order="F")
+        hx = np.zeros((c.ni + 1, c.nj, 4), order="F")
+        he = np.zeros((c.nj + 1, c.ni, 4), order="F")
+        for rc in (self.lib.dense_download(hs, cons.ctypes.data_as(dp), None),
+                   self.lib.dense_get_fluxes(hs, hx.ctypes.data_as(dp), he.ctypes.data_as(dp))):
+            if rc:
+                raise DenseError(rc, self.lib.dense_last_error(hs).decode())
+        return cons, hx, he
+
 
 def _make_function():
     torch = _torch()

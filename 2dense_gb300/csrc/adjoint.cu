@@ -11,16 +11,20 @@
 //     u1 = u0 + dt L(u0),  u2 = 3/4 u0 + 1/4 u1 + 1/4 dt L(u1),  u3 = 1/3 u0 + 2/3 u2 + 2/3 dt L(u2)
 // with dt = cfl / (max(|u|+alpha)/dx + max(|v|+alpha)/dy) of u0.
 //
-// The vector-Jacobian product v -> (dL/du)^T v runs in three kernels per stage:
-//   k_face (one per direction, one thread per face): hbar_f = (v_right - v_left)/dx, then the
-//     reverse mode of the two 5-point reconstructions gives the sensitivities of the stencil's
-//     split fluxes; the 5 values per (sign, equation) go to a face buffer G, and the face adds
-//     h_f * hbar_f to its block's share of v . L(u) (summation by parts);
-//   k_cell (one thread per cell): gathers, in a fixed order, the G entries of every face whose
-//     stencils read the cell or one of its periodic images, applies the transposed Jacobian of
-//     F+- at the cell for both directions, and applies the reverse of the RK stage;
-//   k_dt (one block, once per step): the time step's sensitivity sum_s c_s v_s . L(u_{s-1}),
-//     sent through dt(max wave speeds) to the cells where the maxima are attained.
+// FP64 is the scarce resource on GB300 (about 1.3 TFLOP/s against 7.9 TB/s of HBM), so the
+// reverse sweep does not re-evaluate the reconstructions: when a segment is recomputed from its
+// checkpoint, the flux sweeps run in their taping form (flux_tape of the kernel table), which
+// writes, per face, the gradient g[m] = dW/dlf[m] of each of its 8 reconstructions and the
+// fluxes h -- 352 bytes per face and direction, read back once. The vector-Jacobian product
+// v -> (dL/du)^T v of a stage is then two light kernels:
+//   k_hbar (one thread per face, both directions): hbar_f = (v_right - v_left)/dx, and the
+//     face's share h_f . hbar_f of v . L(u) (summation by parts), summed per block;
+//   k_rev (one thread per cell): for every face whose stencils read the cell or one of its
+//     periodic images, hbar_f g[m] accumulated in a fixed order into the sensitivities of the
+//     cell's F+ and F-; the transposed Jacobian of F+- at the cell (both directions); the
+//     reverse of the RK stage;
+// and once per step k_dt (one block): the time step's sensitivity sum_s c_s v_s . L(u_{s-1}),
+// sent through dt(max wave speeds) to the cells where the maxima are attained.
 // No atomics: every sum has a fixed order, so the gradient is deterministic.
 #include <cuda_runtime.h>
 
@@ -29,6 +33,7 @@
 #include <string>
 #include <vector>
 
+#include "fastmath.cuh"
 #include "handle.h"
 
 namespace dense {
@@ -39,105 +44,34 @@ constexpr double a310 = -1.0 / 6.0, a311 = 5.0 / 6.0, a312 = 1.0 / 3.0;
 constexpr double a320 = 1.0 / 3.0, a321 = 5.0 / 6.0, a322 = -1.0 / 6.0;
 constexpr double kSS = (double)1.0e-6f;      // weno_mod.f90:37, a default-real literal
 constexpr double kPFloor = (double)1.0e-6f;  // get_primary.f90:58
+constexpr double k1312 = 13.0 / 12.0;
 
 struct AdjParams {
     int ni, nj;
     long long plane;  // ni * nj: one variable of a compact interior state
+    long long xs, ys; // face planes: xi nj (ni+1), eta (nj+1) ni
+    int np;           // tape planes per direction (tape_planes)
     double gamma, dx, dy, inv_dx, inv_dy, cfl;
 };
 
-// Reverse mode of one 5-point reconstruction h = W(f): adds hbar * dh/df_m to fbar[m] and
-// returns h. For WENO, h = sum_k a_k q_k / S with S = sum_k a_k, so dh/dq_k = a_k/S and
-// dh/da_k = (q_k - h)/S; a_k depends on f through the smoothness indicators beta_k
-// (JS: a_k = c_k/(eps+beta_k)^2; Z: a_k = c_k (1 + (tau/(eps+beta_k))^2), tau = |beta_2-beta_0|).
-template <int REC>
-__device__ __forceinline__ double recon_rev(const double f[5], double hbar, double fbar[5]) {
-    if (REC == DENSE_RECON_UPWIND5) {
-        const double k = hbar / 60.0;
-        fbar[0] += 2.0 * k; fbar[1] -= 13.0 * k; fbar[2] += 47.0 * k; fbar[3] += 27.0 * k; fbar[4] -= 3.0 * k;
-        return (2.0 * f[0] - 13.0 * f[1] + 47.0 * f[2] + 27.0 * f[3] - 3.0 * f[4]) / 60.0;
-    }
-    constexpr double c[3] = {0.1, 0.6, 0.3};
-    const double q[3] = {a300 * f[0] + a301 * f[1] + a302 * f[2], a310 * f[1] + a311 * f[2] + a312 * f[3],
-                         a320 * f[2] + a321 * f[3] + a322 * f[4]};
-    const double A[3] = {f[0] - 2.0 * f[1] + f[2], f[1] - 2.0 * f[2] + f[3], f[2] - 2.0 * f[3] + f[4]};
-    const double B[3] = {f[0] - 4.0 * f[1] + 3.0 * f[2], f[1] - f[3], 3.0 * f[2] - 4.0 * f[3] + f[4]};
-    double beta[3], id[3], a[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        beta[k] = 13.0 / 12.0 * (A[k] * A[k]) + 0.25 * (B[k] * B[k]);
-        id[k] = 1.0 / (kSS + beta[k]);
-    }
-    const double tau = fabs(beta[2] - beta[0]);
-#pragma unroll
-    for (int k = 0; k < 3; ++k)
-        a[k] = REC == DENSE_RECON_WENOJS5 ? c[k] * (id[k] * id[k]) : c[k] * (1.0 + (tau * id[k]) * (tau * id[k]));
-    const double iS = 1.0 / (a[0] + a[1] + a[2]);
-    const double h = (a[0] * q[0] + a[1] * q[1] + a[2] * q[2]) * iS;
-    double qbar[3], bbar[3], taubar = 0.0;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        qbar[k] = hbar * a[k] * iS;
-        const double abar = hbar * (q[k] - h) * iS;
-        if (REC == DENSE_RECON_WENOJS5) {
-            bbar[k] = -2.0 * abar * a[k] * id[k];                  // da/dbeta = -2 a/(eps+beta)
-        } else {
-            const double r = tau * id[k];
-            bbar[k] = -2.0 * abar * c[k] * r * r * id[k];          // da/dbeta = -2 c r^2/(eps+beta)
-            taubar += 2.0 * abar * c[k] * r * id[k];               // da/dtau  =  2 c r/(eps+beta)
-        }
-    }
-    if (REC == DENSE_RECON_WENOZ5) {
-        const double sg = beta[2] >= beta[0] ? taubar : -taubar;
-        bbar[2] += sg;
-        bbar[0] -= sg;
-    }
-    fbar[0] += qbar[0] * a300;
-    fbar[1] += qbar[0] * a301 + qbar[1] * a310;
-    fbar[2] += qbar[0] * a302 + qbar[1] * a311 + qbar[2] * a320;
-    fbar[3] += qbar[1] * a312 + qbar[2] * a321;
-    fbar[4] += qbar[2] * a322;
-    // beta_k = 13/12 A_k^2 + 1/4 B_k^2: dbeta/dA = 13/6 A, dbeta/dB = B/2
-    double Ab[3], Bb[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) { Ab[k] = bbar[k] * (13.0 / 6.0) * A[k]; Bb[k] = bbar[k] * 0.5 * B[k]; }
-    fbar[0] += Ab[0] + Bb[0];
-    fbar[1] += -2.0 * Ab[0] - 4.0 * Bb[0] + Ab[1] + Bb[1];
-    fbar[2] += Ab[0] + 3.0 * Bb[0] - 2.0 * Ab[1] + Ab[2] + 3.0 * Bb[2];
-    fbar[3] += Ab[1] - Bb[1] - 2.0 * Ab[2] - 4.0 * Bb[2];
-    fbar[4] += Ab[2] + Bb[2];
-    return h;
-}
-
-// get_primary of one cell (get_primary.f90:53-60), with the pressure floor of :58.
+// get_primary of one cell (get_primary.f90:53-60), with the pressure floor of :58; rs = 1/alpha'
+// with alpha'^2 = gamma p / rho, so that alpha = alpha'^2 rs and dalpha/dp = gamma/(2 rho) rs.
 struct Prim {
-    double u, v, p, a, ir;
+    double u, v, p, a, ir, rs;
     bool floored;
 };
 __device__ __forceinline__ Prim prim_of(const double U[4], double gamma) {
     Prim q;
-    q.ir = 1.0 / U[0];
+    q.ir = rcp_nr(U[0]);
     q.u = U[1] * q.ir;
     q.v = U[2] * q.ir;
     q.p = (gamma - 1.0) * (U[3] - 0.5 * U[0] * (q.u * q.u + q.v * q.v));
     q.floored = q.p < 0.0;
     if (q.floored) q.p = kPFloor;
-    q.a = sqrt(gamma * q.p * q.ir);
+    const double a2 = gamma * q.p * q.ir;
+    q.rs = rsqrt_nr(a2);
+    q.a = a2 * q.rs;
     return q;
-}
-
-// LLF split fluxes of one cell in direction DIR (flux_splitting_LLF.f90:67-81).
-template <int DIR>
-__device__ __forceinline__ void llf_fluxes(const double U[4], const Prim& q, double fp[4], double fm[4]) {
-    const double un = DIR == 0 ? q.u : q.v;
-    const double lam = fabs(un) + q.a;
-    const double up = un + lam, um = un - lam;
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-        const double add = c == 1 + DIR ? q.p : (c == 3 ? un * q.p : 0.0);
-        fp[c] = 0.5 * (up * U[c] + add);
-        fm[c] = 0.5 * (um * U[c] + add);
-    }
 }
 
 // Sensitivities of (u_n, alpha, p) pulled back to the conserved variables of the cell.
@@ -146,7 +80,7 @@ __device__ __forceinline__ void prim_pullback(const double U[4], const Prim& q, 
                                               double ab, double pb, double Ub[4]) {
     // alpha = sqrt(gamma p / rho): dalpha/dp = gamma/(2 alpha rho), dalpha/drho = -alpha/(2 rho)
     double rb = -ab * 0.5 * q.a * q.ir;
-    if (!q.floored) pb += ab * gamma * 0.5 / (q.a * U[0]);
+    if (!q.floored) pb += ab * (0.5 * gamma) * q.ir * q.rs;
     // u_n = m_n / rho
     const double un = DIR == 0 ? q.u : q.v;
     Ub[1 + DIR] += unb * q.ir;
@@ -210,119 +144,87 @@ __device__ __forceinline__ double block_sum(double x) {
 }
 
 // ---------------------------------------------------------------------------------------------
-// Face kernel. xi: TX faces x TY rows per block, the tile's cells f0-3 .. f0+TX+1 staged in
-// shared memory; eta: TX columns x TY faces. G[sign][m][eq][...] holds, per face, the
-// sensitivity of the m-th stencil value of the (sign, eq) reconstruction; the layout follows
-// the forward's face arrays (xi [row][face], eta [face][column]).
-template <int DIR, int REC, int TX, int TY>
-__global__ void __launch_bounds__(TX * TY) k_face(AdjParams a, const double* __restrict__ u,
-                                                  const double* __restrict__ w, double* __restrict__ G,
-                                                  double* __restrict__ part) {
-    constexpr int NL = DIR == 0 ? TY : TY + 5;
-    constexpr int NC = DIR == 0 ? TX + 5 : TX;
-    __shared__ double sF[8][NL][NC];
-    const int tx = threadIdx.x, ty = threadIdx.y;
+// Face kernel, both directions (blockIdx.z): hbar per face and equation, and the block's share
+// of v . L(u). Tape and hbar arrays follow the forward's face arrays: xi [nj][ni+1] planes, then
+// eta [nj+1][ni] planes.
+__global__ void __launch_bounds__(256) k_hbar(AdjParams a, const double* __restrict__ w,
+                                              const double* __restrict__ tape, double* __restrict__ hb,
+                                              double* __restrict__ part) {
+    const int dir = blockIdx.z;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     const int ni = a.ni, nj = a.nj;
-    auto stage_cell = [&](int i, int j, int r, int c) {
-        double U[4], fp[4], fm[4];
-#pragma unroll
-        for (int v = 0; v < 4; ++v) U[v] = u[v * a.plane + (long long)j * ni + i];
-        const Prim q = prim_of(U, a.gamma);
-        llf_fluxes<DIR>(U, q, fp, fm);
-#pragma unroll
-        for (int v = 0; v < 4; ++v) { sF[v][r][c] = fp[v]; sF[4 + v][r][c] = fm[v]; }
-    };
-    if (DIR == 0) {
-        const int f0 = blockIdx.x * TX, j = blockIdx.y * TY + ty;
-        if (j < nj)
-            for (int k = tx; k < TX + 5; k += TX) {
-                int i = f0 - 3 + k;           // cells -3 .. ni+2 are read; the rest of the tile is not
-                if (i > ni + 2) break;
-                i = i < 0 ? i + ni : (i >= ni ? i - ni : i);
-                stage_cell(i, j, ty, k);
-            }
-    } else {
-        const int g0 = blockIdx.y * TY, i = blockIdx.x * TX + tx;
-        if (i < ni)
-            for (int k = ty; k < TY + 5; k += TY) {
-                int j = g0 - 3 + k;
-                if (j > nj + 2) break;
-                j = j < 0 ? j + nj : (j >= nj ? j - nj : j);
-                stage_cell(i, j, k, tx);
-            }
-    }
-    __syncthreads();
-
-    const int line = DIR == 0 ? blockIdx.y * TY + ty : blockIdx.x * TX + tx;
-    const int f = DIR == 0 ? blockIdx.x * TX + tx : blockIdx.y * TY + ty;
-    const int nline = DIR == 0 ? nj : ni, n = DIR == 0 ? ni : nj;
+    const int line = dir == 0 ? y : x, f = dir == 0 ? x : y;
+    const int nline = dir == 0 ? nj : ni, n = dir == 0 ? ni : nj;
     double vdl = 0.0;
     if (line < nline && f <= n) {
-        const int t = DIR == 0 ? tx : ty;
-        const double inv = DIR == 0 ? a.inv_dx : a.inv_dy;
-        const long long oR = DIR == 0 ? (long long)line * ni + f : (long long)f * ni + line;
-        const long long oL = oR - (DIR == 0 ? 1 : ni);
-        const long long gs = DIR == 0 ? (long long)nj * (ni + 1) : (long long)(nj + 1) * ni;
-        const long long go = DIR == 0 ? (long long)line * (ni + 1) + f : (long long)f * ni + line;
-#pragma unroll 1
+        const double inv = dir == 0 ? a.inv_dx : a.inv_dy;
+        const long long oR = dir == 0 ? (long long)line * ni + f : (long long)f * ni + line;
+        const long long oL = oR - (dir == 0 ? 1 : ni);
+        const long long ts = dir == 0 ? a.xs : a.ys;
+        const long long to = dir == 0 ? (long long)line * (ni + 1) + f : (long long)f * ni + line;
+        const double* H = tape + (dir == 0 ? 0 : a.np * a.xs) + (long long)(a.np - 4) * ts + to;
+        double* HB = hb + (dir == 0 ? 0 : 4 * a.xs) + to;
+#pragma unroll
         for (int v = 0; v < 4; ++v) {
             const double wr = f < n ? w[v * a.plane + oR] : 0.0;   // face n is the right face of cell n-1 only
             const double wl = f >= 1 ? w[v * a.plane + oL] : 0.0;  // face 0 is the left face of cell 0 only
-            const double hb = (wr - wl) * inv;
-            double lp[5], lm[5], bp[5] = {0, 0, 0, 0, 0}, bm[5] = {0, 0, 0, 0, 0};
-#pragma unroll
-            for (int m = 0; m < 5; ++m) {
-                if (DIR == 0) { lp[m] = sF[v][ty][t + m]; lm[m] = sF[4 + v][ty][t + 5 - m]; }
-                else          { lp[m] = sF[v][t + m][tx]; lm[m] = sF[4 + v][t + 5 - m][tx]; }
-            }
-            const double h = recon_rev<REC>(lp, hb, bp) + recon_rev<REC>(lm, hb, bm);
-            vdl += h * hb;
-#pragma unroll
-            for (int m = 0; m < 5; ++m) {
-                G[((long long)(m * 4 + v)) * gs + go] = bp[m];
-                G[((long long)((5 + m) * 4 + v)) * gs + go] = bm[m];
-            }
+            const double hbv = (wr - wl) * inv;
+            HB[v * ts] = hbv;
+            vdl = fma(hbv, H[v * ts], vdl);
         }
     }
     const double s = block_sum(vdl);
-    if (tx == 0 && ty == 0) part[blockIdx.y * gridDim.x + blockIdx.x] = s;
+    if (threadIdx.x == 0 && threadIdx.y == 0) part[(blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = s;
 }
 
-// Sum of the G entries that read cell x of a line (faces 0..n), over the cell's periodic
-// images: "+" stencils read cell f-3+m, "-" stencils cell f+2-m.
-__device__ __forceinline__ void gather_sign(const double* __restrict__ G, long long gs, long long base,
-                                            long long stride, int k0, int f, int n, double acc[4]) {
-    if (f >= 0 && f <= n) {
+// Sensitivities of the F+ and F- values of cell x of a line (faces 0..n of the line, at offset
+// base + f*stride of their planes): sum over the faces whose "+" stencil reads the cell
+// (face x+3-m reads it as its m-th value) or whose "-" stencil does (face x-2+m), including the
+// faces that read it through a periodic image (x -+ n).
+template <int REC>
+__device__ __forceinline__ void add_face(const double* __restrict__ T, const double* __restrict__ H, long long ts,
+                                         long long off, int s, int m, double acc[4]) {
+    constexpr double cu[5] = {2.0 / 60.0, -13.0 / 60.0, 47.0 / 60.0, 27.0 / 60.0, -3.0 / 60.0};
 #pragma unroll
-        for (int v = 0; v < 4; ++v) acc[v] += G[(long long)(k0 + v) * gs + base + f * stride];
-    }
-    if (f >= n) {  // image x - n, read by face f - n
-#pragma unroll
-        for (int v = 0; v < 4; ++v) acc[v] += G[(long long)(k0 + v) * gs + base + (f - n) * stride];
-    }
-    if (f <= 0) {  // image x + n, read by face f + n
-#pragma unroll
-        for (int v = 0; v < 4; ++v) acc[v] += G[(long long)(k0 + v) * gs + base + (f + n) * stride];
+    for (int v = 0; v < 4; ++v) {
+        const double g = REC == DENSE_RECON_UPWIND5 ? cu[m] : T[(long long)((s * 5 + m) * 4 + v) * ts + off];
+        acc[v] = fma(g, H[v * ts + off], acc[v]);
     }
 }
-__device__ __forceinline__ void gather_line(const double* __restrict__ G, long long gs, long long base,
-                                            long long stride, int x, int n, double gp[4], double gm[4]) {
+template <int REC>
+__device__ __forceinline__ void gather_line(const double* __restrict__ T, const double* __restrict__ H, long long ts,
+                                            long long base, long long stride, int x, int n, double gp[4],
+                                            double gm[4]) {
+    if (x >= 3 && x <= n - 4) {  // every reading face inside 1..n-1: no images
+#pragma unroll
+        for (int m = 0; m < 5; ++m) {
+            add_face<REC>(T, H, ts, base + (long long)(x + 3 - m) * stride, 0, m, gp);
+            add_face<REC>(T, H, ts, base + (long long)(x - 2 + m) * stride, 1, m, gm);
+        }
+        return;
+    }
 #pragma unroll
     for (int m = 0; m < 5; ++m) {
-        gather_sign(G, gs, base, stride, m * 4, x + 3 - m, n, gp);
-        gather_sign(G, gs, base, stride, (5 + m) * 4, x - 2 + m, n, gm);
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+            const int f = s == 0 ? x + 3 - m : x - 2 + m;
+            double* acc = s == 0 ? gp : gm;
+            if (f >= 0 && f <= n) add_face<REC>(T, H, ts, base + (long long)f * stride, s, m, acc);
+            if (f >= n) add_face<REC>(T, H, ts, base + (long long)(f - n) * stride, s, m, acc);  // image x - n
+            if (f <= 0) add_face<REC>(T, H, ts, base + (long long)(f + n) * stride, s, m, acc);  // image x + n
+        }
     }
 }
 
-// Cell kernel: Ub = (dL/du)^T w at the cell, then the reverse of RK stage STAGE
-// (3, 2, 1; 0 = Ub alone). Stage 1 also reduces the wave-speed maxima of its state u0
-// (the time step's input) per block, with their cells.
-template <int STAGE>
-__global__ void __launch_bounds__(256) k_cell(AdjParams a, const double* __restrict__ u,
-                                              const double* __restrict__ w, const double* __restrict__ Gx,
-                                              const double* __restrict__ Gy, double* __restrict__ acc,
-                                              double* __restrict__ out, const double* __restrict__ dtp,
-                                              double* __restrict__ mpart) {
+// Cell kernel: Ub = (dL/du)^T w at the cell from the stage's tape and hbar, then the reverse of
+// RK stage STAGE (3, 2, 1; 0 = Ub alone). Stage 1 also reduces the wave-speed maxima of its
+// state u0 (the time step's input) per block, with their cells.
+template <int STAGE, int REC>
+__global__ void __launch_bounds__(128) k_rev(AdjParams a, const double* __restrict__ u,
+                                             const double* __restrict__ w, const double* __restrict__ tape,
+                                             const double* __restrict__ hb, double* __restrict__ acc,
+                                             double* __restrict__ out, const double* __restrict__ dtp,
+                                             double* __restrict__ mpart) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     const int ni = a.ni, nj = a.nj;
     double e1 = -1.0, e2 = -1.0;
@@ -335,12 +237,12 @@ __global__ void __launch_bounds__(256) k_cell(AdjParams a, const double* __restr
         const Prim q = prim_of(U, a.gamma);
         {
             double gp[4] = {0, 0, 0, 0}, gm[4] = {0, 0, 0, 0};
-            gather_line(Gx, (long long)nj * (ni + 1), (long long)j * (ni + 1), 1, i, ni, gp, gm);
+            gather_line<REC>(tape, hb, a.xs, (long long)j * (ni + 1), 1, i, ni, gp, gm);
             llf_vjp<0>(U, q, a.gamma, gp, gm, Ub);
         }
         {
             double gp[4] = {0, 0, 0, 0}, gm[4] = {0, 0, 0, 0};
-            gather_line(Gy, (long long)(nj + 1) * ni, i, ni, j, nj, gp, gm);
+            gather_line<REC>(tape + a.np * a.xs, hb + 4 * a.xs, a.ys, i, ni, j, nj, gp, gm);
             llf_vjp<1>(U, q, a.gamma, gp, gm, Ub);
         }
         const double dt = STAGE == 0 ? 0.0 : *dtp;
@@ -380,8 +282,8 @@ __global__ void __launch_bounds__(256) k_cell(AdjParams a, const double* __restr
             if (better(oe1, oi1, e1, i1)) { e1 = oe1; i1 = oi1; }
             if (better(oe2, oi2, e2, i2)) { e2 = oe2; i2 = oi2; }
         }
-        __shared__ double se[2][8];
-        __shared__ long long si[2][8];
+        __shared__ double se[2][4];
+        __shared__ long long si[2][4];
         const int tid = threadIdx.x + threadIdx.y * blockDim.x;
         if ((tid & 31) == 0) { se[0][tid >> 5] = e1; se[1][tid >> 5] = e2; si[0][tid >> 5] = i1; si[1][tid >> 5] = i2; }
         __syncthreads();
@@ -466,8 +368,8 @@ using dense::adj::AdjParams;
 
 namespace {
 
-constexpr int kFX = 32, kFY = 4;   // face kernel tiles (xi: faces x rows; eta: columns x faces)
-constexpr int kCX = 32, kCY = 8;   // cell kernel blocks
+constexpr int kCX = 32, kCY = 4;   // cell kernel blocks
+constexpr int kHX = 32, kHY = 8;   // face kernel blocks
 
 thread_local std::string g_adj_err;
 
@@ -479,17 +381,18 @@ struct dense_adjoint {
     int k = 20;                   // checkpoint every k steps
     int ni = 0, nj = 0;
     size_t state = 0;             // doubles per compact state: 4 ni nj
+    size_t tape_stage = 0;        // doubles of one stage's tape (both directions)
     AdjParams ap{};
-    double* ckpt = nullptr;  int ckpt_cap = 0;  // states at steps 0, k, 2k, ...
-    double* dts = nullptr;   int dts_cap = 0;   // dt of every forward step
+    double* ckpt = nullptr;  int ckpt_cap = 0;    // states at steps 0, k, 2k, ...
+    double* dts = nullptr;   int dts_cap = 0;     // dt of every forward step
     int* argmax = nullptr;   int argmax_cap = 0;  // per step: cells of the two maxima
-    double* rec = nullptr;                      // k steps x 3 stage states of one segment
-    double *g = nullptr, *g1 = nullptr, *g2 = nullptr, *acc = nullptr;
-    double *Gx = nullptr, *Gy = nullptr;
-    double* part = nullptr;  int npart = 0, nbx = 0;  // per stage: xi then eta face blocks
+    double* rec = nullptr;                        // k steps x 3 stage states of one segment
+    double* tape = nullptr;                       // k steps x 3 stage tapes of one segment
+    double *g = nullptr, *g1 = nullptr, *g2 = nullptr, *acc = nullptr, *hb = nullptr;
+    double* part = nullptr;  int npart = 0;       // per stage: k_hbar blocks
     double* mpart = nullptr; int nm = 0;
-    dim3 gx, gy, gc;
-    int nsteps = -1;                            // steps of the last forward
+    dim3 gh, gc;
+    int nsteps = -1;                              // steps of the last forward
     cudaEvent_t ev_in = nullptr, ev_out = nullptr;
     long long launches = 0;
     std::string err;
@@ -560,44 +463,56 @@ int restart(dense_adjoint* a, const double* state) {
     return DENSE_OK;
 }
 
+// one stage of the forward solver with taping sweeps: boundary, flux_tape xi and eta, update
+void taped_stage(dense_adjoint* a, int irk, double* tape) {
+    dense_handle* h = a->h;
+    dense::Params p = h->prm;
+    p.tape = tape;
+    h->kt->bc(h->prm, h->stream);
+    h->kt->flux_tape(p, irk, 0, h->stream);
+    h->kt->flux_tape(p, irk, 1, h->stream);
+    h->kt->update(h->prm, irk, h->stream);
+    a->launches += 4;
+}
+
 template <int REC>
-void launch_vjp(dense_adjoint* a, int stage, const double* u, const double* w, double* out, double* part,
+void launch_rev(dense_adjoint* a, int stage, const double* u, const double* tape, const double* w, double* out,
                 const double* dtp, cudaStream_t s) {
     using namespace dense::adj;
-    const dim3 bf(kFX, kFY), bc(kCX, kCY);
-    k_face<0, REC, kFX, kFY><<<a->gx, bf, 0, s>>>(a->ap, u, w, a->Gx, part);
-    k_face<1, REC, kFX, kFY><<<a->gy, bf, 0, s>>>(a->ap, u, w, a->Gy, part + a->nbx);
+    const dim3 bc(kCX, kCY);
     switch (stage) {
-    case 3: k_cell<3><<<a->gc, bc, 0, s>>>(a->ap, u, w, a->Gx, a->Gy, a->acc, out, dtp, nullptr); break;
-    case 2: k_cell<2><<<a->gc, bc, 0, s>>>(a->ap, u, w, a->Gx, a->Gy, a->acc, out, dtp, nullptr); break;
-    case 1: k_cell<1><<<a->gc, bc, 0, s>>>(a->ap, u, w, a->Gx, a->Gy, a->acc, out, dtp, a->mpart); break;
-    default: k_cell<0><<<a->gc, bc, 0, s>>>(a->ap, u, w, a->Gx, a->Gy, nullptr, out, nullptr, nullptr); break;
+    case 3: k_rev<3, REC><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, a->hb, a->acc, out, dtp, nullptr); break;
+    case 2: k_rev<2, REC><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, a->hb, a->acc, out, dtp, nullptr); break;
+    case 1: k_rev<1, REC><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, a->hb, a->acc, out, dtp, a->mpart); break;
+    default: k_rev<0, REC><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, a->hb, nullptr, out, nullptr, nullptr); break;
     }
-    a->launches += 3;
 }
 
-void vjp(dense_adjoint* a, int stage, const double* u, const double* w, double* out, double* part,
-         const double* dtp) {
+// the reverse of one stage: hbar of w on every face (and w . L(u) per block into part), then
+// the cells
+void vjp(dense_adjoint* a, int stage, const double* u, const double* tape, const double* w, double* out,
+         double* part, const double* dtp) {
     cudaStream_t s = a->h->stream;
+    dense::adj::k_hbar<<<a->gh, dim3(kHX, kHY), 0, s>>>(a->ap, w, tape, a->hb, part);
     switch (a->cfg.recon) {
-    case DENSE_RECON_UPWIND5: launch_vjp<DENSE_RECON_UPWIND5>(a, stage, u, w, out, part, dtp, s); break;
-    case DENSE_RECON_WENOJS5: launch_vjp<DENSE_RECON_WENOJS5>(a, stage, u, w, out, part, dtp, s); break;
-    default:                  launch_vjp<DENSE_RECON_WENOZ5>(a, stage, u, w, out, part, dtp, s); break;
+    case DENSE_RECON_UPWIND5: launch_rev<DENSE_RECON_UPWIND5>(a, stage, u, tape, w, out, dtp, s); break;
+    case DENSE_RECON_WENOJS5: launch_rev<DENSE_RECON_WENOJS5>(a, stage, u, tape, w, out, dtp, s); break;
+    default:                  launch_rev<DENSE_RECON_WENOZ5>(a, stage, u, tape, w, out, dtp, s); break;
     }
+    a->launches += 2;
 }
 
-// reverse of one step from its three recorded stage states; g holds dJ/du(n+1) on entry and
-// dJ/du(n) on return
-void reverse_step(dense_adjoint* a, const double* rec_step, int step) {
+// reverse of one step from its three recorded stage states and tapes; g holds dJ/du(n+1) on
+// entry and dJ/du(n) on return
+void reverse_step(dense_adjoint* a, const double* rec_step, const double* tape_step, int step) {
     const double* dtp = a->dts + step;
-    const double* u0 = rec_step;
-    const double* u1 = rec_step + a->state;
-    const double* u2 = rec_step + 2 * a->state;
-    vjp(a, 3, u2, a->g, a->g2, a->part + 2 * a->npart, dtp);
-    vjp(a, 2, u1, a->g2, a->g1, a->part + 1 * a->npart, dtp);
-    vjp(a, 1, u0, a->g1, a->g, a->part, dtp);
+    const double* u[3] = {rec_step, rec_step + a->state, rec_step + 2 * a->state};
+    const double* t[3] = {tape_step, tape_step + a->tape_stage, tape_step + 2 * a->tape_stage};
+    vjp(a, 3, u[2], t[2], a->g, a->g2, a->part + 2 * a->npart, dtp);
+    vjp(a, 2, u[1], t[1], a->g2, a->g1, a->part + 1 * a->npart, dtp);
+    vjp(a, 1, u[0], t[0], a->g1, a->g, a->part, dtp);
     if (!a->cfg.if_const_dt) {
-        dense::adj::k_dt<<<1, 256, 0, a->h->stream>>>(a->ap, a->part, a->npart, a->mpart, a->nm, u0, a->g, dtp,
+        dense::adj::k_dt<<<1, 256, 0, a->h->stream>>>(a->ap, a->part, a->npart, a->mpart, a->nm, u[0], a->g, dtp,
                                                       a->argmax + 2 * step);
         a->launches += 1;
     }
@@ -622,10 +537,16 @@ const char* dense_adjoint_last_error(dense_adjoint_t* a) { return a ? a->err.c_s
 
 long long dense_adjoint_launch_count(dense_adjoint_t* a) { return a ? a->launches : -1; }
 
+int dense_adjoint_get_solver(dense_adjoint_t* a, dense_handle_t** h) {
+    if (!a || !h) return aerr(a, DENSE_ERR_ARG, "null argument");
+    *h = a->h;
+    return DENSE_OK;
+}
+
 void dense_adjoint_destroy(dense_adjoint_t* a) {
     if (!a) return;
     if (a->h) cudaStreamSynchronize(a->h->stream);
-    double* bufs[] = {a->ckpt, a->dts, a->rec, a->g, a->g1, a->g2, a->acc, a->Gx, a->Gy, a->part, a->mpart};
+    double* bufs[] = {a->ckpt, a->dts, a->rec, a->tape, a->g, a->g1, a->g2, a->acc, a->hb, a->part, a->mpart};
     for (double* b : bufs) if (b) cudaFree(b);
     if (a->argmax) cudaFree(a->argmax);
     if (a->ev_in) cudaEventDestroy(a->ev_in);
@@ -664,19 +585,20 @@ int dense_adjoint_create(const dense_config_t* cfg, int checkpoint_every, dense_
     };
     AdjParams& p = a->ap;
     p.ni = cfg->ni; p.nj = cfg->nj; p.plane = (long long)cfg->ni * cfg->nj;
+    p.xs = (long long)cfg->nj * (cfg->ni + 1);
+    p.ys = (long long)(cfg->nj + 1) * cfg->ni;
+    p.np = dense::tape_planes(cfg->recon);
     p.gamma = cfg->gamma; p.dx = cfg->dx; p.dy = cfg->dy; p.inv_dx = 1.0 / cfg->dx; p.inv_dy = 1.0 / cfg->dy;
     p.cfl = cfg->cfl;
-    a->gx = dim3((cfg->ni + 1 + kFX - 1) / kFX, (cfg->nj + kFY - 1) / kFY);
-    a->gy = dim3((cfg->ni + kFX - 1) / kFX, (cfg->nj + 1 + kFY - 1) / kFY);
+    a->tape_stage = (size_t)p.np * (size_t)(p.xs + p.ys);
+    a->gh = dim3((cfg->ni + 1 + kHX - 1) / kHX, (cfg->nj + 1 + kHY - 1) / kHY, 2);
     a->gc = dim3((cfg->ni + kCX - 1) / kCX, (cfg->nj + kCY - 1) / kCY);
-    a->nbx = (int)(a->gx.x * a->gx.y);
-    a->npart = a->nbx + (int)(a->gy.x * a->gy.y);
+    a->npart = (int)(a->gh.x * a->gh.y * a->gh.z);
     a->nm = (int)(a->gc.x * a->gc.y);
-    const size_t fx = (size_t)40 * cfg->nj * (cfg->ni + 1), fy = (size_t)40 * (cfg->nj + 1) * cfg->ni;
     struct B { double** p; size_t n; } bufs[] = {
         {&a->g, a->state}, {&a->g1, a->state}, {&a->g2, a->state}, {&a->acc, a->state},
-        {&a->Gx, fx}, {&a->Gy, fy}, {&a->part, (size_t)3 * a->npart}, {&a->mpart, (size_t)4 * a->nm},
-        {&a->rec, (size_t)3 * a->k * a->state},
+        {&a->hb, (size_t)4 * (p.xs + p.ys)}, {&a->part, (size_t)3 * a->npart}, {&a->mpart, (size_t)4 * a->nm},
+        {&a->rec, (size_t)3 * a->k * a->state}, {&a->tape, (size_t)3 * a->k * a->tape_stage},
     };
     for (auto& b : bufs) {
         cudaError_t e = cudaMalloc((void**)b.p, b.n * sizeof(double));
@@ -699,10 +621,11 @@ int dense_adjoint_forward(dense_adjoint_t* a, const double* u0, int nsteps, doub
     if (!rc) rc = grow(a, &a->dts, &a->dts_cap, nsteps > 0 ? nsteps : 1, 1);
     if (!rc) rc = grow(a, &a->argmax, &a->argmax_cap, nsteps > 0 ? nsteps : 1, 2);
     if (rc) return rc;
-    ACK(a, cudaMemsetAsync(a->argmax, 0xff, (size_t)2 * a->argmax_cap * sizeof(int), a->h->stream));
     a->nsteps = -1;
     rc = begin(a, stream);
-    if (!rc) rc = restart(a, u0);
+    if (rc) return rc;
+    ACK(a, cudaMemsetAsync(a->argmax, 0xff, (size_t)2 * a->argmax_cap * sizeof(int), a->h->stream));
+    rc = restart(a, u0);
     if (rc) return rc;
     AH(a, dense::handle_step_graph(a->h));
     dense_handle* h = a->h;
@@ -733,21 +656,19 @@ int dense_adjoint_backward(dense_adjoint_t* a, const double* gT, double* g0, voi
         const int s0 = seg * a->k, len = std::min(a->k, a->nsteps - s0);
         rc = restart(a, a->ckpt + (size_t)seg * a->state);
         if (rc) return rc;
-        // recompute the segment, recording each stage's input state
+        // recompute the segment with taping sweeps, recording each stage's input state
         for (int s = 0; s < len; ++s) {
             h->kt->step_begin(h->prm, h->stream);
             for (int irk = 1; irk <= 3; ++irk) {
                 rc = from_solver(a, a->rec + ((size_t)s * 3 + irk - 1) * a->state);
                 if (rc) return rc;
-                h->kt->bc(h->prm, h->stream);
-                h->kt->flux(h->prm, irk, 0, h->stream);
-                h->kt->flux(h->prm, irk, 1, h->stream);
-                h->kt->update(h->prm, irk, h->stream);
+                taped_stage(a, irk, a->tape + ((size_t)s * 3 + irk - 1) * a->tape_stage);
             }
             h->kt->step_end(h->prm, h->stream);
-            a->launches += 2 + 3 * dense::handle_stage_launches(h);
+            a->launches += 2;
         }
-        for (int s = len - 1; s >= 0; --s) reverse_step(a, a->rec + (size_t)s * 3 * a->state, s0 + s);
+        for (int s = len - 1; s >= 0; --s)
+            reverse_step(a, a->rec + (size_t)s * 3 * a->state, a->tape + (size_t)s * 3 * a->tape_stage, s0 + s);
     }
     h->prim_slot = -1;
     ACK(a, cudaMemcpyAsync(g0, a->g, a->state * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
@@ -758,8 +679,15 @@ int dense_adjoint_rhs_vjp(dense_adjoint_t* a, const double* u, const double* v, 
                           void* stream) {
     if (!a || !u || !v || !out) return aerr(a, DENSE_ERR_ARG, "null argument");
     int rc = begin(a, stream);
+    if (!rc) rc = restart(a, u);
     if (rc) return rc;
-    vjp(a, 0, u, v, out, a->part, nullptr);
+    // the first stage's sweeps at u tape its reconstructions and fluxes (the update's result is
+    // not used); step_begin opens the stage (the loop bounds are open after restart)
+    a->h->kt->step_begin(a->h->prm, a->h->stream);
+    a->launches += 1;
+    taped_stage(a, 1, a->tape);
+    a->h->prim_slot = -1;
+    vjp(a, 0, u, a->tape, v, out, a->part, nullptr);
     std::vector<double> part(a->npart);
     ACK(a, cudaMemcpyAsync(part.data(), a->part, a->npart * sizeof(double), cudaMemcpyDeviceToHost, a->h->stream));
     rc = finish(a, stream);

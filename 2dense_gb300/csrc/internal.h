@@ -10,6 +10,10 @@ namespace dense {
 
 constexpr int kB = 4;  // ghost layers per side: allocate_block(...,4,4,neq)
 
+// Planes per direction of the adjoint tape (Params::tape): 40 stencil gradients (none for
+// upwind5) and 4 fluxes.
+constexpr int tape_planes(int recon) { return recon == DENSE_RECON_UPWIND5 ? 4 : 44; }
+
 // Device-resident scalars of one block: the module globals of flow_general that the hot path
 // reads and writes (max_eig_i/j, dt, current_time, current_step), plus the loop predicate.
 struct Scalars {
@@ -50,6 +54,11 @@ struct Params {
     double theta_k1, theta_k2;
     int if_const_dt, bodyforce, benchmark, splitting, recon;
     int count_branches;  // accumulate Scalars::branch_count in the AdaWENO sweeps
+    // Tape of the component-wise LLF sweeps for the discrete adjoint (flux_tape launches only):
+    // per direction tape_planes(recon) planes of the direction's face array (xi [nj][ni+1], eta
+    // [nj+1][ni], eta after xi): the reconstructions' stencil gradients g[(s*5 + m)*4 + v] (s = 0
+    // for F+, 1 for F-; none for upwind5, whose gradient is constant), then the fluxes h[v].
+    double* tape;
 };
 
 // One arithmetic variant of the kernels (fast or strict), as a table of launchers.
@@ -69,6 +78,9 @@ struct KernelTable {
     void (*step_end)(const Params&, void* stream);
     // kernel launches issued by flux(dir) for this configuration
     int (*flux_launches)(const Params&, int dir);
+    // flux(dir) of the component-wise LLF/GLF sweeps with reconstruction 251/253/255 that also
+    // writes Params::tape; identical fluxes and state updates
+    void (*flux_tape)(const Params&, int irk, int dir, void* stream);
 };
 
 const KernelTable* kernels_fast();

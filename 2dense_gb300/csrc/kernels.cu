@@ -21,6 +21,7 @@
 //   he[v][g][i]    g = 0..nj interface between padded rows g+3 and g+4
 #include <cuda_runtime.h>
 
+#include "fastmath.cuh"
 #include "internal.h"
 
 #ifndef DENSE_VARIANT_STRICT
@@ -125,22 +126,7 @@ __device__ __forceinline__ double upwind5(const double lf[5]) {
 //    and the AdaWENO test theta > delta becomes sqrt(1-delta) D > sqrt(delta) (N - D) with
 //    N = sum alpha_k D (theta = 1/(1+(sum alpha - 1)^2)), which needs no divide at all.
 // Products of squared d_k stay far inside the double range for d_k in [1e-6, 1e40].
-__device__ __forceinline__ double rcp_nr(double d) {
-    double r;
-    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(d));
-    double e = fma(-d, r, 1.0);
-    r = fma(r, e, r);
-    e = fma(-d, r, 1.0);
-    return fma(r, e, r);
-}
-__device__ __forceinline__ double rsqrt_nr(double x) {
-    double y;
-    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
-    double e = fma(-x * y, y, 1.0);
-    y = fma(0.5 * y, e, y);
-    e = fma(-x * y, y, 1.0);
-    return fma(0.5 * y, e, y);
-}
+// (rcp_nr and rsqrt_nr: fastmath.cuh)
 
 constexpr double k1312 = 13.0 / 12.0;
 
@@ -204,6 +190,63 @@ __device__ __forceinline__ void stencil_from_weights(double w0, double w1, doubl
     W[2] = fma(w2, a320, fma(w1, a311, w0 * a302));
     W[3] = fma(w2, a321, w1 * a312);
     W[4] = w2 * a322;
+}
+
+// Gradient of the WENO reconstruction with respect to its stencil, g[m] = dW/dlf[m], for the
+// discrete adjoint's tape. W = sum_k w_k q_k with w_k = a_k / sum(a): dW/dq_k = w_k and
+// dW/da_k = (q_k - W)/sum(a); a_k depends on lf through beta_k (JS: a_k = c_k/d_k^2, so
+// da_k/dbeta_k = -2 a_k/d_k; Z: a_k = c_k (1 + tau^2/d_k^2), so da_k/dbeta_k = -2 c_k tau^2/d_k^3
+// and da_k/dtau = 2 c_k tau/d_k^2, tau = |beta_2 - beta_0|; d_k = ss + beta_k), and beta_k =
+// 13/12 A_k^2 + 1/4 B_k^2 on the second differences A_k and the first-order combinations B_k.
+// Written over the common denominators of weno_num_fast (n_k = a_k D, N = sum(a) D, D = prod
+// d_k^2, P_k = D/d_k^2), with the quantities W itself needs computed by the same expressions.
+template <int REC>
+__device__ __forceinline__ void recon_grad(const double lf[5], double g[5]) {
+    if (REC == DENSE_RECON_UPWIND5) {
+        g[0] = 2.0 / 60.0; g[1] = -13.0 / 60.0; g[2] = 47.0 / 60.0; g[3] = 27.0 / 60.0; g[4] = -3.0 / 60.0;
+        return;
+    }
+    constexpr bool Z = REC == DENSE_RECON_WENOZ5;
+    double q0, q1, q2, n0, n1, n2, N, D, d0, d1, d2, tau;
+    candidates_fast(lf, q0, q1, q2);
+    betas_fast(lf, d0, d1, d2, tau);
+    weno_num_fast<Z>(lf, n0, n1, n2, N, D);
+    const double iN = rcp_nr(N);
+    const double h = fma(n2, q2, fma(n1, q1, n0 * q0)) * iN;
+    const double w0 = n0 * iN, w1 = n1 * iN, w2 = n2 * iN;
+    const double e0 = d0 * d0, e1 = d1 * d1, e2 = d2 * d2;
+    const double P0 = e1 * e2, P1 = e0 * e2, P2 = e0 * e1;
+    const double iD = rcp_nr(D);
+    const double id0 = d0 * (P0 * iD), id1 = d1 * (P1 * iD), id2 = d2 * (P2 * iD);  // 1/d_k
+    const double A0 = fma(-2.0, lf[1], lf[0]) + lf[2], B0 = fma(3.0, lf[2], fma(-4.0, lf[1], lf[0]));
+    const double A1 = fma(-2.0, lf[2], lf[1]) + lf[3], B1 = lf[1] - lf[3];
+    const double A2 = fma(-2.0, lf[3], lf[2]) + lf[4], B2 = fma(3.0, lf[2], fma(-4.0, lf[3], lf[4]));
+    double bb0, bb1, bb2;  // dW/dbeta_k
+    if (!Z) {
+        bb0 = -2.0 * (q0 - h) * w0 * id0;
+        bb1 = -2.0 * (q1 - h) * w1 * id1;
+        bb2 = -2.0 * (q2 - h) * w2 * id2;
+    } else {
+        // s_k = (q_k - W)/sum(a) * c_k tau / d_k^2 = (q_k - W) c_k tau P_k / N
+        const double s0 = (q0 - h) * (c30 * tau) * (P0 * iN);
+        const double s1 = (q1 - h) * (c31 * tau) * (P1 * iN);
+        const double s2 = (q2 - h) * (c32 * tau) * (P2 * iN);
+        const double tb = 2.0 * (s0 + s1 + s2);  // dW/dtau
+        const double be0 = fma(k1312 * A0, A0, (0.25 * B0) * B0), be2 = fma(k1312 * A2, A2, (0.25 * B2) * B2);
+        const double sg = be2 >= be0 ? tb : -tb;  // dtau/dbeta_2 = -dtau/dbeta_0 = sign(beta_2 - beta_0)
+        bb0 = -2.0 * s0 * tau * id0 - sg;
+        bb1 = -2.0 * s1 * tau * id1;
+        bb2 = -2.0 * s2 * tau * id2 + sg;
+    }
+    const double CA0 = (13.0 / 6.0) * bb0 * A0, CB0 = 0.5 * bb0 * B0;
+    const double CA1 = (13.0 / 6.0) * bb1 * A1, CB1 = 0.5 * bb1 * B1;
+    const double CA2 = (13.0 / 6.0) * bb2 * A2, CB2 = 0.5 * bb2 * B2;
+    stencil_from_weights(w0, w1, w2, g);
+    g[0] += CA0 + CB0;
+    g[1] += fma(-2.0, CA0, fma(-4.0, CB0, CA1 + CB1));
+    g[2] += fma(3.0, CB0, fma(-2.0, CA1, fma(3.0, CB2, CA0 + CA2)));
+    g[3] += fma(-2.0, CA2, fma(-4.0, CB2, CA1 - CB1));
+    g[4] += CA2 + CB2;
 }
 
 template <int REC> __device__ __forceinline__ double recon5(const double lf[5]) {
@@ -426,7 +469,7 @@ __device__ __forceinline__ void stage_scalars(const Params& p, int irk) {
 // Component-wise flux kernel (splittings 101/102/103 with reconstructions 251/253/255).
 // One thread per interface; the tile's per-cell split fluxes are staged in shared memory.
 // xi tile: TX interfaces x TY rows, cells f0+1 .. f0+TX+5; eta tile: TX columns x TY interfaces.
-template <int DIR, int SPL, int REC, int TX, int TY>
+template <int DIR, int SPL, int REC, int TX, int TY, bool TAPE = false>
 __device__ __forceinline__ void flux_cw_block(const Params& p, int irk, int bx, int by) {
     if (!p.sc->active) return;
     constexpr int NL = DIR == 0 ? TY : TY + 5;   // smem rows
@@ -492,6 +535,23 @@ __device__ __forceinline__ void flux_cw_block(const Params& p, int irk, int bx, 
         const double h = recon5<REC>(lp) + recon5<REC>(lm);
         if (DIR == 0) p.hx[(long long)v * p.nj * (p.ni + 1) + (long long)line * (p.ni + 1) + f] = h;
         else          p.he[(long long)v * (p.nj + 1) * p.ni + (long long)f * p.ni + line] = h;
+        if (TAPE) {
+            constexpr int NP = tape_planes(REC);
+            const long long xs = (long long)p.nj * (p.ni + 1);
+            const long long ts = DIR == 0 ? xs : (long long)(p.nj + 1) * p.ni;
+            double* T = p.tape + (DIR == 0 ? 0 : NP * xs) +
+                        (DIR == 0 ? (long long)line * (p.ni + 1) + f : (long long)f * p.ni + line);
+            if (REC != DENSE_RECON_UPWIND5) {
+                double g[5];
+                recon_grad<REC>(lp, g);
+#pragma unroll
+                for (int m = 0; m < 5; ++m) T[(m * 4 + v) * ts] = g[m];
+                recon_grad<REC>(lm, g);
+#pragma unroll
+                for (int m = 0; m < 5; ++m) T[((5 + m) * 4 + v) * ts] = g[m];
+            }
+            T[(NP - 4 + v) * ts] = h;
+        }
     }
 }
 
@@ -1082,9 +1142,9 @@ __device__ __forceinline__ void bc_block(const Params& p, int bx) {
 
 // ---------------------------------------------------------------------------------------------
 // Kernels of one block (instance) of the solver: block coordinates are the launch's own.
-template <int DIR, int SPL, int REC, int TX, int TY>
+template <int DIR, int SPL, int REC, int TX, int TY, bool TAPE = false>
 __global__ void __launch_bounds__(TX* TY) k_flux_cw(Params p, int irk) {
-    flux_cw_block<DIR, SPL, REC, TX, TY>(p, irk, blockIdx.x, blockIdx.y);
+    flux_cw_block<DIR, SPL, REC, TX, TY, TAPE>(p, irk, blockIdx.x, blockIdx.y);
 }
 template <int DIR, bool ADAPT, int TX, int TY>
 __global__ void __launch_bounds__(TX* TY) k_flux_char(Params p, int irk) {
@@ -1187,6 +1247,29 @@ static void launch_flux(const Params& p, int irk, int dir, void* stream) {
     case DENSE_SPLIT_SC:
         if (dir == 0) k_flux_char<0, true, kXTX, kXTY><<<grid_xi(p, kXTX, kXTY), dim3(kXTX, kXTY), 0, s>>>(p, irk);
         else          k_flux_char<1, true, kETX, kETY_ADAPT><<<grid_eta(p, kETX, kETY_ADAPT), dim3(kETX, kETY_ADAPT), 0, s>>>(p, irk);
+        break;
+    default:
+        break;
+    }
+}
+
+// flux(dir) plus the adjoint tape: LLF/GLF with reconstruction 251, 253 or 255 only
+static void launch_flux_tape(const Params& p, int irk, int dir, void* stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    if (p.splitting != DENSE_SPLIT_LLF && p.splitting != DENSE_SPLIT_GLF) return;
+    const dim3 gx = grid_xi(p, kXTX, kXTY), bx(kXTX, kXTY), ge = grid_eta(p, kETX, kETY), be(kETX, kETY);
+    switch (p.recon) {
+    case DENSE_RECON_UPWIND5:
+        if (dir == 0) k_flux_cw<0, 0, 251, kXTX, kXTY, true><<<gx, bx, 0, s>>>(p, irk);
+        else          k_flux_cw<1, 0, 251, kETX, kETY, true><<<ge, be, 0, s>>>(p, irk);
+        break;
+    case DENSE_RECON_WENOJS5:
+        if (dir == 0) k_flux_cw<0, 0, 253, kXTX, kXTY, true><<<gx, bx, 0, s>>>(p, irk);
+        else          k_flux_cw<1, 0, 253, kETX, kETY, true><<<ge, be, 0, s>>>(p, irk);
+        break;
+    case DENSE_RECON_WENOZ5:
+        if (dir == 0) k_flux_cw<0, 0, 255, kXTX, kXTY, true><<<gx, bx, 0, s>>>(p, irk);
+        else          k_flux_cw<1, 0, 255, kETX, kETY, true><<<ge, be, 0, s>>>(p, irk);
         break;
     default:
         break;
@@ -1324,14 +1407,14 @@ void batch_tile_shape(int splitting, int dir, int variant, int* tx, int* ty) {
 const KernelTable* kernels_strict() {
     static const KernelTable t = {"strict", VNS::launch_prim, VNS::launch_bc, VNS::launch_flux,
                                   VNS::launch_update, VNS::launch_step_begin, VNS::launch_step_end,
-                                  VNS::flux_launches};
+                                  VNS::flux_launches, VNS::launch_flux_tape};
     return &t;
 }
 #else
 const KernelTable* kernels_fast() {
     static const KernelTable t = {"fast", VNS::launch_prim, VNS::launch_bc, VNS::launch_flux,
                                   VNS::launch_update, VNS::launch_step_begin, VNS::launch_step_end,
-                                  VNS::flux_launches};
+                                  VNS::flux_launches, VNS::launch_flux_tape};
     return &t;
 }
 #endif
@@ -1346,9 +1429,9 @@ __global__ void k_fastmath(const double* x, double* out, int n) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const double v = x[k];
-    out[4 * k + 0] = dense::fast_impl::rcp_nr(v);
+    out[4 * k + 0] = dense::rcp_nr(v);
     out[4 * k + 1] = 1.0 / v;
-    out[4 * k + 2] = dense::fast_impl::rsqrt_nr(v);
+    out[4 * k + 2] = dense::rsqrt_nr(v);
     out[4 * k + 3] = 1.0 / sqrt(v);
 }
 }  // namespace

@@ -168,6 +168,16 @@ class Solver:
                                        ctypes.byref(s), ctypes.byref(dt)))
         self.current_time, self.current_step, self.dt = t.value, s.value, dt.value
 
+    def steps_async(self, n: int, t_end: float = float("inf"), total_step: int = 2**31 - 1):
+        """``steps`` without waiting; time and step stay on the device (``dense_get_time``)."""
+        self._chk(self.lib.dense_steps_async(self.h, n, t_end, total_step))
+
+    def stream(self) -> int:
+        """The handle's cudaStream_t, as an integer."""
+        s = ctypes.c_void_p()
+        self._chk(self.lib.dense_get_stream(self.h, ctypes.byref(s)))
+        return s.value or 0
+
 
 class BatchSolver:
     """Many independent blocks of uneven size advanced together (the batched form).

@@ -279,13 +279,149 @@ def run_batched(args, dense, lib):
     print(json.dumps(line), flush=True)
 
 
+def run_adjoint(args, dense, lib):
+    """Gradient of a vortex run through the discrete adjoint: 256x256 periodic vortex, LLF +
+    WENO-JS5, CFL 0.4, 400 steps, checkpoints every 20. Loss 1/2 ||rho(T) - rho_target||^2, the
+    target from the unperturbed vortex (eps 5, centre (5,5)); the run starts from that vortex plus
+    a seeded Gaussian density perturbation of amplitude 1e-3. Gradients w.r.t. the perturbation
+    field and (eps, xc, yc), checked against central differences (h = 1e-6) of the CUDA forward."""
+    import torch
+    adjm = importlib.import_module("2dense_gb300.adjoint")
+    ni = args.ni or 256
+    nj = args.nj or 256
+    n, k = args.adj_steps, 20
+    cfg = dense.init_general(dense.config_default(ni=ni, nj=nj, benchmark=11, splitting=101, recon=253,
+                                                  cfl=0.4, var_eps=5.0, var_xc=5.0, var_yc=5.0))[0]
+    adj = adjm.Adjoint(cfg, checkpoint_every=k)
+    Step = adjm.AdjointStep
+    gen = torch.Generator().manual_seed(args.seed)
+    drho_h = (1e-3 * torch.randn(nj, ni, generator=gen, dtype=torch.float64)).pin_memory()
+    drho0 = drho_h.cuda()
+    target = adj.forward(adjm.vortex_state(cfg, 5.0, 5.0, 5.0), n)[0].clone()
+    theta0 = torch.tensor([5.0, 5.0, 5.0], dtype=torch.float64, device="cuda")
+
+    def loss_fn(theta, drho):
+        uT = Step.apply(adjm.vortex_state(cfg, theta[0], theta[1], theta[2], drho), adj, n)
+        return 0.5 * ((uT[0] - target) ** 2).sum()
+
+    def grads(theta, drho):
+        th = theta.detach().clone().requires_grad_(True)
+        dr = drho.detach().clone().requires_grad_(True)
+        loss = loss_fn(th, dr)
+        g_th, g_dr = torch.autograd.grad(loss, [th, dr])
+        return float(loss.detach()), g_th, g_dr
+
+    for _ in range(max(1, args.warmup)):
+        grads(theta0, drho0)
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    reps = max(1, args.steps)
+    fwd_ms, bwd_ms = [], []
+    launches0 = adj.launch_count()
+    with Clocks(0) as clk:
+        for _ in range(reps):
+            th = theta0.clone().requires_grad_(True)
+            dr = drho0.clone().requires_grad_(True)
+            ev[0].record()
+            loss = loss_fn(th, dr)
+            ev[1].record()
+            g_th, g_dr = torch.autograd.grad(loss, [th, dr])
+            ev[2].record()
+            torch.cuda.synchronize()
+            fwd_ms.append(ev[0].elapsed_time(ev[1]))
+            bwd_ms.append(ev[1].elapsed_time(ev[2]))
+    launches = (adj.launch_count() - launches0) // reps
+    fwd, bwd = statistics.median(fwd_ms), statistics.median(bwd_ms)
+    # the plain solver over the same steps, no checkpoints
+    c, cons, prim, x, y = dense.init_general(cfg)
+    with dense.Solver(c) as s:
+        s.upload(cons, prim, x, y)
+        s.steps(2)
+        stream = torch.cuda.ExternalStream(s.stream())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        s.steps_async(n)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        plain_ms = e0.elapsed_time(e1)
+    # end to end: the perturbation from pinned host memory, forward, backward, gradients to host
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    dr = drho_h.cuda(non_blocking=True).requires_grad_(True)
+    th = theta0.clone().requires_grad_(True)
+    g1, g2 = torch.autograd.grad(loss_fn(th, dr), [th, dr])
+    g_host = g2.cpu(), g1.cpu()
+    e2e_s = time.perf_counter() - t0
+    # central differences in eps, xc, yc and along a smooth direction of the perturbation field
+    # (a Gaussian bump): FD(h) at h = 1e-6, FD(h/2), and their Richardson extrapolation
+    # (4 FD(h/2) - FD(h))/3, which removes the h^2 term. Valid where the cells of the wave-speed
+    # maxima do not change between the runs (dt = cfl/(max/dx + max/dy) has a kink there).
+    loss0, g_th, g_dr = grads(theta0, drho0)
+    trace0 = adj.argmax().copy()
+    xs = (torch.arange(ni, dtype=torch.float64, device="cuda") + 0.5) * 10.0 / ni
+    ys = (torch.arange(nj, dtype=torch.float64, device="cuda") + 0.5) * 10.0 / nj
+    Yg, Xg = torch.meshgrid(ys, xs, indexing="ij")
+    bump = torch.exp(-((Xg - 3.0) ** 2 + (Yg - 6.0) ** 2))
+    h = 1e-6
+    fd = {}
+    for name, (dth, ddr, exact) in {
+            "eps": ((1, 0, 0), None, float(g_th[0])), "xc": ((0, 1, 0), None, float(g_th[1])),
+            "yc": ((0, 0, 1), None, float(g_th[2])),
+            "drho_bump": ((0, 0, 0), bump, float((g_dr * bump).sum()))}.items():
+        same, est = True, {}
+        for hh in (h, h / 2):
+            vals = []
+            for sgn in (1.0, -1.0):
+                th = theta0 + sgn * hh * torch.tensor(dth, dtype=torch.float64, device="cuda")
+                dr = drho0 + (sgn * hh * ddr if ddr is not None else 0.0)
+                lv, _, _ = grads(th, dr)
+                vals.append(lv)
+                same = same and np.array_equal(adj.argmax(), trace0)
+            est[hh] = (vals[0] - vals[1]) / (2 * hh)
+        rich = (4 * est[h / 2] - est[h]) / 3
+        rel = lambda x: abs(x - exact) / max(abs(exact), 1e-300)
+        fd[name] = {"adjoint": exact, "fd_h": est[h], "fd_h2": est[h / 2], "richardson": rich,
+                    "rel_err_fd_h": rel(est[h]), "rel_err_richardson": rel(rich),
+                    "max_cells_unchanged": bool(same)}
+    status = 0
+    cells = ni * nj
+    fl = json.load(open(os.path.join(ROOT, "tests", "golden", "flop_counts.json")))["schemes"]["LLF+WENO-JS5"]
+    peak = ctypes.c_double()
+    lib.dense_measure_fp64(0, ctypes.byref(peak))
+    value = cells * n / ((fwd + bwd) * 1e-3)
+    line = {"metric": METRIC + " (forward + adjoint)", "value": value, "unit": UNIT, "n_gpus": 1, "steps": reps,
+            "warmup": args.warmup, "ms_per_step": (fwd + bwd) / n, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"adjoint: vortex {ni}x{nj} periodic, LLF + WENO-JS5, CFL 0.4, {n} steps, "
+                                   f"checkpoint every {k}; loss 1/2||rho(T)-rho_target||^2",
+                       "ni": ni, "nj": nj, "nsteps": n, "checkpoint_every": k,
+                       "l2": "state (2 MB) fits in L2; no flush: each timed rep is a 400-step chain"},
+            "adjoint": {"forward_ms": fwd, "backward_ms": bwd, "plain_forward_ms": plain_ms,
+                        "backward_over_forward": bwd / fwd, "backward_over_plain_forward": bwd / plain_ms,
+                        "loss": loss0, "fd_check": fd, "fd_h": h,
+                        "max_rel_err_fd_h": max(v["rel_err_fd_h"] for v in fd.values()),
+                        "max_rel_err_richardson": max(v["rel_err_richardson"] for v in fd.values())},
+            "e2e": {"value": cells * n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": drho_h.numel() * 8,
+                    "d2h_bytes_per_step": (g_host[0].numel() + g_host[1].numel()) * 8,
+                    "note": "perturbation field from pinned host memory, forward, backward, gradients to host"},
+            "gpu_launches": launches,
+            "roofline": {"bound": "fp64", "achieved": fl["flops_per_cell_update"] * cells * n / (plain_ms * 1e-3) / 1e12,
+                         "peak": peak.value / 1e12, "unit": "TFLOP/s",
+                         "frac": fl["flops_per_cell_update"] * cells * n / (plain_ms * 1e-3) / peak.value,
+                         "of": "the plain forward's reference FLOPs", "traffic": None},
+            "clocks": clk.summary(), "status_flags": status}
+    adj.close()
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="dmr", choices=sorted(WORKLOADS) + ["batched"])
+    ap.add_argument("--workload", default="dmr", choices=sorted(WORKLOADS) + ["batched", "adjoint"])
     ap.add_argument("--strict", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--cpu-steps", type=int, default=20)
@@ -298,7 +434,19 @@ def main():
     ap.add_argument("--batch", type=int, default=512, help="instances of the batched workload")
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--loop-steps", type=int, default=10, help="steps per instance of the looped plain solves")
+    ap.add_argument("--adj-steps", type=int, default=400, help="time steps of the adjoint workload's run")
     args = ap.parse_args()
+    if args.workload == "adjoint":
+        if args.impl == "reference":
+            rank, _, _ = dist_info()
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "the reference has no derivatives; "
+                                  "there is no adjoint to time"}))
+            return
+        import torch
+        torch.cuda.set_device(0)
+        dense = importlib.import_module("2dense_gb300")
+        return run_adjoint(args, dense, dense.load_library())
     if args.workload == "batched":
         if args.impl == "reference":
             rank, _, _ = dist_info()

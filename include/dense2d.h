@@ -287,6 +287,8 @@ int dense_adjoint_get_dts(dense_adjoint_t* a, double* dts, int n);
 /* after dense_adjoint_backward: per step k, the interior cells j*ni+i where max(|u|+alpha) and
    max(|v|+alpha) were attained (idx[2k], idx[2k+1]); -1 for constant dt (the call waits) */
 int dense_adjoint_get_argmax(dense_adjoint_t* a, int* idx, int n);
+/* the forward solver the adjoint drives (its state after the last call; owned by a) */
+int dense_adjoint_get_solver(dense_adjoint_t* a, dense_handle_t** h);
 long long dense_adjoint_launch_count(dense_adjoint_t* a);
 const char* dense_adjoint_last_error(dense_adjoint_t* a);
 
