@@ -49,6 +49,13 @@ WORKLOADS = {
     "rt": (13, 104, 0, 256, 1024, "Rayleigh-Taylor 256x1024 reflective sides, characteristic "
            "WENO-Z + GLF (104), CFL 0.5", "C3 RT 256x1024 CH"),
 }
+# DRAM bytes (read + write) of one launch of the xi sweep, from one ncu --set full capture of
+# that kernel on the same workload (dram__bytes_read.sum + dram__bytes_write.sum); the capture and
+# its command are summarised in the named profiles/ file.
+XI_TRAFFIC = {
+    "dmr": (59.295e6 + 4.802e6, "profiles/dmr_1920x480_adaweno_kernels.md"),
+    "rt": (17.368e6, "profiles/rt_256x1024_characteristic_kernels.md"),
+}
 METRIC = "FP64 WENO5-RK3 cell-updates/s"
 UNIT = "cell-updates/s"
 
@@ -586,7 +593,8 @@ def main():
                 "frac": achieved * 1e12 / peak.value,
                 "peak_source": "measured live: dense_measure_fp64 FMA-throughput probe on this GPU "
                                "(MEASURED_PEAKS.json has no FP64 figure)",
-                "traffic": None,
+                "traffic": XI_TRAFFIC.get(args.workload, (None,))[0] if not (args.ni and args.nj) else None,
+                "traffic_source": XI_TRAFFIC.get(args.workload, (None, None))[1] if not (args.ni and args.nj) else None,
                 "whole_step": {"achieved_tflops": step_flops * value / cells / world / 1e12,
                                "frac": step_flops * value / cells / world / peak.value,
                                "flops_per_cell_update": step_flops / cells},
