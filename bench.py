@@ -125,6 +125,25 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(x: float) -> float:
+    """Max of x over the ranks of the default process group (x itself when there is none): the
+    timed region of N replicas ends when the slowest rank ends."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(cells: int, steps: int, world: int, total_ms: float) -> float:
+    """Whole-job cell-updates/s of `world` replicas, each advancing `cells` cells `steps` steps,
+    over the slowest rank's time."""
+    return cells * steps * world / (total_ms * 1e-3)
+
+
 def wl_t_start(args) -> float:
     """Start time of the timed steps: the midpoint (t = 0.1) of the reference's double Mach
     reflection run to t = 0.2 for the AdaWENO workload, whose cost depends on the flow; t = 0
@@ -134,7 +153,7 @@ def wl_t_start(args) -> float:
     return 0.1 if args.workload == "dmr" else 0.0
 
 
-def cpu_baseline(cfg_tuple, steps: int, state=None, t_start: float = 0.0):
+def cpu_baseline(cfg_tuple, steps: int, state=None, t_start: float = 0.0, one_thread_steps: int = 0):
     """Time the CPU oracle (OpenMP, all host threads) on the workload, from `state`
     (cons, prim, t, step, dt) when given, else from the setup advanced to t_start."""
     from oracle import oracle as orc
@@ -152,11 +171,21 @@ def cpu_baseline(cfg_tuple, steps: int, state=None, t_start: float = 0.0):
     t0 = time.perf_counter()
     o.steps(steps)
     el = time.perf_counter() - t0
-    threads = orc.load(True).oracle_threads()
-    return {"value": ni * nj * steps / el, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{desc}: {steps} step(s) of the C++ restatement of the reference "
-                      f"(OpenMP, {threads} threads, gcc -O2), after 1 warm-up step",
-            "seconds": el}
+    lib = orc.load(True)
+    threads = lib.oracle_threads()
+    out = {"value": ni * nj * steps / el, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"{desc}: {steps} step(s) of the C++ restatement of the reference "
+                     f"(OpenMP, {threads} threads, gcc -O2), after 1 warm-up step",
+           "seconds": el}
+    if one_thread_steps > 0:  # the same code on one core, a shorter sample of the same state
+        lib.oracle_set_threads(1)
+        t0 = time.perf_counter()
+        o.steps(one_thread_steps)
+        el1 = time.perf_counter() - t0
+        lib.oracle_set_threads(threads)
+        out["one_thread"] = {"value": ni * nj * one_thread_steps / el1, "unit": UNIT, "cores": 1,
+                             "steps": one_thread_steps}
+    return out
 
 
 def run_reference_arm(args, wl):
@@ -534,12 +563,8 @@ def main():
     wall = time.perf_counter() - wall0
     step_ms = [a.elapsed_time(b) for a, b in evs]
     launches = s.launch_count() - launches0
-    total_ms = sum(step_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = cells * args.steps * world / (total_ms * 1e-3)
+    total_ms = max_over_ranks(sum(step_ms))
+    value = replica_value(cells, args.steps, world, total_ms)
     status = s.status()
 
     # per-kernel times of the stage, for the roofline of the dominant kernel
@@ -639,7 +664,8 @@ def main():
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_baseline(wl, args.cpu_steps, state=(snap_cons, snap_prim, snap_t, snap_step, snap_dt))
+        cpu = cpu_baseline(wl, args.cpu_steps, state=(snap_cons, snap_prim, snap_t, snap_step, snap_dt),
+                           one_thread_steps=max(1, args.cpu_steps // 10))
         cpu.pop("seconds", None)
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -1121,6 +1121,14 @@ int oracle_threads(void) {
     return 1;
 #endif
 }
+// Threads of the following OpenMP regions (the CPU baseline is timed at 1 thread and at all).
+void oracle_set_threads(int n) {
+#if defined(_OPENMP)
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
 
 // Count the floating-point operations of one full step (all stages) on field values, starting
 // from the given padded state (or the benchmark's setup when cons is NULL).

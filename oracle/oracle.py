@@ -56,6 +56,7 @@ def load(timed: bool = False) -> ctypes.CDLL:
         "oracle_stage": (i, [vp, i]),
         "oracle_steps": (i, [vp, i, ctypes.c_double, i]),
         "oracle_threads": (i, []),
+        "oracle_set_threads": (None, [i]),
         "oracle_count_step": (i, [cfgp, dp, ctypes.POINTER(ctypes.c_longlong)]),
         "oracle_recon": (i, [i, dp, dp]),
         "oracle_roe_lr": (i, [i, ctypes.c_double, dp, dp, dp, dp, dp]),
