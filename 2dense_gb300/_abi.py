@@ -191,6 +191,14 @@ def load_library(path: str | None = None):
         "dense_count_branches": (_c_int, [vp, _c_int]),
         "dense_get_branch_counts": (_c_int, [vp, ctypes.POINTER(ctypes.c_ulonglong)]),
         "dense_stage_noalloc": (_c_int, [cfgp, _c_int, _c_double, vp, vp, vp, vp, vp, vp, dp, vp]),
+        "dense_upload_device": (_c_int, [vp, vp, vp, vp]),
+        "dense_download_device": (_c_int, [vp, vp, vp, vp]),
+        "dense_rhs_device": (_c_int, [vp, _c_int, vp, vp]),
+        "dense_steps_device": (_c_int, [vp, _c_int, _c_double, _c_int, vp]),
+        "dense_stage_device": (_c_int, [vp, _c_int, vp, vp, _c_double, vp]),
+        "dense_batch_upload_device": (_c_int, [vp, _c_int, vp, vp, vp]),
+        "dense_batch_download_device": (_c_int, [vp, _c_int, vp, vp, vp]),
+        "dense_batch_steps_device": (_c_int, [vp, _c_int, _c_double, _c_int, vp]),
         "dense_adjoint_create": (_c_int, [cfgp, _c_int, ctypes.POINTER(vp)]),
         "dense_adjoint_destroy": (None, [vp]),
         "dense_adjoint_forward": (_c_int, [vp, vp, _c_int, vp, vp]),

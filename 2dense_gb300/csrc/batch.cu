@@ -380,4 +380,53 @@ long long dense_batch_cells(dense_batch_t* b) {
     return s;
 }
 
+
+// ---- device-resident states (the PyTorch form) ----------------------------------------------
+static int batch_wait(dense_batch* b, void* caller, bool caller_waits) {
+    cudaEvent_t e;
+    BCK(b, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    cudaStream_t from = caller_waits ? b->stream : (cudaStream_t)caller;
+    cudaStream_t to = caller_waits ? (cudaStream_t)caller : b->stream;
+    cudaError_t r = cudaEventRecord(e, from);
+    if (r == cudaSuccess) r = cudaStreamWaitEvent(to, e, 0);
+    cudaEventDestroy(e);
+    if (r != cudaSuccess) return bset(b, DENSE_ERR_CUDA, std::string("stream order: ") + cudaGetErrorString(r));
+    return DENSE_OK;
+}
+
+int dense_batch_upload_device(dense_batch_t* b, int i, const double* cons, const double* prim, void* stream) {
+    if (!b || !cons || i < 0 || i >= b->n) return bset(b, DENSE_ERR_ARG, "bad instance or null cons");
+    int rc = batch_wait(b, stream, false);
+    if (rc) return rc;
+    const dense_config_t& c = b->cfg[i];
+    const Params& p = b->prm[i];
+    const int NIp = c.ni + 2 * kB, NJp = c.nj + 2 * kB;
+    const size_t row = (size_t)NIp * sizeof(double), pitch = (size_t)p.P * sizeof(double);
+    BCK(b, cudaMemcpy2DAsync(p.cons, pitch, cons, row, row, (size_t)NJp * 4, cudaMemcpyDeviceToDevice, b->stream));
+    if (prim) BCK(b, cudaMemcpy2DAsync(p.prim, pitch, prim, row, row, (size_t)NJp * 5, cudaMemcpyDeviceToDevice, b->stream));
+    b->prim_valid = false;
+    return batch_wait(b, stream, true);
+}
+
+int dense_batch_download_device(dense_batch_t* b, int i, double* cons, double* prim, void* stream) {
+    if (!b || i < 0 || i >= b->n) return bset(b, DENSE_ERR_ARG, "bad instance");
+    int rc = batch_wait(b, stream, false);
+    if (rc) return rc;
+    const dense_config_t& c = b->cfg[i];
+    const Params& p = b->prm[i];
+    const int NIp = c.ni + 2 * kB, NJp = c.nj + 2 * kB;
+    const size_t row = (size_t)NIp * sizeof(double), pitch = (size_t)p.P * sizeof(double);
+    if (cons) BCK(b, cudaMemcpy2DAsync(cons, row, p.cons, pitch, row, (size_t)NJp * 4, cudaMemcpyDeviceToDevice, b->stream));
+    if (prim) BCK(b, cudaMemcpy2DAsync(prim, row, p.prim, pitch, row, (size_t)NJp * 5, cudaMemcpyDeviceToDevice, b->stream));
+    return batch_wait(b, stream, true);
+}
+
+int dense_batch_steps_device(dense_batch_t* b, int nsteps, double t_end, int total_step, void* stream) {
+    if (!b) return bset(b, DENSE_ERR_ARG, "null batch");
+    int rc = batch_wait(b, stream, false);
+    if (!rc) rc = dense_batch_steps_async(b, nsteps, t_end, total_step);
+    if (rc) return rc;
+    return batch_wait(b, stream, true);
+}
+
 }  // extern "C"

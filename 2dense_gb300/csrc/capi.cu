@@ -143,6 +143,39 @@ int build_step_graph(dense_handle* h) {
     return DENSE_OK;
 }
 
+// rhs[v][j][i] = -(hx[v][j][i+1] - hx[v][j][i])/dx - (he[v][j+1][i] - he[v][j][i])/dy
+__global__ void k_rhs(const double* __restrict__ hx, const double* __restrict__ he, int ni, int nj, double dx,
+                      double dy, double* __restrict__ rhs) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= ni || j >= nj) return;
+    const long long xs = (long long)nj * (ni + 1), ys = (long long)(nj + 1) * ni;
+    for (int v = 0; v < 4; ++v) {
+        const double* X = hx + v * xs + (long long)j * (ni + 1) + i;
+        const double* Y = he + v * ys + (long long)j * ni + i;
+        rhs[(long long)v * ni * nj + (long long)j * ni + i] = -(X[1] - X[0]) / dx - (Y[ni] - Y[0]) / dy;
+    }
+}
+
+// order the handle's stream after the caller's, and the caller's after the handle's
+int wait_for(dense_handle* h, void* caller) {
+    cudaEvent_t e;
+    CK(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    cudaError_t r = cudaEventRecord(e, (cudaStream_t)caller);
+    if (r == cudaSuccess) r = cudaStreamWaitEvent(h->stream, e, 0);
+    cudaEventDestroy(e);
+    if (r != cudaSuccess) return seterr(h, DENSE_ERR_CUDA, std::string("stream order: ") + cudaGetErrorString(r));
+    return DENSE_OK;
+}
+int signal_to(dense_handle* h, void* caller) {
+    cudaEvent_t e;
+    CK(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    cudaError_t r = cudaEventRecord(e, h->stream);
+    if (r == cudaSuccess) r = cudaStreamWaitEvent((cudaStream_t)caller, e, 0);
+    cudaEventDestroy(e);
+    if (r != cudaSuccess) return seterr(h, DENSE_ERR_CUDA, std::string("stream order: ") + cudaGetErrorString(r));
+    return DENSE_OK;
+}
+
 }  // namespace
 
 int dense::handle_ensure_prim(dense_handle* h, int slot) { return ensure_prim(h, slot); }
@@ -445,6 +478,94 @@ int dense_profile_stage(dense_handle_t* h, int irk, float* ms) {
     for (auto& e : ev) cudaEventDestroy(e);
     h->prim_slot = irk % 3;
     return launch_check(h);
+}
+
+
+int dense_upload_device(dense_handle_t* h, const double* cons, const double* prim, void* stream) {
+    if (!h || !cons) return seterr(h, DENSE_ERR_ARG, "null handle or cons");
+    int rc = wait_for(h, stream);
+    if (rc) return rc;
+    const size_t row = (size_t)h->NIp * sizeof(double), pitch = (size_t)h->P * sizeof(double);
+    CK(h, cudaMemcpy2DAsync(h->cons, pitch, cons, row, row, (size_t)h->NJp * 4, cudaMemcpyDeviceToDevice, h->stream));
+    if (prim)
+        CK(h, cudaMemcpy2DAsync(h->prim, pitch, prim, row, row, (size_t)h->NJp * 5, cudaMemcpyDeviceToDevice, h->stream));
+    h->uploaded = true;
+    h->prim_slot = -1;
+    rc = ensure_prim(h, 0);
+    if (rc) return rc;
+    return signal_to(h, stream);
+}
+
+int dense_download_device(dense_handle_t* h, double* cons, double* prim, void* stream) {
+    if (!h) return seterr(h, DENSE_ERR_ARG, "null handle");
+    if (!h->uploaded) return seterr(h, DENSE_ERR_STATE, "dense_download_device before an upload");
+    int rc = wait_for(h, stream);
+    if (rc) return rc;
+    const size_t row = (size_t)h->NIp * sizeof(double), pitch = (size_t)h->P * sizeof(double);
+    if (cons)
+        CK(h, cudaMemcpy2DAsync(cons, row, h->cons, pitch, row, (size_t)h->NJp * 4, cudaMemcpyDeviceToDevice, h->stream));
+    if (prim)
+        CK(h, cudaMemcpy2DAsync(prim, row, h->prim, pitch, row, (size_t)h->NJp * 5, cudaMemcpyDeviceToDevice, h->stream));
+    return signal_to(h, stream);
+}
+
+int dense_rhs_device(dense_handle_t* h, int irk, double* rhs, void* stream) {
+    if (!h || !rhs) return seterr(h, DENSE_ERR_ARG, "null argument");
+    if (irk < 1 || irk > 3) return seterr(h, DENSE_ERR_ARG, "irk must be 1, 2 or 3");
+    if (!h->uploaded) return seterr(h, DENSE_ERR_STATE, "dense_rhs_device before an upload");
+    int rc = wait_for(h, stream);
+    if (!rc) rc = ensure_prim(h, irk - 1);
+    if (rc) return rc;
+    k_set_active<<<1, 1, 0, h->stream>>>(h->sc);
+    h->kt->bc(h->prm, h->stream);
+    h->kt->flux(h->prm, irk, 0, h->stream);
+    h->kt->flux(h->prm, irk, 1, h->stream);
+    const dim3 b(32, 8), g((h->cfg.ni + 31) / 32, (h->cfg.nj + 7) / 8);
+    k_rhs<<<g, b, 0, h->stream>>>(h->hx, h->he, h->cfg.ni, h->cfg.nj, h->cfg.dx, h->cfg.dy, rhs);
+    h->launches += 2 + h->kt->flux_launches(h->prm, 0) + h->kt->flux_launches(h->prm, 1) + 1;
+    rc = launch_check(h);
+    if (rc) return rc;
+    return signal_to(h, stream);
+}
+
+// dt_dev: for irk 1 without constant dt receives the CFL time step; otherwise gives it
+__global__ void k_dt_in(Scalars* sc, const double* dt, int irk, int const_dt) {
+    if (irk > 1 || const_dt) sc->dt = *dt;
+}
+__global__ void k_dt_out(const Scalars* sc, double* dt) { *dt = sc->dt; }
+
+int dense_stage_device(dense_handle_t* h, int irk, const double* cons0, double* dt, double current_time,
+                       void* stream) {
+    if (!h || !dt) return seterr(h, DENSE_ERR_ARG, "null argument");
+    if (irk < 1 || irk > 3) return seterr(h, DENSE_ERR_ARG, "irk must be 1, 2 or 3");
+    if (irk > 1 && !cons0) return seterr(h, DENSE_ERR_ARG, "stages 2 and 3 need the step's initial state");
+    if (!h->uploaded) return seterr(h, DENSE_ERR_STATE, "dense_stage_device before an upload");
+    int rc = wait_for(h, stream);
+    if (rc) return rc;
+    if (irk > 1) {
+        const size_t row = (size_t)h->NIp * sizeof(double), pitch = (size_t)h->P * sizeof(double);
+        CK(h, cudaMemcpy2DAsync(h->cons0, pitch, cons0, row, row, (size_t)h->NJp * 4, cudaMemcpyDeviceToDevice,
+                                h->stream));
+    }
+    rc = ensure_prim(h, irk - 1);
+    if (rc) return rc;
+    k_set_loop<<<1, 1, 0, h->stream>>>(h->sc, current_time, 0, 0.0, 0, 1);
+    k_dt_in<<<1, 1, 0, h->stream>>>(h->sc, dt, irk, h->cfg.if_const_dt);
+    enqueue_stage(h, irk);
+    k_dt_out<<<1, 1, 0, h->stream>>>(h->sc, dt);
+    h->launches += 3 + stage_launches(h);
+    rc = launch_check(h);
+    if (rc) return rc;
+    h->prim_slot = irk % 3;
+    return signal_to(h, stream);
+}
+
+int dense_steps_device(dense_handle_t* h, int nsteps, double t_end, int total_step, void* stream) {
+    if (!h) return seterr(h, DENSE_ERR_ARG, "null handle");
+    int rc = wait_for(h, stream);
+    if (!rc) rc = dense_steps_async(h, nsteps, t_end, total_step);
+    if (rc) return rc;
+    return signal_to(h, stream);
 }
 
 }  // extern "C"

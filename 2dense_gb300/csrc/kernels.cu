@@ -1219,10 +1219,38 @@ static inline dim3 grid_eta(const Params& p, int tx, int ty) {
     return dim3((p.ni + tx - 1) / tx, (p.nj + 1 + ty - 1) / ty);
 }
 
+// Streaming multiprocessors of the current device (queried once).
+static int sm_count() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+            n = 152;
+    }
+    return n;
+}
+
+// On small grids the standard tiles give a sweep only one or two blocks per SM, and the SMs that
+// get one more block than the others set the launch's time. Below four blocks per SM the sweep
+// runs with tiles of half the height, which doubles the block count (same arithmetic per
+// interface: the results do not depend on the tile).
 template <int SPL, int REC>
 static void launch_cw(const Params& p, int irk, int dir, cudaStream_t s) {
-    if (dir == 0) k_flux_cw<0, SPL, REC, kXTX, kXTY><<<grid_xi(p, kXTX, kXTY), dim3(kXTX, kXTY), 0, s>>>(p, irk);
-    else          k_flux_cw<1, SPL, REC, kETX, kETY><<<grid_eta(p, kETX, kETY), dim3(kETX, kETY), 0, s>>>(p, irk);
+    const unsigned few = 4u * sm_count();
+    if (dir == 0) {
+        const dim3 g = grid_xi(p, kXTX, kXTY);
+        if (g.x * g.y < few)
+            k_flux_cw<0, SPL, REC, kXTX, kXTY / 2><<<grid_xi(p, kXTX, kXTY / 2), dim3(kXTX, kXTY / 2), 0, s>>>(p, irk);
+        else
+            k_flux_cw<0, SPL, REC, kXTX, kXTY><<<g, dim3(kXTX, kXTY), 0, s>>>(p, irk);
+    } else {
+        const dim3 g = grid_eta(p, kETX, kETY);
+        if (g.x * g.y < few)
+            k_flux_cw<1, SPL, REC, kETX, kETY / 2><<<grid_eta(p, kETX, kETY / 2), dim3(kETX, kETY / 2), 0, s>>>(p, irk);
+        else
+            k_flux_cw<1, SPL, REC, kETX, kETY><<<g, dim3(kETX, kETY), 0, s>>>(p, irk);
+    }
 }
 
 static bool recon_known(int r) {

@@ -210,13 +210,13 @@ def run_reference_arm(args, wl):
     print(json.dumps(line), flush=True)
 
 
-def batched_configs(dense, n: int = 512, seed: int = 2024):
+def batched_configs(dense, n: int = 512, seed: int = 2024, nmin: int = 64, nmax: int = 512):
     """The batched workload: n square periodic instances, N drawn uniformly from
-    {64, 96, ..., 512}; even instances a translating vortex with strength U[1,5] and centre
-    offset U[-1,1]^2, odd ones a Mach 1.2 shock into a density-3 interface of amplitude
-    U[0.01,0.05]; LLF + WENO-Z5, CFL 0.5, each with its own CFL time step."""
+    {nmin, nmin+32, ..., nmax} (64..512 by default); even instances a translating vortex with
+    strength U[1,5] and centre offset U[-1,1]^2, odd ones a Mach 1.2 shock into a density-3
+    interface of amplitude U[0.01,0.05]; LLF + WENO-Z5, CFL 0.5, each with its own CFL time step."""
     rng = np.random.default_rng(seed)
-    sizes = list(range(64, 513, 32))
+    sizes = list(range(nmin, nmax + 1, 32))
     cfgs = []
     for k in range(n):
         N = int(rng.choice(sizes))
@@ -236,7 +236,7 @@ def run_batched(args, dense, lib):
     import torch
     at = importlib.import_module("2dense_gb300.autotune")
     n = args.batch
-    cfgs = batched_configs(dense, n, seed=args.seed)
+    cfgs = batched_configs(dense, n, seed=args.seed, nmin=args.batch_nmin, nmax=args.batch_nmax)
     setups = [dense.init_general(c) for c in cfgs]
     cfgs = [s[0] for s in setups]
     cells = sum(c.ni * c.nj for c in cfgs)
@@ -296,7 +296,8 @@ def run_batched(args, dense, lib):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"batched: {n} periodic instances, N in 64..512 (seed {args.seed}), "
+            "config": {"workload": f"batched: {n} periodic instances, N in {args.batch_nmin}..{args.batch_nmax} "
+                                   f"(seed {args.seed}), "
                                    "vortex / Richtmyer-Meshkov, LLF + WENO-Z5, CFL 0.5",
                        "instances": n, "cells": cells, "n_min": sizes[0], "n_max": sizes[-1],
                        "l2": "inputs larger than L2 (about 1.7 GB per state copy)"},
@@ -469,6 +470,8 @@ def main():
     ap.add_argument("--load-state", default="", help="start from a state written by --save-state")
     ap.add_argument("--batch", type=int, default=512, help="instances of the batched workload")
     ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--batch-nmin", type=int, default=64, help="smallest instance size of the batched workload")
+    ap.add_argument("--batch-nmax", type=int, default=512, help="largest instance size of the batched workload")
     ap.add_argument("--loop-steps", type=int, default=10, help="steps per instance of the looped plain solves")
     ap.add_argument("--adj-steps", type=int, default=400, help="time steps of the adjoint workload's run")
     args = ap.parse_args()

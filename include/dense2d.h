@@ -209,6 +209,26 @@ int dense_get_time(dense_handle_t* h, double* t, int* step, double* dt);
 /* Wait for all work on the handle's stream. */
 int dense_sync(dense_handle_t* h);
 
+/* ---- device-resident state (the PyTorch form): no counterpart in the reference ---------- */
+
+/* Device arrays in the layout of dense_upload's host arrays: cons[4][NJp][NIp] (Fortran
+   cons(NIp,NJp,4)), prim[5][NJp][NIp] (rho, u, v, p, alpha; may be NULL: get_primary of cons).
+   `stream` is the caller's cudaStream_t (0 for the default stream): each call starts after the
+   work already queued there and makes it wait for the call's own work; none blocks the host. */
+int dense_upload_device(dense_handle_t* h, const double* cons, const double* prim, void* stream);
+int dense_download_device(dense_handle_t* h, double* cons, double* prim, void* stream);
+/* rhs[4][nj][ni] = L(u) of the current state, -(h_xi(i+1)-h_xi(i))/dx - (h_eta(j+1)-h_eta(j))/dy,
+   the operator one stage applies (boundary fill and both sweeps of stage `irk`; the state is
+   left unchanged) */
+int dense_rhs_device(dense_handle_t* h, int irk, double* rhs, void* stream);
+/* one stage (dense_stage) on the uploaded state; cons0[4][NJp][NIp] is the step's initial state
+   (needed by stages 2 and 3, NULL for stage 1); *dt (a device double) receives the CFL time step
+   of stage 1 and gives dt to stages 2 and 3 and to constant-dt runs */
+int dense_stage_device(dense_handle_t* h, int irk, const double* cons0, double* dt, double current_time,
+                       void* stream);
+/* nsteps step graphs as dense_steps_async, ordered on the caller's stream */
+int dense_steps_device(dense_handle_t* h, int nsteps, double t_end, int total_step, void* stream);
+
 /* Run one stage with CUDA events between its kernels; ms[0..3] = boundary fill, xi flux,
    eta flux, update (+ get_primary). Advances the state like dense_stage. */
 int dense_profile_stage(dense_handle_t* h, int irk, float* ms);
@@ -257,6 +277,12 @@ int dense_batch_status(dense_batch_t* b, unsigned* flags);
 long long dense_batch_launch_count(dense_batch_t* b);
 long long dense_batch_cells(dense_batch_t* b);
 const char* dense_batch_last_error(dense_batch_t* b);
+/* device-array forms for the PyTorch form (layouts and stream ordering as dense_upload_device;
+   the double Mach reflection and shock / shear layer rules' x, y rows come only from
+   dense_batch_upload) */
+int dense_batch_upload_device(dense_batch_t* b, int i, const double* cons, const double* prim, void* stream);
+int dense_batch_download_device(dense_batch_t* b, int i, double* cons, double* prim, void* stream);
+int dense_batch_steps_device(dense_batch_t* b, int nsteps, double t_end, int total_step, void* stream);
 
 /* ---- discrete adjoint of the time step -------------------------------------------------- */
 
