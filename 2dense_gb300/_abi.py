@@ -191,6 +191,10 @@ def load_library(path: str | None = None):
         "dense_count_branches": (_c_int, [vp, _c_int]),
         "dense_get_branch_counts": (_c_int, [vp, ctypes.POINTER(ctypes.c_ulonglong)]),
         "dense_stage_noalloc": (_c_int, [cfgp, _c_int, _c_double, vp, vp, vp, vp, vp, vp, dp, vp]),
+        "dense_setup_config": (_c_int, [cfgp]),
+        "dense_init_device": (_c_int, [vp]),
+        "dense_vortex_error": (_c_int, [vp, dp, dp]),
+        "dense_batch_init_device": (_c_int, [vp]),
         "dense_upload_device": (_c_int, [vp, vp, vp, vp]),
         "dense_download_device": (_c_int, [vp, vp, vp, vp]),
         "dense_rhs_device": (_c_int, [vp, _c_int, vp, vp]),

@@ -6,6 +6,7 @@ Translation units, compiled in parallel:
   capi.cu     the C ABI (handles, graphs, copies)
   batch.cu    the batched form (many blocks per launch)
   adjoint.cu  the discrete adjoint of the time step
+  setup_device.cu  device-side setups of the variant benchmarks, vortex error norms
   noalloc.cu, probe.cu  the allocation-free stage and the FP64 throughput probes
   host_setup.cpp  namelist reader and initial setups, g++ -ffp-contract=off so the initial
               state rounds exactly like the reference's gfortran -O2 build on x86-64
@@ -68,6 +69,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         "noalloc": [nvcc, *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, "noalloc.cu")],
         "batch": [nvcc, *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, "batch.cu")],
         "adjoint": [nvcc, *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, "adjoint.cu")],
+        "setup_device": [nvcc, *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, "setup_device.cu")],
         "host_setup": ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-c",
                        os.path.join(CSRC, "host_setup.cpp")],
     }

@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "internal.h"
+#include "setups.cuh"
 
 using dense::BatchLaunch;
 using dense::Params;
@@ -380,6 +381,46 @@ long long dense_batch_cells(dense_batch_t* b) {
     return s;
 }
 
+
+// ---- device-side setups ---------------------------------------------------------------------
+// One thread per interior cell of every instance (the 32 x 8 cell map), each instance's setup
+// parameters (eps, xc, yc, amp) from `vars`.
+__global__ void kb_init(const Params* tab, const int3* map, const double* vars) {
+    __shared__ Params sp;
+    const int3 m = map[blockIdx.x];
+    if (threadIdx.x == 0 && threadIdx.y == 0) sp = tab[m.x];
+    __syncthreads();
+    const int i = m.y * blockDim.x + threadIdx.x, j = m.z * blockDim.y + threadIdx.y;
+    const double* v = vars + 4 * m.x;
+    if (i < sp.ni && j < sp.nj) dense::setups::init_cell(sp, v[0], v[1], v[2], v[3], i, j);
+}
+
+int dense_batch_init_device(dense_batch_t* b) {
+    if (!b) return bset(b, DENSE_ERR_ARG, "null batch");
+    std::vector<double> vars((size_t)4 * b->n);
+    for (int i = 0; i < b->n; ++i) {
+        const dense_config_t& c = b->cfg[i];
+        if (c.benchmark != DENSE_BENCH_IVC_PERIODIC && c.benchmark != DENSE_BENCH_RT_REFLECT &&
+            c.benchmark != DENSE_BENCH_RM_PERIODIC)
+            return bset(b, DENSE_ERR_BENCHMARK, "device setups exist for benchmarks 11, 13 and 14");
+        vars[4 * i] = c.var_eps; vars[4 * i + 1] = c.var_xc; vars[4 * i + 2] = c.var_yc; vars[4 * i + 3] = c.var_amp;
+    }
+    BCK(b, cudaMemsetAsync(b->pool, 0, b->pool_bytes, b->stream));
+    double* dv = nullptr;
+    BCK(b, cudaMallocAsync((void**)&dv, vars.size() * sizeof(double), b->stream));
+    BCK(b, cudaMemcpyAsync(dv, vars.data(), vars.size() * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+    kb_init<<<b->bl.nb_cells, dim3(32, 8), 0, b->stream>>>(b->tab, (const int3*)b->bl.map_cells, dv);
+    b->launches += 1;
+    BCK(b, cudaGetLastError());
+    BCK(b, cudaFreeAsync(dv, b->stream));
+    for (int i = 0; i < b->n; ++i) {
+        int rc = dense_batch_set_time(b, i, 0.0, 0);
+        if (rc) return rc;
+    }
+    BCK(b, cudaStreamSynchronize(b->stream));  // vars is a host buffer
+    b->prim_valid = false;
+    return DENSE_OK;
+}
 
 // ---- device-resident states (the PyTorch form) ----------------------------------------------
 static int batch_wait(dense_batch* b, void* caller, bool caller_waits) {

@@ -388,6 +388,29 @@ int dense_read_namelist(const char* path, dense_config_t* cfg) {
     return DENSE_OK;
 }
 
+int dense_setup_config(dense_config_t* cfg) {
+    if (!cfg) return fail(DENSE_ERR_ARG, "null argument");
+    if (cfg->ni < 3 || cfg->nj < 3) return fail(DENSE_ERR_ARG, "ni and nj must be >= 3");
+    const double ni = cfg->ni, nj = cfg->nj;
+    // the geometry lines of setup() above, without the arrays
+    switch (cfg->benchmark) {
+    case DENSE_BENCH_IVC: case DENSE_BENCH_IVC_PERIODIC: cfg->dx = 10.0 / ni; cfg->dy = 10.0 / nj; break;
+    case DENSE_BENCH_SEDOV: cfg->dx = 1.2 / ni; cfg->dy = 1.2 / nj; break;
+    case DENSE_BENCH_RT: case DENSE_BENCH_RT_REFLECT:
+        cfg->if_bodyforce = 1;
+        cfg->gamma = 5.0 / 3.0;
+        cfg->dx = 0.25 / (ni - 1.0); cfg->dy = 1.0 / (nj - 1.0);
+        break;
+    case DENSE_BENCH_RM: case DENSE_BENCH_DMR: cfg->dx = 4.0 / ni; cfg->dy = 1.0 / nj; break;
+    case DENSE_BENCH_RM_PERIODIC: cfg->dx = 1.0 / ni; cfg->dy = 1.0 / nj; break;
+    case DENSE_BENCH_SSL: cfg->dx = 200.0 / ni; cfg->dy = 40.0 / nj; break;
+    case DENSE_BENCH_SHOCKVORTEX: cfg->dx = 2.0 / ni; cfg->dy = 1.0 / nj; break;
+    case DENSE_BENCH_USER: case 7: case 8: break;  // nothing is initialised (init_general.f90:26-33)
+    default: return fail(DENSE_ERR_BENCHMARK, "No such Benchmark index! (init_general.f90:34-36)");
+    }
+    return DENSE_OK;
+}
+
 int dense_array_sizes(const dense_config_t* cfg, long long* cons_count, long long* prim_count,
                       long long* xy_count) {
     if (!cfg || cfg->ni <= 0 || cfg->nj <= 0) return fail(DENSE_ERR_ARG, "bad config");

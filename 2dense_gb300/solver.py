@@ -51,6 +51,15 @@ def read_par_namelist(path: str, cfg: DenseConfig | None = None) -> DenseConfig:
     return c
 
 
+def setup_config(cfg: DenseConfig) -> DenseConfig:
+    """The configuration part of init_general (dx, dy; gamma and the body force for
+    Rayleigh-Taylor) without building the arrays."""
+    lib = _abi.load_library()
+    c = cfg.copy()
+    _check(lib, lib.dense_setup_config(ctypes.byref(c)))
+    return c
+
+
 def init_general(cfg: DenseConfig):
     """init_general (init_general.f90:13-37): returns (cfg, cons, prim, x, y), with cfg.dx/dy
     (and gamma, if_bodyforce for Rayleigh-Taylor) as the setup leaves them."""
@@ -168,6 +177,17 @@ class Solver:
                                        ctypes.byref(s), ctypes.byref(dt)))
         self.current_time, self.current_step, self.dt = t.value, s.value, dt.value
 
+    def init_device(self):
+        """The benchmark's initial state computed on the device (benchmarks 11, 13, 14)."""
+        self._chk(self.lib.dense_init_device(self.h))
+        self.current_time, self.current_step = 0.0, 0
+
+    def vortex_error(self):
+        """(mean, max) of |rho - rho_exact| of the translating vortex at the current time."""
+        l1, linf = ctypes.c_double(), ctypes.c_double()
+        self._chk(self.lib.dense_vortex_error(self.h, ctypes.byref(l1), ctypes.byref(linf)))
+        return l1.value, linf.value
+
     def steps_async(self, n: int, t_end: float = float("inf"), total_step: int = 2**31 - 1):
         """``steps`` without waiting; time and step stay on the device (``dense_get_time``)."""
         self._chk(self.lib.dense_steps_async(self.h, n, t_end, total_step))
@@ -240,6 +260,10 @@ class BatchSolver:
     def steps(self, n: int, t_end: float = float("inf"), total_step: int = 2**31 - 1, wait: bool = True):
         fn = self.lib.dense_batch_steps if wait else self.lib.dense_batch_steps_async
         self._chk(fn(self.h, n, t_end, total_step))
+
+    def init_device(self):
+        """Every instance's initial state computed on the device (benchmarks 11, 13, 14)."""
+        self._chk(self.lib.dense_batch_init_device(self.h))
 
     def set_schedule(self, xi_variant: int, eta_variant: int, order: int):
         self._chk(self.lib.dense_batch_set_schedule(self.h, xi_variant, eta_variant, order))

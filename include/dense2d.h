@@ -130,6 +130,9 @@ int dense_read_namelist(const char* path, dense_config_t* cfg);
    and if_bodyforce=1 as init_RT_general.f90:9-10 does). Ghost cells are zeroed, like
    allocate_block (flow_mod_general.f90:207-208), except where the setup writes them. */
 int dense_init_setup(dense_config_t* cfg, double* cons, double* prim, double* x, double* y);
+/* the configuration part of dense_init_setup alone: cfg->dx, cfg->dy (and gamma, if_bodyforce
+   for Rayleigh-Taylor), without building any array */
+int dense_setup_config(dense_config_t* cfg);
 
 /* Bytes of the host arrays for cfg: cons, prim, x (== y). */
 int dense_array_sizes(const dense_config_t* cfg, long long* cons_count, long long* prim_count,
@@ -209,6 +212,17 @@ int dense_get_time(dense_handle_t* h, double* t, int* step, double* dt);
 /* Wait for all work on the handle's stream. */
 int dense_sync(dense_handle_t* h);
 
+/* ---- device-side setups and error norms: no counterpart in the reference ------------------ */
+
+/* The initial state of the handle's benchmark computed on the device (benchmarks 11, 13 and 14,
+   the variants that workloads generate in bulk; cfg as dense_setup_config leaves it), time and
+   step set to 0. Same formulas as dense_init_setup with CUDA's pow/exp/cos/sqrt: within a few
+   ulp of the host setup, not bit-identical to it. */
+int dense_init_device(dense_handle_t* h);
+/* Translating vortex (11): mean and max over the interior of |rho - rho_exact| at the handle's
+   current time, rho_exact the initial vortex moved by (t, t) on the periodic square (syncs). */
+int dense_vortex_error(dense_handle_t* h, double* l1, double* linf);
+
 /* ---- device-resident state (the PyTorch form): no counterpart in the reference ---------- */
 
 /* Device arrays in the layout of dense_upload's host arrays: cons[4][NJp][NIp] (Fortran
@@ -277,6 +291,9 @@ int dense_batch_status(dense_batch_t* b, unsigned* flags);
 long long dense_batch_launch_count(dense_batch_t* b);
 long long dense_batch_cells(dense_batch_t* b);
 const char* dense_batch_last_error(dense_batch_t* b);
+/* every instance's initial state computed on the device (dense_init_device; benchmarks 11, 13,
+   14), times and steps set to 0 */
+int dense_batch_init_device(dense_batch_t* b);
 /* device-array forms for the PyTorch form (layouts and stream ordering as dense_upload_device;
    the double Mach reflection and shock / shear layer rules' x, y rows come only from
    dense_batch_upload) */

@@ -123,3 +123,12 @@ def test_shock_vortex_post_shock_state_matches_shock_relation(dense):
     c, cons, prim, x, y = dense.init_general(dense.config_default(ni=40, nj=20, benchmark=9))
     right = prim[-5, 10, :4]  # last interior column (x > 0.5)
     assert right[0] == g["rho"] and right[1] == g["u"] and right[3] == g["p"]
+
+
+def test_setup_config_matches_init_general(dense):
+    """dense_setup_config gives the configuration dense_init_setup leaves, without the arrays."""
+    for b in (1, 2, 3, 4, 5, 6, 9, 11, 13, 14):
+        c = dense.config_default(ni=40, nj=24, benchmark=b)
+        a = dense.init_general(c)[0]
+        g = dense.setup_config(c)
+        assert (g.dx, g.dy, g.gamma, g.if_bodyforce) == (a.dx, a.dy, a.gamma, a.if_bodyforce), b
