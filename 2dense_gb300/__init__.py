@@ -9,4 +9,4 @@ importing ``Solver`` without it raises.
 from ._abi import (DenseConfig, DenseError, default_config, load_library, array_sizes,  # noqa: F401
                    LIB_PATH)
 from .solver import (BatchSolver, Solver, config_default, init_general,  # noqa: F401
-                     read_par_namelist, setup_config)
+                     read_binary, read_par_namelist, setup_config)

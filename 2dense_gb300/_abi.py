@@ -192,6 +192,11 @@ def load_library(path: str | None = None):
         "dense_get_branch_counts": (_c_int, [vp, ctypes.POINTER(ctypes.c_ulonglong)]),
         "dense_stage_noalloc": (_c_int, [cfgp, _c_int, _c_double, vp, vp, vp, vp, vp, vp, dp, vp]),
         "dense_setup_config": (_c_int, [cfgp]),
+        "dense_write_tecplot": (_c_int, [vp, ctypes.c_char_p]),
+        "dense_write_binary": (_c_int, [vp, ctypes.c_char_p]),
+        "dense_read_binary": (_c_int, [ctypes.c_char_p, cfgp, dp, dp, dp, ctypes.POINTER(_c_int), dp]),
+        "dense_run": (_c_int, [vp, ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(_c_int)]),
+        "dense_grid_coords": (_c_int, [cfgp, dp, dp, dp, dp]),
         "dense_init_device": (_c_int, [vp]),
         "dense_vortex_error": (_c_int, [vp, dp, dp]),
         "dense_batch_init_device": (_c_int, [vp]),

@@ -7,6 +7,7 @@ Translation units, compiled in parallel:
   batch.cu    the batched form (many blocks per launch)
   adjoint.cu  the discrete adjoint of the time step
   setup_device.cu  device-side setups of the variant benchmarks, vortex error norms
+  io.cu       the save path: Tecplot and checkpoint files, the driver loop with device-side saves
   noalloc.cu, probe.cu  the allocation-free stage and the FP64 throughput probes
   host_setup.cpp  namelist reader and initial setups, g++ -ffp-contract=off so the initial
               state rounds exactly like the reference's gfortran -O2 build on x86-64
@@ -70,6 +71,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         "batch": [nvcc, *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, "batch.cu")],
         "adjoint": [nvcc, *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, "adjoint.cu")],
         "setup_device": [nvcc, *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, "setup_device.cu")],
+        "io": [nvcc, *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, "io.cu")],
         "host_setup": ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-c",
                        os.path.join(CSRC, "host_setup.cpp")],
     }
@@ -90,7 +92,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
             print(txt)
         objs.append(obj)
     tmp = LIB + ".tmp"
-    link = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcuda"]
+    link = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcuda", "-lpthread"]
     r = subprocess.run(link, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{' '.join(link)}\n{r.stdout.decode()}")

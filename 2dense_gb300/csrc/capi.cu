@@ -12,6 +12,7 @@
 #include "handle.h"
 
 extern "C" const char* dense_host_last_error(void);
+extern "C" const char* dense_io_last_error(void);
 
 using dense::KernelTable;
 using dense::Params;
@@ -187,6 +188,8 @@ extern "C" {
 const char* dense_last_error(dense_handle_t* h) {
     if (h) return h->err.c_str();
     if (!g_err.empty()) return g_err.c_str();
+    const char* io = dense_io_last_error();
+    if (io && *io) return io;
     return dense_host_last_error();
 }
 

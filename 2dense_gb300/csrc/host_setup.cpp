@@ -411,6 +411,33 @@ int dense_setup_config(dense_config_t* cfg) {
     return DENSE_OK;
 }
 
+int dense_grid_coords(const dense_config_t* cfg, double* x, double* y, double* vx, double* vy) {
+    if (!cfg || cfg->ni < 1 || cfg->nj < 1) return fail(DENSE_ERR_ARG, "bad config");
+    const int ni = cfg->ni, nj = cfg->nj, b = cfg->benchmark;
+    const bool vertex = b == DENSE_BENCH_RT || b == DENSE_BENCH_RT_REFLECT;  // init_RT_general.f90:16-22
+    const bool none = b == DENSE_BENCH_USER || b == 7 || b == 8;
+    const double ys = b == DENSE_BENCH_SSL ? 40.0 / 2.0 : 0.0;             // init_ssl_general.f90:28
+    const double dx = cfg->dx, dy = cfg->dy;
+    // cell coordinates x(ni,nj), y(ni,nj) as the setups write them
+    for (int j = 1; j <= nj; ++j)
+        for (int i = 1; i <= ni; ++i) {
+            const size_t o = (size_t)(i - 1) + (size_t)ni * (j - 1);
+            const double cx = none ? 0.0 : vertex ? (i - 1.0) * dx : (i - 0.5) * dx;
+            const double cy = none ? 0.0 : vertex ? (j - 1.0) * dy : (j - 0.5) * dy - ys;
+            if (x) x[o] = cx;
+            if (y) y[o] = cy;
+        }
+    // vertex coordinates vet_x(ni+1,nj+1), vet_y (e.g. init_IVC_general.f90:28-29; RT :29-30)
+    for (int j = 1; j <= nj + 1; ++j)
+        for (int i = 1; i <= ni + 1; ++i) {
+            const size_t o = (size_t)(i - 1) + (size_t)(ni + 1) * (j - 1);
+            const double ox = vertex ? 1.5 : 1.0;
+            if (vx) vx[o] = none ? 0.0 : (i - ox) * dx;
+            if (vy) vy[o] = none ? 0.0 : (j - ox) * dy - ys;
+        }
+    return DENSE_OK;
+}
+
 int dense_array_sizes(const dense_config_t* cfg, long long* cons_count, long long* prim_count,
                       long long* xy_count) {
     if (!cfg || cfg->ni <= 0 || cfg->nj <= 0) return fail(DENSE_ERR_ARG, "bad config");

@@ -32,6 +32,12 @@ struct Scalars {
     // per sweep direction d (xi 0, eta 1) at [4d + k]: k = 0 smooth branch, 1 characteristic
     // branch, 2 warps, 3 warps with a characteristic lane
     unsigned long long branch_count[8];
+    // save predicate of the driver loop (dense_run, general_main.f90:40-41): with save_mode set,
+    // a step after which step % save_step == 0 or elasp >= dt_save holds the following steps
+    // (their while-condition fails) until the host has taken the save and clears `hold`
+    int save_mode, hold;
+    long long save_step;
+    double dt_save;
 };
 
 // Everything a kernel needs, passed by value.

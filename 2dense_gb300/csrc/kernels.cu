@@ -1194,13 +1194,16 @@ __global__ void kb_bc(const Params* tab, const int3* map) {
 // Step bookkeeping (general_main.f90:23-37): the while-condition at the start of a step and the
 // time/step advance at its end.
 __device__ __forceinline__ void k_step_begin_body(Scalars* sc) {
-    sc->active = (sc->t < sc->t_end) && (sc->step < sc->total_step);
+    sc->active = (sc->t < sc->t_end) && (sc->step < sc->total_step) && !sc->hold;
 }
 __device__ __forceinline__ void k_step_end_body(Scalars* sc) {
     if (sc->active) {
         sc->step += 1;
         sc->t = sc->t + sc->dt;
         sc->elasp = sc->elasp + sc->dt;
+        // general_main.f90:40: MOD(current_step, save_step) == 0 .or. elasp_time >= dt_save
+        if (sc->save_mode && ((sc->save_step > 0 && sc->step % sc->save_step == 0) || sc->elasp >= sc->dt_save))
+            sc->hold = 1;
     }
 }
 __global__ void k_step_begin(Scalars* sc) { k_step_begin_body(sc); }

@@ -60,6 +60,21 @@ def setup_config(cfg: DenseConfig) -> DenseConfig:
     return c
 
 
+def read_binary(path: str, cfg: DenseConfig | None = None):
+    """load_date_binary: (cfg with ni, nj, dx, dy from the file, cons(NIp,NJp,4), x, y, step,
+    time) of a checkpoint written by write_binary / the reference."""
+    lib = _abi.load_library()
+    c = config_default() if cfg is None else cfg.copy()
+    _check(lib, lib.dense_read_binary(path.encode(), ctypes.byref(c), None, None, None, None, None))
+    cons = np.zeros((c.ni + 8, c.nj + 8, 4), order="F")
+    x = np.zeros((c.ni, c.nj), order="F")
+    y = np.zeros((c.ni, c.nj), order="F")
+    st, t = ctypes.c_int(), ctypes.c_double()
+    _check(lib, lib.dense_read_binary(path.encode(), ctypes.byref(c), _ptr(cons), _ptr(x), _ptr(y),
+                                      ctypes.byref(st), ctypes.byref(t)))
+    return c, cons, x, y, st.value, t.value
+
+
 def init_general(cfg: DenseConfig):
     """init_general (init_general.f90:13-37): returns (cfg, cons, prim, x, y), with cfg.dx/dy
     (and gamma, if_bodyforce for Rayleigh-Taylor) as the setup leaves them."""
@@ -187,6 +202,25 @@ class Solver:
         l1, linf = ctypes.c_double(), ctypes.c_double()
         self._chk(self.lib.dense_vortex_error(self.h, ctypes.byref(l1), ctypes.byref(linf)))
         return l1.value, linf.value
+
+    def write_tecplot(self, path: str):
+        """write_tec_at_time_cartisian: the Tecplot ASCII file of the current state."""
+        self._chk(self.lib.dense_write_tecplot(self.h, path.encode()))
+
+    def write_binary(self, path: str):
+        """write_date_binary: the unformatted checkpoint of the current state."""
+        self._chk(self.lib.dense_write_binary(self.h, path.encode()))
+
+    def run(self, out_dir: str, namelist: str | None = None) -> int:
+        """The loop of general_main.f90 with its saves into out_dir (see dense_run); returns the
+        number of saves."""
+        n = ctypes.c_int()
+        self._chk(self.lib.dense_run(self.h, out_dir.encode(), namelist.encode() if namelist else None,
+                                     ctypes.byref(n)))
+        t, s, dt = ctypes.c_double(), ctypes.c_int(), ctypes.c_double()
+        self._chk(self.lib.dense_get_time(self.h, ctypes.byref(t), ctypes.byref(s), ctypes.byref(dt)))
+        self.current_time, self.current_step, self.dt = t.value, s.value, dt.value
+        return n.value
 
     def steps_async(self, n: int, t_end: float = float("inf"), total_step: int = 2**31 - 1):
         """``steps`` without waiting; time and step stay on the device (``dense_get_time``)."""

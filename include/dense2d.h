@@ -212,6 +212,37 @@ int dense_get_time(dense_handle_t* h, double* t, int* step, double* dt);
 /* Wait for all work on the handle's stream. */
 int dense_sync(dense_handle_t* h);
 
+/* ---- save path: the driver loop's files (general_main.f90:40-60) ------------------------- */
+
+/* write_tec_at_time_cartisian (output_test_general.f90:18-59): Tecplot ASCII of the current
+   state at `path` -- title and variables lines, one zone of (ni+1) x (nj+1) vertices
+   (vet_x, vet_y as the setups define them), then prim(:,:,1..6) of the interior, cell-centred,
+   one value per line with 17 significant digits. Like the reference, the header names seven
+   variables and six primitive blocks follow (prim_lastvar_index = 6, var_index.f90:11). */
+int dense_write_tecplot(dense_handle_t* h, const char* path);
+/* write_date_binary (read_WriteAndLoad.f90:1-26): the unformatted checkpoint, gfortran
+   sequential records (4-byte lengths around each): (step int32, time), num_block = 1,
+   index = 1, (ni, nj), (bfsize_i, bfsize_j), cons(NIp,NJp,4), x(ni,nj), y(ni,nj), (dx, dy). */
+int dense_write_binary(dense_handle_t* h, const char* path);
+/* load_date_binary (read_WriteAndLoad.f90:28-70): read such a checkpoint; sets cfg->ni, nj,
+   bfsize, dx, dy and fills cons(NIp,NJp,4), x, y (each may be NULL; size them after a first
+   call with NULL arrays), *step and *time. */
+int dense_read_binary(const char* path, dense_config_t* cfg, double* cons, double* x, double* y,
+                      int* step, double* time);
+/* The loop of general_main.f90:23-60 on the device: steps while current_time < total_time and
+   current_step < total_step; after every step with MOD(current_step, save_step) == 0 or
+   elasp_time >= dt_save it writes 2d_<step>.dat2d (if_save_binary) and 2d_<step>.dat
+   (if_save_tec, which also resets elasp_time) into `dir`, then reads `namelist_path` again
+   (if not NULL) and applies it (dense_reconfigure); at the end it writes the final
+   2d_<step>.dat. The saves are formatted and written by a host thread from a device snapshot
+   while the device runs on. *saves counts them (may be NULL). The reference's CpuTime.dat log
+   is not written. */
+int dense_run(dense_handle_t* h, const char* dir, const char* namelist_path, int* saves);
+
+/* Cell x(ni,nj), y(ni,nj) and vertex vet_x(ni+1,nj+1), vet_y coordinates of cfg's benchmark as
+   the setups define them (any pointer may be NULL). */
+int dense_grid_coords(const dense_config_t* cfg, double* x, double* y, double* vx, double* vy);
+
 /* ---- device-side setups and error norms: no counterpart in the reference ------------------ */
 
 /* The initial state of the handle's benchmark computed on the device (benchmarks 11, 13 and 14,
