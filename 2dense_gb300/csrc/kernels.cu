@@ -139,13 +139,11 @@ __device__ __forceinline__ void betas_fast(const double lf[5], double& d0, doubl
     const double b1 = lf[1] - lf[3];
     const double a2 = fma(-2.0, lf[3], lf[2]) + lf[4];
     const double b2 = fma(3.0, lf[2], fma(-4.0, lf[3], lf[4]));
-    const double be0 = fma(k1312 * a0, a0, (0.25 * b0) * b0);
-    const double be1 = fma(k1312 * a1, a1, (0.25 * b1) * b1);
-    const double be2 = fma(k1312 * a2, a2, (0.25 * b2) * b2);
-    tau = fabs(be2 - be0);
-    d0 = kSS + be0;
-    d1 = kSS + be1;
-    d2 = kSS + be2;
+    // d_k = ss + beta_k with ss added inside the last FMA; tau = |beta_2 - beta_0| = |d_2 - d_0|
+    d0 = fma(k1312 * a0, a0, fma(0.25 * b0, b0, kSS));
+    d1 = fma(k1312 * a1, a1, fma(0.25 * b1, b1, kSS));
+    d2 = fma(k1312 * a2, a2, fma(0.25 * b2, b2, kSS));
+    tau = fabs(d2 - d0);
 }
 
 // Weight numerators n_k = alpha_k D and their sum N = (sum alpha) D.
@@ -232,8 +230,7 @@ __device__ __forceinline__ void recon_grad(const double lf[5], double g[5]) {
         const double s1 = (q1 - h) * (c31 * tau) * (P1 * iN);
         const double s2 = (q2 - h) * (c32 * tau) * (P2 * iN);
         const double tb = 2.0 * (s0 + s1 + s2);  // dW/dtau
-        const double be0 = fma(k1312 * A0, A0, (0.25 * B0) * B0), be2 = fma(k1312 * A2, A2, (0.25 * B2) * B2);
-        const double sg = be2 >= be0 ? tb : -tb;  // dtau/dbeta_2 = -dtau/dbeta_0 = sign(beta_2 - beta_0)
+        const double sg = d2 >= d0 ? tb : -tb;  // dtau/dbeta_2 = -dtau/dbeta_0 = sign(beta_2 - beta_0)
         bb0 = -2.0 * s0 * tau * id0 - sg;
         bb1 = -2.0 * s1 * tau * id1;
         bb2 = -2.0 * s2 * tau * id2 + sg;
@@ -585,6 +582,10 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
     __shared__ double sQ[4][NL][NC];  // rho, u, v, and p (H when kStageHS)
     __shared__ double sS[kStageHS ? NL : 1][kStageHS ? NC : 1];
     __shared__ double hbuf[ADAPT ? 2 : 1][4][ADAPT ? NT : 1];
+    // AdaWENO's scalar surrogates rho + F+-(normal momentum) of the tile's cells, staged once per
+    // cell; they live in hbuf until the indicators are taken (a barrier separates the two uses)
+    static_assert(!ADAPT || 2 * NL * NC <= 8 * NT, "surrogates must fit in hbuf");
+    double (*sur)[NL][NC] = reinterpret_cast<double (*)[NL][NC]>(&hbuf[0][0][0]);
     __shared__ int queue[ADAPT ? 2 * NT : 1];
     __shared__ int qn;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + ty * TX;
@@ -612,6 +613,10 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
         }
 #pragma unroll
         for (int v = 0; v < 4; ++v) { sF[v][r][c] = fp[v]; sF[4 + v][r][c] = fm[v]; sQ[v][r][c] = q[v]; }
+        if constexpr (ADAPT) {
+            sur[0][r][c] = q[0] + fp[1 + DIR];
+            sur[1][r][c] = q[0] + fm[1 + DIR];
+        }
     };
     if (DIR == 0) {
         const int f0 = bx * TX, j = by * TY + ty;
@@ -721,8 +726,8 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
             double lp[5], lm[5];
 #pragma unroll
             for (int m = 0; m < 5; ++m) {
-                lp[m] = SQ(0, t + m, tx, ty) + SF(1 + DIR, t + m, tx, ty);
-                lm[m] = SQ(0, t + 5 - m, tx, ty) + SF(5 + DIR, t + 5 - m, tx, ty);
+                lp[m] = DIR == 0 ? sur[0][ty][t + m] : sur[0][t + m][tx];
+                lm[m] = DIR == 0 ? sur[1][ty][t + 5 - m] : sur[1][t + 5 - m][tx];
             }
 #if FAST
 #pragma unroll
@@ -741,6 +746,7 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
             smooth[1] = th > p.delta;
 #endif
         }
+        __syncthreads();  // the surrogates are consumed; hbuf takes the smooth results next
         if (p.count_branches) {
             const int ns = valid ? (int)smooth[0] + (int)smooth[1] : 0;
             const int nc = valid ? 2 - ns : 0;
