@@ -146,12 +146,10 @@ __device__ __forceinline__ void betas_fast(const double lf[5], double& d0, doubl
     tau = fabs(d2 - d0);
 }
 
-// Weight numerators n_k = alpha_k D and their sum N = (sum alpha) D.
+// Weight numerators n_k = alpha_k D and their sum N = (sum alpha) D, from d_k = ss + beta_k.
 template <bool Z>
-__device__ __forceinline__ void weno_num_fast(const double lf[5], double& n0, double& n1, double& n2,
-                                              double& N, double& D) {
-    double d0, d1, d2, tau;
-    betas_fast(lf, d0, d1, d2, tau);
+__device__ __forceinline__ void weno_num_from_d(double d0, double d1, double d2, double tau, double& n0,
+                                                double& n1, double& n2, double& N, double& D) {
     const double e0 = d0 * d0, e1 = d1 * d1, e2 = d2 * d2;
     const double P0 = e1 * e2, P1 = e0 * e2, P2 = e0 * e1;
     D = e0 * P0;
@@ -166,6 +164,13 @@ __device__ __forceinline__ void weno_num_fast(const double lf[5], double& n0, do
         n2 = c32 * P2;
     }
     N = n0 + n1 + n2;
+}
+template <bool Z>
+__device__ __forceinline__ void weno_num_fast(const double lf[5], double& n0, double& n1, double& n2,
+                                              double& N, double& D) {
+    double d0, d1, d2, tau;
+    betas_fast(lf, d0, d1, d2, tau);
+    weno_num_from_d<Z>(d0, d1, d2, tau, n0, n1, n2, N, D);
 }
 
 __device__ __forceinline__ void candidates_fast(const double lf[5], double& q0, double& q1, double& q2) {
@@ -571,21 +576,39 @@ __global__ void k_flux_noop(Params p, int irk) {
 // branch would hold whole warps for the sake of one or two lanes; instead each thread does its
 // smooth signs and queues its characteristic (interface, sign) items in shared memory, and the
 // whole block then works through the queue on full warps.
+// Dynamic shared memory of one characteristic sweep block, in doubles: the tile's split fluxes
+// sF[8][NL][NC] and primitives sQ[4][NL][NC]; per-cell sqrt(rho) sS (104, fast); and one region
+// R that AdaWENO uses three times over: the scalar surrogates sur[2][NL][NC] and, from them,
+// the staged indicator terms (fast: second differences D2, ss + 13/12 D2^2 and first differences
+// per sign, 6 x [NL][NC]), read by the interfaces; then, after a barrier, the per-sign results
+// hbuf[2][4][NT].
+template <int DIR, bool ADAPT, int TX, int TY>
+struct CharTile {
+    static constexpr int NL = DIR == 0 ? TY : TY + 5;
+    static constexpr int NC = DIR == 0 ? TX + 5 : TX;
+    static constexpr int NT = TX * TY;
+    static constexpr int NCELL = NL * NC;
+    static constexpr bool kStageHS = FAST && !ADAPT;
+    static constexpr bool kStageInd = FAST && ADAPT;
+    static constexpr int kF = 0, kQ = kF + 8 * NCELL, kS = kQ + 4 * NCELL;
+    static constexpr int kR = kS + (kStageHS ? NCELL : 0);
+    static constexpr int kRSize = !ADAPT ? 0
+                                  : (kStageInd ? (8 * NCELL > 8 * NT ? 8 * NCELL : 8 * NT)
+                                               : (2 * NCELL > 8 * NT ? 2 * NCELL : 8 * NT));
+    static constexpr size_t bytes = sizeof(double) * (size_t)(kR + kRSize);
+};
+
 template <int DIR, bool ADAPT, int TX, int TY>
 __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx, int by) {
     if (!p.sc->active) return;
-    constexpr int NL = DIR == 0 ? TY : TY + 5;
-    constexpr int NC = DIR == 0 ? TX + 5 : TX;
-    constexpr int NT = TX * TY;
-    constexpr bool kStageHS = FAST && !ADAPT;  // per-cell enthalpy and sqrt(rho) in shared memory
-    __shared__ double sF[8][NL][NC];
-    __shared__ double sQ[4][NL][NC];  // rho, u, v, and p (H when kStageHS)
-    __shared__ double sS[kStageHS ? NL : 1][kStageHS ? NC : 1];
-    __shared__ double hbuf[ADAPT ? 2 : 1][4][ADAPT ? NT : 1];
-    // AdaWENO's scalar surrogates rho + F+-(normal momentum) of the tile's cells, staged once per
-    // cell; they live in hbuf until the indicators are taken (a barrier separates the two uses)
-    static_assert(!ADAPT || 2 * NL * NC <= 8 * NT, "surrogates must fit in hbuf");
-    double (*sur)[NL][NC] = reinterpret_cast<double (*)[NL][NC]>(&hbuf[0][0][0]);
+    using L = CharTile<DIR, ADAPT, TX, TY>;
+    constexpr int NL = L::NL, NC = L::NC, NT = L::NT, NCELL = L::NCELL;
+    constexpr bool kStageHS = L::kStageHS, kStageInd = L::kStageInd;
+    extern __shared__ __align__(16) double dsm[];
+    double* const sF = dsm + L::kF;
+    double* const sQ = dsm + L::kQ;
+    double* const sS = dsm + L::kS;
+    double* const sR = dsm + L::kR;
     __shared__ int queue[ADAPT ? 2 * NT : 1];
     __shared__ int qn;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + ty * TX;
@@ -595,7 +618,10 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
     const int NIp = p.ni + 2 * kB, NJp = p.nj + 2 * kB;
     const double g1 = p.gamma - 1.0, kg = p.gamma / (p.gamma - 1.0);
     if (ADAPT && tid == 0) qn = 0;
-    (void)g1; (void)kg;
+    (void)g1; (void)kg; (void)NL;
+    // tile cell (r, c) -> offset; k runs along the sweep, (ox, oy) is the interface's tile position
+    auto at = [](int r, int c) { return r * NC + c; };
+    auto atk = [&](int k, int ox, int oy) { return DIR == 0 ? at(oy, k) : at(k, ox); };
 
     // phase 1: split fluxes (and primitives) of the tile's cells
     auto cell = [&](int I, int J, int r, int c) {
@@ -609,13 +635,17 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
         if constexpr (kStageHS) {
             const double ir = rcp_nr(q[0]);
             q[3] = fma(kg * q[3], ir, 0.5 * fma(q[1], q[1], q[2] * q[2]));
-            sS[r][c] = q[0] * rsqrt_nr(q[0]);
+            sS[at(r, c)] = q[0] * rsqrt_nr(q[0]);
         }
 #pragma unroll
-        for (int v = 0; v < 4; ++v) { sF[v][r][c] = fp[v]; sF[4 + v][r][c] = fm[v]; sQ[v][r][c] = q[v]; }
-        if constexpr (ADAPT) {
-            sur[0][r][c] = q[0] + fp[1 + DIR];
-            sur[1][r][c] = q[0] + fm[1 + DIR];
+        for (int v = 0; v < 4; ++v) {
+            sF[v * NCELL + at(r, c)] = fp[v];
+            sF[(4 + v) * NCELL + at(r, c)] = fm[v];
+            sQ[v * NCELL + at(r, c)] = q[v];
+        }
+        if constexpr (ADAPT) {  // AdaWENO's scalar surrogates rho + F+-(normal momentum)
+            sR[at(r, c)] = q[0] + fp[1 + DIR];
+            sR[NCELL + at(r, c)] = q[0] + fm[1 + DIR];
         }
     };
     if (DIR == 0) {
@@ -635,14 +665,40 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
     }
     __syncthreads();
 
+    // phase 1b (AdaWENO, fast): the surrogates' second differences D2, the squared-difference
+    // term ss + 13/12 D2^2 of the smoothness indicators, and first differences, once per cell
+    // and sign; an interface's indicators then need only its first-order terms. Signs read their
+    // stencils in opposite directions: "+" cells k-1, k, k+1; "-" cells k+1, k, k-1.
+    double* const sD2 = sR + 2 * NCELL;   // [2][NCELL]
+    double* const sA2 = sR + 4 * NCELL;   // [2][NCELL]
+    double* const sDl = sR + 6 * NCELL;   // [2][NCELL]: sur(k+1) - sur(k)
+    if constexpr (kStageInd) {
+        constexpr int KN = DIR == 0 ? TX + 5 : TY + 5;   // cells along the sweep
+        constexpr int KL = DIR == 0 ? TY : TX;           // lines
+        for (int e = tid; e < KL * (KN - 2); e += NT) {
+            const int line = e / (KN - 2), k = 1 + e % (KN - 2);
+            const int o = DIR == 0 ? at(line, k) : at(k, line);
+            const int om = DIR == 0 ? at(line, k - 1) : at(k - 1, line);
+            const int op = DIR == 0 ? at(line, k + 1) : at(k + 1, line);
+#pragma unroll
+            for (int sg = 0; sg < 2; ++sg) {
+                const double* su = sR + sg * NCELL;
+                const double a = sg == 0 ? fma(-2.0, su[o], su[om]) + su[op] : fma(-2.0, su[o], su[op]) + su[om];
+                sD2[sg * NCELL + o] = a;
+                sA2[sg * NCELL + o] = fma(k1312 * a, a, kSS);
+                sDl[sg * NCELL + o] = su[op] - su[o];
+            }
+        }
+        __syncthreads();
+    }
+
     int line, f;
     if (DIR == 0) { line = by * TY + ty; f = bx * TX + tx; }
     else          { line = bx * TX + tx; f = by * TY + ty; }
     const int nline = DIR == 0 ? p.nj : p.ni, nface = DIR == 0 ? p.ni + 1 : p.nj + 1;
     const bool valid = line < nline && f < nface;
-    // tile accessors for the interface at tile position (ox, oy); k runs along the sweep
-    auto SF = [&](int q, int k, int ox, int oy) -> double { return DIR == 0 ? sF[q][oy][k] : sF[q][k][ox]; };
-    auto SQ = [&](int q, int k, int ox, int oy) -> double { return DIR == 0 ? sQ[q][oy][k] : sQ[q][k][ox]; };
+    auto SF = [&](int q, int k, int ox, int oy) -> double { return sF[q * NCELL + atk(k, ox, oy)]; };
+    auto SQ = [&](int q, int k, int ox, int oy) -> double { return sQ[q * NCELL + atk(k, ox, oy)]; };
 #if FAST
     using EigT = EigFast;
 #else
@@ -654,8 +710,8 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
 #if FAST
         double sl, sr, hl, hr;
         if constexpr (kStageHS) {
-            sl = DIR == 0 ? sS[oy][kl] : sS[kl][ox];
-            sr = DIR == 0 ? sS[oy][kr] : sS[kr][ox];
+            sl = sS[atk(kl, ox, oy)];
+            sr = sS[atk(kr, ox, oy)];
             hl = SQ(3, kl, ox, oy);
             hr = SQ(3, kr, ox, oy);
         } else {
@@ -699,6 +755,7 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
             else          p.he[(long long)v * (p.nj + 1) * p.ni + (long long)f * p.ni + line] = hsum[v];
         }
     };
+    auto hbuf = [&](int s, int c, int i) -> double& { return sR[(s * 4 + c) * NT + i]; };
 
     if constexpr (!ADAPT) {
         // 104: every interface takes the characteristic branch for both signs
@@ -723,22 +780,38 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
         bool smooth[2] = {true, true};
         double wsur[2][3];
         if (valid) {
-            double lp[5], lm[5];
-#pragma unroll
-            for (int m = 0; m < 5; ++m) {
-                lp[m] = DIR == 0 ? sur[0][ty][t + m] : sur[0][t + m][tx];
-                lm[m] = DIR == 0 ? sur[1][ty][t + 5 - m] : sur[1][t + 5 - m][tx];
-            }
 #if FAST
 #pragma unroll
             for (int s = 0; s < 2; ++s) {
+                // "+": substencils centred on cells t+1, t+2, t+3; "-": on t+4, t+3, t+2
+                const int c0 = s == 0 ? t + 1 : t + 4, c2 = s == 0 ? t + 3 : t + 2, cm = t + 2;
+                const double* D2 = sD2 + s * NCELL;
+                const double* A2 = sA2 + s * NCELL;
+                const double* Dl = sDl + s * NCELL;
+                const double A0 = D2[atk(c0, tx, ty)], A2v = D2[atk(c2, tx, ty)];
+                const double dl1 = Dl[atk(s == 0 ? t + 1 : t + 3, tx, ty)];
+                const double dl2 = Dl[atk(t + 2, tx, ty)];
+                // B0 = lf0 - 4 lf1 + 3 lf2, B1 = lf1 - lf3, B2 = 3 lf2 - 4 lf3 + lf4 from A and the
+                // first differences (signs mirrored for "-")
+                const double B0 = s == 0 ? fma(2.0, dl1, A0) : fma(-2.0, dl1, A0);
+                const double B1 = dl1 + dl2;
+                const double B2 = s == 0 ? fma(-2.0, dl2, A2v) : fma(2.0, dl2, A2v);
+                const double d0 = fma(0.25 * B0, B0, A2[atk(c0, tx, ty)]);
+                const double d1 = fma(0.25 * B1, B1, A2[atk(cm + (s == 0 ? 0 : 1), tx, ty)]);
+                const double d2 = fma(0.25 * B2, B2, A2[atk(c2, tx, ty)]);
                 double n0, n1, n2, N, D;
-                weno_num_fast<true>(s == 0 ? lp : lm, n0, n1, n2, N, D);
+                weno_num_from_d<true>(d0, d1, d2, fabs(d2 - d0), n0, n1, n2, N, D);
                 smooth[s] = p.theta_k1 * D > p.theta_k2 * (N - D);
                 const double r = rcp_nr(N);
                 wsur[s][0] = n0 * r; wsur[s][1] = n1 * r; wsur[s][2] = n2 * r;
             }
 #else
+            double lp[5], lm[5];
+#pragma unroll
+            for (int m = 0; m < 5; ++m) {
+                lp[m] = sR[atk(t + m, tx, ty)];
+                lm[m] = sR[NCELL + atk(t + 5 - m, tx, ty)];
+            }
             double th;
             weno5z_omega_theta(lp, wsur[0][0], wsur[0][1], wsur[0][2], th);
             smooth[0] = th > p.delta;
@@ -746,7 +819,7 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
             smooth[1] = th > p.delta;
 #endif
         }
-        __syncthreads();  // the surrogates are consumed; hbuf takes the smooth results next
+        __syncthreads();  // the staged surrogate terms are consumed; the region takes the results next
         if (p.count_branches) {
             const int ns = valid ? (int)smooth[0] + (int)smooth[1] : 0;
             const int nc = valid ? 2 - ns : 0;
@@ -775,7 +848,7 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
                     h[c] = fma(W[4], F[4][c], fma(W[3], F[3][c], fma(W[2], F[2][c], fma(W[1], F[1][c], W[0] * F[0][c]))));
                 if (valid && smooth[s]) {
 #pragma unroll
-                    for (int c = 0; c < 4; ++c) hbuf[s][c][tid] = h[c];
+                    for (int c = 0; c < 4; ++c) hbuf(s, c, tid) = h[c];
                 } else if (valid) {
                     queue[atomicAdd(&qn, 1)] = 2 * tid + s;
                 }
@@ -797,7 +870,7 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
                 }
 #endif
 #pragma unroll
-                for (int c = 0; c < 4; ++c) hbuf[s][c][tid] = h[c];
+                for (int c = 0; c < 4; ++c) hbuf(s, c, tid) = h[c];
             } else {
                 queue[atomicAdd(&qn, 1)] = 2 * tid + s;
             }
@@ -814,14 +887,14 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
             stencil(ox, oy, s, F);
             char_recon(e, F, h);
 #pragma unroll
-            for (int c = 0; c < 4; ++c) hbuf[s][c][owner] = h[c];
+            for (int c = 0; c < 4; ++c) hbuf(s, c, owner) = h[c];
         }
         __syncthreads();
         // phase 2c: h = h+ + h- (sum_field, field_op.f90:1-21)
         if (valid) {
             double hsum[4];
 #pragma unroll
-            for (int c = 0; c < 4; ++c) hsum[c] = hbuf[0][c][tid] + hbuf[1][c][tid];
+            for (int c = 0; c < 4; ++c) hsum[c] = hbuf(0, c, tid) + hbuf(1, c, tid);
             store(hsum);
         }
     }
@@ -1278,12 +1351,12 @@ static void launch_flux(const Params& p, int irk, int dir, void* stream) {
         break;
     }
     case DENSE_SPLIT_CH:
-        if (dir == 0) k_flux_char<0, false, kXTX, kXTY><<<grid_xi(p, kXTX, kXTY), dim3(kXTX, kXTY), 0, s>>>(p, irk);
-        else          k_flux_char<1, false, kETX, kETY><<<grid_eta(p, kETX, kETY), dim3(kETX, kETY), 0, s>>>(p, irk);
+        if (dir == 0) k_flux_char<0, false, kXTX, kXTY><<<grid_xi(p, kXTX, kXTY), dim3(kXTX, kXTY), CharTile<0, false, kXTX, kXTY>::bytes, s>>>(p, irk);
+        else          k_flux_char<1, false, kETX, kETY><<<grid_eta(p, kETX, kETY), dim3(kETX, kETY), CharTile<1, false, kETX, kETY>::bytes, s>>>(p, irk);
         break;
     case DENSE_SPLIT_SC:
-        if (dir == 0) k_flux_char<0, true, kXTX, kXTY><<<grid_xi(p, kXTX, kXTY), dim3(kXTX, kXTY), 0, s>>>(p, irk);
-        else          k_flux_char<1, true, kETX, kETY_ADAPT><<<grid_eta(p, kETX, kETY_ADAPT), dim3(kETX, kETY_ADAPT), 0, s>>>(p, irk);
+        if (dir == 0) k_flux_char<0, true, kXTX, kXTY><<<grid_xi(p, kXTX, kXTY), dim3(kXTX, kXTY), CharTile<0, true, kXTX, kXTY>::bytes, s>>>(p, irk);
+        else          k_flux_char<1, true, kETX, kETY_ADAPT><<<grid_eta(p, kETX, kETY_ADAPT), dim3(kETX, kETY_ADAPT), CharTile<1, true, kETX, kETY_ADAPT>::bytes, s>>>(p, irk);
         break;
     default:
         break;
@@ -1381,12 +1454,12 @@ static void batch_flux(const BatchLaunch& b, int irk, int dir, void* stream) {
         break;  // unknown reconstruction: rejected when the batch is created
     }
     case DENSE_SPLIT_CH:
-        if (dir == 0) kb_flux_char<0, false, kXTX, kXTY><<<b.nb_xi, dim3(kXTX, kXTY), 0, s>>>(b.tab, as_map(b.map_xi), irk);
-        else          kb_flux_char<1, false, kETX, kETY><<<b.nb_eta, dim3(kETX, kETY), 0, s>>>(b.tab, as_map(b.map_eta), irk);
+        if (dir == 0) kb_flux_char<0, false, kXTX, kXTY><<<b.nb_xi, dim3(kXTX, kXTY), CharTile<0, false, kXTX, kXTY>::bytes, s>>>(b.tab, as_map(b.map_xi), irk);
+        else          kb_flux_char<1, false, kETX, kETY><<<b.nb_eta, dim3(kETX, kETY), CharTile<1, false, kETX, kETY>::bytes, s>>>(b.tab, as_map(b.map_eta), irk);
         break;
     case DENSE_SPLIT_SC:
-        if (dir == 0) kb_flux_char<0, true, kXTX, kXTY><<<b.nb_xi, dim3(kXTX, kXTY), 0, s>>>(b.tab, as_map(b.map_xi), irk);
-        else          kb_flux_char<1, true, kETX, kETY_ADAPT><<<b.nb_eta, dim3(kETX, kETY_ADAPT), 0, s>>>(b.tab, as_map(b.map_eta), irk);
+        if (dir == 0) kb_flux_char<0, true, kXTX, kXTY><<<b.nb_xi, dim3(kXTX, kXTY), CharTile<0, true, kXTX, kXTY>::bytes, s>>>(b.tab, as_map(b.map_xi), irk);
+        else          kb_flux_char<1, true, kETX, kETY_ADAPT><<<b.nb_eta, dim3(kETX, kETY_ADAPT), CharTile<1, true, kETX, kETY_ADAPT>::bytes, s>>>(b.tab, as_map(b.map_eta), irk);
         break;
     default:
         break;
@@ -1411,16 +1484,38 @@ static void batch_step_end(const BatchLaunch& b, void* stream) {
     kb_step_end<<<(b.n + 127) / 128, 128, 0, (cudaStream_t)stream>>>(b.tab, b.n);
 }
 
+// The characteristic sweeps take their tile from dynamic shared memory; the larger tiles need
+// more than the default 48 KB, which a kernel has to be allowed once.
+template <class K>
+static void allow_smem(K kernel, size_t bytes) {
+    if (bytes > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+static bool allow_char_smem() {
+    allow_smem(k_flux_char<0, false, kXTX, kXTY>, CharTile<0, false, kXTX, kXTY>::bytes);
+    allow_smem(k_flux_char<1, false, kETX, kETY>, CharTile<1, false, kETX, kETY>::bytes);
+    allow_smem(k_flux_char<0, true, kXTX, kXTY>, CharTile<0, true, kXTX, kXTY>::bytes);
+    allow_smem(k_flux_char<1, true, kETX, kETY_ADAPT>, CharTile<1, true, kETX, kETY_ADAPT>::bytes);
+    allow_smem(kb_flux_char<0, false, kXTX, kXTY>, CharTile<0, false, kXTX, kXTY>::bytes);
+    allow_smem(kb_flux_char<1, false, kETX, kETY>, CharTile<1, false, kETX, kETY>::bytes);
+    allow_smem(kb_flux_char<0, true, kXTX, kXTY>, CharTile<0, true, kXTX, kXTY>::bytes);
+    allow_smem(kb_flux_char<1, true, kETX, kETY_ADAPT>, CharTile<1, true, kETX, kETY_ADAPT>::bytes);
+    return true;
+}
+
 }  // namespace VNS
 
 #if DENSE_VARIANT_STRICT
 const BatchKernelTable* batch_kernels_strict() {
+    static const bool smem_ok = VNS::allow_char_smem();
+    (void)smem_ok;
     static const BatchKernelTable t = {VNS::batch_prim, VNS::batch_bc, VNS::batch_flux, VNS::batch_update,
                                        VNS::batch_step_begin, VNS::batch_step_end};
     return &t;
 }
 #else
 const BatchKernelTable* batch_kernels_fast() {
+    static const bool smem_ok = VNS::allow_char_smem();
+    (void)smem_ok;
     static const BatchKernelTable t = {VNS::batch_prim, VNS::batch_bc, VNS::batch_flux, VNS::batch_update,
                                        VNS::batch_step_begin, VNS::batch_step_end};
     return &t;
@@ -1442,6 +1537,8 @@ void batch_tile_shape(int splitting, int dir, int variant, int* tx, int* ty) {
 
 #if DENSE_VARIANT_STRICT
 const KernelTable* kernels_strict() {
+    static const bool smem_ok = VNS::allow_char_smem();
+    (void)smem_ok;
     static const KernelTable t = {"strict", VNS::launch_prim, VNS::launch_bc, VNS::launch_flux,
                                   VNS::launch_update, VNS::launch_step_begin, VNS::launch_step_end,
                                   VNS::flux_launches, VNS::launch_flux_tape};
@@ -1449,6 +1546,8 @@ const KernelTable* kernels_strict() {
 }
 #else
 const KernelTable* kernels_fast() {
+    static const bool smem_ok = VNS::allow_char_smem();
+    (void)smem_ok;
     static const KernelTable t = {"fast", VNS::launch_prim, VNS::launch_bc, VNS::launch_flux,
                                   VNS::launch_update, VNS::launch_step_begin, VNS::launch_step_end,
                                   VNS::flux_launches, VNS::launch_flux_tape};
