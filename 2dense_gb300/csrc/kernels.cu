@@ -1292,7 +1292,7 @@ __global__ void k_step_end(Scalars* sc) { k_step_end_body(sc); }
 // Launchers
 constexpr int kXTX = 32, kXTY = 4;   // xi tile
 constexpr int kETX = 32, kETY = 8;   // eta tile
-constexpr int kETY_ADAPT = 6;        // AdaWENO eta tile: its work queue must fit the 48 KB static smem
+constexpr int kETY_ADAPT = 8;        // AdaWENO eta tile
 
 static inline dim3 grid_xi(const Params& p, int tx, int ty) {
     return dim3((p.ni + 1 + tx - 1) / tx, (p.nj + ty - 1) / ty);
@@ -1524,7 +1524,7 @@ const BatchKernelTable* batch_kernels_fast() {
 void batch_tile_shape(int splitting, int dir, int variant, int* tx, int* ty) {
     if (splitting == DENSE_SPLIT_CH || splitting == DENSE_SPLIT_SC) {
         *tx = 32;
-        *ty = dir == 0 ? 4 : (splitting == DENSE_SPLIT_SC ? 6 : 8);
+        *ty = dir == 0 ? 4 : (splitting == DENSE_SPLIT_SC ? VNS::kETY_ADAPT : VNS::kETY);
         return;
     }
     static const int xi[kTileVariants][2] = {{32, 4}, {64, 2}, {32, 8}};
