@@ -1293,6 +1293,7 @@ __global__ void k_step_end(Scalars* sc) { k_step_end_body(sc); }
 constexpr int kXTX = 32, kXTY = 4;   // xi tile
 constexpr int kETX = 32, kETY = 8;   // eta tile
 constexpr int kETY_ADAPT = 8;        // AdaWENO eta tile
+constexpr int kCXTX = 64, kCXTY = 2; // characteristic xi tile
 
 static inline dim3 grid_xi(const Params& p, int tx, int ty) {
     return dim3((p.ni + 1 + tx - 1) / tx, (p.nj + ty - 1) / ty);
@@ -1351,11 +1352,11 @@ static void launch_flux(const Params& p, int irk, int dir, void* stream) {
         break;
     }
     case DENSE_SPLIT_CH:
-        if (dir == 0) k_flux_char<0, false, kXTX, kXTY><<<grid_xi(p, kXTX, kXTY), dim3(kXTX, kXTY), CharTile<0, false, kXTX, kXTY>::bytes, s>>>(p, irk);
+        if (dir == 0) k_flux_char<0, false, kCXTX, kCXTY><<<grid_xi(p, kCXTX, kCXTY), dim3(kCXTX, kCXTY), CharTile<0, false, kCXTX, kCXTY>::bytes, s>>>(p, irk);
         else          k_flux_char<1, false, kETX, kETY><<<grid_eta(p, kETX, kETY), dim3(kETX, kETY), CharTile<1, false, kETX, kETY>::bytes, s>>>(p, irk);
         break;
     case DENSE_SPLIT_SC:
-        if (dir == 0) k_flux_char<0, true, kXTX, kXTY><<<grid_xi(p, kXTX, kXTY), dim3(kXTX, kXTY), CharTile<0, true, kXTX, kXTY>::bytes, s>>>(p, irk);
+        if (dir == 0) k_flux_char<0, true, kCXTX, kCXTY><<<grid_xi(p, kCXTX, kCXTY), dim3(kCXTX, kCXTY), CharTile<0, true, kCXTX, kCXTY>::bytes, s>>>(p, irk);
         else          k_flux_char<1, true, kETX, kETY_ADAPT><<<grid_eta(p, kETX, kETY_ADAPT), dim3(kETX, kETY_ADAPT), CharTile<1, true, kETX, kETY_ADAPT>::bytes, s>>>(p, irk);
         break;
     default:
@@ -1454,11 +1455,11 @@ static void batch_flux(const BatchLaunch& b, int irk, int dir, void* stream) {
         break;  // unknown reconstruction: rejected when the batch is created
     }
     case DENSE_SPLIT_CH:
-        if (dir == 0) kb_flux_char<0, false, kXTX, kXTY><<<b.nb_xi, dim3(kXTX, kXTY), CharTile<0, false, kXTX, kXTY>::bytes, s>>>(b.tab, as_map(b.map_xi), irk);
+        if (dir == 0) kb_flux_char<0, false, kCXTX, kCXTY><<<b.nb_xi, dim3(kCXTX, kCXTY), CharTile<0, false, kCXTX, kCXTY>::bytes, s>>>(b.tab, as_map(b.map_xi), irk);
         else          kb_flux_char<1, false, kETX, kETY><<<b.nb_eta, dim3(kETX, kETY), CharTile<1, false, kETX, kETY>::bytes, s>>>(b.tab, as_map(b.map_eta), irk);
         break;
     case DENSE_SPLIT_SC:
-        if (dir == 0) kb_flux_char<0, true, kXTX, kXTY><<<b.nb_xi, dim3(kXTX, kXTY), CharTile<0, true, kXTX, kXTY>::bytes, s>>>(b.tab, as_map(b.map_xi), irk);
+        if (dir == 0) kb_flux_char<0, true, kCXTX, kCXTY><<<b.nb_xi, dim3(kCXTX, kCXTY), CharTile<0, true, kCXTX, kCXTY>::bytes, s>>>(b.tab, as_map(b.map_xi), irk);
         else          kb_flux_char<1, true, kETX, kETY_ADAPT><<<b.nb_eta, dim3(kETX, kETY_ADAPT), CharTile<1, true, kETX, kETY_ADAPT>::bytes, s>>>(b.tab, as_map(b.map_eta), irk);
         break;
     default:
@@ -1491,13 +1492,13 @@ static void allow_smem(K kernel, size_t bytes) {
     if (bytes > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 static bool allow_char_smem() {
-    allow_smem(k_flux_char<0, false, kXTX, kXTY>, CharTile<0, false, kXTX, kXTY>::bytes);
+    allow_smem(k_flux_char<0, false, kCXTX, kCXTY>, CharTile<0, false, kCXTX, kCXTY>::bytes);
     allow_smem(k_flux_char<1, false, kETX, kETY>, CharTile<1, false, kETX, kETY>::bytes);
-    allow_smem(k_flux_char<0, true, kXTX, kXTY>, CharTile<0, true, kXTX, kXTY>::bytes);
+    allow_smem(k_flux_char<0, true, kCXTX, kCXTY>, CharTile<0, true, kCXTX, kCXTY>::bytes);
     allow_smem(k_flux_char<1, true, kETX, kETY_ADAPT>, CharTile<1, true, kETX, kETY_ADAPT>::bytes);
-    allow_smem(kb_flux_char<0, false, kXTX, kXTY>, CharTile<0, false, kXTX, kXTY>::bytes);
+    allow_smem(kb_flux_char<0, false, kCXTX, kCXTY>, CharTile<0, false, kCXTX, kCXTY>::bytes);
     allow_smem(kb_flux_char<1, false, kETX, kETY>, CharTile<1, false, kETX, kETY>::bytes);
-    allow_smem(kb_flux_char<0, true, kXTX, kXTY>, CharTile<0, true, kXTX, kXTY>::bytes);
+    allow_smem(kb_flux_char<0, true, kCXTX, kCXTY>, CharTile<0, true, kCXTX, kCXTY>::bytes);
     allow_smem(kb_flux_char<1, true, kETX, kETY_ADAPT>, CharTile<1, true, kETX, kETY_ADAPT>::bytes);
     return true;
 }
@@ -1523,8 +1524,8 @@ const BatchKernelTable* batch_kernels_fast() {
 // Tile shapes of the batched sweeps (the shapes instantiated above).
 void batch_tile_shape(int splitting, int dir, int variant, int* tx, int* ty) {
     if (splitting == DENSE_SPLIT_CH || splitting == DENSE_SPLIT_SC) {
-        *tx = 32;
-        *ty = dir == 0 ? 4 : (splitting == DENSE_SPLIT_SC ? VNS::kETY_ADAPT : VNS::kETY);
+        *tx = dir == 0 ? VNS::kCXTX : VNS::kETX;
+        *ty = dir == 0 ? VNS::kCXTY : (splitting == DENSE_SPLIT_SC ? VNS::kETY_ADAPT : VNS::kETY);
         return;
     }
     static const int xi[kTileVariants][2] = {{32, 4}, {64, 2}, {32, 8}};
