@@ -1292,7 +1292,7 @@ __global__ void k_step_end(Scalars* sc) { k_step_end_body(sc); }
 // Launchers
 constexpr int kXTX = 32, kXTY = 4;   // xi tile
 constexpr int kETX = 32, kETY = 8;   // eta tile
-constexpr int kETY_ADAPT = 8;        // AdaWENO eta tile
+constexpr int kCETX = 16, kETY_ADAPT = 16;  // AdaWENO eta tile
 constexpr int kCXTX = 64, kCXTY = 2; // characteristic xi tile
 
 static inline dim3 grid_xi(const Params& p, int tx, int ty) {
@@ -1357,7 +1357,7 @@ static void launch_flux(const Params& p, int irk, int dir, void* stream) {
         break;
     case DENSE_SPLIT_SC:
         if (dir == 0) k_flux_char<0, true, kCXTX, kCXTY><<<grid_xi(p, kCXTX, kCXTY), dim3(kCXTX, kCXTY), CharTile<0, true, kCXTX, kCXTY>::bytes, s>>>(p, irk);
-        else          k_flux_char<1, true, kETX, kETY_ADAPT><<<grid_eta(p, kETX, kETY_ADAPT), dim3(kETX, kETY_ADAPT), CharTile<1, true, kETX, kETY_ADAPT>::bytes, s>>>(p, irk);
+        else          k_flux_char<1, true, kCETX, kETY_ADAPT><<<grid_eta(p, kCETX, kETY_ADAPT), dim3(kCETX, kETY_ADAPT), CharTile<1, true, kCETX, kETY_ADAPT>::bytes, s>>>(p, irk);
         break;
     default:
         break;
@@ -1460,7 +1460,7 @@ static void batch_flux(const BatchLaunch& b, int irk, int dir, void* stream) {
         break;
     case DENSE_SPLIT_SC:
         if (dir == 0) kb_flux_char<0, true, kCXTX, kCXTY><<<b.nb_xi, dim3(kCXTX, kCXTY), CharTile<0, true, kCXTX, kCXTY>::bytes, s>>>(b.tab, as_map(b.map_xi), irk);
-        else          kb_flux_char<1, true, kETX, kETY_ADAPT><<<b.nb_eta, dim3(kETX, kETY_ADAPT), CharTile<1, true, kETX, kETY_ADAPT>::bytes, s>>>(b.tab, as_map(b.map_eta), irk);
+        else          kb_flux_char<1, true, kCETX, kETY_ADAPT><<<b.nb_eta, dim3(kCETX, kETY_ADAPT), CharTile<1, true, kCETX, kETY_ADAPT>::bytes, s>>>(b.tab, as_map(b.map_eta), irk);
         break;
     default:
         break;
@@ -1485,21 +1485,22 @@ static void batch_step_end(const BatchLaunch& b, void* stream) {
     kb_step_end<<<(b.n + 127) / 128, 128, 0, (cudaStream_t)stream>>>(b.tab, b.n);
 }
 
-// The characteristic sweeps take their tile from dynamic shared memory; the larger tiles need
-// more than the default 48 KB, which a kernel has to be allowed once.
+// The characteristic sweeps take their tile from dynamic shared memory; with their static work
+// queue the larger tiles need more than the default 48 KB a block may use, which a kernel has to
+// be allowed once (set for every tile, whatever its size).
 template <class K>
 static void allow_smem(K kernel, size_t bytes) {
-    if (bytes > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 static bool allow_char_smem() {
     allow_smem(k_flux_char<0, false, kCXTX, kCXTY>, CharTile<0, false, kCXTX, kCXTY>::bytes);
     allow_smem(k_flux_char<1, false, kETX, kETY>, CharTile<1, false, kETX, kETY>::bytes);
     allow_smem(k_flux_char<0, true, kCXTX, kCXTY>, CharTile<0, true, kCXTX, kCXTY>::bytes);
-    allow_smem(k_flux_char<1, true, kETX, kETY_ADAPT>, CharTile<1, true, kETX, kETY_ADAPT>::bytes);
+    allow_smem(k_flux_char<1, true, kCETX, kETY_ADAPT>, CharTile<1, true, kCETX, kETY_ADAPT>::bytes);
     allow_smem(kb_flux_char<0, false, kCXTX, kCXTY>, CharTile<0, false, kCXTX, kCXTY>::bytes);
     allow_smem(kb_flux_char<1, false, kETX, kETY>, CharTile<1, false, kETX, kETY>::bytes);
     allow_smem(kb_flux_char<0, true, kCXTX, kCXTY>, CharTile<0, true, kCXTX, kCXTY>::bytes);
-    allow_smem(kb_flux_char<1, true, kETX, kETY_ADAPT>, CharTile<1, true, kETX, kETY_ADAPT>::bytes);
+    allow_smem(kb_flux_char<1, true, kCETX, kETY_ADAPT>, CharTile<1, true, kCETX, kETY_ADAPT>::bytes);
     return true;
 }
 
@@ -1524,7 +1525,7 @@ const BatchKernelTable* batch_kernels_fast() {
 // Tile shapes of the batched sweeps (the shapes instantiated above).
 void batch_tile_shape(int splitting, int dir, int variant, int* tx, int* ty) {
     if (splitting == DENSE_SPLIT_CH || splitting == DENSE_SPLIT_SC) {
-        *tx = dir == 0 ? VNS::kCXTX : VNS::kETX;
+        *tx = dir == 0 ? VNS::kCXTX : (splitting == DENSE_SPLIT_SC ? VNS::kCETX : VNS::kETX);
         *ty = dir == 0 ? VNS::kCXTY : (splitting == DENSE_SPLIT_SC ? VNS::kETY_ADAPT : VNS::kETY);
         return;
     }
