@@ -1292,8 +1292,12 @@ __global__ void k_step_end(Scalars* sc) { k_step_end_body(sc); }
 // Launchers
 constexpr int kXTX = 32, kXTY = 4;   // xi tile
 constexpr int kETX = 32, kETY = 8;   // eta tile
-constexpr int kCETX = 16, kETY_ADAPT = 16;  // AdaWENO eta tile
-constexpr int kCXTX = 64, kCXTY = 2; // characteristic xi tile
+// characteristic sweeps: eta tiles of 4 columns x 64 interfaces, AdaWENO xi tiles of one row of
+// 256 interfaces (long lines along the sweep stage fewer halo cells per interface: 1.04 in xi and
+// 1.08 in eta against 1.16 and 1.63 for 32 x 4 and 32 x 8; measured on the 1920 x 480 double
+// Mach reflection, these shapes took the sweeps from 0.430 / 0.427 to 0.397 / 0.376 ms)
+constexpr int kCETX = 4, kCETY = 64;
+constexpr int kCXTX = 256, kCXTY = 1;
 
 static inline dim3 grid_xi(const Params& p, int tx, int ty) {
     return dim3((p.ni + 1 + tx - 1) / tx, (p.nj + ty - 1) / ty);
@@ -1352,12 +1356,12 @@ static void launch_flux(const Params& p, int irk, int dir, void* stream) {
         break;
     }
     case DENSE_SPLIT_CH:
-        if (dir == 0) k_flux_char<0, false, kCXTX, kCXTY><<<grid_xi(p, kCXTX, kCXTY), dim3(kCXTX, kCXTY), CharTile<0, false, kCXTX, kCXTY>::bytes, s>>>(p, irk);
-        else          k_flux_char<1, false, kETX, kETY><<<grid_eta(p, kETX, kETY), dim3(kETX, kETY), CharTile<1, false, kETX, kETY>::bytes, s>>>(p, irk);
+        if (dir == 0) k_flux_char<0, false, kXTX, kXTY><<<grid_xi(p, kXTX, kXTY), dim3(kXTX, kXTY), CharTile<0, false, kXTX, kXTY>::bytes, s>>>(p, irk);
+        else          k_flux_char<1, false, kCETX, kCETY><<<grid_eta(p, kCETX, kCETY), dim3(kCETX, kCETY), CharTile<1, false, kCETX, kCETY>::bytes, s>>>(p, irk);
         break;
     case DENSE_SPLIT_SC:
         if (dir == 0) k_flux_char<0, true, kCXTX, kCXTY><<<grid_xi(p, kCXTX, kCXTY), dim3(kCXTX, kCXTY), CharTile<0, true, kCXTX, kCXTY>::bytes, s>>>(p, irk);
-        else          k_flux_char<1, true, kCETX, kETY_ADAPT><<<grid_eta(p, kCETX, kETY_ADAPT), dim3(kCETX, kETY_ADAPT), CharTile<1, true, kCETX, kETY_ADAPT>::bytes, s>>>(p, irk);
+        else          k_flux_char<1, true, kCETX, kCETY><<<grid_eta(p, kCETX, kCETY), dim3(kCETX, kCETY), CharTile<1, true, kCETX, kCETY>::bytes, s>>>(p, irk);
         break;
     default:
         break;
@@ -1455,12 +1459,12 @@ static void batch_flux(const BatchLaunch& b, int irk, int dir, void* stream) {
         break;  // unknown reconstruction: rejected when the batch is created
     }
     case DENSE_SPLIT_CH:
-        if (dir == 0) kb_flux_char<0, false, kCXTX, kCXTY><<<b.nb_xi, dim3(kCXTX, kCXTY), CharTile<0, false, kCXTX, kCXTY>::bytes, s>>>(b.tab, as_map(b.map_xi), irk);
-        else          kb_flux_char<1, false, kETX, kETY><<<b.nb_eta, dim3(kETX, kETY), CharTile<1, false, kETX, kETY>::bytes, s>>>(b.tab, as_map(b.map_eta), irk);
+        if (dir == 0) kb_flux_char<0, false, kXTX, kXTY><<<b.nb_xi, dim3(kXTX, kXTY), CharTile<0, false, kXTX, kXTY>::bytes, s>>>(b.tab, as_map(b.map_xi), irk);
+        else          kb_flux_char<1, false, kCETX, kCETY><<<b.nb_eta, dim3(kCETX, kCETY), CharTile<1, false, kCETX, kCETY>::bytes, s>>>(b.tab, as_map(b.map_eta), irk);
         break;
     case DENSE_SPLIT_SC:
         if (dir == 0) kb_flux_char<0, true, kCXTX, kCXTY><<<b.nb_xi, dim3(kCXTX, kCXTY), CharTile<0, true, kCXTX, kCXTY>::bytes, s>>>(b.tab, as_map(b.map_xi), irk);
-        else          kb_flux_char<1, true, kCETX, kETY_ADAPT><<<b.nb_eta, dim3(kCETX, kETY_ADAPT), CharTile<1, true, kCETX, kETY_ADAPT>::bytes, s>>>(b.tab, as_map(b.map_eta), irk);
+        else          kb_flux_char<1, true, kCETX, kCETY><<<b.nb_eta, dim3(kCETX, kCETY), CharTile<1, true, kCETX, kCETY>::bytes, s>>>(b.tab, as_map(b.map_eta), irk);
         break;
     default:
         break;
@@ -1493,14 +1497,14 @@ static void allow_smem(K kernel, size_t bytes) {
     cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 static bool allow_char_smem() {
-    allow_smem(k_flux_char<0, false, kCXTX, kCXTY>, CharTile<0, false, kCXTX, kCXTY>::bytes);
-    allow_smem(k_flux_char<1, false, kETX, kETY>, CharTile<1, false, kETX, kETY>::bytes);
+    allow_smem(k_flux_char<0, false, kXTX, kXTY>, CharTile<0, false, kXTX, kXTY>::bytes);
+    allow_smem(k_flux_char<1, false, kCETX, kCETY>, CharTile<1, false, kCETX, kCETY>::bytes);
     allow_smem(k_flux_char<0, true, kCXTX, kCXTY>, CharTile<0, true, kCXTX, kCXTY>::bytes);
-    allow_smem(k_flux_char<1, true, kCETX, kETY_ADAPT>, CharTile<1, true, kCETX, kETY_ADAPT>::bytes);
-    allow_smem(kb_flux_char<0, false, kCXTX, kCXTY>, CharTile<0, false, kCXTX, kCXTY>::bytes);
-    allow_smem(kb_flux_char<1, false, kETX, kETY>, CharTile<1, false, kETX, kETY>::bytes);
+    allow_smem(k_flux_char<1, true, kCETX, kCETY>, CharTile<1, true, kCETX, kCETY>::bytes);
+    allow_smem(kb_flux_char<0, false, kXTX, kXTY>, CharTile<0, false, kXTX, kXTY>::bytes);
+    allow_smem(kb_flux_char<1, false, kCETX, kCETY>, CharTile<1, false, kCETX, kCETY>::bytes);
     allow_smem(kb_flux_char<0, true, kCXTX, kCXTY>, CharTile<0, true, kCXTX, kCXTY>::bytes);
-    allow_smem(kb_flux_char<1, true, kCETX, kETY_ADAPT>, CharTile<1, true, kCETX, kETY_ADAPT>::bytes);
+    allow_smem(kb_flux_char<1, true, kCETX, kCETY>, CharTile<1, true, kCETX, kCETY>::bytes);
     return true;
 }
 
@@ -1525,8 +1529,9 @@ const BatchKernelTable* batch_kernels_fast() {
 // Tile shapes of the batched sweeps (the shapes instantiated above).
 void batch_tile_shape(int splitting, int dir, int variant, int* tx, int* ty) {
     if (splitting == DENSE_SPLIT_CH || splitting == DENSE_SPLIT_SC) {
-        *tx = dir == 0 ? VNS::kCXTX : (splitting == DENSE_SPLIT_SC ? VNS::kCETX : VNS::kETX);
-        *ty = dir == 0 ? VNS::kCXTY : (splitting == DENSE_SPLIT_SC ? VNS::kETY_ADAPT : VNS::kETY);
+        // xi: 32 x 4 for 104, 256 x 1 for AdaWENO; eta: 4 x 64
+        *tx = dir == 0 ? (splitting == DENSE_SPLIT_SC ? VNS::kCXTX : VNS::kXTX) : VNS::kCETX;
+        *ty = dir == 0 ? (splitting == DENSE_SPLIT_SC ? VNS::kCXTY : VNS::kXTY) : VNS::kCETY;
         return;
     }
     static const int xi[kTileVariants][2] = {{32, 4}, {64, 2}, {32, 8}};
