@@ -1308,13 +1308,13 @@ static inline dim3 grid_eta(const Params& p, int tx, int ty) {
 
 // Streaming multiprocessors of the current device (queried once).
 static int sm_count() {
-    static int n = 0;
-    if (n == 0) {
-        int dev = 0;
+    static const int n = [] {  // thread-safe one-time initialisation
+        int dev = 0, m = 0;
         if (cudaGetDevice(&dev) != cudaSuccess ||
-            cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
-            n = 152;
-    }
+            cudaDeviceGetAttribute(&m, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || m <= 0)
+            m = 152;
+        return m;
+    }();
     return n;
 }
 
