@@ -194,6 +194,8 @@ def load_library(path: str | None = None):
         "dense_setup_config": (_c_int, [cfgp]),
         "dense_write_tecplot": (_c_int, [vp, ctypes.c_char_p]),
         "dense_write_binary": (_c_int, [vp, ctypes.c_char_p]),
+        "dense_write_theta": (_c_int, [vp, ctypes.c_char_p]),
+        "dense_get_theta": (_c_int, [vp, dp]),
         "dense_read_binary": (_c_int, [ctypes.c_char_p, cfgp, dp, dp, dp, ctypes.POINTER(_c_int), dp]),
         "dense_run": (_c_int, [vp, ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(_c_int)]),
         "dense_grid_coords": (_c_int, [cfgp, dp, dp, dp, dp]),

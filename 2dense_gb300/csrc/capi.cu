@@ -93,7 +93,19 @@ void fill_params(dense_handle* h) {
     p.bodyforce = c.if_bodyforce && (c.benchmark == DENSE_BENCH_RT || c.benchmark == DENSE_BENCH_RT_REFLECT);
     p.benchmark = c.benchmark; p.splitting = c.splitting; p.recon = c.recon;
     p.count_branches = h->count_branches;
+    p.tape = nullptr;
+    p.theta = c.if_save_theta && c.splitting == DENSE_SPLIT_SC ? h->theta : nullptr;
     h->kt = c.strict ? dense::kernels_strict() : dense::kernels_fast();
+}
+
+// the indicator buffer, allocated while a configuration saves it
+int ensure_theta(dense_handle* h) {
+    if (!h->theta && h->cfg.if_save_theta && h->cfg.splitting == DENSE_SPLIT_SC) {
+        const size_t n = (size_t)2 * ((size_t)h->cfg.nj * (h->cfg.ni + 1) + (size_t)(h->cfg.nj + 1) * h->cfg.ni);
+        CK(h, cudaMalloc((void**)&h->theta, n * sizeof(double)));
+        CK(h, cudaMemsetAsync(h->theta, 0, n * sizeof(double), h->stream));
+    }
+    return DENSE_OK;
 }
 
 void drop_graph(dense_handle* h) {
@@ -220,6 +232,7 @@ int dense_create(const dense_config_t* cfg, dense_handle_t** out) {
         e = cudaMemsetAsync(*a.p, 0, a.n * sizeof(double), h->stream);
         if (e != cudaSuccess) { g_err = std::string("cudaMemset: ") + cudaGetErrorString(e); return cleanup(DENSE_ERR_CUDA); }
     }
+    if (ensure_theta(h) != DENSE_OK) { g_err = h->err; return cleanup(DENSE_ERR_NOMEM); }
     e = cudaMalloc((void**)&h->sc, sizeof(Scalars));
     if (e != cudaSuccess) { g_err = std::string("cudaMalloc: ") + cudaGetErrorString(e); return cleanup(DENSE_ERR_NOMEM); }
     Scalars s0{};
@@ -236,7 +249,7 @@ int dense_create(const dense_config_t* cfg, dense_handle_t** out) {
 void dense_destroy(dense_handle_t* h) {
     if (!h) return;
     drop_graph(h);
-    double* bufs[] = {h->cons, h->prim, h->cons0, h->hx, h->he, h->xbot, h->xtop, h->yleft};
+    double* bufs[] = {h->cons, h->prim, h->cons0, h->hx, h->he, h->xbot, h->xtop, h->yleft, h->theta};
     for (double* b : bufs) if (b) cudaFree(b);
     if (h->sc) cudaFree(h->sc);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -353,6 +366,8 @@ int dense_reconfigure(dense_handle_t* h, const dense_config_t* cfg) {
     int rc = check_config(h, cfg);
     if (rc) return rc;
     h->cfg = *cfg;
+    rc = ensure_theta(h);
+    if (rc) return rc;
     fill_params(h);
     drop_graph(h);
     h->prim_slot = -1;  // gamma may have changed: recompute primitives before the next stage

@@ -15,6 +15,7 @@ struct dense_handle {
     int device = 0;
     double *cons = nullptr, *prim = nullptr, *cons0 = nullptr, *hx = nullptr, *he = nullptr;
     double *xbot = nullptr, *xtop = nullptr, *yleft = nullptr;
+    double* theta = nullptr;  // AdaWENO indicators of the last stage, while if_save_theta
     dense::Scalars* sc = nullptr;
     dense::Params prm{};
     int NIp = 0, NJp = 0, P = 0;

@@ -65,6 +65,9 @@ struct Params {
     // [nj+1][ni], eta after xi): the reconstructions' stencil gradients g[(s*5 + m)*4 + v] (s = 0
     // for F+, 1 for F-; none for upwind5, whose gradient is constant), then the fluxes h[v].
     double* tape;
+    // AdaWENO indicator theta of every (interface, sign) of the last stage, when it is saved
+    // (if_save_theta): xi [2][nj][ni+1], then eta [2][nj+1][ni] (sign 0 = "+"); else null
+    double* theta;
 };
 
 // One arithmetic variant of the kernels (fast or strict), as a table of launchers.

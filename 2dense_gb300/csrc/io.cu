@@ -47,7 +47,12 @@ struct HostState {
     long long step = 0;
     double t = 0.0;
     std::vector<double> cons, prim;
+    std::vector<double> theta;  // AdaWENO indicators, xi [2][nj][ni+1] then eta [2][nj+1][ni]; empty: none
 };
+
+size_t theta_size(const dense_config_t& c) {
+    return (size_t)2 * ((size_t)c.nj * (c.ni + 1) + (size_t)(c.nj + 1) * c.ni);
+}
 
 // One value per line, as list-directed output writes them (17 significant digits: the file
 // reads back to the same doubles).
@@ -79,6 +84,44 @@ int write_tec(dense_handle* h, const HostState& s, const std::string& path) {
                 const size_t o = (size_t)j * NIp + i;
                 const double v = var < 5 ? s.prim[var * P + o] : std::log(s.prim[3 * P + o]) - std::log(s.prim[o]);
                 put_value(f, v);
+            }
+    const bool ok = std::ferror(f) == 0;
+    std::fclose(f);
+    if (!ok) return ioerr(h, DENSE_ERR_IO, "write failed: " + path);
+    return DENSE_OK;
+}
+
+// write_theta_at_time_cartisian (output_test_general.f90:61-119): the AdaWENO indicator per
+// cell, the larger of its two faces' values, for xi "+" / "-" and eta "+" / "-"; zeros when the
+// sweeps have none (the reference's theta arrays start at zero, flow_mod_general.f90:241-250).
+int write_theta(dense_handle* h, const HostState& s, const std::string& path) {
+    const dense_config_t& c = s.cfg;
+    const int ni = c.ni, nj = c.nj;
+    std::vector<double> vx((size_t)(ni + 1) * (nj + 1)), vy(vx.size());
+    int rc = dense_grid_coords(&c, nullptr, nullptr, vx.data(), vy.data());
+    if (rc) return ioerr(h, rc, "grid coordinates");
+    FILE* f = std::fopen(path.c_str(), "w");
+    if (!f) return ioerr(h, DENSE_ERR_IO, "cannot open " + path);
+    std::vector<char> buf(1 << 20);
+    std::setvbuf(f, buf.data(), _IOFBF, buf.size());
+    std::fprintf(f, " title=\"flow time %#.17G\"\n", s.t);
+    std::fprintf(f, " variables=\"x\",\"y\",\"xp\",\"xn\",\"ep\",\"en\"\n");
+    std::fprintf(f, " ZONE I=%12d  J=%12d DATAPACKING=BLOCK, VARLOCATION=([3-6]=CELLCENTERED)\n", ni + 1, nj + 1);
+    for (double v : vx) put_value(f, v);
+    for (double v : vy) put_value(f, v);
+    const size_t xs = (size_t)nj * (ni + 1), es = (size_t)(nj + 1) * ni;
+    const bool have = !s.theta.empty();
+    for (int sg = 0; sg < 2; ++sg)
+        for (int j = 0; j < nj; ++j)
+            for (int i = 0; i < ni; ++i) {
+                const double* T = have ? s.theta.data() + sg * xs + (size_t)j * (ni + 1) : nullptr;
+                put_value(f, have ? std::fmax(T[i], T[i + 1]) : 0.0);
+            }
+    for (int sg = 0; sg < 2; ++sg)
+        for (int j = 0; j < nj; ++j)
+            for (int i = 0; i < ni; ++i) {
+                const double* T = have ? s.theta.data() + 2 * xs + sg * es : nullptr;
+                put_value(f, have ? std::fmax(T[(size_t)j * ni + i], T[(size_t)(j + 1) * ni + i]) : 0.0);
             }
     const bool ok = std::ferror(f) == 0;
     std::fclose(f);
@@ -142,6 +185,12 @@ std::string save_name(const std::string& dir, long long step, const char* ext) {
     return dir.empty() ? std::string(b) : dir + "/" + b;
 }
 
+std::string theta_name(const std::string& dir, long long step) {
+    char b[64];
+    std::snprintf(b, sizeof b, "2d_theta_%lld.dat", step);  // output_test_general.f90:72
+    return dir.empty() ? std::string(b) : dir + "/" + b;
+}
+
 // the handle's state (cons, prim interior as the last get_primary left them) on the host
 int snapshot_now(dense_handle* h, HostState& s) {
     s.cfg = h->cfg;
@@ -151,6 +200,12 @@ int snapshot_now(dense_handle* h, HostState& s) {
     const size_t row = (size_t)NIp * sizeof(double), pitch = (size_t)h->P * sizeof(double);
     ICK(h, cudaMemcpy2DAsync(s.cons.data(), row, h->cons, pitch, row, (size_t)NJp * 4, cudaMemcpyDeviceToHost, h->stream));
     ICK(h, cudaMemcpy2DAsync(s.prim.data(), row, h->prim, pitch, row, (size_t)NJp * 5, cudaMemcpyDeviceToHost, h->stream));
+    s.theta.clear();
+    if (h->prm.theta) {
+        s.theta.resize(theta_size(h->cfg));
+        ICK(h, cudaMemcpyAsync(s.theta.data(), h->prm.theta, s.theta.size() * sizeof(double),
+                               cudaMemcpyDeviceToHost, h->stream));
+    }
     Scalars sc{};
     ICK(h, cudaMemcpyAsync(&sc, h->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, h->stream));
     ICK(h, cudaStreamSynchronize(h->stream));
@@ -185,6 +240,23 @@ int dense_write_tecplot(dense_handle_t* h, const char* path) {
     if (!rc) rc = snapshot_now(h, s);
     if (rc) return rc;
     return write_tec(h, s, path);
+}
+
+int dense_write_theta(dense_handle_t* h, const char* path) {
+    if (!h || !path) return ioerr(h, DENSE_ERR_ARG, "null argument");
+    if (!h->uploaded) return ioerr(h, DENSE_ERR_STATE, "dense_write_theta before an upload");
+    HostState s;
+    int rc = snapshot_now(h, s);
+    if (rc) return rc;
+    return write_theta(h, s, path);
+}
+
+int dense_get_theta(dense_handle_t* h, double* theta) {
+    if (!h || !theta) return ioerr(h, DENSE_ERR_ARG, "null argument");
+    if (!h->prm.theta) return ioerr(h, DENSE_ERR_STATE, "no indicators: if_save_theta is off or the splitting is not 105");
+    ICK(h, cudaMemcpyAsync(theta, h->prm.theta, theta_size(h->cfg) * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    ICK(h, cudaStreamSynchronize(h->stream));
+    return DENSE_OK;
 }
 
 int dense_write_binary(dense_handle_t* h, const char* path) {
@@ -236,8 +308,8 @@ int dense_run(dense_handle_t* h, const char* dir, const char* namelist_path, int
     const std::string d = dir ? dir : "";
     const int kChunk = 32;  // step graphs between looks at the device's loop state
     double* snap = nullptr;
-    const size_t plane = (size_t)h->NJp * h->P;
-    ICK(h, cudaMalloc((void**)&snap, plane * 9 * sizeof(double)));
+    const size_t plane = (size_t)h->NJp * h->P, nth = theta_size(h->cfg);
+    ICK(h, cudaMalloc((void**)&snap, (plane * 9 + nth) * sizeof(double)));
     cudaEvent_t ev = nullptr;
     cudaStream_t io = nullptr;
     cudaError_t ce = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
@@ -273,13 +345,17 @@ int dense_run(dense_handle_t* h, const char* dir, const char* namelist_path, int
             ce = cudaMemcpyAsync(snap, h->cons, plane * 4 * sizeof(double), cudaMemcpyDeviceToDevice, h->stream);
             if (ce == cudaSuccess) ce = cudaMemcpyAsync(snap + plane * 4, h->prim, plane * 5 * sizeof(double),
                                                         cudaMemcpyDeviceToDevice, h->stream);
+            const bool with_theta = h->prm.theta != nullptr;
+            if (ce == cudaSuccess && with_theta)
+                ce = cudaMemcpyAsync(snap + plane * 9, h->prm.theta, nth * sizeof(double), cudaMemcpyDeviceToDevice,
+                                     h->stream);
             if (ce == cudaSuccess) ce = cudaEventRecord(ev, h->stream);
             if (ce != cudaSuccess) { rc = ioerr(h, DENSE_ERR_CUDA, std::string("snapshot: ") + cudaGetErrorString(ce)); break; }
             const dense_config_t cfg = h->cfg;
             const long long step = sc.step;
             const double t = sc.t;
             const int NIp = h->NIp, NJp = h->NJp, P = h->P;
-            writer = std::thread([&writer_rc, h, snap, ev, io, cfg, step, t, NIp, NJp, P, plane, d]() {
+            writer = std::thread([&writer_rc, h, snap, ev, io, cfg, step, t, NIp, NJp, P, plane, nth, with_theta, d]() {
                 HostState s;
                 s.cfg = cfg; s.step = step; s.t = t;
                 s.cons.assign((size_t)NIp * NJp * 4, 0.0);
@@ -291,11 +367,17 @@ int dense_run(dense_handle_t* h, const char* dir, const char* namelist_path, int
                 if (e == cudaSuccess)
                     e = cudaMemcpy2DAsync(s.prim.data(), rowb, snap + plane * 4, pitch, rowb, (size_t)NJp * 5,
                                           cudaMemcpyDeviceToHost, io);
+                if (e == cudaSuccess && with_theta) {
+                    s.theta.resize(nth);
+                    e = cudaMemcpyAsync(s.theta.data(), snap + plane * 9, nth * sizeof(double), cudaMemcpyDeviceToHost, io);
+                }
                 if (e == cudaSuccess) e = cudaStreamSynchronize(io);
                 if (e != cudaSuccess) { writer_rc = DENSE_ERR_CUDA; return; }
                 int r = DENSE_OK;
                 if (cfg.if_save_binary) r = write_bin(nullptr, s, save_name(d, step, ".dat2d"));
                 if (!r && cfg.if_save_tec) r = write_tec(nullptr, s, save_name(d, step, ".dat"));
+                // write_tec_at_time writes the indicators too (output_test_general.f90:10-12)
+                if (!r && cfg.if_save_tec && cfg.if_save_theta) r = write_theta(nullptr, s, theta_name(d, step));
                 writer_rc = r;
             });
             ++saves;
@@ -329,8 +411,9 @@ int dense_run(dense_handle_t* h, const char* dir, const char* namelist_path, int
     // general_main.f90:59-60: get_primary and the final Tecplot file
     HostState s;
     rc = snapshot_now(h, s);
-    if (rc) return rc;
-    return write_tec(h, s, save_name(d, s.step, ".dat"));
+    if (!rc) rc = write_tec(h, s, save_name(d, s.step, ".dat"));
+    if (!rc && h->cfg.if_save_theta) rc = write_theta(h, s, theta_name(d, s.step));
+    return rc;
 }
 
 // errors of calls without a handle (dense_read_binary), read by dense_last_error(NULL)

@@ -756,6 +756,12 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
         }
     };
     auto hbuf = [&](int s, int c, int i) -> double& { return sR[(s * 4 + c) * NT + i]; };
+    // the indicator of a valid interface and sign into Params::theta (get_theta_*, SC.f90:1-64)
+    auto theta_out = [&](int s, double th) {
+        const long long xs = (long long)p.nj * (p.ni + 1), es = (long long)(p.nj + 1) * p.ni;
+        if (DIR == 0) p.theta[s * xs + (long long)line * (p.ni + 1) + f] = th;
+        else          p.theta[2 * xs + s * es + (long long)f * p.ni + line] = th;
+    };
 
     if constexpr (!ADAPT) {
         // 104: every interface takes the characteristic branch for both signs
@@ -804,6 +810,10 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
                 smooth[s] = p.theta_k1 * D > p.theta_k2 * (N - D);
                 const double r = rcp_nr(N);
                 wsur[s][0] = n0 * r; wsur[s][1] = n1 * r; wsur[s][2] = n2 * r;
+                if (p.theta) {  // theta = 1/(1 + (sum alpha - 1)^2), sum alpha = N/D
+                    const double sm1 = N / D - 1.0;
+                    theta_out(s, 1.0 / (1.0 + sm1 * sm1));
+                }
             }
 #else
             double lp[5], lm[5];
@@ -815,8 +825,10 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
             double th;
             weno5z_omega_theta(lp, wsur[0][0], wsur[0][1], wsur[0][2], th);
             smooth[0] = th > p.delta;
+            if (p.theta) theta_out(0, th);
             weno5z_omega_theta(lm, wsur[1][0], wsur[1][1], wsur[1][2], th);
             smooth[1] = th > p.delta;
+            if (p.theta) theta_out(1, th);
 #endif
         }
         __syncthreads();  // the staged surrogate terms are consumed; the region takes the results next

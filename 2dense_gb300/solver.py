@@ -207,6 +207,19 @@ class Solver:
         """write_tec_at_time_cartisian: the Tecplot ASCII file of the current state."""
         self._chk(self.lib.dense_write_tecplot(self.h, path.encode()))
 
+    def write_theta(self, path: str):
+        """write_theta_at_time_cartisian: the AdaWENO indicators of the last stage per cell."""
+        self._chk(self.lib.dense_write_theta(self.h, path.encode()))
+
+    def theta(self):
+        """theta of every (interface, sign) of the last stage: (xi [2, nj, ni+1], eta [2, nj+1, ni]),
+        with the splitting 105 and cfg.if_save_theta set."""
+        ni, nj = self.cfg.ni, self.cfg.nj
+        out = np.zeros(2 * (nj * (ni + 1) + (nj + 1) * ni))
+        self._chk(self.lib.dense_get_theta(self.h, _ptr(out)))
+        xs = 2 * nj * (ni + 1)
+        return out[:xs].reshape(2, nj, ni + 1), out[xs:].reshape(2, nj + 1, ni)
+
     def write_binary(self, path: str):
         """write_date_binary: the unformatted checkpoint of the current state."""
         self._chk(self.lib.dense_write_binary(self.h, path.encode()))

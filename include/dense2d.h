@@ -220,6 +220,14 @@ int dense_sync(dense_handle_t* h);
    one value per line with 17 significant digits. Like the reference, the header names seven
    variables and six primitive blocks follow (prim_lastvar_index = 6, var_index.f90:11). */
 int dense_write_tecplot(dense_handle_t* h, const char* path);
+/* write_theta_at_time_cartisian (output_test_general.f90:61-119): the AdaWENO indicators of
+   the last stage per cell (the larger of its two faces' theta) for xi +/- and eta +/-, as
+   Tecplot ASCII; zeros unless the splitting is 105 and cfg.if_save_theta is set (the sweeps
+   record theta only then). */
+int dense_write_theta(dense_handle_t* h, const char* path);
+/* theta of every (interface, sign) of the last stage: xi [2][nj][ni+1] then eta [2][nj+1][ni]
+   (sign 0 = "+"); DENSE_ERR_STATE unless the splitting is 105 and cfg.if_save_theta is set */
+int dense_get_theta(dense_handle_t* h, double* theta);
 /* write_date_binary (read_WriteAndLoad.f90:1-26): the unformatted checkpoint, gfortran
    sequential records (4-byte lengths around each): (step int32, time), num_block = 1,
    index = 1, (ni, nj), (bfsize_i, bfsize_j), cons(NIp,NJp,4), x(ni,nj), y(ni,nj), (dx, dy). */
@@ -232,9 +240,9 @@ int dense_read_binary(const char* path, dense_config_t* cfg, double* cons, doubl
 /* The loop of general_main.f90:23-60 on the device: steps while current_time < total_time and
    current_step < total_step; after every step with MOD(current_step, save_step) == 0 or
    elasp_time >= dt_save it writes 2d_<step>.dat2d (if_save_binary) and 2d_<step>.dat
-   (if_save_tec, which also resets elasp_time) into `dir`, then reads `namelist_path` again
-   (if not NULL) and applies it (dense_reconfigure); at the end it writes the final
-   2d_<step>.dat. The saves are formatted and written by a host thread from a device snapshot
+   (if_save_tec, which also resets elasp_time; and 2d_theta_<step>.dat if if_save_theta) into
+   `dir`, then reads `namelist_path` again (if not NULL) and applies it (dense_reconfigure); at
+   the end it writes the final 2d_<step>.dat (and 2d_theta_<step>.dat). The saves are formatted and written by a host thread from a device snapshot
    while the device runs on. *saves counts them (may be NULL). The reference's CpuTime.dat log
    is not written. */
 int dense_run(dense_handle_t* h, const char* dir, const char* namelist_path, int* saves);

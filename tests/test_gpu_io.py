@@ -121,3 +121,34 @@ def test_run_reads_the_namelist_at_saves(dense, tmp_path):
         saves = s.run(str(out), namelist=str(nml))
         assert s.current_step == 15
     assert saves == 1 and (out / "2d_15.dat").exists()
+
+
+@pytest.mark.parametrize("strict", [1, 0])
+def test_adaweno_indicators_match_the_oracle(dense, orc, tmp_path, strict):
+    """theta of every (interface, sign) of the last stage, and the theta file built from them."""
+    cfg = dense.config_default(ni=48, nj=24, benchmark=5, splitting=105, recon=0, cfl=0.5,
+                               if_save_theta=1, strict=strict)
+    c, cons, prim, x, y = dense.init_general(cfg)
+    with dense.Solver(c) as s:
+        s.upload(cons, prim, x, y)
+        s.steps(3)
+        tx, te = s.theta()
+        s.write_theta(str(tmp_path / "th.dat"))
+    o = orc.OracleSolver(c)
+    o.steps(3)
+    txp, txn, tep, ten = o.theta()
+    ref = [txp[0].T, txn[0].T, tep[0], ten[0]]  # -> [nj][ni+1] and [nj+1][ni]
+    got = [tx[0], tx[1], te[0], te[1]]
+    for g, r in zip(got, ref):
+        if strict:
+            np.testing.assert_array_equal(g, r)
+        else:
+            # theta = 1/(1 + (sum alpha - 1)^2) near shocks amplifies the fast state's 1e-13
+            # differences from the reference by the indicator's ~1/(ss + beta) sensitivity
+            np.testing.assert_allclose(g, r, rtol=1e-7, atol=1e-15)
+    head, vals = tecplot(tmp_path / "th.dat")
+    assert head[1].strip() == 'variables="x","y","xp","xn","ep","en"'
+    nv, nc = 49 * 25, 48 * 24
+    blocks = vals[2 * nv:].reshape(4, 24, 48)
+    np.testing.assert_array_equal(blocks[0], np.maximum(tx[0][:, :-1], tx[0][:, 1:]))
+    np.testing.assert_array_equal(blocks[3], np.maximum(te[1][:-1, :], te[1][1:, :]))
