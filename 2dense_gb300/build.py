@@ -92,7 +92,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
             print(txt)
         objs.append(obj)
     tmp = LIB + ".tmp"
-    link = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcuda", "-lpthread"]
+    link = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcuda", "-lpthread", "-ldl"]
     r = subprocess.run(link, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{' '.join(link)}\n{r.stdout.decode()}")

@@ -35,6 +35,7 @@
 
 #include "fastmath.cuh"
 #include "handle.h"
+#include "nvtx.h"
 
 namespace dense {
 namespace adj {
@@ -614,6 +615,7 @@ int dense_adjoint_create(const dense_config_t* cfg, int checkpoint_every, dense_
 }
 
 int dense_adjoint_forward(dense_adjoint_t* a, const double* u0, int nsteps, double* uT, void* stream) {
+    dense::NvtxRange nvtx_("dense_adjoint_forward");
     if (!a || !u0 || !uT) return aerr(a, DENSE_ERR_ARG, "null argument");
     if (nsteps < 0) return aerr(a, DENSE_ERR_ARG, "nsteps < 0");
     const int nseg = (nsteps + a->k - 1) / a->k;
@@ -645,6 +647,7 @@ int dense_adjoint_forward(dense_adjoint_t* a, const double* u0, int nsteps, doub
 }
 
 int dense_adjoint_backward(dense_adjoint_t* a, const double* gT, double* g0, void* stream) {
+    dense::NvtxRange nvtx_("dense_adjoint_backward");
     if (!a || !gT || !g0) return aerr(a, DENSE_ERR_ARG, "null argument");
     if (a->nsteps < 0) return aerr(a, DENSE_ERR_STATE, "dense_adjoint_backward before dense_adjoint_forward");
     int rc = begin(a, stream);
@@ -677,6 +680,7 @@ int dense_adjoint_backward(dense_adjoint_t* a, const double* gT, double* g0, voi
 
 int dense_adjoint_rhs_vjp(dense_adjoint_t* a, const double* u, const double* v, double* out, double* vdotl,
                           void* stream) {
+    dense::NvtxRange nvtx_("dense_adjoint_rhs_vjp");
     if (!a || !u || !v || !out) return aerr(a, DENSE_ERR_ARG, "null argument");
     int rc = begin(a, stream);
     if (!rc) rc = restart(a, u);

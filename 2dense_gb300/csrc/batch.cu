@@ -14,6 +14,7 @@
 
 #include "internal.h"
 #include "setups.cuh"
+#include "nvtx.h"
 
 using dense::BatchLaunch;
 using dense::Params;
@@ -271,6 +272,7 @@ void dense_batch_destroy(dense_batch_t* b) {
 
 int dense_batch_upload(dense_batch_t* b, int i, const double* cons, const double* prim, const double* x,
                        const double* y) {
+    dense::NvtxRange nvtx_("dense_batch_upload");
     if (!b || !cons || i < 0 || i >= b->n) return bset(b, DENSE_ERR_ARG, "bad instance or null cons");
     const dense_config_t& c = b->cfg[i];
     const Params& p = b->prm[i];
@@ -296,6 +298,7 @@ int dense_batch_set_time(dense_batch_t* b, int i, double t, int step) {
 }
 
 int dense_batch_steps_async(dense_batch_t* b, int nsteps, double t_end, int total_step) {
+    dense::NvtxRange nvtx_("dense_batch_steps");
     if (!b || nsteps < 0) return bset(b, DENSE_ERR_ARG, "bad argument");
     int rc = ensure_prim(b);
     if (rc) return rc;
@@ -329,6 +332,7 @@ int dense_batch_get_time(dense_batch_t* b, int i, double* t, int* step, double* 
 }
 
 int dense_batch_download(dense_batch_t* b, int i, double* cons, double* prim) {
+    dense::NvtxRange nvtx_("dense_batch_download");
     if (!b || i < 0 || i >= b->n) return bset(b, DENSE_ERR_ARG, "bad instance");
     const dense_config_t& c = b->cfg[i];
     const Params& p = b->prm[i];

@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "handle.h"
+#include "nvtx.h"
 
 extern "C" const char* dense_host_last_error(void);
 extern "C" const char* dense_io_last_error(void);
@@ -257,6 +258,7 @@ void dense_destroy(dense_handle_t* h) {
 }
 
 int dense_upload(dense_handle_t* h, const double* cons, const double* prim, const double* x, const double* y) {
+    dense::NvtxRange nvtx_("dense_upload");
     if (!h || !cons) return seterr(h, DENSE_ERR_ARG, "null handle or cons");
     const dense_config_t& c = h->cfg;
     const size_t row = (size_t)h->NIp * sizeof(double), pitch = (size_t)h->P * sizeof(double);
@@ -282,6 +284,7 @@ int dense_upload(dense_handle_t* h, const double* cons, const double* prim, cons
 }
 
 int dense_stage(dense_handle_t* h, int irk, double current_time, double* dt_inout) {
+    dense::NvtxRange nvtx_("dense_stage");
     if (!h) return seterr(h, DENSE_ERR_ARG, "null handle");
     if (irk < 1 || irk > 3) return seterr(h, DENSE_ERR_ARG, "irk must be 1, 2 or 3");
     if (!h->uploaded) return seterr(h, DENSE_ERR_STATE, "dense_stage before dense_upload");
@@ -303,6 +306,7 @@ int dense_stage(dense_handle_t* h, int irk, double current_time, double* dt_inou
 
 int dense_steps(dense_handle_t* h, int nsteps, double t_end, int total_step, double* t_inout,
                 int* step_inout, double* dt_out) {
+    dense::NvtxRange nvtx_("dense_steps");
     if (!h || !t_inout || !step_inout) return seterr(h, DENSE_ERR_ARG, "null argument");
     if (nsteps < 0) return seterr(h, DENSE_ERR_ARG, "nsteps < 0");
     if (!h->uploaded) return seterr(h, DENSE_ERR_STATE, "dense_steps before dense_upload");
@@ -326,6 +330,7 @@ int dense_steps(dense_handle_t* h, int nsteps, double t_end, int total_step, dou
 }
 
 int dense_download(dense_handle_t* h, double* cons, double* prim) {
+    dense::NvtxRange nvtx_("dense_download");
     if (!h) return seterr(h, DENSE_ERR_ARG, "null handle");
     if (!h->uploaded) return seterr(h, DENSE_ERR_STATE, "dense_download before dense_upload");
     const size_t row = (size_t)h->NIp * sizeof(double), pitch = (size_t)h->P * sizeof(double);
@@ -415,6 +420,7 @@ int dense_get_stream(dense_handle_t* h, void** stream) {
 }
 
 int dense_steps_async(dense_handle_t* h, int nsteps, double t_end, int total_step) {
+    dense::NvtxRange nvtx_("dense_steps_async");
     if (!h) return seterr(h, DENSE_ERR_ARG, "null handle");
     if (nsteps < 0) return seterr(h, DENSE_ERR_ARG, "nsteps < 0");
     if (!h->uploaded) return seterr(h, DENSE_ERR_STATE, "dense_steps_async before dense_upload");
@@ -500,6 +506,7 @@ int dense_profile_stage(dense_handle_t* h, int irk, float* ms) {
 
 
 int dense_upload_device(dense_handle_t* h, const double* cons, const double* prim, void* stream) {
+    dense::NvtxRange nvtx_("dense_upload_device");
     if (!h || !cons) return seterr(h, DENSE_ERR_ARG, "null handle or cons");
     int rc = wait_for(h, stream);
     if (rc) return rc;
@@ -515,6 +522,7 @@ int dense_upload_device(dense_handle_t* h, const double* cons, const double* pri
 }
 
 int dense_download_device(dense_handle_t* h, double* cons, double* prim, void* stream) {
+    dense::NvtxRange nvtx_("dense_download_device");
     if (!h) return seterr(h, DENSE_ERR_ARG, "null handle");
     if (!h->uploaded) return seterr(h, DENSE_ERR_STATE, "dense_download_device before an upload");
     int rc = wait_for(h, stream);
@@ -528,6 +536,7 @@ int dense_download_device(dense_handle_t* h, double* cons, double* prim, void* s
 }
 
 int dense_rhs_device(dense_handle_t* h, int irk, double* rhs, void* stream) {
+    dense::NvtxRange nvtx_("dense_rhs_device");
     if (!h || !rhs) return seterr(h, DENSE_ERR_ARG, "null argument");
     if (irk < 1 || irk > 3) return seterr(h, DENSE_ERR_ARG, "irk must be 1, 2 or 3");
     if (!h->uploaded) return seterr(h, DENSE_ERR_STATE, "dense_rhs_device before an upload");
@@ -554,6 +563,7 @@ __global__ void k_dt_out(const Scalars* sc, double* dt) { *dt = sc->dt; }
 
 int dense_stage_device(dense_handle_t* h, int irk, const double* cons0, double* dt, double current_time,
                        void* stream) {
+    dense::NvtxRange nvtx_("dense_stage_device");
     if (!h || !dt) return seterr(h, DENSE_ERR_ARG, "null argument");
     if (irk < 1 || irk > 3) return seterr(h, DENSE_ERR_ARG, "irk must be 1, 2 or 3");
     if (irk > 1 && !cons0) return seterr(h, DENSE_ERR_ARG, "stages 2 and 3 need the step's initial state");
@@ -579,6 +589,7 @@ int dense_stage_device(dense_handle_t* h, int irk, const double* cons0, double* 
 }
 
 int dense_steps_device(dense_handle_t* h, int nsteps, double t_end, int total_step, void* stream) {
+    dense::NvtxRange nvtx_("dense_steps_device");
     if (!h) return seterr(h, DENSE_ERR_ARG, "null handle");
     int rc = wait_for(h, stream);
     if (!rc) rc = dense_steps_async(h, nsteps, t_end, total_step);

@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "handle.h"
+#include "nvtx.h"
 
 extern "C" int dense_grid_coords(const dense_config_t* cfg, double* x, double* y, double* vx, double* vy);
 
@@ -233,6 +234,7 @@ __global__ void k_release(Scalars* sc, int reset_elasp) {
 extern "C" {
 
 int dense_write_tecplot(dense_handle_t* h, const char* path) {
+    dense::NvtxRange nvtx_("dense_write_tecplot");
     if (!h || !path) return ioerr(h, DENSE_ERR_ARG, "null argument");
     if (!h->uploaded) return ioerr(h, DENSE_ERR_STATE, "dense_write_tecplot before an upload");
     HostState s;
@@ -243,6 +245,7 @@ int dense_write_tecplot(dense_handle_t* h, const char* path) {
 }
 
 int dense_write_theta(dense_handle_t* h, const char* path) {
+    dense::NvtxRange nvtx_("dense_write_theta");
     if (!h || !path) return ioerr(h, DENSE_ERR_ARG, "null argument");
     if (!h->uploaded) return ioerr(h, DENSE_ERR_STATE, "dense_write_theta before an upload");
     HostState s;
@@ -260,6 +263,7 @@ int dense_get_theta(dense_handle_t* h, double* theta) {
 }
 
 int dense_write_binary(dense_handle_t* h, const char* path) {
+    dense::NvtxRange nvtx_("dense_write_binary");
     if (!h || !path) return ioerr(h, DENSE_ERR_ARG, "null argument");
     if (!h->uploaded) return ioerr(h, DENSE_ERR_STATE, "dense_write_binary before an upload");
     HostState s;
@@ -303,6 +307,7 @@ int dense_read_binary(const char* path, dense_config_t* cfg, double* cons, doubl
 }
 
 int dense_run(dense_handle_t* h, const char* dir, const char* namelist_path, int* saves_out) {
+    dense::NvtxRange nvtx_("dense_run");
     if (!h) return ioerr(h, DENSE_ERR_ARG, "null handle");
     if (!h->uploaded) return ioerr(h, DENSE_ERR_STATE, "dense_run before an upload");
     const std::string d = dir ? dir : "";
