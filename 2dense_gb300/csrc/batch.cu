@@ -33,6 +33,8 @@ struct dense_batch {
     BatchLaunch bl{};
     const dense::BatchKernelTable* kt = nullptr;
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;  // the eta sweeps' branch of the step graph
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cudaGraphExec_t graph = nullptr;
     int graph_nodes = 0;
     int order = 0;                // block order: 0 instance-major, 1 largest first, 2 interleaved
@@ -156,17 +158,35 @@ int ensure_prim(dense_batch* b) {
 
 int build_graph(dense_batch* b) {
     if (b->graph) return DENSE_OK;
+    if (!b->side) {
+        BCK(b, cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
+        BCK(b, cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming));
+        BCK(b, cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming));
+    }
     cudaGraph_t g = nullptr;
     BCK(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     b->kt->step_begin(b->bl, b->stream);
-    for (int irk = 1; irk <= 3; ++irk) {
+    // per stage: boundary; the eta sweep as a branch beside the xi sweep (both read the stage
+    // input, each writes its own face fluxes); the update after both
+    cudaError_t ce = cudaSuccess;
+    for (int irk = 1; irk <= 3 && ce == cudaSuccess; ++irk) {
         b->kt->bc(b->bl, b->stream);
+        ce = cudaEventRecord(b->ev_fork, b->stream);
+        if (ce == cudaSuccess) ce = cudaStreamWaitEvent(b->side, b->ev_fork, 0);
+        if (ce != cudaSuccess) break;
+        b->kt->flux(b->bl, irk, 1, b->side);
         b->kt->flux(b->bl, irk, 0, b->stream);
-        b->kt->flux(b->bl, irk, 1, b->stream);
+        ce = cudaEventRecord(b->ev_join, b->side);
+        if (ce == cudaSuccess) ce = cudaStreamWaitEvent(b->stream, b->ev_join, 0);
+        if (ce != cudaSuccess) break;
         b->kt->update(b->bl, irk, b->stream);
     }
     b->kt->step_end(b->bl, b->stream);
     cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+    if (e == cudaSuccess && ce != cudaSuccess) {
+        cudaGraphDestroy(g);
+        e = ce;
+    }
     if (e != cudaSuccess) return bset(b, DENSE_ERR_CUDA, std::string("stream capture: ") + cudaGetErrorString(e));
     e = cudaGraphInstantiate(&b->graph, g, 0);
     cudaGraphDestroy(g);
@@ -266,6 +286,9 @@ void dense_batch_destroy(dense_batch_t* b) {
     if (b->maps) cudaFree(b->maps);
     if (b->tab) cudaFree(b->tab);
     if (b->pool) cudaFree(b->pool);
+    if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+    if (b->ev_join) cudaEventDestroy(b->ev_join);
+    if (b->side) cudaStreamDestroy(b->side);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
 }

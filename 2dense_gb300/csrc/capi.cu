@@ -141,14 +141,41 @@ int stage_launches(dense_handle* h) {
     return 2 + h->kt->flux_launches(h->prm, 0) + h->kt->flux_launches(h->prm, 1);
 }
 
+// The stage as graph nodes: the two sweeps read the same stage input and write separate face
+// fluxes, so the eta sweep is a branch beside the xi sweep; its blocks fill the SMs the xi
+// sweep's last wave leaves idle. The update joins both.
+cudaError_t capture_stage(dense_handle* h, int irk) {
+    h->kt->bc(h->prm, h->stream);
+    cudaError_t e = cudaEventRecord(h->ev_fork, h->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(h->side, h->ev_fork, 0);
+    if (e != cudaSuccess) return e;
+    h->kt->flux(h->prm, irk, 1, h->side);
+    h->kt->flux(h->prm, irk, 0, h->stream);
+    e = cudaEventRecord(h->ev_join, h->side);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(h->stream, h->ev_join, 0);
+    if (e != cudaSuccess) return e;
+    h->kt->update(h->prm, irk, h->stream);
+    return cudaSuccess;
+}
+
 int build_step_graph(dense_handle* h) {
     if (h->step_graph) return DENSE_OK;
+    if (!h->side) {
+        CK(h, cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
+        CK(h, cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
+        CK(h, cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
+    }
     cudaGraph_t g = nullptr;
     CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     h->kt->step_begin(h->prm, h->stream);
-    for (int irk = 1; irk <= 3; ++irk) enqueue_stage(h, irk);
+    cudaError_t ce = cudaSuccess;
+    for (int irk = 1; irk <= 3 && ce == cudaSuccess; ++irk) ce = capture_stage(h, irk);
     h->kt->step_end(h->prm, h->stream);
     cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+    if (e == cudaSuccess && ce != cudaSuccess) {
+        cudaGraphDestroy(g);
+        e = ce;
+    }
     if (e != cudaSuccess) return seterr(h, DENSE_ERR_CUDA, std::string("stream capture: ") + cudaGetErrorString(e));
     e = cudaGraphInstantiate(&h->step_graph, g, 0);
     cudaGraphDestroy(g);
@@ -253,6 +280,9 @@ void dense_destroy(dense_handle_t* h) {
     double* bufs[] = {h->cons, h->prim, h->cons0, h->hx, h->he, h->xbot, h->xtop, h->yleft, h->theta};
     for (double* b : bufs) if (b) cudaFree(b);
     if (h->sc) cudaFree(h->sc);
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->ev_join) cudaEventDestroy(h->ev_join);
+    if (h->side) cudaStreamDestroy(h->side);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
 }

@@ -23,6 +23,10 @@ struct dense_handle {
     int prim_slot = -1;  // stage slot whose max wave speeds match the current state, or -1
     cudaGraphExec_t step_graph = nullptr;
     int graph_nodes = 0;
+    // the step graph runs a stage's eta sweep beside its xi sweep: the branch is captured on
+    // `side` between the two events
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     long long launches = 0;
     int count_branches = 0;
     std::string err;

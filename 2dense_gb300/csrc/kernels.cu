@@ -186,6 +186,34 @@ template <bool Z> __device__ __forceinline__ double weno_fast(const double lf[5]
     return fma(n2, q2, fma(n1, q1, n0 * q0)) * rcp_nr(N);
 }
 
+// Second-difference term of a smoothness indicator, ss + 13/12 A^2 with A = lm - 2 lc + lr: it
+// depends on one cell and its two neighbours only, so a sweep computes it once per cell and sign
+// and each of the three interfaces that use it reads it (the "-" sign passes its neighbours in
+// mirrored order, as its stencil reads them).
+__device__ __forceinline__ double ind_second(double lm, double lc, double lr) {
+    const double a = fma(-2.0, lc, lm) + lr;
+    return fma(k1312 * a, a, kSS);
+}
+// d_k = ss + beta_k from the staged terms s_k = ss + 13/12 A_k^2 of the three substencils
+// (centred on lf[1], lf[2], lf[3]): beta_k adds the first-order term 1/4 B_k^2.
+__device__ __forceinline__ void betas_staged(const double lf[5], double s0, double s1, double s2, double& d0,
+                                             double& d1, double& d2) {
+    const double b0 = fma(3.0, lf[2], fma(-4.0, lf[1], lf[0]));
+    const double b1 = lf[1] - lf[3];
+    const double b2 = fma(3.0, lf[2], fma(-4.0, lf[3], lf[4]));
+    d0 = fma(0.25 * b0, b0, s0);
+    d1 = fma(0.25 * b1, b1, s1);
+    d2 = fma(0.25 * b2, b2, s2);
+}
+// WENO reconstruction from d_k = ss + beta_k
+template <bool Z>
+__device__ __forceinline__ double weno_from_d(const double lf[5], double d0, double d1, double d2) {
+    double q0, q1, q2, n0, n1, n2, N, D;
+    candidates_fast(lf, q0, q1, q2);
+    weno_num_from_d<Z>(d0, d1, d2, fabs(d2 - d0), n0, n1, n2, N, D);
+    return fma(n2, q2, fma(n1, q1, n0 * q0)) * rcp_nr(N);
+}
+
 // The five coefficients of h = sum_k w_k q_k as one 5-point stencil: W[m] lf[m].
 __device__ __forceinline__ void stencil_from_weights(double w0, double w1, double w2, double W[5]) {
     W[0] = w0 * a300;
@@ -203,17 +231,19 @@ __device__ __forceinline__ void stencil_from_weights(double w0, double w1, doubl
 // 13/12 A_k^2 + 1/4 B_k^2 on the second differences A_k and the first-order combinations B_k.
 // Written over the common denominators of weno_num_fast (n_k = a_k D, N = sum(a) D, D = prod
 // d_k^2, P_k = D/d_k^2), with the quantities W itself needs computed by the same expressions.
+// The caller passes d_k = ss + beta_k as its own reconstruction computed them, so that the two
+// share every common term.
 template <int REC>
-__device__ __forceinline__ void recon_grad(const double lf[5], double g[5]) {
+__device__ __forceinline__ void recon_grad(const double lf[5], double d0, double d1, double d2, double g[5]) {
     if (REC == DENSE_RECON_UPWIND5) {
         g[0] = 2.0 / 60.0; g[1] = -13.0 / 60.0; g[2] = 47.0 / 60.0; g[3] = 27.0 / 60.0; g[4] = -3.0 / 60.0;
         return;
     }
     constexpr bool Z = REC == DENSE_RECON_WENOZ5;
-    double q0, q1, q2, n0, n1, n2, N, D, d0, d1, d2, tau;
+    double q0, q1, q2, n0, n1, n2, N, D;
+    const double tau = fabs(d2 - d0);
     candidates_fast(lf, q0, q1, q2);
-    betas_fast(lf, d0, d1, d2, tau);
-    weno_num_fast<Z>(lf, n0, n1, n2, N, D);
+    weno_num_from_d<Z>(d0, d1, d2, tau, n0, n1, n2, N, D);
     const double iN = rcp_nr(N);
     const double h = fma(n2, q2, fma(n1, q1, n0 * q0)) * iN;
     const double w0 = n0 * iN, w1 = n1 * iN, w2 = n2 * iN;
@@ -471,12 +501,29 @@ __device__ __forceinline__ void stage_scalars(const Params& p, int irk) {
 // Component-wise flux kernel (splittings 101/102/103 with reconstructions 251/253/255).
 // One thread per interface; the tile's per-cell split fluxes are staged in shared memory.
 // xi tile: TX interfaces x TY rows, cells f0+1 .. f0+TX+5; eta tile: TX columns x TY interfaces.
+// Dynamic shared memory of one block, in doubles: the split fluxes sF[8][NL][NC] (F+ of the four
+// components, then F-) and, for the WENO reconstructions of the fast variant, the indicators'
+// second-difference terms sS[8][NL][NC] of the same cells (F+ then F-).
+template <int DIR, int REC, int TX, int TY>
+struct CwTile {
+    static constexpr int NL = DIR == 0 ? TY : TY + 5;   // smem rows
+    static constexpr int NC = DIR == 0 ? TX + 5 : TX;   // smem columns
+    static constexpr int NCELL = NL * NC;
+    static constexpr bool kStageS = FAST && REC != DENSE_RECON_UPWIND5;
+    static constexpr size_t bytes = sizeof(double) * (size_t)NCELL * (kStageS ? 16 : 8);
+};
+
 template <int DIR, int SPL, int REC, int TX, int TY, bool TAPE = false>
 __device__ __forceinline__ void flux_cw_block(const Params& p, int irk, int bx, int by) {
     if (!p.sc->active) return;
-    constexpr int NL = DIR == 0 ? TY : TY + 5;   // smem rows
-    constexpr int NC = DIR == 0 ? TX + 5 : TX;   // smem columns
-    __shared__ double sF[8][NL][NC];
+    using L = CwTile<DIR, REC, TX, TY>;
+    constexpr int NL = L::NL, NC = L::NC, NCELL = L::NCELL;
+    constexpr bool kStageS = L::kStageS;
+    extern __shared__ __align__(16) double dsm[];
+    double* const sF = dsm;
+    double* const sS = dsm + 8 * NCELL;
+    (void)sS; (void)NL;
+    auto at = [](int r, int c) { return r * NC + c; };
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int slot = irk - 1;
     if (DIR == 0 && bx == 0 && by == 0 && tx == 0 && ty == 0) stage_scalars(p, irk);
@@ -499,7 +546,7 @@ __device__ __forceinline__ void flux_cw_block(const Params& p, int irk, int bx, 
                           p.gamma, fp, fm);
         }
 #pragma unroll
-        for (int v = 0; v < 4; ++v) { sF[v][r][c] = fp[v]; sF[4 + v][r][c] = fm[v]; }
+        for (int v = 0; v < 4; ++v) { sF[v * NCELL + at(r, c)] = fp[v]; sF[(4 + v) * NCELL + at(r, c)] = fm[v]; }
     };
     if (DIR == 0) {
         const int f0 = bx * TX, j = by * TY + ty;
@@ -518,6 +565,23 @@ __device__ __forceinline__ void flux_cw_block(const Params& p, int irk, int bx, 
     }
     __syncthreads();
 
+    // phase 1b (fast WENO): the indicators' second-difference terms, once per cell and sign for
+    // the cells with both neighbours in the tile ("+" reads a cell's neighbours as k-1, k, k+1,
+    // "-" as k+1, k, k-1)
+    if constexpr (kStageS) {
+        constexpr int KN = DIR == 0 ? TX + 5 : TY + 5;   // cells along the sweep
+        const int tid = tx + ty * TX;
+        for (int e = tid; e < 8 * NCELL; e += TX * TY) {
+            const int q = e / NCELL, o = e - q * NCELL;
+            const int k = DIR == 0 ? o % NC : o / NC;
+            if (k == 0 || k == KN - 1) continue;
+            const int st = DIR == 0 ? 1 : NC;             // neighbour along the sweep
+            const double* F = sF + q * NCELL + o;
+            sS[e] = q < 4 ? ind_second(F[-st], F[0], F[st]) : ind_second(F[st], F[0], F[-st]);
+        }
+        __syncthreads();
+    }
+
     // phase 2: reconstruction at the interface
     int line, f;  // line = row j (xi) or column i (eta); f = interface index
     if (DIR == 0) { line = by * TY + ty; f = bx * TX + tx; }
@@ -525,34 +589,61 @@ __device__ __forceinline__ void flux_cw_block(const Params& p, int irk, int bx, 
     const int nline = DIR == 0 ? p.nj : p.ni, nface = DIR == 0 ? p.ni + 1 : p.nj + 1;
     if (line >= nline || f >= nface) return;
     const int t = DIR == 0 ? tx : ty;  // position of the interface in the tile
+    auto atk = [&](int k) { return DIR == 0 ? at(ty, k) : at(k, tx); };
+    // this interface's entry of the adjoint's tape (planes of one direction: 10 x 4 gradient
+    // entries per stencil point and component, then the 4 face fluxes)
+    double* const tape_at = !TAPE ? nullptr
+                            : p.tape + (DIR == 0 ? 0 : tape_planes(REC) * (long long)p.nj * (p.ni + 1)) +
+                                  (DIR == 0 ? (long long)line * (p.ni + 1) + f : (long long)f * p.ni + line);
+    (void)tape_at;
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
         double lp[5], lm[5];
 #pragma unroll
         for (int m = 0; m < 5; ++m) {
             // "+": lf(m) = F+(cell f+3+m), smem index t+2+m; "-": lf(m) = F-(cell f+4-m), index t+3-m
-            if (DIR == 0) { lp[m] = sF[v][ty][t + m]; lm[m] = sF[4 + v][ty][t + 5 - m]; }
-            else          { lp[m] = sF[v][t + m][tx]; lm[m] = sF[4 + v][t + 5 - m][tx]; }
+            lp[m] = sF[v * NCELL + atk(t + m)];
+            lm[m] = sF[(4 + v) * NCELL + atk(t + 5 - m)];
         }
-        const double h = recon5<REC>(lp) + recon5<REC>(lm);
+        // the adjoint's tape: the reconstruction's gradient for stencil slot m0 (0 "+", 5 "-")
+        [[maybe_unused]] auto tape_grad = [&](const double lf[5], double d0, double d1, double d2, int m0) {
+            if constexpr (TAPE && REC != DENSE_RECON_UPWIND5) {
+                const long long ts = DIR == 0 ? (long long)p.nj * (p.ni + 1) : (long long)(p.nj + 1) * p.ni;
+                double g[5];
+                recon_grad<REC>(lf, d0, d1, d2, g);
+#pragma unroll
+                for (int m = 0; m < 5; ++m) tape_at[((m0 + m) * 4 + v) * ts] = g[m];
+            }
+        };
+        double h;
+        if constexpr (kStageS) {
+            // "+" substencils centred on tile cells t+1, t+2, t+3; "-" on t+4, t+3, t+2
+            constexpr bool Z = REC == DENSE_RECON_WENOZ5;
+            const double* Sp = sS + v * NCELL;
+            const double* Sm = sS + (4 + v) * NCELL;
+            double d0, d1, d2;
+            betas_staged(lp, Sp[atk(t + 1)], Sp[atk(t + 2)], Sp[atk(t + 3)], d0, d1, d2);
+            const double hp = weno_from_d<Z>(lp, d0, d1, d2);
+            tape_grad(lp, d0, d1, d2, 0);
+            betas_staged(lm, Sm[atk(t + 4)], Sm[atk(t + 3)], Sm[atk(t + 2)], d0, d1, d2);
+            const double hm = weno_from_d<Z>(lm, d0, d1, d2);
+            tape_grad(lm, d0, d1, d2, 5);
+            h = hp + hm;
+        } else {
+            h = recon5<REC>(lp) + recon5<REC>(lm);
+            if constexpr (TAPE && REC != DENSE_RECON_UPWIND5) {
+                double d0, d1, d2, tau;
+                betas_fast(lp, d0, d1, d2, tau);
+                tape_grad(lp, d0, d1, d2, 0);
+                betas_fast(lm, d0, d1, d2, tau);
+                tape_grad(lm, d0, d1, d2, 5);
+            }
+        }
         if (DIR == 0) p.hx[(long long)v * p.nj * (p.ni + 1) + (long long)line * (p.ni + 1) + f] = h;
         else          p.he[(long long)v * (p.nj + 1) * p.ni + (long long)f * p.ni + line] = h;
-        if (TAPE) {
-            constexpr int NP = tape_planes(REC);
-            const long long xs = (long long)p.nj * (p.ni + 1);
-            const long long ts = DIR == 0 ? xs : (long long)(p.nj + 1) * p.ni;
-            double* T = p.tape + (DIR == 0 ? 0 : NP * xs) +
-                        (DIR == 0 ? (long long)line * (p.ni + 1) + f : (long long)f * p.ni + line);
-            if (REC != DENSE_RECON_UPWIND5) {
-                double g[5];
-                recon_grad<REC>(lp, g);
-#pragma unroll
-                for (int m = 0; m < 5; ++m) T[(m * 4 + v) * ts] = g[m];
-                recon_grad<REC>(lm, g);
-#pragma unroll
-                for (int m = 0; m < 5; ++m) T[((5 + m) * 4 + v) * ts] = g[m];
-            }
-            T[(NP - 4 + v) * ts] = h;
+        if constexpr (TAPE) {
+            const long long ts = DIR == 0 ? (long long)p.nj * (p.ni + 1) : (long long)(p.nj + 1) * p.ni;
+            tape_at[(tape_planes(REC) - 4 + v) * ts] = h;
         }
     }
 }
@@ -947,7 +1038,12 @@ __device__ __forceinline__ void prim_cell(const Params& p, long long o, const do
     const double u = q[1] / rho;
     const double v = q[2] / rho;
 #endif
+#if FAST
+    // rho (u^2 + v^2) = m_u u + m_v v
+    double pr = (p.gamma - 1.0) * fma(-0.5, fma(q[1], u, q[2] * v), q[3]);
+#else
     double pr = (p.gamma - 1.0) * (q[3] - 0.5 * rho * (u * u + v * v));
+#endif
     if (pr < 0.0) { pr = kPFloor; flags |= DENSE_FLAG_P_FLOOR; }
 #if FAST
     const double a2 = p.gamma * pr * ir;
@@ -1004,6 +1100,12 @@ __device__ __forceinline__ void update_block(const Params& p, int bx, int by) {
         const long long hxs = (long long)p.nj * (p.ni + 1), hes = (long long)(p.nj + 1) * p.ni;
         const long long hxo = (long long)j * (p.ni + 1) + i, heo = (long long)j * p.ni + i;
         const double rho_in = p.cons[o], rv_in = p.cons[2 * p.plane + o];
+#if FAST
+        // stage 2: 3/4 q0 + 1/4 (...); stage 3: 1/3 q0 + 2/3 (...)
+        const double ka = IRK == 2 ? 3.0 / 4.0 : 1.0 / 3.0, kb = IRK == 2 ? 1.0 / 4.0 : 2.0 / 3.0;
+        const double cx = kb * dtdx, cy = kb * dtdy;
+        (void)ka; (void)cx; (void)cy;
+#endif
         double q[4];
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
@@ -1014,12 +1116,15 @@ __device__ __forceinline__ void update_block(const Params& p, int bx, int by) {
             if (IRK == 1) {
                 p.cons0[v * p.plane + o] = qc;
                 qn = qc - dtdx * dh_dxi - dtdy * dh_deta;
-            } else if (IRK == 2) {
-                const double q0 = p.cons0[v * p.plane + o];
-                qn = 3.0 / 4.0 * q0 + 1.0 / 4.0 * qc - 1.0 / 4.0 * (dtdx * dh_dxi + dtdy * dh_deta);
             } else {
                 const double q0 = p.cons0[v * p.plane + o];
-                qn = 1.0 / 3.0 * q0 + 2.0 / 3.0 * qc - 2.0 / 3.0 * (dtdx * dh_dxi + dtdy * dh_deta);
+#if FAST
+                // a q0 + b (qc - (dt/dx dh_xi + dt/dy dh_eta)), b folded into dt/dx and dt/dy
+                qn = fma(ka, q0, fma(kb, qc, -fma(cx, dh_dxi, cy * dh_deta)));
+#else
+                if (IRK == 2) qn = 3.0 / 4.0 * q0 + 1.0 / 4.0 * qc - 1.0 / 4.0 * (dtdx * dh_dxi + dtdy * dh_deta);
+                else          qn = 1.0 / 3.0 * q0 + 2.0 / 3.0 * qc - 2.0 / 3.0 * (dtdx * dh_dxi + dtdy * dh_deta);
+#endif
             }
             q[v] = qn;
         }
@@ -1233,12 +1338,17 @@ __device__ __forceinline__ void bc_block(const Params& p, int bx) {
 
 // ---------------------------------------------------------------------------------------------
 // Kernels of one block (instance) of the solver: block coordinates are the launch's own.
+// Resident blocks the register allocation of a characteristic sweep is sized for. AdaWENO's
+// blocks stall on the barriers of their work queue, which a third block per SM hides (80
+// registers instead of 94, a few bytes spilled: the xi sweep 2 % faster on the 1920 x 480 double
+// Mach reflection); the 104 eta sweep lost 4 % that way and keeps its natural 96 registers.
+constexpr int char_min_blocks(bool adapt) { return adapt ? 3 : 1; }
 template <int DIR, int SPL, int REC, int TX, int TY, bool TAPE = false>
 __global__ void __launch_bounds__(TX* TY) k_flux_cw(Params p, int irk) {
     flux_cw_block<DIR, SPL, REC, TX, TY, TAPE>(p, irk, blockIdx.x, blockIdx.y);
 }
 template <int DIR, bool ADAPT, int TX, int TY>
-__global__ void __launch_bounds__(TX* TY) k_flux_char(Params p, int irk) {
+__global__ void __launch_bounds__(TX* TY, char_min_blocks(ADAPT)) k_flux_char(Params p, int irk) {
     flux_char_block<DIR, ADAPT, TX, TY>(p, irk, blockIdx.x, blockIdx.y);
 }
 __global__ void k_prim(Params p, int slot) { prim_block(p, slot, blockIdx.x, blockIdx.y); }
@@ -1262,7 +1372,7 @@ __global__ void __launch_bounds__(TX* TY) kb_flux_cw(const Params* tab, const in
     flux_cw_block<DIR, SPL, REC, TX, TY>(sp, irk, m.y, m.z);
 }
 template <int DIR, bool ADAPT, int TX, int TY>
-__global__ void __launch_bounds__(TX* TY) kb_flux_char(const Params* tab, const int3* map, int irk) {
+__global__ void __launch_bounds__(TX* TY, char_min_blocks(ADAPT)) kb_flux_char(const Params* tab, const int3* map, int irk) {
     DENSE_BATCH_PROLOGUE
     flux_char_block<DIR, ADAPT, TX, TY>(sp, irk, m.y, m.z);
 }
@@ -1330,6 +1440,12 @@ static int sm_count() {
     return n;
 }
 
+// A component-wise sweep on its tile's dynamic shared memory.
+template <int DIR, int SPL, int REC, int TX, int TY, bool TAPE = false>
+static void cw_launch(dim3 g, const Params& p, int irk, cudaStream_t s) {
+    k_flux_cw<DIR, SPL, REC, TX, TY, TAPE><<<g, dim3(TX, TY), CwTile<DIR, REC, TX, TY>::bytes, s>>>(p, irk);
+}
+
 // On small grids the standard tiles give a sweep only one or two blocks per SM, and the SMs that
 // get one more block than the others set the launch's time. Below four blocks per SM the sweep
 // runs with tiles of half the height, which doubles the block count (same arithmetic per
@@ -1339,16 +1455,12 @@ static void launch_cw(const Params& p, int irk, int dir, cudaStream_t s) {
     const unsigned few = 4u * sm_count();
     if (dir == 0) {
         const dim3 g = grid_xi(p, kXTX, kXTY);
-        if (g.x * g.y < few)
-            k_flux_cw<0, SPL, REC, kXTX, kXTY / 2><<<grid_xi(p, kXTX, kXTY / 2), dim3(kXTX, kXTY / 2), 0, s>>>(p, irk);
-        else
-            k_flux_cw<0, SPL, REC, kXTX, kXTY><<<g, dim3(kXTX, kXTY), 0, s>>>(p, irk);
+        if (g.x * g.y < few) cw_launch<0, SPL, REC, kXTX, kXTY / 2>(grid_xi(p, kXTX, kXTY / 2), p, irk, s);
+        else                 cw_launch<0, SPL, REC, kXTX, kXTY>(g, p, irk, s);
     } else {
         const dim3 g = grid_eta(p, kETX, kETY);
-        if (g.x * g.y < few)
-            k_flux_cw<1, SPL, REC, kETX, kETY / 2><<<grid_eta(p, kETX, kETY / 2), dim3(kETX, kETY / 2), 0, s>>>(p, irk);
-        else
-            k_flux_cw<1, SPL, REC, kETX, kETY><<<g, dim3(kETX, kETY), 0, s>>>(p, irk);
+        if (g.x * g.y < few) cw_launch<1, SPL, REC, kETX, kETY / 2>(grid_eta(p, kETX, kETY / 2), p, irk, s);
+        else                 cw_launch<1, SPL, REC, kETX, kETY>(g, p, irk, s);
     }
 }
 
@@ -1384,19 +1496,19 @@ static void launch_flux(const Params& p, int irk, int dir, void* stream) {
 static void launch_flux_tape(const Params& p, int irk, int dir, void* stream) {
     cudaStream_t s = (cudaStream_t)stream;
     if (p.splitting != DENSE_SPLIT_LLF && p.splitting != DENSE_SPLIT_GLF) return;
-    const dim3 gx = grid_xi(p, kXTX, kXTY), bx(kXTX, kXTY), ge = grid_eta(p, kETX, kETY), be(kETX, kETY);
+    const dim3 gx = grid_xi(p, kXTX, kXTY), ge = grid_eta(p, kETX, kETY);
     switch (p.recon) {
     case DENSE_RECON_UPWIND5:
-        if (dir == 0) k_flux_cw<0, 0, 251, kXTX, kXTY, true><<<gx, bx, 0, s>>>(p, irk);
-        else          k_flux_cw<1, 0, 251, kETX, kETY, true><<<ge, be, 0, s>>>(p, irk);
+        if (dir == 0) cw_launch<0, 0, 251, kXTX, kXTY, true>(gx, p, irk, s);
+        else          cw_launch<1, 0, 251, kETX, kETY, true>(ge, p, irk, s);
         break;
     case DENSE_RECON_WENOJS5:
-        if (dir == 0) k_flux_cw<0, 0, 253, kXTX, kXTY, true><<<gx, bx, 0, s>>>(p, irk);
-        else          k_flux_cw<1, 0, 253, kETX, kETY, true><<<ge, be, 0, s>>>(p, irk);
+        if (dir == 0) cw_launch<0, 0, 253, kXTX, kXTY, true>(gx, p, irk, s);
+        else          cw_launch<1, 0, 253, kETX, kETY, true>(ge, p, irk, s);
         break;
     case DENSE_RECON_WENOZ5:
-        if (dir == 0) k_flux_cw<0, 0, 255, kXTX, kXTY, true><<<gx, bx, 0, s>>>(p, irk);
-        else          k_flux_cw<1, 0, 255, kETX, kETY, true><<<ge, be, 0, s>>>(p, irk);
+        if (dir == 0) cw_launch<0, 0, 255, kXTX, kXTY, true>(gx, p, irk, s);
+        else          cw_launch<1, 0, 255, kETX, kETY, true>(ge, p, irk, s);
         break;
     default:
         break;
@@ -1442,8 +1554,12 @@ static inline const int3* as_map(const void* m) { return (const int3*)m; }
 
 template <int SPL, int REC, int XTX, int XTY, int ETX, int ETY>
 static void batch_cw(const BatchLaunch& b, int irk, int dir, cudaStream_t s) {
-    if (dir == 0) kb_flux_cw<0, SPL, REC, XTX, XTY><<<b.nb_xi, dim3(XTX, XTY), 0, s>>>(b.tab, as_map(b.map_xi), irk);
-    else          kb_flux_cw<1, SPL, REC, ETX, ETY><<<b.nb_eta, dim3(ETX, ETY), 0, s>>>(b.tab, as_map(b.map_eta), irk);
+    if (dir == 0)
+        kb_flux_cw<0, SPL, REC, XTX, XTY><<<b.nb_xi, dim3(XTX, XTY), CwTile<0, REC, XTX, XTY>::bytes, s>>>(
+            b.tab, as_map(b.map_xi), irk);
+    else
+        kb_flux_cw<1, SPL, REC, ETX, ETY><<<b.nb_eta, dim3(ETX, ETY), CwTile<1, REC, ETX, ETY>::bytes, s>>>(
+            b.tab, as_map(b.map_eta), irk);
 }
 // xi tiles: (32,4) (64,2) (32,8); eta tiles: (32,8) (32,4) (64,4)
 template <int SPL, int REC>
@@ -1501,14 +1617,39 @@ static void batch_step_end(const BatchLaunch& b, void* stream) {
     kb_step_end<<<(b.n + 127) / 128, 128, 0, (cudaStream_t)stream>>>(b.tab, b.n);
 }
 
-// The characteristic sweeps take their tile from dynamic shared memory; with their static work
-// queue the larger tiles need more than the default 48 KB a block may use, which a kernel has to
-// be allowed once (set for every tile, whatever its size).
+// The sweeps take their tile from dynamic shared memory; with the static work queue of the
+// characteristic sweeps and the batched kernels' staged parameters, the larger tiles need more
+// than the default 48 KB a block may use, which a kernel has to be allowed once (set for every
+// tile, whatever its size).
 template <class K>
 static void allow_smem(K kernel, size_t bytes) {
     cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
-static bool allow_char_smem() {
+template <int SPL, int REC>
+static void allow_cw_smem() {
+    allow_smem(k_flux_cw<0, SPL, REC, kXTX, kXTY>, CwTile<0, REC, kXTX, kXTY>::bytes);
+    allow_smem(k_flux_cw<0, SPL, REC, kXTX, kXTY / 2>, CwTile<0, REC, kXTX, kXTY / 2>::bytes);
+    allow_smem(k_flux_cw<1, SPL, REC, kETX, kETY>, CwTile<1, REC, kETX, kETY>::bytes);
+    allow_smem(k_flux_cw<1, SPL, REC, kETX, kETY / 2>, CwTile<1, REC, kETX, kETY / 2>::bytes);
+    if (SPL == 0) {
+        allow_smem(k_flux_cw<0, 0, REC, kXTX, kXTY, true>, CwTile<0, REC, kXTX, kXTY>::bytes);
+        allow_smem(k_flux_cw<1, 0, REC, kETX, kETY, true>, CwTile<1, REC, kETX, kETY>::bytes);
+    }
+    // the batched tile variants of batch_cw_variant
+    allow_smem(kb_flux_cw<0, SPL, REC, 32, 4>, CwTile<0, REC, 32, 4>::bytes);
+    allow_smem(kb_flux_cw<0, SPL, REC, 64, 2>, CwTile<0, REC, 64, 2>::bytes);
+    allow_smem(kb_flux_cw<0, SPL, REC, 32, 8>, CwTile<0, REC, 32, 8>::bytes);
+    allow_smem(kb_flux_cw<1, SPL, REC, 32, 8>, CwTile<1, REC, 32, 8>::bytes);
+    allow_smem(kb_flux_cw<1, SPL, REC, 32, 4>, CwTile<1, REC, 32, 4>::bytes);
+    allow_smem(kb_flux_cw<1, SPL, REC, 64, 4>, CwTile<1, REC, 64, 4>::bytes);
+}
+static bool allow_tile_smem() {
+    allow_cw_smem<0, 251>();
+    allow_cw_smem<1, 251>();
+    allow_cw_smem<0, 253>();
+    allow_cw_smem<1, 253>();
+    allow_cw_smem<0, 255>();
+    allow_cw_smem<1, 255>();
     allow_smem(k_flux_char<0, false, kXTX, kXTY>, CharTile<0, false, kXTX, kXTY>::bytes);
     allow_smem(k_flux_char<1, false, kCETX, kCETY>, CharTile<1, false, kCETX, kCETY>::bytes);
     allow_smem(k_flux_char<0, true, kCXTX, kCXTY>, CharTile<0, true, kCXTX, kCXTY>::bytes);
@@ -1524,7 +1665,7 @@ static bool allow_char_smem() {
 
 #if DENSE_VARIANT_STRICT
 const BatchKernelTable* batch_kernels_strict() {
-    static const bool smem_ok = VNS::allow_char_smem();
+    static const bool smem_ok = VNS::allow_tile_smem();
     (void)smem_ok;
     static const BatchKernelTable t = {VNS::batch_prim, VNS::batch_bc, VNS::batch_flux, VNS::batch_update,
                                        VNS::batch_step_begin, VNS::batch_step_end};
@@ -1532,7 +1673,7 @@ const BatchKernelTable* batch_kernels_strict() {
 }
 #else
 const BatchKernelTable* batch_kernels_fast() {
-    static const bool smem_ok = VNS::allow_char_smem();
+    static const bool smem_ok = VNS::allow_tile_smem();
     (void)smem_ok;
     static const BatchKernelTable t = {VNS::batch_prim, VNS::batch_bc, VNS::batch_flux, VNS::batch_update,
                                        VNS::batch_step_begin, VNS::batch_step_end};
@@ -1556,7 +1697,7 @@ void batch_tile_shape(int splitting, int dir, int variant, int* tx, int* ty) {
 
 #if DENSE_VARIANT_STRICT
 const KernelTable* kernels_strict() {
-    static const bool smem_ok = VNS::allow_char_smem();
+    static const bool smem_ok = VNS::allow_tile_smem();
     (void)smem_ok;
     static const KernelTable t = {"strict", VNS::launch_prim, VNS::launch_bc, VNS::launch_flux,
                                   VNS::launch_update, VNS::launch_step_begin, VNS::launch_step_end,
@@ -1565,7 +1706,7 @@ const KernelTable* kernels_strict() {
 }
 #else
 const KernelTable* kernels_fast() {
-    static const bool smem_ok = VNS::allow_char_smem();
+    static const bool smem_ok = VNS::allow_tile_smem();
     (void)smem_ok;
     static const KernelTable t = {"fast", VNS::launch_prim, VNS::launch_bc, VNS::launch_flux,
                                   VNS::launch_update, VNS::launch_step_begin, VNS::launch_step_end,
