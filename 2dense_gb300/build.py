@@ -1,8 +1,9 @@
 """Build of the in-tree shared library ``csrc/_build/libdense2d.so`` (sm_103a only).
 
 Translation units, compiled in parallel:
-  kernels.cu  twice: -DDENSE_VARIANT_STRICT=0 (fast: FMA contraction) and
-              -DDENSE_VARIANT_STRICT=1 -fmad=false (strict: the reference's rounding)
+  kernels.cu  three times: -DDENSE_VARIANT_STRICT=0 (fast: FMA contraction),
+              -DDENSE_VARIANT_STRICT=1 -fmad=false (strict: the reference's rounding) and
+              -DDENSE_VARIANT_STRICT=0 -DDENSE_CHECK=1 (checked: fast with every index checked)
   capi.cu     the C ABI (handles, graphs, copies)
   batch.cu    the batched form (many blocks per launch)
   adjoint.cu  the discrete adjoint of the time step
@@ -65,6 +66,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
                          os.path.join(CSRC, "kernels.cu")],
         "kernels_strict": [nvcc, *ARCH, *NVCC_FLAGS, "-DDENSE_VARIANT_STRICT=1", "-fmad=false",
                            "-c", os.path.join(CSRC, "kernels.cu")],
+        "kernels_checked": [nvcc, *ARCH, *NVCC_FLAGS, "-DDENSE_VARIANT_STRICT=0", "-DDENSE_CHECK=1", "-c",
+                            os.path.join(CSRC, "kernels.cu")],
         "capi": [nvcc, *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, "capi.cu")],
         "probe": [nvcc, *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, "probe.cu")],
         "noalloc": [nvcc, *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, "noalloc.cu")],

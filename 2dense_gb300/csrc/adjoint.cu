@@ -464,8 +464,10 @@ int restart(dense_adjoint* a, const double* state) {
     return DENSE_OK;
 }
 
-// one stage of the forward solver with taping sweeps: boundary, flux_tape xi and eta, update
-void taped_stage(dense_adjoint* a, int irk, double* tape) {
+// one stage of the forward solver with taping sweeps: boundary, flux_tape xi and eta, update.
+// Launched directly on the solver's stream: forking the eta sweep onto a second stream, which
+// pays in the step graph, made the eagerly launched backward 34 % slower.
+int taped_stage(dense_adjoint* a, int irk, double* tape) {
     dense_handle* h = a->h;
     dense::Params p = h->prm;
     p.tape = tape;
@@ -474,6 +476,7 @@ void taped_stage(dense_adjoint* a, int irk, double* tape) {
     h->kt->flux_tape(p, irk, 1, h->stream);
     h->kt->update(h->prm, irk, h->stream);
     a->launches += 4;
+    return DENSE_OK;
 }
 
 template <int REC>
@@ -664,8 +667,8 @@ int dense_adjoint_backward(dense_adjoint_t* a, const double* gT, double* g0, voi
             h->kt->step_begin(h->prm, h->stream);
             for (int irk = 1; irk <= 3; ++irk) {
                 rc = from_solver(a, a->rec + ((size_t)s * 3 + irk - 1) * a->state);
+                if (!rc) rc = taped_stage(a, irk, a->tape + ((size_t)s * 3 + irk - 1) * a->tape_stage);
                 if (rc) return rc;
-                taped_stage(a, irk, a->tape + ((size_t)s * 3 + irk - 1) * a->tape_stage);
             }
             h->kt->step_end(h->prm, h->stream);
             a->launches += 2;
@@ -689,7 +692,8 @@ int dense_adjoint_rhs_vjp(dense_adjoint_t* a, const double* u, const double* v, 
     // not used); step_begin opens the stage (the loop bounds are open after restart)
     a->h->kt->step_begin(a->h->prm, a->h->stream);
     a->launches += 1;
-    taped_stage(a, 1, a->tape);
+    rc = taped_stage(a, 1, a->tape);
+    if (rc) return rc;
     a->h->prim_slot = -1;
     vjp(a, 0, u, a->tape, v, out, a->part, nullptr);
     std::vector<double> part(a->npart);

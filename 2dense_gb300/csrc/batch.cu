@@ -211,6 +211,8 @@ int dense_batch_create(int n, const dense_config_t* cfgs, dense_batch_t** out) {
             return bset(nullptr, DENSE_ERR_ARG, "instance " + std::to_string(i) + ": bad size, bfsize, neq, stages or dx/dy");
         if (c.splitting < DENSE_SPLIT_LLF || c.splitting > DENSE_SPLIT_SC)
             return bset(nullptr, DENSE_ERR_SPLITTING, "No such Selection (flux_splitting.f90:30-32)");
+        if (c.strict < 0 || c.strict > 2)
+            return bset(nullptr, DENSE_ERR_ARG, "instance " + std::to_string(i) + ": strict must be 0, 1 or 2");
         if (c.splitting != c0.splitting || c.recon != c0.recon || c.strict != c0.strict)
             return bset(nullptr, DENSE_ERR_ARG, "all instances of a batch share splitting, recon and strict");
         const int bm = c.benchmark;
@@ -225,7 +227,7 @@ int dense_batch_create(int n, const dense_config_t* cfgs, dense_batch_t** out) {
     b->n = n;
     b->cfg.assign(cfgs, cfgs + n);
     b->prm.resize(n);
-    b->kt = c0.strict ? dense::batch_kernels_strict() : dense::batch_kernels_fast();
+    b->kt = dense::batch_kernels_for(c0.strict);
     auto fail = [&](int code, const std::string& m) { g_err = m; dense_batch_destroy(b); return code; };
     if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess)
         return fail(DENSE_ERR_CUDA, "cudaStreamCreate failed");

@@ -72,6 +72,7 @@ int check_config(dense_handle* h, const dense_config_t* c) {
     if (!valid_bench(c->benchmark))
         return seterr(h, DENSE_ERR_BENCHMARK, "No such Benchmark index! (boundary_general.f90:26-28)");
     if (c->dx <= 0.0 || c->dy <= 0.0) return seterr(h, DENSE_ERR_ARG, "dx and dy must be set (dense_init_setup)");
+    if (c->strict < 0 || c->strict > 2) return seterr(h, DENSE_ERR_ARG, "strict must be 0 (fast), 1 (strict) or 2 (checked)");
     return DENSE_OK;
 }
 
@@ -96,7 +97,7 @@ void fill_params(dense_handle* h) {
     p.count_branches = h->count_branches;
     p.tape = nullptr;
     p.theta = c.if_save_theta && c.splitting == DENSE_SPLIT_SC ? h->theta : nullptr;
-    h->kt = c.strict ? dense::kernels_strict() : dense::kernels_fast();
+    h->kt = dense::kernels_for(c.strict);
 }
 
 // the indicator buffer, allocated while a configuration saves it
@@ -158,13 +159,18 @@ cudaError_t capture_stage(dense_handle* h, int irk) {
     return cudaSuccess;
 }
 
+// the side stream and the fork/join events of a stage's two sweeps
+int ensure_side(dense_handle* h) {
+    if (!h->side) CK(h, cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
+    if (!h->ev_fork) CK(h, cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
+    if (!h->ev_join) CK(h, cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
+    return DENSE_OK;
+}
+
 int build_step_graph(dense_handle* h) {
     if (h->step_graph) return DENSE_OK;
-    if (!h->side) {
-        CK(h, cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
-        CK(h, cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
-        CK(h, cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
-    }
+    int rc = ensure_side(h);
+    if (rc) return rc;
     cudaGraph_t g = nullptr;
     CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     h->kt->step_begin(h->prm, h->stream);

@@ -94,6 +94,12 @@ struct KernelTable {
 
 const KernelTable* kernels_fast();
 const KernelTable* kernels_strict();
+const KernelTable* kernels_checked();
+// the kernel table of a configuration's variant (dense_config_t::strict: 0 fast, 1 strict,
+// 2 checked)
+inline const KernelTable* kernels_for(int strict) {
+    return strict == 1 ? kernels_strict() : strict == 2 ? kernels_checked() : kernels_fast();
+}
 
 // ---- batched form: many independent blocks of uneven size advanced by one launch per phase
 struct int3_ { int x, y, z; };  // host mirror of CUDA's int3 (instance, block x, block y)
@@ -124,5 +130,9 @@ struct BatchKernelTable {
 };
 const BatchKernelTable* batch_kernels_fast();
 const BatchKernelTable* batch_kernels_strict();
+const BatchKernelTable* batch_kernels_checked();
+inline const BatchKernelTable* batch_kernels_for(int strict) {
+    return strict == 1 ? batch_kernels_strict() : strict == 2 ? batch_kernels_checked() : batch_kernels_fast();
+}
 
 }  // namespace dense

@@ -1,12 +1,16 @@
 // kernels.cu — sm_103a kernels of 2DENSE's per-stage hot path.
 //
-// This file is compiled twice into the same library:
+// This file is compiled three times into the same library:
 //   -DDENSE_VARIANT_STRICT=1 -fmad=false : dense::kernels_strict(). Every expression keeps the
 //      reference's evaluation order (left to right as written in the Fortran), no FMA is
 //      contracted and divide/sqrt are IEEE, so results are bit-identical to the reference's
 //      x86-64 arithmetic (except the SSL inflow rule, which calls tanh/cos/exp).
 //   -DDENSE_VARIANT_STRICT=0             : dense::kernels_fast(). FMA contraction and the
 //      algebraic rewrites marked FAST below; agrees with the reference to ~1e-14 per step.
+//   -DDENSE_VARIANT_STRICT=0 -DDENSE_CHECK=1 : dense::kernels_checked(), the debug build of the
+//      fast variant: every index into a state, face, tape or shared-memory array is checked
+//      against its array (chk below); one outside sets DENSE_FLAG_BOUNDS in the status word and
+//      is clamped into the array, so a bad index is reported, never dereferenced.
 //
 // All arithmetic is FP64. On GB300 the FP64 pipe, not HBM, bounds every kernel here (about
 // 4-7 kFLOP per cell-update against 256 B of compulsory traffic), so the kernels are built to
@@ -27,9 +31,15 @@
 #ifndef DENSE_VARIANT_STRICT
 #error "DENSE_VARIANT_STRICT must be defined (0 or 1)"
 #endif
+#ifndef DENSE_CHECK
+#define DENSE_CHECK 0
+#endif
 #if DENSE_VARIANT_STRICT
 #define VNS strict_impl
 #define FAST 0
+#elif DENSE_CHECK
+#define VNS checked_impl
+#define FAST 1
 #else
 #define VNS fast_impl
 #define FAST 1
@@ -37,6 +47,21 @@
 
 namespace dense {
 namespace VNS {
+
+// Index x of an array of n elements. The checked variant flags and clamps one outside [0, n);
+// the others compile the test away.
+template <class T>
+__device__ __forceinline__ T chk(const Params& p, T x, T n) {
+#if DENSE_CHECK
+    if (x < 0 || x >= n) {
+        atomicOr(&p.sc->status, DENSE_FLAG_BOUNDS);
+        return x < 0 ? 0 : n - 1;
+    }
+#else
+    (void)p; (void)n;
+#endif
+    return x;
+}
 
 // ---------------------------------------------------------------------------------------------
 // weno module constants (source/inv_scheme/weno_mod.f90:3-14,37)
@@ -477,7 +502,15 @@ __device__ __forceinline__ void char_weno_fast(const EigFast& e, const double F[
 
 // ---------------------------------------------------------------------------------------------
 // Index helpers
-__device__ __forceinline__ long long cidx(const Params& p, int I, int J) { return (long long)J * p.P + I; }
+__device__ __forceinline__ long long cidx(const Params& p, int I, int J) {
+    return (long long)chk(p, J, p.nj + 2 * kB) * p.P + chk(p, I, p.P);
+}
+// Face f of line `line` in plane v of direction DIR's face array (xi [nj][ni+1], eta [nj+1][ni]).
+template <int DIR>
+__device__ __forceinline__ long long fidx(const Params& p, int v, int line, int f) {
+    if (DIR == 0) return (long long)v * p.nj * (p.ni + 1) + (long long)chk(p, line, p.nj) * (p.ni + 1) + chk(p, f, p.ni + 1);
+    return (long long)v * (p.nj + 1) * p.ni + (long long)chk(p, f, p.nj + 1) * p.ni + chk(p, line, p.ni);
+}
 
 // Per-stage scalar work, done by one thread before the sweeps read or the update uses them:
 // the CFL time step (time_advance_general.f90:20-24), dt/dx, dt/dy, and the reset of the max
@@ -523,7 +556,7 @@ __device__ __forceinline__ void flux_cw_block(const Params& p, int irk, int bx, 
     double* const sF = dsm;
     double* const sS = dsm + 8 * NCELL;
     (void)sS; (void)NL;
-    auto at = [](int r, int c) { return r * NC + c; };
+    auto at = [&](int r, int c) { return chk(p, r, NL) * NC + chk(p, c, NC); };
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int slot = irk - 1;
     if (DIR == 0 && bx == 0 && by == 0 && tx == 0 && ty == 0) stage_scalars(p, irk);
@@ -594,7 +627,7 @@ __device__ __forceinline__ void flux_cw_block(const Params& p, int irk, int bx, 
     // entries per stencil point and component, then the 4 face fluxes)
     double* const tape_at = !TAPE ? nullptr
                             : p.tape + (DIR == 0 ? 0 : tape_planes(REC) * (long long)p.nj * (p.ni + 1)) +
-                                  (DIR == 0 ? (long long)line * (p.ni + 1) + f : (long long)f * p.ni + line);
+                                  fidx<DIR>(p, 0, line, f);
     (void)tape_at;
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
@@ -639,8 +672,7 @@ __device__ __forceinline__ void flux_cw_block(const Params& p, int irk, int bx, 
                 tape_grad(lm, d0, d1, d2, 5);
             }
         }
-        if (DIR == 0) p.hx[(long long)v * p.nj * (p.ni + 1) + (long long)line * (p.ni + 1) + f] = h;
-        else          p.he[(long long)v * (p.nj + 1) * p.ni + (long long)f * p.ni + line] = h;
+        (DIR == 0 ? p.hx : p.he)[fidx<DIR>(p, v, line, f)] = h;
         if constexpr (TAPE) {
             const long long ts = DIR == 0 ? (long long)p.nj * (p.ni + 1) : (long long)(p.nj + 1) * p.ni;
             tape_at[(tape_planes(REC) - 4 + v) * ts] = h;
@@ -711,7 +743,7 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
     if (ADAPT && tid == 0) qn = 0;
     (void)g1; (void)kg; (void)NL;
     // tile cell (r, c) -> offset; k runs along the sweep, (ox, oy) is the interface's tile position
-    auto at = [](int r, int c) { return r * NC + c; };
+    auto at = [&](int r, int c) { return chk(p, r, NL) * NC + chk(p, c, NC); };
     auto atk = [&](int k, int ox, int oy) { return DIR == 0 ? at(oy, k) : at(k, ox); };
 
     // phase 1: split fluxes (and primitives) of the tile's cells
@@ -842,16 +874,14 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
     auto store = [&](const double hsum[4]) {
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
-            if (DIR == 0) p.hx[(long long)v * p.nj * (p.ni + 1) + (long long)line * (p.ni + 1) + f] = hsum[v];
-            else          p.he[(long long)v * (p.nj + 1) * p.ni + (long long)f * p.ni + line] = hsum[v];
+            (DIR == 0 ? p.hx : p.he)[fidx<DIR>(p, v, line, f)] = hsum[v];
         }
     };
-    auto hbuf = [&](int s, int c, int i) -> double& { return sR[(s * 4 + c) * NT + i]; };
+    auto hbuf = [&](int s, int c, int i) -> double& { return sR[(s * 4 + c) * NT + chk(p, i, (int)NT)]; };
     // the indicator of a valid interface and sign into Params::theta (get_theta_*, SC.f90:1-64)
     auto theta_out = [&](int s, double th) {
         const long long xs = (long long)p.nj * (p.ni + 1), es = (long long)(p.nj + 1) * p.ni;
-        if (DIR == 0) p.theta[s * xs + (long long)line * (p.ni + 1) + f] = th;
-        else          p.theta[2 * xs + s * es + (long long)f * p.ni + line] = th;
+        p.theta[(DIR == 0 ? s * xs : 2 * xs + s * es) + fidx<DIR>(p, 0, line, f)] = th;
     };
 
     if constexpr (!ADAPT) {
@@ -953,7 +983,7 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
 #pragma unroll
                     for (int c = 0; c < 4; ++c) hbuf(s, c, tid) = h[c];
                 } else if (valid) {
-                    queue[atomicAdd(&qn, 1)] = 2 * tid + s;
+                    queue[chk(p, atomicAdd(&qn, 1), (int)(2 * NT))] = 2 * tid + s;
                 }
             }
             continue;
@@ -975,7 +1005,7 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
 #pragma unroll
                 for (int c = 0; c < 4; ++c) hbuf(s, c, tid) = h[c];
             } else {
-                queue[atomicAdd(&qn, 1)] = 2 * tid + s;
+                queue[chk(p, atomicAdd(&qn, 1), (int)(2 * NT))] = 2 * tid + s;
             }
         }
         __syncthreads();
@@ -1097,8 +1127,10 @@ __device__ __forceinline__ void update_block(const Params& p, int bx, int by) {
         const Scalars* sc = p.sc;
         const double dtdx = sc->dtdx, dtdy = sc->dtdy, dt = sc->dt;
         const long long o = cidx(p, i + kB, j + kB);
+        // the cell's faces: xi left/right, eta bottom/top; planes hxs, hes apart
         const long long hxs = (long long)p.nj * (p.ni + 1), hes = (long long)(p.nj + 1) * p.ni;
-        const long long hxo = (long long)j * (p.ni + 1) + i, heo = (long long)j * p.ni + i;
+        const long long hxl = fidx<0>(p, 0, j, i), hxr = fidx<0>(p, 0, j, i + 1);
+        const long long hel = fidx<1>(p, 0, i, j), her = fidx<1>(p, 0, i, j + 1);
         const double rho_in = p.cons[o], rv_in = p.cons[2 * p.plane + o];
 #if FAST
         // stage 2: 3/4 q0 + 1/4 (...); stage 3: 1/3 q0 + 2/3 (...)
@@ -1109,8 +1141,8 @@ __device__ __forceinline__ void update_block(const Params& p, int bx, int by) {
         double q[4];
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
-            const double dh_dxi = p.hx[v * hxs + hxo + 1] - p.hx[v * hxs + hxo];
-            const double dh_deta = p.he[v * hes + heo + p.ni] - p.he[v * hes + heo];
+            const double dh_dxi = p.hx[v * hxs + hxr] - p.hx[v * hxs + hxl];
+            const double dh_deta = p.he[v * hes + her] - p.he[v * hes + hel];
             const double qc = p.cons[v * p.plane + o];
             double qn;
             if (IRK == 1) {
@@ -1286,7 +1318,7 @@ __device__ __forceinline__ void bc_block(const Params& p, int bx) {
         break;
     }
     case kDMRBottom: {  // boundary_doublemach_general.f90:14-48
-        if (p.xbot[line] >= 1.0 / 6.0) {
+        if (p.xbot[chk(p, line, p.ni)] >= 1.0 / 6.0) {
 #pragma unroll
             for (int k = 0; k < kB; ++k) {
                 Cell g;
@@ -1311,14 +1343,14 @@ __device__ __forceinline__ void bc_block(const Params& p, int bx) {
             if (side == kBottom) state_from(gamma, 2.0, 0.0, 0.0, 1.0, g);
             else state_from(gamma, 1.0, 0.0, 0.0, 2.5, g);
         } else if (rule == kDMRTop) {  // boundary_doublemach_general.f90:51-76, time at the step's start
-            if (p.xtop[line] < (1.0 / 6.0 + (1.0 + 20.0 * p.sc->t) / sqrt(3.0)))
+            if (p.xtop[chk(p, line, p.ni)] < (1.0 / 6.0 + (1.0 + 20.0 * p.sc->t) / sqrt(3.0)))
                 state_from(gamma, 8.0, (double)8.25f * sqrt(3.0) * 0.5, -(double)8.25f * 0.5, 116.5, g);
             else
                 state_from(gamma, 1.4, 0.0, 0.0, 1.0, g);
         } else if (rule == kDMRInflow) {  // boundary_doublemach_general.f90:79-99
             state_from(gamma, 8.0, (double)8.25f * sqrt(3.0) * 0.5, -(double)8.25f * 0.5, 116.5, g);
         } else if (rule == kSSLInflow) {  // boundary_ssl_general.f90:40-66
-            const double yy = p.yleft[line];
+            const double yy = p.yleft[chk(p, line, p.nj)];
             const double rho = yy >= 0.0 ? 1.6374 : 0.3626, pr = 0.3327;
             const double pie = 3.141592653589793115997963468544185161590576171875;
             const double t = p.sc->t;
@@ -1450,17 +1482,17 @@ static void cw_launch(dim3 g, const Params& p, int irk, cudaStream_t s) {
 // get one more block than the others set the launch's time. Below four blocks per SM the sweep
 // runs with tiles of half the height, which doubles the block count (same arithmetic per
 // interface: the results do not depend on the tile).
-template <int SPL, int REC>
+template <int SPL, int REC, bool TAPE = false>
 static void launch_cw(const Params& p, int irk, int dir, cudaStream_t s) {
     const unsigned few = 4u * sm_count();
     if (dir == 0) {
         const dim3 g = grid_xi(p, kXTX, kXTY);
-        if (g.x * g.y < few) cw_launch<0, SPL, REC, kXTX, kXTY / 2>(grid_xi(p, kXTX, kXTY / 2), p, irk, s);
-        else                 cw_launch<0, SPL, REC, kXTX, kXTY>(g, p, irk, s);
+        if (g.x * g.y < few) cw_launch<0, SPL, REC, kXTX, kXTY / 2, TAPE>(grid_xi(p, kXTX, kXTY / 2), p, irk, s);
+        else                 cw_launch<0, SPL, REC, kXTX, kXTY, TAPE>(g, p, irk, s);
     } else {
         const dim3 g = grid_eta(p, kETX, kETY);
-        if (g.x * g.y < few) cw_launch<1, SPL, REC, kETX, kETY / 2>(grid_eta(p, kETX, kETY / 2), p, irk, s);
-        else                 cw_launch<1, SPL, REC, kETX, kETY>(g, p, irk, s);
+        if (g.x * g.y < few) cw_launch<1, SPL, REC, kETX, kETY / 2, TAPE>(grid_eta(p, kETX, kETY / 2), p, irk, s);
+        else                 cw_launch<1, SPL, REC, kETX, kETY, TAPE>(g, p, irk, s);
     }
 }
 
@@ -1496,20 +1528,10 @@ static void launch_flux(const Params& p, int irk, int dir, void* stream) {
 static void launch_flux_tape(const Params& p, int irk, int dir, void* stream) {
     cudaStream_t s = (cudaStream_t)stream;
     if (p.splitting != DENSE_SPLIT_LLF && p.splitting != DENSE_SPLIT_GLF) return;
-    const dim3 gx = grid_xi(p, kXTX, kXTY), ge = grid_eta(p, kETX, kETY);
     switch (p.recon) {
-    case DENSE_RECON_UPWIND5:
-        if (dir == 0) cw_launch<0, 0, 251, kXTX, kXTY, true>(gx, p, irk, s);
-        else          cw_launch<1, 0, 251, kETX, kETY, true>(ge, p, irk, s);
-        break;
-    case DENSE_RECON_WENOJS5:
-        if (dir == 0) cw_launch<0, 0, 253, kXTX, kXTY, true>(gx, p, irk, s);
-        else          cw_launch<1, 0, 253, kETX, kETY, true>(ge, p, irk, s);
-        break;
-    case DENSE_RECON_WENOZ5:
-        if (dir == 0) cw_launch<0, 0, 255, kXTX, kXTY, true>(gx, p, irk, s);
-        else          cw_launch<1, 0, 255, kETX, kETY, true>(ge, p, irk, s);
-        break;
+    case DENSE_RECON_UPWIND5: launch_cw<0, 251, true>(p, irk, dir, s); break;
+    case DENSE_RECON_WENOJS5: launch_cw<0, 253, true>(p, irk, dir, s); break;
+    case DENSE_RECON_WENOZ5:  launch_cw<0, 255, true>(p, irk, dir, s); break;
     default:
         break;
     }
@@ -1631,9 +1653,11 @@ static void allow_cw_smem() {
     allow_smem(k_flux_cw<0, SPL, REC, kXTX, kXTY / 2>, CwTile<0, REC, kXTX, kXTY / 2>::bytes);
     allow_smem(k_flux_cw<1, SPL, REC, kETX, kETY>, CwTile<1, REC, kETX, kETY>::bytes);
     allow_smem(k_flux_cw<1, SPL, REC, kETX, kETY / 2>, CwTile<1, REC, kETX, kETY / 2>::bytes);
-    if (SPL == 0) {
+    if (SPL == 0) {  // the adjoint's taping sweeps
         allow_smem(k_flux_cw<0, 0, REC, kXTX, kXTY, true>, CwTile<0, REC, kXTX, kXTY>::bytes);
+        allow_smem(k_flux_cw<0, 0, REC, kXTX, kXTY / 2, true>, CwTile<0, REC, kXTX, kXTY / 2>::bytes);
         allow_smem(k_flux_cw<1, 0, REC, kETX, kETY, true>, CwTile<1, REC, kETX, kETY>::bytes);
+        allow_smem(k_flux_cw<1, 0, REC, kETX, kETY / 2, true>, CwTile<1, REC, kETX, kETY / 2>::bytes);
     }
     // the batched tile variants of batch_cw_variant
     allow_smem(kb_flux_cw<0, SPL, REC, 32, 4>, CwTile<0, REC, 32, 4>::bytes);
@@ -1665,6 +1689,14 @@ static bool allow_tile_smem() {
 
 #if DENSE_VARIANT_STRICT
 const BatchKernelTable* batch_kernels_strict() {
+    static const bool smem_ok = VNS::allow_tile_smem();
+    (void)smem_ok;
+    static const BatchKernelTable t = {VNS::batch_prim, VNS::batch_bc, VNS::batch_flux, VNS::batch_update,
+                                       VNS::batch_step_begin, VNS::batch_step_end};
+    return &t;
+}
+#elif DENSE_CHECK
+const BatchKernelTable* batch_kernels_checked() {
     static const bool smem_ok = VNS::allow_tile_smem();
     (void)smem_ok;
     static const BatchKernelTable t = {VNS::batch_prim, VNS::batch_bc, VNS::batch_flux, VNS::batch_update,
@@ -1704,6 +1736,15 @@ const KernelTable* kernels_strict() {
                                   VNS::flux_launches, VNS::launch_flux_tape};
     return &t;
 }
+#elif DENSE_CHECK
+const KernelTable* kernels_checked() {
+    static const bool smem_ok = VNS::allow_tile_smem();
+    (void)smem_ok;
+    static const KernelTable t = {"checked", VNS::launch_prim, VNS::launch_bc, VNS::launch_flux,
+                                  VNS::launch_update, VNS::launch_step_begin, VNS::launch_step_end,
+                                  VNS::flux_launches, VNS::launch_flux_tape};
+    return &t;
+}
 #else
 const KernelTable* kernels_fast() {
     static const bool smem_ok = VNS::allow_tile_smem();
@@ -1717,7 +1758,7 @@ const KernelTable* kernels_fast() {
 
 }  // namespace dense
 
-#if !DENSE_VARIANT_STRICT
+#if !DENSE_VARIANT_STRICT && !DENSE_CHECK
 // Accuracy check of the fast reciprocal and inverse square root against CUDA's IEEE divide and
 // square root: out[4k..4k+3] = (rcp_nr(x), 1/x, rsqrt_nr(x), 1/sqrt(x)) for each x[k].
 namespace {

@@ -134,7 +134,7 @@ extern "C" int dense_stage_noalloc(const dense_config_t* cfg, int irk, double cu
     p.if_const_dt = cfg->if_const_dt;
     p.bodyforce = cfg->if_bodyforce && (b == DENSE_BENCH_RT || b == DENSE_BENCH_RT_REFLECT);
     p.benchmark = b; p.splitting = cfg->splitting; p.recon = cfg->recon;
-    const dense::KernelTable* kt = cfg->strict ? dense::kernels_strict() : dense::kernels_fast();
+    const dense::KernelTable* kt = dense::kernels_for(cfg->strict);
 
     cudaStream_t s = (cudaStream_t)stream;
     k_noalloc_scalars<<<1, 1, 0, s>>>(ptr.sc, irk - 1, current_time, *dt_inout);

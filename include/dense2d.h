@@ -49,6 +49,8 @@ extern "C" {
 #define DENSE_FLAG_RECON_NOOP   0x10u /* unknown scheme_inv_index: h stays zero, as in the
                                          reference's silent no-op (scheme_invs_general.f90:4-27) */
 #define DENSE_FLAG_TIMEOUT      0x20u /* a bounded device wait gave up                        */
+#define DENSE_FLAG_BOUNDS       0x40u /* checked variant (strict = 2): an array index fell outside
+                                         its array; it was clamped, not dereferenced            */
 
 /* ---- scheme and benchmark indices (the reference's namelist values) --------------------- */
 #define DENSE_SPLIT_LLF   101  /* local Lax-Friedrichs       flux_splitting_LLF.f90:13-77    */
@@ -109,7 +111,9 @@ typedef struct dense_config_t {
     /* kernel variant: 0 = fast (FMA contraction and algebraic rewrites, agrees with the
        reference to <= 1e-12 relative after one step); 1 = strict (the reference's evaluation
        order, no FMA contraction, IEEE divide and sqrt: bit-identical on the reference's
-       x86-64 arithmetic except where a boundary rule calls a transcendental function) */
+       x86-64 arithmetic except where a boundary rule calls a transcendental function);
+       2 = checked (debug build of the fast variant: the same results, with every array index
+       checked against its array; a bad one sets DENSE_FLAG_BOUNDS) */
     int strict;
     int reserved[7];
 } dense_config_t;
