@@ -707,8 +707,13 @@ __global__ void k_flux_noop(Params p, int irk) {
 // hbuf[2][4][NT].
 template <int DIR, bool ADAPT, int TX, int TY>
 struct CharTile {
+    // interfaces of a tile along the sweep: a one-row xi tile of TX threads covers TX - 5
+    // interfaces, so that its TX cells take one thread each (staging in one pass, with no warp
+    // left to stage a second round of halo cells while the others wait at the barrier)
+    static constexpr bool kFit = DIR == 0 && TY == 1;
+    static constexpr int KW = DIR == 0 ? (kFit ? TX - 5 : TX) : TY;
     static constexpr int NL = DIR == 0 ? TY : TY + 5;
-    static constexpr int NC = DIR == 0 ? TX + 5 : TX;
+    static constexpr int NC = DIR == 0 ? KW + 5 : TX;
     static constexpr int NT = TX * TY;
     static constexpr int NCELL = NL * NC;
     static constexpr bool kStageHS = FAST && !ADAPT;
@@ -772,9 +777,9 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
         }
     };
     if (DIR == 0) {
-        const int f0 = bx * TX, j = by * TY + ty;
+        const int f0 = bx * L::KW, j = by * TY + ty;
         if (j < p.nj)
-            for (int k = tx; k < TX + 5; k += TX) {
+            for (int k = tx; k < L::KW + 5; k += TX) {
                 const int I = f0 + 1 + k;
                 if (I < NIp) cell(I, j + kB, ty, k);
             }
@@ -796,7 +801,7 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
     double* const sA2 = sR + 4 * NCELL;   // [2][NCELL]
     double* const sDl = sR + 6 * NCELL;   // [2][NCELL]: sur(k+1) - sur(k)
     if constexpr (kStageInd) {
-        constexpr int KN = DIR == 0 ? TX + 5 : TY + 5;   // cells along the sweep
+        constexpr int KN = L::KW + 5;                    // cells along the sweep
         constexpr int KL = DIR == 0 ? TY : TX;           // lines
         for (int e = tid; e < KL * (KN - 2); e += NT) {
             const int line = e / (KN - 2), k = 1 + e % (KN - 2);
@@ -816,10 +821,10 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
     }
 
     int line, f;
-    if (DIR == 0) { line = by * TY + ty; f = bx * TX + tx; }
+    if (DIR == 0) { line = by * TY + ty; f = bx * L::KW + tx; }
     else          { line = bx * TX + tx; f = by * TY + ty; }
     const int nline = DIR == 0 ? p.nj : p.ni, nface = DIR == 0 ? p.ni + 1 : p.nj + 1;
-    const bool valid = line < nline && f < nface;
+    const bool valid = line < nline && f < nface && (DIR != 0 || tx < L::KW);
     auto SF = [&](int q, int k, int ox, int oy) -> double { return sF[q * NCELL + atk(k, ox, oy)]; };
     auto SQ = [&](int q, int k, int ox, int oy) -> double { return sQ[q * NCELL + atk(k, ox, oy)]; };
 #if FAST
@@ -971,10 +976,11 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
         for (int s = 0; s < 2; ++s) {
 #if FAST
             // the smooth result is computed by every lane (uniform, no divergence) and kept
-            // only where the smooth branch is taken
+            // only where the smooth branch is taken; the lanes past a fitted xi tile's last
+            // interface read that interface's stencil
             {
                 double F[5][4], h[4], W[5];
-                stencil(tx, ty, s, F);
+                stencil(DIR == 0 && tx >= L::KW ? L::KW - 1 : tx, ty, s, F);
                 stencil_from_weights(wsur[s][0], wsur[s][1], wsur[s][2], W);
 #pragma unroll
                 for (int c = 0; c < 4; ++c)
@@ -1447,9 +1453,10 @@ __global__ void k_step_end(Scalars* sc) { k_step_end_body(sc); }
 constexpr int kXTX = 32, kXTY = 4;   // xi tile
 constexpr int kETX = 32, kETY = 8;   // eta tile
 // characteristic sweeps: eta tiles of 4 columns x 64 interfaces, AdaWENO xi tiles of one row of
-// 256 interfaces (long lines along the sweep stage fewer halo cells per interface: 1.04 in xi and
-// 1.08 in eta against 1.16 and 1.63 for 32 x 4 and 32 x 8; measured on the 1920 x 480 double
-// Mach reflection, these shapes took the sweeps from 0.430 / 0.427 to 0.397 / 0.376 ms)
+// 256 threads (251 interfaces, 256 cells; long lines along the sweep stage fewer halo cells per
+// interface: 1.02 in xi and 1.08 in eta against 1.16 and 1.63 for 32 x 4 and 32 x 8; measured on
+// the 1920 x 480 double Mach reflection, these shapes took the sweeps from 0.430 / 0.427 to
+// 0.385 / 0.374 ms)
 constexpr int kCETX = 4, kCETY = 64;
 constexpr int kCXTX = 256, kCXTY = 1;
 
@@ -1516,7 +1523,7 @@ static void launch_flux(const Params& p, int irk, int dir, void* stream) {
         else          k_flux_char<1, false, kCETX, kCETY><<<grid_eta(p, kCETX, kCETY), dim3(kCETX, kCETY), CharTile<1, false, kCETX, kCETY>::bytes, s>>>(p, irk);
         break;
     case DENSE_SPLIT_SC:
-        if (dir == 0) k_flux_char<0, true, kCXTX, kCXTY><<<grid_xi(p, kCXTX, kCXTY), dim3(kCXTX, kCXTY), CharTile<0, true, kCXTX, kCXTY>::bytes, s>>>(p, irk);
+        if (dir == 0) k_flux_char<0, true, kCXTX, kCXTY><<<grid_xi(p, CharTile<0, true, kCXTX, kCXTY>::KW, kCXTY), dim3(kCXTX, kCXTY), CharTile<0, true, kCXTX, kCXTY>::bytes, s>>>(p, irk);
         else          k_flux_char<1, true, kCETX, kCETY><<<grid_eta(p, kCETX, kCETY), dim3(kCETX, kCETY), CharTile<1, true, kCETX, kCETY>::bytes, s>>>(p, irk);
         break;
     default:
@@ -1714,8 +1721,9 @@ const BatchKernelTable* batch_kernels_fast() {
 // Tile shapes of the batched sweeps (the shapes instantiated above).
 void batch_tile_shape(int splitting, int dir, int variant, int* tx, int* ty) {
     if (splitting == DENSE_SPLIT_CH || splitting == DENSE_SPLIT_SC) {
-        // xi: 32 x 4 for 104, 256 x 1 for AdaWENO; eta: 4 x 64
-        *tx = dir == 0 ? (splitting == DENSE_SPLIT_SC ? VNS::kCXTX : VNS::kXTX) : VNS::kCETX;
+        // xi: 32 x 4 for 104, one row of 251 interfaces (256 threads) for AdaWENO; eta: 4 x 64
+        *tx = dir == 0 ? (splitting == DENSE_SPLIT_SC ? VNS::CharTile<0, true, VNS::kCXTX, VNS::kCXTY>::KW : VNS::kXTX)
+                       : VNS::kCETX;
         *ty = dir == 0 ? (splitting == DENSE_SPLIT_SC ? VNS::kCXTY : VNS::kXTY) : VNS::kCETY;
         return;
     }
