@@ -188,7 +188,9 @@ __device__ __forceinline__ void weno_num_from_d(double d0, double d1, double d2,
         n1 = c31 * P1;
         n2 = c32 * P2;
     }
-    N = n0 + n1 + n2;
+    // written as rounded adds: with FMA contraction on, n_k (products) and this sum could fuse
+    // differently in different kernels, and the plain and taping sweeps must agree bit for bit
+    N = __dadd_rn(__dadd_rn(n0, n1), n2);
 }
 template <bool Z>
 __device__ __forceinline__ void weno_num_fast(const double lf[5], double& n0, double& n1, double& n2,
@@ -236,7 +238,8 @@ __device__ __forceinline__ double weno_from_d(const double lf[5], double d0, dou
     double q0, q1, q2, n0, n1, n2, N, D;
     candidates_fast(lf, q0, q1, q2);
     weno_num_from_d<Z>(d0, d1, d2, fabs(d2 - d0), n0, n1, n2, N, D);
-    return fma(n2, q2, fma(n1, q1, n0 * q0)) * rcp_nr(N);
+    // a rounded product: the caller adds the two signs' values, which must not fuse with it
+    return __dmul_rn(fma(n2, q2, fma(n1, q1, n0 * q0)), rcp_nr(N));
 }
 
 // The five coefficients of h = sum_k w_k q_k as one 5-point stencil: W[m] lf[m].
@@ -279,31 +282,33 @@ __device__ __forceinline__ void recon_grad(const double lf[5], double d0, double
     const double A0 = fma(-2.0, lf[1], lf[0]) + lf[2], B0 = fma(3.0, lf[2], fma(-4.0, lf[1], lf[0]));
     const double A1 = fma(-2.0, lf[2], lf[1]) + lf[3], B1 = lf[1] - lf[3];
     const double A2 = fma(-2.0, lf[3], lf[2]) + lf[4], B2 = fma(3.0, lf[2], fma(-4.0, lf[3], lf[4]));
-    double bb0, bb1, bb2;  // dW/dbeta_k
+    // r_k = -1/2 dW/dbeta_k. With dbeta_k/dlf = 13/6 A_k dA_k/dlf + 1/2 B_k dB_k/dlf, beta_k's
+    // share of dW/dlf is -13/3 r_k A_k dA_k/dlf - r_k B_k dB_k/dlf.
+    double r0, r1, r2;
     if (!Z) {
-        bb0 = -2.0 * (q0 - h) * w0 * id0;
-        bb1 = -2.0 * (q1 - h) * w1 * id1;
-        bb2 = -2.0 * (q2 - h) * w2 * id2;
+        r0 = (q0 - h) * (w0 * id0);
+        r1 = (q1 - h) * (w1 * id1);
+        r2 = (q2 - h) * (w2 * id2);
     } else {
         // s_k = (q_k - W)/sum(a) * c_k tau / d_k^2 = (q_k - W) c_k tau P_k / N
         const double s0 = (q0 - h) * (c30 * tau) * (P0 * iN);
         const double s1 = (q1 - h) * (c31 * tau) * (P1 * iN);
         const double s2 = (q2 - h) * (c32 * tau) * (P2 * iN);
-        const double tb = 2.0 * (s0 + s1 + s2);  // dW/dtau
-        const double sg = d2 >= d0 ? tb : -tb;  // dtau/dbeta_2 = -dtau/dbeta_0 = sign(beta_2 - beta_0)
-        bb0 = -2.0 * s0 * tau * id0 - sg;
-        bb1 = -2.0 * s1 * tau * id1;
-        bb2 = -2.0 * s2 * tau * id2 + sg;
+        // dW/dtau = 2 (s0 + s1 + s2); dtau/dbeta_2 = -dtau/dbeta_0 = sign(beta_2 - beta_0)
+        const double sh = d2 >= d0 ? s0 + s1 + s2 : -(s0 + s1 + s2);
+        r0 = fma(s0 * tau, id0, sh);
+        r1 = s1 * tau * id1;
+        r2 = fma(s2 * tau, id2, -sh);
     }
-    const double CA0 = (13.0 / 6.0) * bb0 * A0, CB0 = 0.5 * bb0 * B0;
-    const double CA1 = (13.0 / 6.0) * bb1 * A1, CB1 = 0.5 * bb1 * B1;
-    const double CA2 = (13.0 / 6.0) * bb2 * A2, CB2 = 0.5 * bb2 * B2;
-    stencil_from_weights(w0, w1, w2, g);
-    g[0] += CA0 + CB0;
-    g[1] += fma(-2.0, CA0, fma(-4.0, CB0, CA1 + CB1));
-    g[2] += fma(3.0, CB0, fma(-2.0, CA1, fma(3.0, CB2, CA0 + CA2)));
-    g[3] += fma(-2.0, CA2, fma(-4.0, CB2, CA1 - CB1));
-    g[4] += CA2 + CB2;
+    const double PA0 = r0 * A0, PA1 = r1 * A1, PA2 = r2 * A2;
+    const double NB0 = r0 * B0, NB1 = r1 * B1, NB2 = r2 * B2;
+    constexpr double k = -13.0 / 3.0;
+    // g[m] = sum_k w_k dq_k/dlf[m] (the 5-point stencil of the weights) + the indicators' shares
+    g[0] = fma(a300, w0, fma(k, PA0, -NB0));
+    g[1] = fma(a301, w0, fma(a310, w1, fma(-2.0 * k, PA0, fma(k, PA1, fma(4.0, NB0, -NB1)))));
+    g[2] = fma(a302, w0, fma(a311, w1, fma(a320, w2, fma(k, PA0, fma(-2.0 * k, PA1, fma(k, PA2, -3.0 * (NB0 + NB2)))))));
+    g[3] = fma(a312, w1, fma(a321, w2, fma(k, PA1, fma(-2.0 * k, PA2, fma(4.0, NB2, NB1)))));
+    g[4] = fma(a322, w2, fma(k, PA2, -NB2));
 }
 
 template <int REC> __device__ __forceinline__ double recon5(const double lf[5]) {
