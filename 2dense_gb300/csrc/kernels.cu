@@ -1216,7 +1216,11 @@ __device__ __forceinline__ void store_cell(const Params& p, int I, int J, const 
     for (int v = 0; v < 5; ++v) p.prim[v * p.plane + o] = g.q[v];
 }
 // Copy with the normal velocity negated (reflective wall): comp = 1 (u, x-walls) or 2 (v, y-walls)
-__device__ __forceinline__ void reflect(Cell& g, int comp) { g.c[comp] = -g.c[comp]; g.q[comp] = -g.q[comp]; }
+__device__ __forceinline__ void reflect(Cell& g, int comp) {
+    // constant indices keep the cell in registers (a run-time index would put it in local memory)
+    if (comp == 1) { g.c[1] = -g.c[1]; g.q[1] = -g.q[1]; }
+    else           { g.c[2] = -g.c[2]; g.q[2] = -g.q[2]; }
+}
 // Recursive 4/3, -1/3 extrapolation (boundary_ivc_general.f90:101-119). Strict: the reference's
 // two divides; fast: multiplies by the rounded constants (within an ulp, and no serial divides
 // in the boundary kernel's dependent chain).
@@ -1289,21 +1293,43 @@ __device__ __forceinline__ void bc_block(const Params& p, int bx) {
     case kReflect: {
         // periodic: ghost k copies the interior cell k+1 in from the opposite side
         // reflect:  ghost k mirrors the interior cell k+1 in from the same side, normal velocity negated
-#pragma unroll
-        for (int k = 0; k < kB; ++k) {
-            ghost(k, gi, gj);
+        auto source = [&](int k, int& si_, int& sj_) {
+            int gi_, gj_;
+            ghost(k, gi_, gj_);
             if (rule == kPeriodic) {
-                if (side == kBottom) { si = I; sj = nj + gj; }
-                else if (side == kTop) { si = I; sj = gj - nj; }
-                else if (side == kLeft) { si = ni + gi; sj = J; }
-                else { si = gi - ni; sj = J; }
+                if (side == kBottom) { si_ = I; sj_ = nj + gj_; }
+                else if (side == kTop) { si_ = I; sj_ = gj_ - nj; }
+                else if (side == kLeft) { si_ = ni + gi_; sj_ = J; }
+                else { si_ = gi_ - ni; sj_ = J; }
             } else {
-                inner(k + 1, si, sj);
+                inner(k + 1, si_, sj_);
             }
-            Cell g;
-            load_cell(p, si, sj, g);
-            if (rule == kReflect) reflect(g, vert ? 2 : 1);
-            store_cell(p, gi, gj, g);
+        };
+        if ((vert ? nj : ni) >= kB) {
+            // the four sources are interior cells: load them all, then store (one round trip
+            // of memory latency instead of four; the compiler cannot reorder the loads above
+            // the stores itself, not knowing the ghost and interior cells apart)
+            Cell g[kB];
+#pragma unroll
+            for (int k = 0; k < kB; ++k) { source(k, si, sj); load_cell(p, si, sj, g[k]); }
+#pragma unroll
+            for (int k = 0; k < kB; ++k) {
+                if (rule == kReflect) reflect(g[k], vert ? 2 : 1);
+                ghost(k, gi, gj);
+                store_cell(p, gi, gj, g[k]);
+            }
+        } else {
+            // fewer interior cells than ghost layers: an outer layer's source is a ghost cell
+            // written by an inner layer, so the layers go in the reference's order
+#pragma unroll
+            for (int k = 0; k < kB; ++k) {
+                source(k, si, sj);
+                Cell g;
+                load_cell(p, si, sj, g);
+                if (rule == kReflect) reflect(g, vert ? 2 : 1);
+                ghost(k, gi, gj);
+                store_cell(p, gi, gj, g);
+            }
         }
         break;
     }
@@ -1329,7 +1355,15 @@ __device__ __forceinline__ void bc_block(const Params& p, int bx) {
         break;
     }
     case kDMRBottom: {  // boundary_doublemach_general.f90:14-48
-        if (p.xbot[chk(p, line, p.ni)] >= 1.0 / 6.0) {
+        if (p.xbot[chk(p, line, p.ni)] >= 1.0 / 6.0) {  // reflecting wall
+            if (nj >= kB) {  // interior sources: all loads first, as for kReflect
+                Cell g[kB];
+#pragma unroll
+                for (int k = 0; k < kB; ++k) { inner(k + 1, si, sj); load_cell(p, si, sj, g[k]); }
+#pragma unroll
+                for (int k = 0; k < kB; ++k) { reflect(g[k], 2); ghost(k, gi, gj); store_cell(p, gi, gj, g[k]); }
+                break;
+            }
 #pragma unroll
             for (int k = 0; k < kB; ++k) {
                 Cell g;
