@@ -1319,10 +1319,16 @@ __device__ __forceinline__ void bc_block(const Params& p, int bx) {
                 store_cell(p, gi, gj, g[k]);
             }
         } else {
-            // fewer interior cells than ghost layers: an outer layer's source is a ghost cell
-            // written by an inner layer, so the layers go in the reference's order
+            // fewer interior cells (3) than ghost layers: one periodic source is a ghost cell of
+            // the same side, so the layers go in the reference's order -- bottom and left from
+            // the outermost layer in (the source is read before it is refilled), top and right
+            // from the innermost out (boundary_ivc_general.f90:13-35, boundary_rt_general.f90:
+            // 129-151). A mirror source there is a ghost of the opposite side, which another
+            // thread fills at the same time; the reference leaves such grids undefined too
+            // (its result depends on which side its loops reach first).
 #pragma unroll
-            for (int k = 0; k < kB; ++k) {
+            for (int kk = 0; kk < kB; ++kk) {
+                const int k = (side == kBottom || side == kLeft) ? kB - 1 - kk : kk;
                 source(k, si, sj);
                 Cell g;
                 load_cell(p, si, sj, g);

@@ -78,6 +78,16 @@ def test_one_step_schemes_strict_bitwise(dense, orc, bench, split, recon):
     assert dt == sc["dt"] and t == sc["time"]
 
 
+@pytest.mark.parametrize("ni,nj", [(16, 3), (3, 16), (3, 3)])
+@pytest.mark.parametrize("split,recon", [(101, 253), (105, 0)])
+def test_grids_narrower_than_the_ghost_layers_strict(dense, orc, ni, nj, split, recon):
+    """Three cells across a periodic direction: the fourth ghost layer's source is a ghost
+    cell of the same side, filled in the reference's order (bottom/left outermost first)."""
+    cfg = make_cfg(dense, 11, split, recon, ni, nj, strict=1)
+    g, gp, o, op, dt, t, sc, flags = run_pair(dense, orc, cfg, 2)
+    np.testing.assert_array_equal(interior(g), interior(o))
+
+
 @pytest.mark.parametrize("bench,split,recon,ni,nj", BENCHMARKS)
 def test_one_step_benchmarks_fast(dense, orc, bench, split, recon, ni, nj):
     cfg = make_cfg(dense, bench, split, recon, ni, nj)
