@@ -330,6 +330,22 @@ template <int REC> __device__ __forceinline__ double recon5(const double lf[5]) 
 template <int DIR>
 __device__ __forceinline__ void lf_split(const double U[4], double un, double p, double lam,
                                          double fp[4], double fm[4]) {
+#if FAST
+    // F+- = (u_n U + P)/2 +- (lam/2) U, P = (0, p e_n, u_n p): 16 operations instead of 19.
+    // The prim u_n and the conserved U stay separate factors as in the reference: in an
+    // extrapolated ghost cell m_n is not rho u_n.
+    const double hu = 0.5 * un, hl = 0.5 * lam;
+    double G[4];
+    G[0] = hu * U[0];
+    if (DIR == 0) { G[1] = fma(hu, U[1], 0.5 * p); G[2] = hu * U[2]; }
+    else          { G[1] = hu * U[1]; G[2] = fma(hu, U[2], 0.5 * p); }
+    G[3] = fma(hu, U[3], hu * p);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        fp[c] = fma(hl, U[c], G[c]);
+        fm[c] = fma(-hl, U[c], G[c]);
+    }
+#else
     const double up = un + lam, um = un - lam, upp = un * p;
     fp[0] = 0.5 * (up * U[0]);
     fm[0] = 0.5 * (um * U[0]);
@@ -342,6 +358,7 @@ __device__ __forceinline__ void lf_split(const double U[4], double un, double p,
     }
     fp[3] = 0.5 * (up * U[3] + upp);
     fm[3] = 0.5 * (um * U[3] + upp);
+#endif
 }
 
 // Steger-Warming (flux_splitting_SW.f90:42-91 xi, :110-160 eta)
