@@ -732,9 +732,9 @@ struct CharTile {
     // interfaces of a tile along the sweep: a one-row xi tile of TX threads covers TX - 5
     // interfaces, so that its TX cells take one thread each (staging in one pass, with no warp
     // left to stage a second round of halo cells while the others wait at the barrier)
-    static constexpr bool kFit = DIR == 0 && TY == 1;
-    static constexpr int KW = DIR == 0 ? (kFit ? TX - 5 : TX) : TY;
-    static constexpr int NL = DIR == 0 ? TY : TY + 5;
+    static constexpr bool kFit = DIR == 0 ? TY == 1 : TX <= 2;
+    static constexpr int KW = DIR == 0 ? (kFit ? TX - 5 : TX) : (kFit ? TY - 5 : TY);
+    static constexpr int NL = DIR == 0 ? TY : KW + 5;
     static constexpr int NC = DIR == 0 ? KW + 5 : TX;
     static constexpr int NT = TX * TY;
     static constexpr int NCELL = NL * NC;
@@ -806,9 +806,9 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
                 if (I < NIp) cell(I, j + kB, ty, k);
             }
     } else {
-        const int g0 = by * TY, i = bx * TX + tx;
+        const int g0 = by * L::KW, i = bx * TX + tx;
         if (i < p.ni)
-            for (int k = ty; k < TY + 5; k += TY) {
+            for (int k = ty; k < L::KW + 5; k += TY) {
                 const int J = g0 + 1 + k;
                 if (J < NJp) cell(i + kB, J, k, tx);
             }
@@ -844,9 +844,9 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
 
     int line, f;
     if (DIR == 0) { line = by * TY + ty; f = bx * L::KW + tx; }
-    else          { line = bx * TX + tx; f = by * TY + ty; }
+    else          { line = bx * TX + tx; f = by * L::KW + ty; }
     const int nline = DIR == 0 ? p.nj : p.ni, nface = DIR == 0 ? p.ni + 1 : p.nj + 1;
-    const bool valid = line < nline && f < nface && (DIR != 0 || tx < L::KW);
+    const bool valid = line < nline && f < nface && (DIR == 0 ? tx : ty) < L::KW;
     auto SF = [&](int q, int k, int ox, int oy) -> double { return sF[q * NCELL + atk(k, ox, oy)]; };
     auto SQ = [&](int q, int k, int ox, int oy) -> double { return sQ[q * NCELL + atk(k, ox, oy)]; };
 #if FAST
@@ -1002,7 +1002,7 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
             // interface read that interface's stencil
             {
                 double F[5][4], h[4], W[5];
-                stencil(DIR == 0 && tx >= L::KW ? L::KW - 1 : tx, ty, s, F);
+                stencil(DIR == 0 && tx >= L::KW ? L::KW - 1 : tx, DIR == 1 && ty >= L::KW ? L::KW - 1 : ty, s, F);
                 stencil_from_weights(wsur[s][0], wsur[s][1], wsur[s][2], W);
 #pragma unroll
                 for (int c = 0; c < 4; ++c)
@@ -1518,9 +1518,13 @@ constexpr int kETX = 32, kETY = 8;   // eta tile
 // 256 threads (251 interfaces, 256 cells; long lines along the sweep stage fewer halo cells per
 // interface: 1.02 in xi and 1.08 in eta against 1.16 and 1.63 for 32 x 4 and 32 x 8; measured on
 // the 1920 x 480 double Mach reflection, these shapes took the sweeps from 0.430 / 0.427 to
-// 0.385 / 0.374 ms)
+// 0.385 / 0.374 ms, the eta tile below to 0.355 ms)
 constexpr int kCETX = 4, kCETY = 64;
 constexpr int kCXTX = 256, kCXTY = 1;
+// AdaWENO eta tiles: 2 columns of 128 threads (123 interfaces, 128 cells each): every thread
+// stages one cell, and 123-interface columns cover 481 interfaces in 4 tiles with 2 % idle
+// lanes against 6 % for 64-interface columns
+constexpr int kAETX = 2, kAETY = 128;
 
 static inline dim3 grid_xi(const Params& p, int tx, int ty) {
     return dim3((p.ni + 1 + tx - 1) / tx, (p.nj + ty - 1) / ty);
@@ -1586,7 +1590,7 @@ static void launch_flux(const Params& p, int irk, int dir, void* stream) {
         break;
     case DENSE_SPLIT_SC:
         if (dir == 0) k_flux_char<0, true, kCXTX, kCXTY><<<grid_xi(p, CharTile<0, true, kCXTX, kCXTY>::KW, kCXTY), dim3(kCXTX, kCXTY), CharTile<0, true, kCXTX, kCXTY>::bytes, s>>>(p, irk);
-        else          k_flux_char<1, true, kCETX, kCETY><<<grid_eta(p, kCETX, kCETY), dim3(kCETX, kCETY), CharTile<1, true, kCETX, kCETY>::bytes, s>>>(p, irk);
+        else          k_flux_char<1, true, kAETX, kAETY><<<grid_eta(p, kAETX, CharTile<1, true, kAETX, kAETY>::KW), dim3(kAETX, kAETY), CharTile<1, true, kAETX, kAETY>::bytes, s>>>(p, irk);
         break;
     default:
         break;
@@ -1683,7 +1687,7 @@ static void batch_flux(const BatchLaunch& b, int irk, int dir, void* stream) {
         break;
     case DENSE_SPLIT_SC:
         if (dir == 0) kb_flux_char<0, true, kCXTX, kCXTY><<<b.nb_xi, dim3(kCXTX, kCXTY), CharTile<0, true, kCXTX, kCXTY>::bytes, s>>>(b.tab, as_map(b.map_xi), irk);
-        else          kb_flux_char<1, true, kCETX, kCETY><<<b.nb_eta, dim3(kCETX, kCETY), CharTile<1, true, kCETX, kCETY>::bytes, s>>>(b.tab, as_map(b.map_eta), irk);
+        else          kb_flux_char<1, true, kAETX, kAETY><<<b.nb_eta, dim3(kAETX, kAETY), CharTile<1, true, kAETX, kAETY>::bytes, s>>>(b.tab, as_map(b.map_eta), irk);
         break;
     default:
         break;
@@ -1746,11 +1750,11 @@ static bool allow_tile_smem() {
     allow_smem(k_flux_char<0, false, kXTX, kXTY>, CharTile<0, false, kXTX, kXTY>::bytes);
     allow_smem(k_flux_char<1, false, kCETX, kCETY>, CharTile<1, false, kCETX, kCETY>::bytes);
     allow_smem(k_flux_char<0, true, kCXTX, kCXTY>, CharTile<0, true, kCXTX, kCXTY>::bytes);
-    allow_smem(k_flux_char<1, true, kCETX, kCETY>, CharTile<1, true, kCETX, kCETY>::bytes);
+    allow_smem(k_flux_char<1, true, kAETX, kAETY>, CharTile<1, true, kAETX, kAETY>::bytes);
     allow_smem(kb_flux_char<0, false, kXTX, kXTY>, CharTile<0, false, kXTX, kXTY>::bytes);
     allow_smem(kb_flux_char<1, false, kCETX, kCETY>, CharTile<1, false, kCETX, kCETY>::bytes);
     allow_smem(kb_flux_char<0, true, kCXTX, kCXTY>, CharTile<0, true, kCXTX, kCXTY>::bytes);
-    allow_smem(kb_flux_char<1, true, kCETX, kCETY>, CharTile<1, true, kCETX, kCETY>::bytes);
+    allow_smem(kb_flux_char<1, true, kAETX, kAETY>, CharTile<1, true, kAETX, kAETY>::bytes);
     return true;
 }
 
@@ -1784,9 +1788,12 @@ const BatchKernelTable* batch_kernels_fast() {
 void batch_tile_shape(int splitting, int dir, int variant, int* tx, int* ty) {
     if (splitting == DENSE_SPLIT_CH || splitting == DENSE_SPLIT_SC) {
         // xi: 32 x 4 for 104, one row of 251 interfaces (256 threads) for AdaWENO; eta: 4 x 64
-        *tx = dir == 0 ? (splitting == DENSE_SPLIT_SC ? VNS::CharTile<0, true, VNS::kCXTX, VNS::kCXTY>::KW : VNS::kXTX)
-                       : VNS::kCETX;
-        *ty = dir == 0 ? (splitting == DENSE_SPLIT_SC ? VNS::kCXTY : VNS::kXTY) : VNS::kCETY;
+        // for 104, 2 columns of 123 interfaces (256 threads) for AdaWENO
+        const bool sc = splitting == DENSE_SPLIT_SC;
+        *tx = dir == 0 ? (sc ? VNS::CharTile<0, true, VNS::kCXTX, VNS::kCXTY>::KW : VNS::kXTX)
+                       : (sc ? VNS::kAETX : VNS::kCETX);
+        *ty = dir == 0 ? (sc ? VNS::kCXTY : VNS::kXTY)
+                       : (sc ? VNS::CharTile<1, true, VNS::kAETX, VNS::kAETY>::KW : VNS::kCETY);
         return;
     }
     static const int xi[kTileVariants][2] = {{32, 4}, {64, 2}, {32, 8}};
