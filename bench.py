@@ -53,7 +53,7 @@ WORKLOADS = {
 # that kernel on the same workload (dram__bytes_read.sum + dram__bytes_write.sum); the capture and
 # its command are summarised in the named profiles/ file.
 XI_TRAFFIC = {
-    "dmr": (59.295e6 + 3.469e6, "profiles/dmr_1920x480_adaweno_kernels.md"),
+    "dmr": (59.297e6 + 3.388e6, "profiles/dmr_1920x480_adaweno_kernels.md"),
     "rt": (17.368e6, "profiles/rt_256x1024_characteristic_kernels.md"),
     "ivc": (2.373e6, "profiles/ivc_200x200_weno_js_kernels.md"),
 }
