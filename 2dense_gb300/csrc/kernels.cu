@@ -1523,7 +1523,8 @@ constexpr int kCETX = 4, kCETY = 64;
 constexpr int kCXTX = 256, kCXTY = 1;
 // AdaWENO eta tiles: 2 columns of 128 threads (123 interfaces, 128 cells each): every thread
 // stages one cell, and 123-interface columns cover 481 interfaces in 4 tiles with 2 % idle
-// lanes against 6 % for 64-interface columns
+// lanes against 6 % for 64-interface columns. (The 104 eta sweep, at 102 registers a thread,
+// ran 5 % slower on such tiles on the 256 x 1024 Rayleigh-Taylor case and keeps 4 x 64.)
 constexpr int kAETX = 2, kAETY = 128;
 
 static inline dim3 grid_xi(const Params& p, int tx, int ty) {
@@ -1586,7 +1587,7 @@ static void launch_flux(const Params& p, int irk, int dir, void* stream) {
     }
     case DENSE_SPLIT_CH:
         if (dir == 0) k_flux_char<0, false, kXTX, kXTY><<<grid_xi(p, kXTX, kXTY), dim3(kXTX, kXTY), CharTile<0, false, kXTX, kXTY>::bytes, s>>>(p, irk);
-        else          k_flux_char<1, false, kCETX, kCETY><<<grid_eta(p, kCETX, kCETY), dim3(kCETX, kCETY), CharTile<1, false, kCETX, kCETY>::bytes, s>>>(p, irk);
+        else          k_flux_char<1, false, kCETX, kCETY><<<grid_eta(p, kCETX, CharTile<1, false, kCETX, kCETY>::KW), dim3(kCETX, kCETY), CharTile<1, false, kCETX, kCETY>::bytes, s>>>(p, irk);
         break;
     case DENSE_SPLIT_SC:
         if (dir == 0) k_flux_char<0, true, kCXTX, kCXTY><<<grid_xi(p, CharTile<0, true, kCXTX, kCXTY>::KW, kCXTY), dim3(kCXTX, kCXTY), CharTile<0, true, kCXTX, kCXTY>::bytes, s>>>(p, irk);
@@ -1793,7 +1794,8 @@ void batch_tile_shape(int splitting, int dir, int variant, int* tx, int* ty) {
         *tx = dir == 0 ? (sc ? VNS::CharTile<0, true, VNS::kCXTX, VNS::kCXTY>::KW : VNS::kXTX)
                        : (sc ? VNS::kAETX : VNS::kCETX);
         *ty = dir == 0 ? (sc ? VNS::kCXTY : VNS::kXTY)
-                       : (sc ? VNS::CharTile<1, true, VNS::kAETX, VNS::kAETY>::KW : VNS::kCETY);
+                       : (sc ? VNS::CharTile<1, true, VNS::kAETX, VNS::kAETY>::KW
+                             : VNS::CharTile<1, false, VNS::kCETX, VNS::kCETY>::KW);
         return;
     }
     static const int xi[kTileVariants][2] = {{32, 4}, {64, 2}, {32, 8}};
