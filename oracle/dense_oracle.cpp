@@ -915,7 +915,7 @@ template <class T> struct Solver {
                 }
             break;
         }
-        case 11: {  // periodic translating vortex (BASELINE form of the IVC test)
+        case 11: {  // periodic translating vortex (the IVC test with a freestream, periodic in x and y)
             double eps = cfg.var_eps, xc = cfg.var_xc, yc = cfg.var_yc;
             cell_centres(10.0, 10.0, 0.0);
             for (int j = 1; j <= nj; ++j)
