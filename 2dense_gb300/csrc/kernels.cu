@@ -1617,8 +1617,14 @@ static int flux_launches(const Params& p, int dir) {
     return 1;
 }
 
+// Cell blocks of 32 x 8; on grids that give fewer than four of them per SM, blocks of 32 x 2
+// even out the last wave (one atomic per block: few blocks on those grids either way)
+static dim3 cell_block(const Params& p) {
+    const unsigned big = (unsigned)((p.ni + 31) / 32) * (unsigned)((p.nj + 7) / 8);
+    return big < 4u * sm_count() ? dim3(32, 2) : dim3(32, 8);
+}
 static void launch_prim(const Params& p, int slot, void* stream) {
-    dim3 b(32, 8), g((p.ni + 31) / 32, (p.nj + 7) / 8);
+    const dim3 b = cell_block(p), g((p.ni + 31) / 32, (p.nj + b.y - 1) / b.y);
     k_prim<<<g, b, 0, (cudaStream_t)stream>>>(p, slot);
 }
 // One warp per block: a grid's few thousand ghost lines spread over all SMs, so the latency of
@@ -1630,7 +1636,7 @@ static void launch_bc(const Params& p, void* stream) {
     k_bc<<<(n + kBcThreads - 1) / kBcThreads, kBcThreads, 0, (cudaStream_t)stream>>>(p);
 }
 static void launch_update(const Params& p, int irk, void* stream) {
-    dim3 b(32, 8), g((p.ni + 31) / 32, (p.nj + 7) / 8);
+    const dim3 b = cell_block(p), g((p.ni + 31) / 32, (p.nj + b.y - 1) / b.y);
     cudaStream_t s = (cudaStream_t)stream;
     if (irk == 1) k_update<1><<<g, b, 0, s>>>(p);
     else if (irk == 2) k_update<2><<<g, b, 0, s>>>(p);
