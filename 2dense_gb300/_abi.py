@@ -27,6 +27,7 @@ FLAG_P_FLOOR = 0x04
 FLAG_ROE_IMAG = 0x08
 FLAG_RECON_NOOP = 0x10
 FLAG_TIMEOUT = 0x20
+FLAG_BOUNDS = 0x40  # checked variant (strict = 2): an index outside its array
 
 ERROR_NAMES = {
     1: "DENSE_ERR_ARG", 2: "DENSE_ERR_SPLITTING", 3: "DENSE_ERR_BENCHMARK",

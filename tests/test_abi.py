@@ -2,6 +2,7 @@
 and its host-side parts (defaults, namelist reader, initial setups, argument checks) behave like
 the reference. No GPU is touched."""
 import ctypes
+import importlib
 import json
 import os
 import re
@@ -79,6 +80,8 @@ def test_namelist_errors(dense, tmp_path):
     ("bfsize", 3, 1),
     ("stages", 2, 1),
     ("ni", 2, 1),
+    ("strict", 3, 1),        # variants: 0 fast, 1 strict, 2 checked
+    ("strict", -1, 1),
 ])
 def test_create_rejects_bad_config(dense, field, value, code):
     lib = dense.load_library()
@@ -89,6 +92,15 @@ def test_create_rejects_bad_config(dense, field, value, code):
     assert rc == code
     assert not h.value
     assert lib.dense_last_error(None)
+
+
+def test_status_flags_match_python_mirror(dense):
+    abi = importlib.import_module("2dense_gb300._abi")
+    header = open(os.path.join(ROOT, "include", "dense2d.h")).read()
+    for name in ("NAN", "NEG_RHO", "P_FLOOR", "ROE_IMAG", "RECON_NOOP", "TIMEOUT", "BOUNDS"):
+        m = re.search(r"#define DENSE_FLAG_%s\s+(0x[0-9a-fA-F]+)u" % name, header)
+        assert m, name
+        assert getattr(abi, "FLAG_" + name) == int(m.group(1), 16), name
 
 
 @pytest.mark.parametrize("bench", [1, 2, 3, 4, 5, 6, 9, 11, 13, 14])
