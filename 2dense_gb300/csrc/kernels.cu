@@ -729,9 +729,11 @@ __global__ void k_flux_noop(Params p, int irk) {
 // hbuf[2][4][NT].
 template <int DIR, bool ADAPT, int TX, int TY>
 struct CharTile {
-    // interfaces of a tile along the sweep: a one-row xi tile of TX threads covers TX - 5
-    // interfaces, so that its TX cells take one thread each (staging in one pass, with no warp
-    // left to stage a second round of halo cells while the others wait at the barrier)
+    // interfaces of a tile along the sweep (KW): a one-row xi tile of TX threads covers TX - 5
+    // interfaces, and an eta tile of one or two columns of TY threads TY - 5 per column, so that
+    // the tile's cells take one thread each (staging in one pass, with no warp left to stage a
+    // second round of halo cells while the others wait at the barrier); other tiles cover one
+    // interface per thread
     static constexpr bool kFit = DIR == 0 ? TY == 1 : TX <= 2;
     static constexpr int KW = DIR == 0 ? (kFit ? TX - 5 : TX) : (kFit ? TY - 5 : TY);
     static constexpr int NL = DIR == 0 ? TY : KW + 5;
