@@ -226,6 +226,7 @@ int signal_to(dense_handle* h, void* caller) {
 }  // namespace
 
 int dense::handle_ensure_prim(dense_handle* h, int slot) { return ensure_prim(h, slot); }
+void dense::set_last_error(const char* msg) { g_err = msg ? msg : ""; }
 int dense::handle_step_graph(dense_handle* h) { return build_step_graph(h); }
 int dense::handle_stage_launches(dense_handle* h) { return stage_launches(h); }
 

@@ -101,6 +101,10 @@ inline const KernelTable* kernels_for(int strict) {
     return strict == 1 ? kernels_strict() : strict == 2 ? kernels_checked() : kernels_fast();
 }
 
+// The error text that dense_last_error(NULL) returns, for entry points without a handle that
+// live outside capi.cu (the allocation-free stage); the calling thread's own copy.
+void set_last_error(const char* msg);
+
 // ---- batched form: many independent blocks of uneven size advanced by one launch per phase
 struct int3_ { int x, y, z; };  // host mirror of CUDA's int3 (instance, block x, block y)
 

@@ -19,9 +19,17 @@
 //    from two host threads -- race on the arrays and must be serialised by the caller;
 //  * the first call on a device resolves the device addresses of the arrays
 //    (cudaGetSymbolAddress) with that device current; make that first call before any stream
-//    capture begins. Later calls allocate nothing and call no allocating routine.
+//    capture begins. Later calls allocate nothing and call no allocating routine. A call made
+//    in a new context of the device (after cudaDeviceReset, say) resolves them again;
+//  * after the stage the call reads the device status word back: a NaN, a non-positive density
+//    or a negative Roe sound speed squared returns DENSE_ERR_NUMERIC, an index outside its array
+//    in the checked variant (strict = 2) DENSE_ERR_ARG, each with the flags in the error text
+//    (dense_last_error(NULL)). The pressure floor and an unknown reconstruction index are not
+//    failures, as in the reference, which goes on after both.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <cstdio>
 #include <mutex>
 #include <string>
 
@@ -38,21 +46,41 @@ __device__ __align__(256) dense::Scalars g_scalars_scratch;
 struct DevicePtrs {
     double* flux = nullptr;
     dense::Scalars* sc = nullptr;
+    CUcontext ctx = nullptr;  // the context the addresses belong to
 };
 DevicePtrs g_ptrs[kMaxDevices];
 std::mutex g_mu;
-thread_local std::string g_err;
 
+// the message goes where dense_last_error(NULL) reads it
 int fail(int code, const std::string& msg) {
-    g_err = msg;
+    dense::set_last_error(msg.c_str());
     return code;
 }
 
-// Device addresses of the scratch arrays on the current device, resolved once per device.
+// The current context, through the runtime's driver entry point (the library does not link the
+// driver library itself, so it still loads on machines without one).
+CUcontext current_context() {
+    using Fn = CUresult (*)(CUcontext*);
+    static const Fn fn = [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess || q != cudaDriverEntryPointSuccess)
+            return (Fn) nullptr;
+        return (Fn)f;
+    }();
+    CUcontext ctx = nullptr;
+    if (!fn || fn(&ctx) != CUDA_SUCCESS) ctx = nullptr;
+    return ctx;
+}
+
+// Device addresses of the scratch arrays on the current device, resolved once per device and
+// context (the module, and with it the arrays, is loaded again in a new context).
 int resolve(int dev, DevicePtrs& out) {
     std::lock_guard<std::mutex> lock(g_mu);
     DevicePtrs& p = g_ptrs[dev];
-    if (!p.flux) {
+    const CUcontext ctx = current_context();
+    if (!p.flux || p.ctx != ctx) {
         void* f = nullptr;
         void* s = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&f, g_flux_scratch);
@@ -61,6 +89,7 @@ int resolve(int dev, DevicePtrs& out) {
         if (e != cudaSuccess) return fail(DENSE_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
         p.flux = (double*)f;
         p.sc = (dense::Scalars*)s;
+        p.ctx = ctx;
     }
     out = p;
     return DENSE_OK;
@@ -98,6 +127,8 @@ extern "C" int dense_stage_noalloc(const dense_config_t* cfg, int irk, double cu
     if (cfg->splitting < DENSE_SPLIT_LLF || cfg->splitting > DENSE_SPLIT_SC)
         return fail(DENSE_ERR_SPLITTING, "No such Selection (flux_splitting.f90:30-32)");
     if (cfg->dx <= 0.0 || cfg->dy <= 0.0) return fail(DENSE_ERR_ARG, "dx and dy must be set");
+    if (cfg->strict < 0 || cfg->strict > 2)
+        return fail(DENSE_ERR_ARG, "strict must be 0 (fast), 1 (strict) or 2 (checked)");
     const int b = cfg->benchmark;
     const bool bench_ok = b == 0 || (b >= 1 && b <= 9) || b == DENSE_BENCH_IVC_PERIODIC ||
                           b == DENSE_BENCH_RT_REFLECT || b == DENSE_BENCH_RM_PERIODIC;
@@ -153,9 +184,21 @@ extern "C" int dense_stage_noalloc(const dense_config_t* cfg, int irk, double cu
     e = cudaGetLastError();
     if (e != cudaSuccess) return fail(DENSE_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));
     double dt = 0.0;
+    unsigned flags = 0;
     e = cudaMemcpyAsync(&dt, &ptr.sc->dt, sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(&flags, &ptr.sc->status, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return fail(DENSE_ERR_CUDA, std::string("sync: ") + cudaGetErrorString(e));
     *dt_inout = dt;
+    char hex[16];
+    snprintf(hex, sizeof hex, "0x%02x", flags);
+    if (flags & DENSE_FLAG_BOUNDS)
+        return fail(DENSE_ERR_ARG, std::string("device status flags ") + hex +
+                                       ": an array index fell outside its array (checked variant)");
+    if (flags & (DENSE_FLAG_NAN | DENSE_FLAG_NEG_RHO | DENSE_FLAG_ROE_IMAG))
+        return fail(DENSE_ERR_NUMERIC, std::string("device status flags ") + hex +
+                                           ": NaN (0x01), density <= 0 (0x02) or Roe sound speed "
+                                           "squared < 0 (0x08) in the stage");
     return DENSE_OK;
 }

@@ -49,14 +49,6 @@ WORKLOADS = {
     "rt": (13, 104, 0, 256, 1024, "Rayleigh-Taylor 256x1024 reflective sides, characteristic "
            "WENO-Z + GLF (104), CFL 0.5", "C3 RT 256x1024 CH"),
 }
-# DRAM bytes (read + write) of one launch of the xi sweep, from one ncu --set full capture of
-# that kernel on the same workload (dram__bytes_read.sum + dram__bytes_write.sum); the capture and
-# its command are summarised in the named profiles/ file.
-XI_TRAFFIC = {
-    "dmr": (59.297e6 + 3.388e6, "profiles/dmr_1920x480_adaweno_kernels.md"),
-    "rt": (17.368e6, "profiles/rt_256x1024_characteristic_kernels.md"),
-    "ivc": (2.373e6, "profiles/ivc_200x200_weno_js_kernels.md"),
-}
 METRIC = "FP64 WENO5-RK3 cell-updates/s"
 UNIT = "cell-updates/s"
 
@@ -154,9 +146,47 @@ def wl_t_start(args) -> float:
     return 0.1 if args.workload == "dmr" else 0.0
 
 
-def cpu_baseline(cfg_tuple, steps: int, state=None, t_start: float = 0.0, one_thread_steps: int = 0):
+def wl_config(args, wl) -> dict:
+    """The workload as both arms name it (the same dict in the GPU line and the reference arm's
+    line): grid, scheme, the nominal start time of the timed steps and how each arm treats L2."""
+    bench, split, recon, ni, nj, desc, _ = wl
+    return {"workload": desc, "benchmark": bench, "splitting": split, "recon": recon,
+            "ni": ni, "nj": nj, "cells": ni * nj, "t_start": wl_t_start(args),
+            "start": "the setup advanced by the solver under test to t_start (untimed), then the "
+                     "warm-up steps",
+            "l2": "GPU arm: flushed between timed steps (256 MiB write); CPU arm: not applicable"}
+
+
+def parity_check(cfg_tuple, state, gpu_cons) -> dict:
+    """Relative L-inf error per conserved field (density, momentum vector, energy; the largest
+    of the three) of one GPU step against one step of the CPU oracle's parity build from the same
+    state bits."""
+    from oracle import oracle as orc
+    bench, split, recon, ni, nj, desc, _ = cfg_tuple
+    cfg = orc.default_config(ni=ni, nj=nj, benchmark=bench, splitting=split, recon=recon, cfl=0.5,
+                             var_eps=5.0, var_xc=5.0, var_yc=5.0)
+    o = orc.OracleSolver(cfg)
+    cons, prim, t, step, dt = state
+    o.set_state(cons, prim)
+    o.set_time(t, step, dt)
+    o.steps(1)
+    ref = o.get_state()[0][4:-4, 4:-4]
+    got = gpu_cons[4:-4, 4:-4]
+    errs = []
+    for fields in ([0], [1, 2], [3]):
+        d = np.sqrt(sum((got[..., v] - ref[..., v]) ** 2 for v in fields))
+        n = np.sqrt(sum(ref[..., v] ** 2 for v in fields))
+        errs.append(float(d.max() / max(n.max(), 1e-300)))
+    return {"rel_linf": max(errs), "tolerance": 1e-12, "pass": max(errs) <= 1e-12,
+            "what": "one step of the timed kernels from the first timed step's start state against "
+                    "the CPU oracle (parity build) from the same bits"}
+
+
+def cpu_baseline(cfg_tuple, steps: int, state=None, t_start: float = 0.0, one_thread_steps: int = 0,
+                 warmup: int = 1):
     """Time the CPU oracle (OpenMP, all host threads) on the workload, from `state`
-    (cons, prim, t, step, dt) when given, else from the setup advanced to t_start."""
+    (cons, prim, t, step, dt) when given, else from the setup advanced to t_start and then
+    `warmup` steps."""
     from oracle import oracle as orc
     bench, split, recon, ni, nj, desc, _ = cfg_tuple
     cfg = orc.default_config(ni=ni, nj=nj, benchmark=bench, splitting=split, recon=recon, cfl=0.5,
@@ -168,7 +198,8 @@ def cpu_baseline(cfg_tuple, steps: int, state=None, t_start: float = 0.0, one_th
         o.set_time(t, step, dt)
     elif t_start > 0:
         o.steps(10 ** 7, t_end=t_start)
-    o.steps(1)  # warm-up
+    o.steps(max(1, warmup))  # warm-up
+    t_exact = o.scalars()["time"]
     t0 = time.perf_counter()
     o.steps(steps)
     el = time.perf_counter() - t0
@@ -176,8 +207,8 @@ def cpu_baseline(cfg_tuple, steps: int, state=None, t_start: float = 0.0, one_th
     threads = lib.oracle_threads()
     out = {"value": ni * nj * steps / el, "unit": UNIT, "cores": threads, "kind": "port",
            "sample": f"{desc}: {steps} step(s) of the C++ restatement of the reference "
-                     f"(OpenMP, {threads} threads, gcc -O2), after 1 warm-up step",
-           "seconds": el}
+                     f"(OpenMP, {threads} threads, gcc -O2), after {max(1, warmup)} warm-up step(s)",
+           "seconds": el, "t_start_exact": t_exact}
     if one_thread_steps > 0:  # the same code on one core, a shorter sample of the same state
         lib.oracle_set_threads(1)
         t0 = time.perf_counter()
@@ -194,16 +225,15 @@ def run_reference_arm(args, wl):
     if rank != 0:
         return
     steps = max(1, args.steps)
-    # each step a bounded sample: full-size oracle steps take ~0.05-1 s on 16 cores; the oracle
-    # first advances itself (untimed) to the start time of the GPU arm's timed steps
-    cb = cpu_baseline(wl, steps=min(steps, 10), t_start=wl_t_start(args))
-    bench, split, recon, ni, nj, desc, _ = wl
+    warmup = max(0, args.warmup)
+    # the oracle first advances itself (untimed) to the start time of the GPU arm's timed steps,
+    # then takes the same warm-up and timed steps as the GPU arm
+    cb = cpu_baseline(wl, steps=steps, t_start=wl_t_start(args), warmup=warmup)
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT,
-            "n_gpus": args.gpus, "steps": min(steps, 10), "warmup": 1,
-            "ms_per_step": 1e3 * cb["seconds"] / min(steps, 10), "higher_is_better": True,
+            "n_gpus": args.gpus, "steps": steps, "warmup": warmup,
+            "ms_per_step": 1e3 * cb["seconds"] / steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": desc, "benchmark": bench, "splitting": split, "recon": recon,
-                       "ni": ni, "nj": nj, "t_start": wl_t_start(args), "l2": "not applicable (CPU)"},
+            "config": wl_config(args, wl), "t_start_exact": cb["t_start_exact"],
             "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
             "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "the reference is Fortran; no Fortran compiler exists on this image or the GPU "
@@ -622,8 +652,9 @@ def main():
                 "frac": achieved * 1e12 / peak.value,
                 "peak_source": "measured live: dense_measure_fp64 FMA-throughput probe on this GPU "
                                "(MEASURED_PEAKS.json has no FP64 figure)",
-                "traffic": XI_TRAFFIC.get(args.workload, (None,))[0] if not (args.ni and args.nj) else None,
-                "traffic_source": XI_TRAFFIC.get(args.workload, (None, None))[1] if not (args.ni and args.nj) else None,
+                "traffic": None,
+                "traffic_note": "DRAM bytes need an ncu capture, which this run does not take; "
+                                "the committed ncu summaries of this kernel give them",
                 "whole_step": {"achieved_tflops": step_flops * value / cells / world / 1e12,
                                "frac": step_flops * value / cells / world / peak.value,
                                "flops_per_cell_update": step_flops / cells},
@@ -667,21 +698,25 @@ def main():
            "api": "dense_upload(cons from pinned host) + dense_steps(1) + dense_download(cons)"}
 
     cpu = None
+    parity = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_baseline(wl, args.cpu_steps, state=(snap_cons, snap_prim, snap_t, snap_step, snap_dt),
-                           one_thread_steps=max(1, args.cpu_steps // 10))
+        snap = (snap_cons, snap_prim, snap_t, snap_step, snap_dt)
+        cpu = cpu_baseline(wl, args.cpu_steps, state=snap, one_thread_steps=max(1, args.cpu_steps // 10))
         cpu.pop("seconds", None)
+        cpu.pop("t_start_exact", None)
+        # the timed kernels' first step from the same start state, against the oracle
+        s.upload(snap_cons, snap_prim, x, y)
+        s.current_time, s.current_step, s.dt = snap_t, snap_step, snap_dt
+        s.steps(1)
+        parity = parity_check(wl, snap, s.download(False))
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": desc, "benchmark": bench, "splitting": split, "recon": recon,
-                       "ni": ni, "nj": nj, "cells": cells, "strict": args.strict,
-                       "t_start": snap_t, "start": "state at t_start produced by this solver "
-                                                   "before the warm-up (0 = the initial setup)",
-                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                       "l2": "flushed between timed steps (256 MiB write)"},
+            "config": wl_config(args, wl), "t_start_exact": snap_t, "strict": args.strict,
+            "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
             "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
+            "parity_checked": parity,
             "clocks": clk.summary(), "status_flags": status, "wall_s_timed_region": wall}
     if rank == 0:
         print(json.dumps(line), flush=True)

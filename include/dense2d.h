@@ -394,8 +394,13 @@ const char* dense_adjoint_last_error(dense_adjoint_t* a);
    library, held by every GPU that loads it until exit: grids needing more than 2^20 doubles of
    fluxes (4 nj (ni+1) + 4 (nj+1) ni, about 360 x 360 cells) fail with DENSE_ERR_LIMIT. All calls
    share that array, so calls whose GPU work overlaps race and must be serialised. The first
-   call on a device resolves the array's device address; make it before any stream capture. The
-   call allocates nothing and calls no allocating routine. */
+   call on a device (and the first in a new context of it, after cudaDeviceReset) resolves the
+   array's device address; make it before any stream capture. The call allocates nothing and
+   calls no allocating routine. After the stage it reads the device status word: a NaN, a
+   density <= 0 or a Roe sound speed squared < 0 returns DENSE_ERR_NUMERIC, an index outside its
+   array in the checked variant (strict = 2) DENSE_ERR_ARG, with the flags in
+   dense_last_error(NULL); the pressure floor and an unknown reconstruction index are not
+   failures. */
 int dense_stage_noalloc(const dense_config_t* cfg, int irk, double current_time, double* cons,
                         double* prim, double* cons0, const double* xbot, const double* xtop,
                         const double* yleft, double* dt_inout, void* stream);

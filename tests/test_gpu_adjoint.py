@@ -150,3 +150,52 @@ def test_rejects_unsupported_configurations(dense, adjoint):
             setattr(cfg, k, v)
         with pytest.raises(dense.DenseError):
             adjoint.Adjoint(cfg)
+
+
+def test_gradients_at_the_adjoint_configuration_size(dense, adjoint):
+    """The adjoint configuration's grid (256 x 256 periodic vortex, LLF + WENO-JS5, CFL 0.4,
+    checkpoints every 20 steps) over 40 steps: gradients of 1/2 ||rho(T) - rho_target||^2 with
+    respect to (eps, xc, yc) and along a smooth direction of a seeded Gaussian density
+    perturbation (amplitude 1e-3) against Richardson-extrapolated central differences,
+    (4 FD(h/2) - FD(h)) / 3 at h = 1e-6, within 1e-6 relative. The extrapolation removes the
+    difference's own h^2 term, which the WENO weights of a field carrying 1e-3 noise make as
+    large as 1e-5 relative at h = 1e-6."""
+    ni = nj = 256
+    n, k, h = 40, 20, 1e-6
+    cfg = vortex_cfg(dense, 253, ni=ni, nj=nj, cfl=0.4, var_eps=5.0, var_xc=5.0, var_yc=5.0)
+    c = dense.init_general(cfg)[0]
+    with adjoint.Adjoint(c, checkpoint_every=k) as adj:
+        target = adj.forward(adjoint.vortex_state(c, 5.0, 5.0, 5.0), n)[0].clone()
+        gen = torch.Generator().manual_seed(2024)
+        drho0 = (1e-3 * torch.randn(nj, ni, generator=gen, dtype=torch.float64)).cuda()
+        theta0 = torch.tensor([5.0, 5.0, 5.0], dtype=torch.float64, device="cuda")
+
+        def loss_and_grads(th, dr):
+            th = th.detach().clone().requires_grad_(True)
+            dr = dr.detach().clone().requires_grad_(True)
+            uT = adjoint.AdjointStep.apply(adjoint.vortex_state(c, th[0], th[1], th[2], dr), adj, n)
+            loss = 0.5 * ((uT[0] - target) ** 2).sum()
+            g_th, g_dr = torch.autograd.grad(loss, [th, dr])
+            return float(loss.detach()), g_th, g_dr
+
+        _, g_th, g_dr = loss_and_grads(theta0, drho0)
+        am0 = adj.argmax().copy()
+        xs = (torch.arange(ni, dtype=torch.float64, device="cuda") + 0.5) * 10.0 / ni
+        Yg, Xg = torch.meshgrid(xs, xs, indexing="ij")
+        bump = torch.exp(-((Xg - 3.0) ** 2 + (Yg - 6.0) ** 2))
+        dirs = {"eps": ((1, 0, 0), None, float(g_th[0])), "xc": ((0, 1, 0), None, float(g_th[1])),
+                "yc": ((0, 0, 1), None, float(g_th[2])),
+                "bump": ((0, 0, 0), bump, float((g_dr * bump).sum()))}
+        for name, (dth, ddr, exact) in dirs.items():
+            est = {}
+            for hh in (h, h / 2):
+                vals = []
+                for sgn in (1.0, -1.0):
+                    th = theta0 + sgn * hh * torch.tensor(dth, dtype=torch.float64, device="cuda")
+                    dr = drho0 + (sgn * hh * ddr if ddr is not None else 0.0)
+                    vals.append(loss_and_grads(th, dr)[0])
+                    # the time step is not differentiable where the cells of its maxima switch
+                    assert np.array_equal(adj.argmax(), am0), name
+                est[hh] = (vals[0] - vals[1]) / (2 * hh)
+            rich = (4 * est[h / 2] - est[h]) / 3
+            assert abs(rich - exact) <= 1e-6 * abs(exact), (name, rich, exact, est)

@@ -173,3 +173,150 @@ def test_free_stream_preserved(dense):
             s.steps(3)
             g = s.download(False)
         np.testing.assert_allclose(interior(g), interior(cons), rtol=0, atol=1e-14)
+
+
+# ---- parity across tile seams and at the headline configurations' own sizes ------------------
+#
+# The AdaWENO (105) sweeps cover 251 interfaces per xi tile and 123 per eta tile, the
+# characteristic WENO-Z (104) eta sweep 64, the component-wise sweeps 32 x 4 / 32 x 8. The grids
+# below give every sweep at least three tiles along its direction, so every seam between tiles
+# (halo cells staged by both neighbours, characteristic items queued on either side) is compared
+# with the oracle.
+
+def random_state(c, seed):
+    """Seeded positive state, rough at the grid scale: most AdaWENO (interface, sign) pairs take
+    the characteristic branch, the rest the smooth one, both on every tile seam."""
+    rng = np.random.default_rng(seed)
+    shape = (c.ni + 8, c.nj + 8)
+    rho = rng.uniform(0.5, 2.0, shape)
+    u, v = rng.uniform(-1.0, 1.0, shape), rng.uniform(-1.0, 1.0, shape)
+    p = rng.uniform(0.5, 2.0, shape)
+    cons = np.zeros(shape + (4,), order="F")
+    cons[..., 0] = rho
+    cons[..., 1] = rho * u
+    cons[..., 2] = rho * v
+    cons[..., 3] = p / (c.gamma - 1.0) + 0.5 * rho * (u * u + v * v)
+    return cons
+
+
+def step_from(dense, orc, cfg, cons, prim, x, y, t=0.0, step=0, dt=None, nsteps=1):
+    """nsteps from the same state bits on the GPU (variant cfg.strict) and in the oracle."""
+    o = orc.OracleSolver(cfg)
+    o.set_state(cons, prim)
+    o.set_time(t, step, cfg.dt if dt is None else dt)
+    o.steps(nsteps)
+    o.get_primary()
+    with dense.Solver(cfg) as s:
+        s.upload(cons, prim, x, y)
+        s.current_time, s.current_step = t, step
+        if dt is not None:
+            s.dt = dt
+        s.steps(nsteps)
+        g_cons, g_prim = s.download()
+        flags = s.status()
+        g_t, g_dt = s.current_time, s.dt
+    o_cons, o_prim = o.get_state()
+    return g_cons, g_prim, o_cons, o_prim, g_t, g_dt, o.scalars(), flags
+
+
+@pytest.mark.parametrize("split,recon,ni,nj", [
+    (105, 0, 760, 380),     # AdaWENO: 4 xi tiles of 251 interfaces, 4 eta tiles of 123
+    (104, 0, 160, 200),     # characteristic WENO-Z: 4 eta tiles of 64
+    (101, 253, 136, 40),    # component-wise: 5 xi tiles of 32, 5 eta tiles of 8
+])
+def test_random_state_across_tile_seams(dense, orc, split, recon, ni, nj):
+    for strict in (1, 0):
+        c, _, _, x, y = dense.init_general(make_cfg(dense, 11, split, recon, ni, nj, strict=strict,
+                                                    cfl=0.4))
+        cons = random_state(c, seed=7 * ni + nj + split)
+        g, gp, o, op, t, dt, sc, flags = step_from(dense, orc, c, cons, None, x, y)
+        if strict:
+            np.testing.assert_array_equal(interior(g), interior(o))
+            np.testing.assert_array_equal(interior(gp)[..., :5], interior(op)[..., :5])
+            assert dt == sc["dt"]
+        else:
+            assert rel_linf(interior(g), interior(o)) <= TOL_STEP
+
+
+@pytest.mark.parametrize("bench,ni,nj", [(5, 1200, 300), (11, 760, 380)])
+def test_adaweno_multi_tile_setups_strict_three_steps(dense, orc, bench, ni, nj):
+    cfg = make_cfg(dense, bench, 105, 0, ni, nj, strict=1)
+    g, gp, o, op, dt, t, sc, flags = run_pair(dense, orc, cfg, 3)
+    np.testing.assert_array_equal(interior(g), interior(o))
+    np.testing.assert_array_equal(interior(gp)[..., :5], interior(op)[..., :5])
+    assert dt == sc["dt"] and t == sc["time"]
+
+
+@pytest.mark.parametrize("strict", [1, 0])
+def test_double_mach_1920x480_first_step(dense, orc, strict):
+    """The headline configuration (double Mach reflection, 1920 x 480, AdaWENO, CFL 0.5) at its
+    own size: one step from the setup."""
+    cfg = make_cfg(dense, 5, 105, 0, 1920, 480, strict=strict)
+    g, gp, o, op, dt, t, sc, flags = run_pair(dense, orc, cfg, 1)
+    if strict:
+        np.testing.assert_array_equal(interior(g), interior(o))
+        assert dt == sc["dt"]
+    else:
+        assert rel_linf(interior(g), interior(o)) <= TOL_STEP
+        assert abs(dt - sc["dt"]) <= 1e-13 * sc["dt"]
+
+
+@pytest.fixture(scope="module")
+def dmr_developed(dense):
+    """The double Mach reflection at 1920 x 480 advanced by the fast kernels to t >= 0.1 (the
+    state the throughput is measured from): reflected shocks, the Mach stem and the slip line
+    are resolved, and AdaWENO takes its characteristic branch along all of them."""
+    cfg = make_cfg(dense, 5, 105, 0, 1920, 480)
+    c, cons, prim, x, y = dense.init_general(cfg)
+    with dense.Solver(c) as s:
+        s.upload(cons, prim, x, y)
+        s.steps(100000, t_end=0.1)
+        g_cons, g_prim = s.download()
+        assert s.status() & 0x03 == 0
+        return c, g_cons, g_prim, x, y, s.current_time, s.current_step, s.dt
+
+
+@pytest.mark.parametrize("strict", [1, 0])
+def test_double_mach_1920x480_developed_state(dense, orc, dmr_developed, strict):
+    """One step from the developed state on both sides. Every AdaWENO switch theta > delta is
+    taken on a realistic distribution of theta near delta; the fast kernels' divide-free form of
+    the test must pick the same branch wherever the oracle does (a flipped branch moves a flux by
+    far more than 1e-12)."""
+    c, cons, prim, x, y, t, step, dt = dmr_developed
+    cfg = c.copy()
+    cfg.strict = strict
+    g, gp, o, op, gt, gdt, sc, flags = step_from(dense, orc, cfg, cons, prim, x, y, t, step, dt)
+    assert t > 0.1 - 1e-3
+    if strict:
+        np.testing.assert_array_equal(interior(g), interior(o))
+        assert gdt == sc["dt"] and gt == sc["time"]
+    else:
+        assert rel_linf(interior(g), interior(o)) <= TOL_STEP
+        assert flags & 0x03 == 0
+
+
+@pytest.mark.parametrize("strict", [1, 0])
+def test_rayleigh_taylor_256x1024_first_step(dense, orc, strict):
+    """The Rayleigh-Taylor configuration at its own size (reflective side walls, characteristic
+    WENO-Z + GLF, body force): one step from the setup."""
+    cfg = make_cfg(dense, 13, 104, 0, 256, 1024, strict=strict)
+    g, gp, o, op, dt, t, sc, flags = run_pair(dense, orc, cfg, 1)
+    if strict:
+        np.testing.assert_array_equal(interior(g), interior(o))
+    else:
+        assert rel_linf(interior(g), interior(o)) <= TOL_STEP
+
+
+def test_vortex_200x200_100_steps(dense, orc):
+    """The isentropic vortex configuration at its own size (200 x 200 periodic, LLF + WENO-JS5,
+    CFL 0.5): relative L1 of density after 100 steps within 1e-10 (fast kernels), and the strict
+    kernels bit-identical to the oracle after the same 100 steps."""
+    cfg = make_cfg(dense, 11, 101, 253, 200, 200)
+    g, gp, o, op, dt, t, sc, flags = run_pair(dense, orc, cfg, 100)
+    rg, ro = interior(g)[..., 0], interior(o)[..., 0]
+    assert np.abs(rg - ro).sum() / np.abs(ro).sum() <= TOL_L1_100
+    assert abs(t - sc["time"]) <= 1e-12 * sc["time"]
+    cfg = make_cfg(dense, 11, 101, 253, 200, 200, strict=1)
+    g, gp, o, op, dt, t, sc, flags = run_pair(dense, orc, cfg, 100)
+    np.testing.assert_array_equal(interior(g), interior(o))
+    assert t == sc["time"]

@@ -69,6 +69,53 @@ def test_noalloc_stage_matches_handle_stage(dense, bench, split, recon, ni, nj):
             np.testing.assert_allclose(interior(got_prim), interior(ref_prim)[..., :5], rtol=1e-12, atol=1e-14)
 
 
+def _stage(lib, c, irk, cons_d, prim_d, cons0_d, xbot, xtop, yleft, dt, stream):
+    vp = ctypes.c_void_p
+    return lib.dense_stage_noalloc(ctypes.byref(c), irk, 0.0, vp(cons_d.data_ptr()),
+                                   vp(prim_d.data_ptr()), vp(cons0_d.data_ptr()),
+                                   vp(xbot.data_ptr()), vp(xtop.data_ptr()), vp(yleft.data_ptr()),
+                                   ctypes.byref(dt), vp(stream))
+
+
+def test_noalloc_reports_a_nan_in_the_state(dense):
+    """The device status word is read back after the stage: a NaN planted in the caller's state
+    returns DENSE_ERR_NUMERIC with the flag in the error text, and the next clean call succeeds
+    (the word is cleared at every call)."""
+    torch = pytest.importorskip("torch")
+    lib = dense.load_library()
+    ni, nj = 40, 36
+    cfg = dense.config_default(ni=ni, nj=nj, benchmark=11, splitting=101, recon=253, cfl=0.5)
+    c, cons, prim, x, y = dense.init_general(cfg)
+    pitch = (ni + 9) & ~1
+    bad = cons.copy()
+    bad[20, 18, 0] = np.nan
+    xbot = torch.from_numpy(np.ascontiguousarray(x[:, 0])).cuda()
+    xtop = torch.from_numpy(np.ascontiguousarray(x[:, nj - 1])).cuda()
+    yleft = torch.from_numpy(np.ascontiguousarray(y[0, :])).cuda()
+    stream = torch.cuda.current_stream().cuda_stream
+    for state, expect in ((bad, 5), (cons, 0)):  # DENSE_ERR_NUMERIC, then DENSE_OK
+        cons_d = to_device(torch, state, 4, pitch)
+        prim_d = to_device(torch, prim, 5, pitch)
+        cons0_d = torch.zeros_like(cons_d)
+        dt = ctypes.c_double(c.dt)
+        rc = _stage(lib, c, 1, cons_d, prim_d, cons0_d, xbot, xtop, yleft, dt, stream)
+        assert rc == expect
+        if expect:
+            assert b"0x01" in lib.dense_last_error(None)
+
+
+def test_noalloc_rejects_an_unknown_kernel_variant(dense):
+    lib = dense.load_library()
+    cfg = dense.config_default(ni=40, nj=36, benchmark=11, splitting=101, recon=253,
+                               dx=0.25, dy=0.25, strict=3)
+    dt = ctypes.c_double(0.0)
+    dummy = ctypes.c_void_p(16)  # rejected before any device access
+    rc = lib.dense_stage_noalloc(ctypes.byref(cfg), 1, 0.0, dummy, dummy, dummy, None, None,
+                                 None, ctypes.byref(dt), None)
+    assert rc == 1  # DENSE_ERR_ARG
+    assert b"strict" in lib.dense_last_error(None)
+
+
 def test_noalloc_rejects_grids_beyond_the_scratch(dense):
     lib = dense.load_library()
     cfg = dense.config_default(ni=400, nj=400, benchmark=11, splitting=101, recon=253,
@@ -80,3 +127,4 @@ def test_noalloc_rejects_grids_beyond_the_scratch(dense):
     rc = lib.dense_stage_noalloc(ctypes.byref(cfg), 1, 0.0, dummy, dummy, dummy, None, None,
                                  None, ctypes.byref(dt), None)
     assert rc == 10  # DENSE_ERR_LIMIT
+    assert b"fixed scratch" in lib.dense_last_error(None)
