@@ -55,9 +55,11 @@ struct Params {
     int P;           // row pitch of the padded arrays, in doubles
     long long plane; // doubles per variable plane = NJp * P
     double gamma, cfl, delta, dx, dy, dt_const;
-    // AdaWENO switch theta > delta written without a divide (fast kernels):
-    // theta_k1 * D > theta_k2 * (N - D) with theta_k1 = sqrt(1-delta), theta_k2 = sqrt(delta)
-    double theta_k1, theta_k2;
+    // AdaWENO switch theta > delta written without a divide (fast kernels): with
+    // theta = 1/(1 + (sum alpha - 1)^2) and sum alpha - 1 = tau^2 Q / D >= 0 (common denominator D),
+    // theta > delta <=> D > theta_kk tau^2 Q, theta_kk = sqrt(delta/(1-delta)) for 0 <= delta < 1;
+    // 0 for delta < 0 (always smooth), +inf for delta >= 1 (never smooth)
+    double theta_kk;
     int if_const_dt, bodyforce, benchmark, splitting, recon;
     int count_branches;  // accumulate Scalars::branch_count in the AdaWENO sweeps
     // Tape of the component-wise LLF sweeps for the discrete adjoint (flux_tape launches only):

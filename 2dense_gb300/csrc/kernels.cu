@@ -251,6 +251,16 @@ __device__ __forceinline__ void stencil_from_weights(double w0, double w1, doubl
     W[4] = w2 * a322;
 }
 
+// The same 5-point stencil from u0 = w0/c0 and u2 = w2/c2 of WENO-Z weights that sum to one
+// (w1 = 1 - w0 - w2): the linear weights c_k and the candidates' coefficients fold into constants.
+__device__ __forceinline__ void stencil_from_u(double u0, double u2, double W[5]) {
+    W[0] = (c30 * a300) * u0;
+    W[1] = fma(c30 * (a301 - a310), u0, fma(-c32 * a310, u2, a310));
+    W[2] = fma(c30 * (a302 - a311), u0, fma(c32 * (a320 - a311), u2, a311));
+    W[3] = fma(-c30 * a312, u0, fma(c32 * (a321 - a312), u2, a312));
+    W[4] = (c32 * a322) * u2;
+}
+
 // Gradient of the WENO reconstruction with respect to its stencil, g[m] = dW/dlf[m], for the
 // discrete adjoint's tape. W = sum_k w_k q_k with w_k = a_k / sum(a): dW/dq_k = w_k and
 // dW/da_k = (q_k - W)/sum(a); a_k depends on lf through beta_k (JS: a_k = c_k/d_k^2, so
@@ -817,16 +827,19 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
     }
     __syncthreads();
 
-    // phase 1b (AdaWENO, fast): the surrogates' second differences D2, the squared-difference
-    // term ss + 13/12 D2^2 of the smoothness indicators, and first differences, once per cell
-    // and sign; an interface's indicators then need only its first-order terms. Signs read their
-    // stencils in opposite directions: "+" cells k-1, k, k+1; "-" cells k+1, k, k-1.
-    double* const sD2 = sR + 2 * NCELL;   // [2][NCELL]
-    double* const sA2 = sR + 4 * NCELL;   // [2][NCELL]
+    // phase 1b (AdaWENO, fast): per cell and sign, half the surrogate's second difference
+    // A/2 = (sur(k-1) + sur(k+1))/2 - sur(k) (symmetric, so the same for both stencil
+    // directions), the squared-difference term ss + 13/12 A^2 = ss + 13/3 (A/2)^2 of the
+    // smoothness indicators, and the first difference sur(k+1) - sur(k); an interface's
+    // indicators then need only their first-order terms. Halving A lets the interfaces form
+    // B_k/2 with an add and square it in the indicator's FMA, with no 1/4 factor.
+    double* const sD2 = sR + 2 * NCELL;   // [2][NCELL]: A/2
+    double* const sA2 = sR + 4 * NCELL;   // [2][NCELL]: ss + 13/12 A^2
     double* const sDl = sR + 6 * NCELL;   // [2][NCELL]: sur(k+1) - sur(k)
     if constexpr (kStageInd) {
         constexpr int KN = L::KW + 5;                    // cells along the sweep
         constexpr int KL = DIR == 0 ? TY : TX;           // lines
+        constexpr double k133 = 13.0 / 3.0;
         for (int e = tid; e < KL * (KN - 2); e += NT) {
             const int line = e / (KN - 2), k = 1 + e % (KN - 2);
             const int o = DIR == 0 ? at(line, k) : at(k, line);
@@ -835,9 +848,9 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
 #pragma unroll
             for (int sg = 0; sg < 2; ++sg) {
                 const double* su = sR + sg * NCELL;
-                const double a = sg == 0 ? fma(-2.0, su[o], su[om]) + su[op] : fma(-2.0, su[o], su[op]) + su[om];
-                sD2[sg * NCELL + o] = a;
-                sA2[sg * NCELL + o] = fma(k1312 * a, a, kSS);
+                const double ah = fma(0.5, su[om] + su[op], -su[o]);
+                sD2[sg * NCELL + o] = ah;
+                sA2[sg * NCELL + o] = fma(k133 * ah, ah, kSS);
                 sDl[sg * NCELL + o] = su[op] - su[o];
             }
         }
@@ -944,24 +957,32 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
                 const double* D2 = sD2 + s * NCELL;
                 const double* A2 = sA2 + s * NCELL;
                 const double* Dl = sDl + s * NCELL;
-                const double A0 = D2[atk(c0, tx, ty)], A2v = D2[atk(c2, tx, ty)];
+                const double A0h = D2[atk(c0, tx, ty)], A2h = D2[atk(c2, tx, ty)];
                 const double dl1 = Dl[atk(s == 0 ? t + 1 : t + 3, tx, ty)];
                 const double dl2 = Dl[atk(t + 2, tx, ty)];
-                // B0 = lf0 - 4 lf1 + 3 lf2, B1 = lf1 - lf3, B2 = 3 lf2 - 4 lf3 + lf4 from A and the
-                // first differences (signs mirrored for "-")
-                const double B0 = s == 0 ? fma(2.0, dl1, A0) : fma(-2.0, dl1, A0);
+                // B0 = lf0 - 4 lf1 + 3 lf2 = A0 +- 2 dl1, B1 = lf1 - lf3 = -+(dl1 + dl2),
+                // B2 = 3 lf2 - 4 lf3 + lf4 = A2 -+ 2 dl2 (upper signs "+", lower "-"), halved
+                const double B0h = s == 0 ? A0h + dl1 : A0h - dl1;
                 const double B1 = dl1 + dl2;
-                const double B2 = s == 0 ? fma(-2.0, dl2, A2v) : fma(2.0, dl2, A2v);
-                const double d0 = fma(0.25 * B0, B0, A2[atk(c0, tx, ty)]);
+                const double B2h = s == 0 ? A2h - dl2 : A2h + dl2;
+                const double d0 = fma(B0h, B0h, A2[atk(c0, tx, ty)]);
                 const double d1 = fma(0.25 * B1, B1, A2[atk(cm + (s == 0 ? 0 : 1), tx, ty)]);
-                const double d2 = fma(0.25 * B2, B2, A2[atk(c2, tx, ty)]);
-                double n0, n1, n2, N, D;
-                weno_num_from_d<true>(d0, d1, d2, fabs(d2 - d0), n0, n1, n2, N, D);
-                smooth[s] = p.theta_k1 * D > p.theta_k2 * (N - D);
-                const double r = rcp_nr(N);
-                wsur[s][0] = n0 * r; wsur[s][1] = n1 * r; wsur[s][2] = n2 * r;
-                if (p.theta) {  // theta = 1/(1 + (sum alpha - 1)^2), sum alpha = N/D
-                    const double sm1 = N / D - 1.0;
+                const double d2 = fma(B2h, B2h, A2[atk(c2, tx, ty)]);
+                // WENO-Z over the common denominator D = prod d_k^2, P_k = D/d_k^2, T = tau^2:
+                // alpha_k D = c_k (D + T P_k); since sum c_k = 1, (sum alpha - 1) D = T Q with
+                // Q = sum c_k P_k, and theta > delta <=> D > theta_kk T Q
+                const double e0 = d0 * d0, e1 = d1 * d1, e2 = d2 * d2;
+                const double P0 = e1 * e2, P1 = e0 * e2, P2 = e0 * e1;
+                const double D = e0 * P0;
+                const double dd = d2 - d0, T = dd * dd;
+                const double Q = fma(c31, P1, c30 * P0) + c32 * P2;
+                smooth[s] = fma(-p.theta_kk * T, Q, D) > 0.0;
+                const double r = rcp_nr(fma(T, Q, D));
+                // u_k = alpha_k / (c_k sum alpha); the weights are w_k = c_k u_k, w1 = 1 - w0 - w2
+                wsur[s][0] = fma(T, P0, D) * r;
+                wsur[s][2] = fma(T, P2, D) * r;
+                if (p.theta) {  // theta = 1/(1 + (sum alpha - 1)^2), sum alpha - 1 = T Q / D
+                    const double sm1 = T * Q / D;
                     theta_out(s, 1.0 / (1.0 + sm1 * sm1));
                 }
             }
@@ -1005,7 +1026,7 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
             {
                 double F[5][4], h[4], W[5];
                 stencil(DIR == 0 && tx >= L::KW ? L::KW - 1 : tx, DIR == 1 && ty >= L::KW ? L::KW - 1 : ty, s, F);
-                stencil_from_weights(wsur[s][0], wsur[s][1], wsur[s][2], W);
+                stencil_from_u(wsur[s][0], wsur[s][2], W);
 #pragma unroll
                 for (int c = 0; c < 4; ++c)
                     h[c] = fma(W[4], F[4][c], fma(W[3], F[3][c], fma(W[2], F[2][c], fma(W[1], F[1][c], W[0] * F[0][c]))));
