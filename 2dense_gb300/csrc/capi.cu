@@ -94,6 +94,7 @@ void fill_params(dense_handle* h) {
     // the body force is nonzero only where boundary_rt_general refreshes it (:154-155)
     p.bodyforce = c.if_bodyforce && (c.benchmark == DENSE_BENCH_RT || c.benchmark == DENSE_BENCH_RT_REFLECT);
     p.benchmark = c.benchmark; p.splitting = c.splitting; p.recon = c.recon;
+    p.periodic_ghosts = dense::periodic_ghosts(c.benchmark, c.ni, c.nj);
     p.count_branches = h->count_branches;
     p.tape = nullptr;
     p.theta = c.if_save_theta && c.splitting == DENSE_SPLIT_SC ? h->theta : nullptr;
@@ -144,9 +145,11 @@ int stage_launches(dense_handle* h) {
 
 // The stage as graph nodes: the two sweeps read the same stage input and write separate face
 // fluxes, so the eta sweep is a branch beside the xi sweep; its blocks fill the SMs the xi
-// sweep's last wave leaves idle. The update joins both.
+// sweep's last wave leaves idle. The update joins both. On grids periodic in x and y the
+// previous stage's update has written the ghost layers already, so stages 2 and 3 launch no
+// boundary fill (stage 1 keeps it: the step may start from an uploaded state).
 cudaError_t capture_stage(dense_handle* h, int irk) {
-    h->kt->bc(h->prm, h->stream);
+    if (irk == 1 || !h->prm.periodic_ghosts) h->kt->bc(h->prm, h->stream);
     cudaError_t e = cudaEventRecord(h->ev_fork, h->stream);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(h->side, h->ev_fork, 0);
     if (e != cudaSuccess) return e;
@@ -186,7 +189,7 @@ int build_step_graph(dense_handle* h) {
     e = cudaGraphInstantiate(&h->step_graph, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return seterr(h, DENSE_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
-    h->graph_nodes = 2 + 3 * stage_launches(h);
+    h->graph_nodes = 2 + 3 * stage_launches(h) - (h->prm.periodic_ghosts ? 2 : 0);
     return DENSE_OK;
 }
 

@@ -61,6 +61,10 @@ struct Params {
     // 0 for delta < 0 (always smooth), +inf for delta >= 1 (never smooth)
     double theta_kk;
     int if_const_dt, bodyforce, benchmark, splitting, recon;
+    // periodic in x and y with at least 2 kB cells each way (benchmarks 11 and 14): the update
+    // also writes each boundary cell's periodic images into the ghost layers, which is the whole
+    // of the next stage's boundary fill (set by periodic_ghosts() below)
+    int periodic_ghosts;
     int count_branches;  // accumulate Scalars::branch_count in the AdaWENO sweeps
     // Tape of the component-wise LLF sweeps for the discrete adjoint (flux_tape launches only):
     // per direction tape_planes(recon) planes of the direction's face array (xi [nj][ni+1], eta
@@ -71,6 +75,12 @@ struct Params {
     // (if_save_theta): xi [2][nj][ni+1], then eta [2][nj+1][ni] (sign 0 = "+"); else null
     double* theta;
 };
+
+// Whether the update of a configuration writes the periodic ghost images (Params::periodic_ghosts).
+inline int periodic_ghosts(int benchmark, int ni, int nj) {
+    return (benchmark == DENSE_BENCH_IVC_PERIODIC || benchmark == DENSE_BENCH_RM_PERIODIC) &&
+           ni >= 2 * kB && nj >= 2 * kB;
+}
 
 // One arithmetic variant of the kernels (fast or strict), as a table of launchers.
 struct KernelTable {

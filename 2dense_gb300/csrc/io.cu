@@ -10,6 +10,7 @@
 // one is written.
 #include <cuda_runtime.h>
 
+#include <chrono>
 #include <cinttypes>
 #include <cmath>
 #include <cstdio>
@@ -335,12 +336,18 @@ int dense_run(dense_handle_t* h, const char* dir, const char* namelist_path, int
         h->launches += 1;
     };
     bounds();
+    // cpu_t of general_main.f90:22-31: wall time of the step loop, saves excluded
+    double cpu_t = 0.0;
+    long long last_step = 0;
     for (;;) {
+        const auto t0 = std::chrono::steady_clock::now();
         rc = dense_steps_async(h, kChunk, h->cfg.total_time, h->cfg.total_step);
         if (rc) break;
         Scalars sc{};
         ce = cudaMemcpyAsync(&sc, h->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, h->stream);
         if (ce == cudaSuccess) ce = cudaStreamSynchronize(h->stream);
+        cpu_t += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        last_step = sc.step;
         if (ce != cudaSuccess) { rc = ioerr(h, DENSE_ERR_CUDA, std::string("dense_run: ") + cudaGetErrorString(ce)); break; }
         if (sc.hold) {
             // general_main.f90:40-54: the binary checkpoint, then get_primary and the Tecplot
@@ -413,6 +420,14 @@ int dense_run(dense_handle_t* h, const char* dir, const char* namelist_path, int
     cudaFree(snap);
     if (rc) return rc;
     if (saves_out) *saves_out = saves;
+    // general_main.f90:20,56-58: the timing log, appended
+    if (FILE* f = fopen((d.empty() ? std::string("CpuTime.dat") : d + "/CpuTime.dat").c_str(), "a")) {
+        fprintf(f, " Total time and steps:%25.17g%12lld\n", cpu_t, last_step);
+        fprintf(f, " averaged time:%25.17g\n", cpu_t / (double)last_step);
+        fclose(f);
+    } else {
+        return ioerr(h, DENSE_ERR_IO, "cannot open CpuTime.dat in " + d);
+    }
     // general_main.f90:59-60: get_primary and the final Tecplot file
     HostState s;
     rc = snapshot_now(h, s);

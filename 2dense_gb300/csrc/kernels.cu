@@ -155,19 +155,22 @@ __device__ __forceinline__ double upwind5(const double lf[5]) {
 
 constexpr double k1312 = 13.0 / 12.0;
 
-// d_k = ss + beta_k and tau = |beta_2 - beta_0| with beta_k = 13/12 a_k^2 + 1/4 b_k^2.
+// d_k = ss + beta_k and tau = |beta_2 - beta_0| with beta_k = 13/12 a_k^2 + 1/4 b_k^2. For the
+// outer substencils the halves a_k/2, b_k/2 are formed directly (b_0 = a_0 + 2 (lf2 - lf1),
+// b_2 = a_2 + 2 (lf2 - lf3)), so that 13/12 a^2 + 1/4 b^2 = 13/3 (a/2)^2 + (b/2)^2 needs no 1/4.
 __device__ __forceinline__ void betas_fast(const double lf[5], double& d0, double& d1, double& d2,
                                            double& tau) {
-    const double a0 = fma(-2.0, lf[1], lf[0]) + lf[2];
-    const double b0 = fma(3.0, lf[2], fma(-4.0, lf[1], lf[0]));
+    constexpr double k133 = 13.0 / 3.0;
+    const double a0h = fma(0.5, lf[0] + lf[2], -lf[1]);
+    const double b0h = a0h + (lf[2] - lf[1]);
     const double a1 = fma(-2.0, lf[2], lf[1]) + lf[3];
     const double b1 = lf[1] - lf[3];
-    const double a2 = fma(-2.0, lf[3], lf[2]) + lf[4];
-    const double b2 = fma(3.0, lf[2], fma(-4.0, lf[3], lf[4]));
+    const double a2h = fma(0.5, lf[2] + lf[4], -lf[3]);
+    const double b2h = a2h + (lf[2] - lf[3]);
     // d_k = ss + beta_k with ss added inside the last FMA; tau = |beta_2 - beta_0| = |d_2 - d_0|
-    d0 = fma(k1312 * a0, a0, fma(0.25 * b0, b0, kSS));
+    d0 = fma(k133 * a0h, a0h, fma(b0h, b0h, kSS));
     d1 = fma(k1312 * a1, a1, fma(0.25 * b1, b1, kSS));
-    d2 = fma(k1312 * a2, a2, fma(0.25 * b2, b2, kSS));
+    d2 = fma(k133 * a2h, a2h, fma(b2h, b2h, kSS));
     tau = fabs(d2 - d0);
 }
 
@@ -192,13 +195,6 @@ __device__ __forceinline__ void weno_num_from_d(double d0, double d1, double d2,
     // differently in different kernels, and the plain and taping sweeps must agree bit for bit
     N = __dadd_rn(__dadd_rn(n0, n1), n2);
 }
-template <bool Z>
-__device__ __forceinline__ void weno_num_fast(const double lf[5], double& n0, double& n1, double& n2,
-                                              double& N, double& D) {
-    double d0, d1, d2, tau;
-    betas_fast(lf, d0, d1, d2, tau);
-    weno_num_from_d<Z>(d0, d1, d2, tau, n0, n1, n2, N, D);
-}
 
 __device__ __forceinline__ void candidates_fast(const double lf[5], double& q0, double& q1, double& q2) {
     q0 = fma(a302, lf[2], fma(a301, lf[1], a300 * lf[0]));
@@ -206,11 +202,38 @@ __device__ __forceinline__ void candidates_fast(const double lf[5], double& q0, 
     q2 = fma(a322, lf[4], fma(a321, lf[3], a320 * lf[2]));
 }
 
+// The candidates scaled by the linear weights, c_k q_k (the constants folded together).
+__device__ __forceinline__ void candidates_c(const double lf[5], double& q0, double& q1, double& q2) {
+    q0 = fma(c30 * a302, lf[2], fma(c30 * a301, lf[1], (c30 * a300) * lf[0]));
+    q1 = fma(c31 * a312, lf[3], fma(c31 * a311, lf[2], (c31 * a310) * lf[1]));
+    q2 = fma(c32 * a322, lf[4], fma(c32 * a321, lf[3], (c32 * a320) * lf[2]));
+}
+
+// WENO reconstruction from d_k = ss + beta_k: h = sum_k v_k (c_k q_k) / sum_k c_k v_k with
+// v_k = alpha_k D / c_k, i.e. P_k (JS) or D + tau^2 P_k (Z), over the common denominator D.
+// Every operation is an explicit FMA or a product feeding one, so no kernel contracts it
+// differently from another (the plain and taping sweeps agree bit for bit); the result is a
+// rounded product, which the caller's sum of the two signs must not fuse with.
+template <bool Z>
+__device__ __forceinline__ double weno_from_d(const double lf[5], double d0, double d1, double d2) {
+    double q0, q1, q2;
+    candidates_c(lf, q0, q1, q2);
+    const double e0 = d0 * d0, e1 = d1 * d1, e2 = d2 * d2;
+    double v0 = e1 * e2, v1 = e0 * e2, v2 = e0 * e1;
+    if (Z) {
+        const double D = e0 * v0, dd = d2 - d0, T = dd * dd;
+        v0 = fma(T, v0, D);
+        v1 = fma(T, v1, D);
+        v2 = fma(T, v2, D);
+    }
+    const double N = fma(c32, v2, fma(c31, v1, c30 * v0));
+    return __dmul_rn(fma(v2, q2, fma(v1, q1, v0 * q0)), rcp_nr(N));
+}
+
 template <bool Z> __device__ __forceinline__ double weno_fast(const double lf[5]) {
-    double q0, q1, q2, n0, n1, n2, N, D;
-    candidates_fast(lf, q0, q1, q2);
-    weno_num_fast<Z>(lf, n0, n1, n2, N, D);
-    return fma(n2, q2, fma(n1, q1, n0 * q0)) * rcp_nr(N);
+    double d0, d1, d2, tau;
+    betas_fast(lf, d0, d1, d2, tau);
+    return weno_from_d<Z>(lf, d0, d1, d2);
 }
 
 // Second-difference term of a smoothness indicator, ss + 13/12 A^2 with A = lm - 2 lc + lr: it
@@ -231,15 +254,6 @@ __device__ __forceinline__ void betas_staged(const double lf[5], double s0, doub
     d0 = fma(0.25 * b0, b0, s0);
     d1 = fma(0.25 * b1, b1, s1);
     d2 = fma(0.25 * b2, b2, s2);
-}
-// WENO reconstruction from d_k = ss + beta_k
-template <bool Z>
-__device__ __forceinline__ double weno_from_d(const double lf[5], double d0, double d1, double d2) {
-    double q0, q1, q2, n0, n1, n2, N, D;
-    candidates_fast(lf, q0, q1, q2);
-    weno_num_from_d<Z>(d0, d1, d2, fabs(d2 - d0), n0, n1, n2, N, D);
-    // a rounded product: the caller adds the two signs' values, which must not fuse with it
-    return __dmul_rn(fma(n2, q2, fma(n1, q1, n0 * q0)), rcp_nr(N));
 }
 
 // The five coefficients of h = sum_k w_k q_k as one 5-point stencil: W[m] lf[m].
@@ -267,7 +281,7 @@ __device__ __forceinline__ void stencil_from_u(double u0, double u2, double W[5]
 // da_k/dbeta_k = -2 a_k/d_k; Z: a_k = c_k (1 + tau^2/d_k^2), so da_k/dbeta_k = -2 c_k tau^2/d_k^3
 // and da_k/dtau = 2 c_k tau/d_k^2, tau = |beta_2 - beta_0|; d_k = ss + beta_k), and beta_k =
 // 13/12 A_k^2 + 1/4 B_k^2 on the second differences A_k and the first-order combinations B_k.
-// Written over the common denominators of weno_num_fast (n_k = a_k D, N = sum(a) D, D = prod
+// Written over the common denominators of weno_num_from_d (n_k = a_k D, N = sum(a) D, D = prod
 // d_k^2, P_k = D/d_k^2), with the quantities W itself needs computed by the same expressions.
 // The caller passes d_k = ss + beta_k as its own reconstruction computed them, so that the two
 // share every common term.
@@ -1017,28 +1031,49 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
                 if (any_c) atomicAdd(&p.sc->branch_count[4 * DIR + 3], 1ull);
             }
         }
-#pragma unroll
-        for (int s = 0; s < 2; ++s) {
 #if FAST
-            // the smooth result is computed by every lane (uniform, no divergence) and kept
-            // only where the smooth branch is taken; the lanes past a fitted xi tile's last
-            // interface read that interface's stencil
-            {
-                double F[5][4], h[4], W[5];
-                stencil(DIR == 0 && tx >= L::KW ? L::KW - 1 : tx, DIR == 1 && ty >= L::KW ? L::KW - 1 : ty, s, F);
-                stencil_from_u(wsur[s][0], wsur[s][2], W);
+        // The smooth results are computed by every lane (uniform, no divergence) and kept only
+        // where the smooth branch is taken; the lanes past a fitted xi tile's last interface read
+        // that interface's stencils. The "-" sign's stencil sum continues the "+" sign's FMA
+        // chain, so a lane smooth in both signs has h = h+ + h- with no separate sum; a lane
+        // smooth in "-" only keeps (h+ + h-) - h+.
+        {
+            const int ox = DIR == 0 && tx >= L::KW ? L::KW - 1 : tx;
+            const int oy = DIR == 1 && ty >= L::KW ? L::KW - 1 : ty;
+            double F[5][4], W[5], hp[4], hs[4];
+            stencil(ox, oy, 0, F);
+            stencil_from_u(wsur[0][0], wsur[0][2], W);
 #pragma unroll
-                for (int c = 0; c < 4; ++c)
-                    h[c] = fma(W[4], F[4][c], fma(W[3], F[3][c], fma(W[2], F[2][c], fma(W[1], F[1][c], W[0] * F[0][c]))));
-                if (valid && smooth[s]) {
+            for (int c = 0; c < 4; ++c)
+                hp[c] = fma(W[4], F[4][c], fma(W[3], F[3][c], fma(W[2], F[2][c], fma(W[1], F[1][c], W[0] * F[0][c]))));
+            stencil(ox, oy, 1, F);
+            stencil_from_u(wsur[1][0], wsur[1][2], W);
 #pragma unroll
-                    for (int c = 0; c < 4; ++c) hbuf(s, c, tid) = h[c];
-                } else if (valid) {
-                    queue[chk(p, atomicAdd(&qn, 1), (int)(2 * NT))] = 2 * tid + s;
+            for (int c = 0; c < 4; ++c)
+                hs[c] = fma(W[4], F[4][c], fma(W[3], F[3][c], fma(W[2], F[2][c], fma(W[1], F[1][c], fma(W[0], F[0][c], hp[c])))));
+            if (valid) {
+                if (smooth[0] && smooth[1]) {
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) hbuf(0, c, tid) = hs[c];
+                } else {
+                    if (smooth[0]) {
+#pragma unroll
+                        for (int c = 0; c < 4; ++c) hbuf(0, c, tid) = hp[c];
+                    } else {
+                        queue[chk(p, atomicAdd(&qn, 1), (int)(2 * NT))] = 2 * tid;
+                    }
+                    if (smooth[1]) {
+#pragma unroll
+                        for (int c = 0; c < 4; ++c) hbuf(1, c, tid) = hs[c] - hp[c];
+                    } else {
+                        queue[chk(p, atomicAdd(&qn, 1), (int)(2 * NT))] = 2 * tid + 1;
+                    }
                 }
             }
-            continue;
-#endif
+        }
+#else
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
             if (!valid) continue;
             if (smooth[s]) {
                 double F[5][4], h[4];
@@ -1059,6 +1094,7 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
                 queue[chk(p, atomicAdd(&qn, 1), (int)(2 * NT))] = 2 * tid + s;
             }
         }
+#endif
         __syncthreads();
         // phase 2b: the block works through the characteristic items (SC.f90:126-163)
         const int nq = qn;
@@ -1077,8 +1113,13 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
         // phase 2c: h = h+ + h- (sum_field, field_op.f90:1-21)
         if (valid) {
             double hsum[4];
+#if FAST
+            const bool both = smooth[0] && smooth[1];
+#else
+            const bool both = false;
+#endif
 #pragma unroll
-            for (int c = 0; c < 4; ++c) hsum[c] = hbuf(0, c, tid) + hbuf(1, c, tid);
+            for (int c = 0; c < 4; ++c) hsum[c] = both ? hbuf(0, c, tid) : hbuf(0, c, tid) + hbuf(1, c, tid);
             store(hsum);
         }
     }
@@ -1107,9 +1148,10 @@ __device__ __forceinline__ void block_max_atomic(double e1, double e2, double* s
     }
 }
 
-// get_primary at one interior cell (get_primary.f90:53-73); returns the two wave speeds.
+// get_primary at one interior cell (get_primary.f90:53-73); returns the two wave speeds and,
+// in pv, the primitives it stored.
 __device__ __forceinline__ void prim_cell(const Params& p, long long o, const double q[4], double& e1,
-                                          double& e2, unsigned& flags) {
+                                          double& e2, unsigned& flags, double pv[5]) {
     const double rho = q[0];
 #if FAST
     const double ir = rcp_nr(rho);
@@ -1137,6 +1179,7 @@ __device__ __forceinline__ void prim_cell(const Params& p, long long o, const do
     p.prim[2 * p.plane + o] = v;
     p.prim[3 * p.plane + o] = pr;
     p.prim[4 * p.plane + o] = alpha;
+    pv[0] = rho; pv[1] = u; pv[2] = v; pv[3] = pr; pv[4] = alpha;
     e1 = fabs(u) + alpha;
     e2 = fabs(v) + alpha;
     // numeric checks on the bit patterns (integer pipe): rho <= 0 or NaN, and any NaN
@@ -1156,10 +1199,10 @@ __device__ __forceinline__ void prim_block(const Params& p, int slot, int bx, in
     unsigned flags = 0;
     if (i < p.ni && j < p.nj) {
         const long long o = cidx(p, i + kB, j + kB);
-        double q[4];
+        double q[4], pv[5];
 #pragma unroll
         for (int v = 0; v < 4; ++v) q[v] = p.cons[v * p.plane + o];
-        prim_cell(p, o, q, e1, e2, flags);
+        prim_cell(p, o, q, e1, e2, flags, pv);
     }
     if (flags) atomicOr(&p.sc->status, flags);
     block_max_atomic(e1, e2, p.sc->maxeig[slot]);
@@ -1220,7 +1263,24 @@ __device__ __forceinline__ void update_block(const Params& p, int bx, int by) {
         }
 #pragma unroll
         for (int v = 0; v < 4; ++v) p.cons[v * p.plane + o] = q[v];
-        prim_cell(p, o, q, e1, e2, flags);
+        double pv[5];
+        prim_cell(p, o, q, e1, e2, flags, pv);
+        if (p.periodic_ghosts) {
+            // the cell's periodic images in the ghost layers (the periodic rule of the boundary
+            // fill, boundary_ivc_general.f90:37-59): a ghost of layer k copies the interior cell
+            // k+1 in from the opposite side; the corner ghosts are never read
+            const int I = i + kB, J = j + kB;
+            const int Ig = i < kB ? I + p.ni : (i >= p.ni - kB ? I - p.ni : -1);
+            const int Jg = j < kB ? J + p.nj : (j >= p.nj - kB ? J - p.nj : -1);
+            auto put = [&](long long g) {
+#pragma unroll
+                for (int v = 0; v < 4; ++v) p.cons[v * p.plane + g] = q[v];
+#pragma unroll
+                for (int v = 0; v < 5; ++v) p.prim[v * p.plane + g] = pv[v];
+            };
+            if (Ig >= 0) put(cidx(p, Ig, J));
+            if (Jg >= 0) put(cidx(p, I, Jg));
+        }
     }
     if (flags) atomicOr(&p.sc->status, flags);
     block_max_atomic(e1, e2, p.sc->maxeig[IRK % 3]);

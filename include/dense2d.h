@@ -247,8 +247,9 @@ int dense_read_binary(const char* path, dense_config_t* cfg, double* cons, doubl
    (if_save_tec, which also resets elasp_time; and 2d_theta_<step>.dat if if_save_theta) into
    `dir`, then reads `namelist_path` again (if not NULL) and applies it (dense_reconfigure); at
    the end it writes the final 2d_<step>.dat (and 2d_theta_<step>.dat). The saves are formatted and written by a host thread from a device snapshot
-   while the device runs on. *saves counts them (may be NULL). The reference's CpuTime.dat log
-   is not written. */
+   while the device runs on. *saves counts them (may be NULL). At the end it appends the
+   reference's timing log to `dir`/CpuTime.dat (general_main.f90:20,56-58): the wall time of the
+   step loop without the saves, the step count, and their ratio. */
 int dense_run(dense_handle_t* h, const char* dir, const char* namelist_path, int* saves);
 
 /* Cell x(ni,nj), y(ni,nj) and vertex vet_x(ni+1,nj+1), vet_y coordinates of cfg's benchmark as

@@ -75,6 +75,11 @@ def test_run_saves_like_the_reference_loop(dense, tmp_path):
     for k in (10, 20):
         assert (tmp_path / f"2d_{k}.dat2d").exists() and (tmp_path / f"2d_{k}.dat").exists()
     assert (tmp_path / "2d_25.dat").exists() and not (tmp_path / "2d_25.dat2d").exists()
+    # the timing log of general_main.f90:20,56-58: total loop time and steps, then the average
+    log = (tmp_path / "CpuTime.dat").read_text().splitlines()
+    assert log[0].split(":")[0].strip() == "Total time and steps" and int(log[0].split()[-1]) == 25
+    total = float(log[0].split(":")[1].split()[0])
+    assert total > 0 and float(log[1].split(":")[1]) == pytest.approx(total / 25, rel=1e-12)
     with dense.Solver(c) as p:
         p.upload(cons, prim, x, y)
         p.steps(20)
