@@ -1,6 +1,6 @@
-// adjoint.cu — the discrete adjoint of the plain solver's time step: LLF splitting (101) with
-// upwind5 / WENO-JS5 / WENO-Z5 reconstruction (251/253/255) and TVD-RK3 with the CFL time step,
-// on grids periodic in x and y (benchmarks 11 and 14).
+// adjoint.cu — the discrete adjoint of the plain solver's time step: LLF or GLF splitting
+// (101, 102) with upwind5 / WENO-JS5 / WENO-Z5 reconstruction (251/253/255) and TVD-RK3 with the
+// CFL time step, on grids periodic in x and y (benchmarks 11 and 14).
 //
 // The forward step (time_rk3_general, time_advance_general.f90:9-267) applies per stage
 //     L(u)_c = -(h_{f+1} - h_f)/dx - (g_{f'+1} - g_{f'})/dy,     cell c between faces f, f+1,
@@ -25,6 +25,11 @@
 //     reverse of the RK stage;
 // and once per step k_dt (one block): the time step's sensitivity sum_s c_s v_s . L(u_{s-1}),
 // sent through dt(max wave speeds) to the cells where the maxima are attained.
+// GLF (flux_splitting_GLF.f90:13-70) splits with the stage's global lambda = max over the cells
+// of |u_n| + alpha of the stage input instead of the cell's own: k_maxarg / k_maxred find that
+// maximum and its cell before the stage's reverse, k_rev uses it as a constant and sums the
+// sensitivity of lambda over all cells per block, and k_lamg sends the total through lambda to
+// the cell of the maximum (the gradient of a max flows to its argmax, ties to the lowest cell).
 // No atomics: every sum has a fixed order, so the gradient is deterministic.
 #include <cuda_runtime.h>
 
@@ -97,13 +102,16 @@ __device__ __forceinline__ void prim_pullback(const double U[4], const Prim& q, 
     Ub[0] += rb;
 }
 
-// Ub += (dF+/dU)^T gp + (dF-/dU)^T gm at one cell, direction DIR.
-template <int DIR>
-__device__ __forceinline__ void llf_vjp(const double U[4], const Prim& q, double gamma, const double gp[4],
-                                        const double gm[4], double Ub[4]) {
+// Ub += (dF+/dU)^T gp + (dF-/dU)^T gm at one cell, direction DIR, with F+- = 0.5((u_n +- lambda)
+// U + P): LLF's lambda = |u_n| + alpha of the cell is pulled back here; GLF's lambda (lam_g, the
+// global maximum) is a constant at the cell, and its sensitivity is returned for the caller to
+// send to the cell of the maximum.
+template <int DIR, bool GLF>
+__device__ __forceinline__ double llf_vjp(const double U[4], const Prim& q, double gamma, const double gp[4],
+                                          const double gm[4], double lam_g, double Ub[4]) {
     const double un = DIR == 0 ? q.u : q.v;
     const double s = un >= 0.0 ? 1.0 : -1.0;
-    const double lam = s * un + q.a;
+    const double lam = GLF ? lam_g : s * un + q.a;
     const double up = un + lam, um = un - lam;
     double Sp = 0.0, Sm = 0.0;
 #pragma unroll
@@ -116,9 +124,10 @@ __device__ __forceinline__ void llf_vjp(const double U[4], const Prim& q, double
     Sm *= 0.5;
     const double g3 = gp[3] + gm[3];
     const double lamb = Sp - Sm;
-    const double unb = Sp + Sm + 0.5 * q.p * g3 + s * lamb;
+    const double unb = Sp + Sm + 0.5 * q.p * g3 + (GLF ? 0.0 : s * lamb);
     const double pb = 0.5 * (gp[1 + DIR] + gm[1 + DIR]) + 0.5 * un * g3;
-    prim_pullback<DIR>(U, q, gamma, unb, lamb, pb, Ub);
+    prim_pullback<DIR>(U, q, gamma, unb, GLF ? 0.0 : lamb, pb, Ub);
+    return lamb;
 }
 
 // Ub += scale * d(|u_n| + alpha)/dU at one cell.
@@ -127,6 +136,51 @@ __device__ __forceinline__ void wave_speed_vjp(const double U[4], double gamma, 
     const Prim q = prim_of(U, gamma);
     const double un = DIR == 0 ? q.u : q.v;
     prim_pullback<DIR>(U, q, gamma, (un >= 0.0 ? 1.0 : -1.0) * scale, scale, 0.0, Ub);
+}
+
+// Block-wide (max, lowest index) of two (value, cell) pairs; the result is valid in thread 0.
+__device__ __forceinline__ bool argmax_better(double ea, long long ia, double eb, long long ib) {
+    return ea > eb || (ea == eb && ia < ib);
+}
+__device__ __forceinline__ void block_argmax(double& e1, long long& i1, double& e2, long long& i2) {
+#pragma unroll
+    for (int s = 16; s; s >>= 1) {
+        const double oe1 = __shfl_xor_sync(0xffffffffu, e1, s), oe2 = __shfl_xor_sync(0xffffffffu, e2, s);
+        const long long oi1 = __shfl_xor_sync(0xffffffffu, i1, s), oi2 = __shfl_xor_sync(0xffffffffu, i2, s);
+        if (argmax_better(oe1, oi1, e1, i1)) { e1 = oe1; i1 = oi1; }
+        if (argmax_better(oe2, oi2, e2, i2)) { e2 = oe2; i2 = oi2; }
+    }
+    __shared__ double se[2][32];
+    __shared__ long long si[2][32];
+    const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+    if ((tid & 31) == 0) { se[0][tid >> 5] = e1; se[1][tid >> 5] = e2; si[0][tid >> 5] = i1; si[1][tid >> 5] = i2; }
+    __syncthreads();
+    if (tid == 0) {
+        const int nw = (blockDim.x * blockDim.y + 31) / 32;
+        for (int k = 1; k < nw; ++k) {
+            if (argmax_better(se[0][k], si[0][k], e1, i1)) { e1 = se[0][k]; i1 = si[0][k]; }
+            if (argmax_better(se[1][k], si[1][k], e2, i2)) { e2 = se[1][k]; i2 = si[1][k]; }
+        }
+    }
+}
+
+// Deterministic block sum of two values (fixed lane and warp order); valid in thread 0.
+__device__ __forceinline__ void block_sum2(double& x, double& y) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        x += __shfl_xor_sync(0xffffffffu, x, o);
+        y += __shfl_xor_sync(0xffffffffu, y, o);
+    }
+    __shared__ double red2[2][32];
+    const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+    const int nw = (blockDim.x * blockDim.y + 31) / 32;
+    if ((tid & 31) == 0) { red2[0][tid >> 5] = x; red2[1][tid >> 5] = y; }
+    __syncthreads();
+    if (tid == 0) {
+        x = 0.0;
+        y = 0.0;
+        for (int w = 0; w < nw; ++w) { x += red2[0][w]; y += red2[1][w]; }
+    }
 }
 
 // Deterministic block sum (fixed lane and warp order); the result is valid in thread 0.
@@ -219,17 +273,20 @@ __device__ __forceinline__ void gather_line(const double* __restrict__ T, const 
 
 // Cell kernel: Ub = (dL/du)^T w at the cell from the stage's tape and hbar, then the reverse of
 // RK stage STAGE (3, 2, 1; 0 = Ub alone). Stage 1 also reduces the wave-speed maxima of its
-// state u0 (the time step's input) per block, with their cells.
-template <int STAGE, int REC>
+// state u0 (the time step's input) per block, with their cells. GLF: lamv holds the stage's
+// global lambda of both directions; the sensitivities of lambda are summed per block into lpart.
+template <int STAGE, int REC, bool GLF>
 __global__ void __launch_bounds__(128) k_rev(AdjParams a, const double* __restrict__ u,
                                              const double* __restrict__ w, const double* __restrict__ tape,
                                              const double* __restrict__ hb, double* __restrict__ acc,
                                              double* __restrict__ out, const double* __restrict__ dtp,
-                                             double* __restrict__ mpart) {
+                                             double* __restrict__ mpart, const double* __restrict__ lamv,
+                                             double* __restrict__ lpart) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     const int ni = a.ni, nj = a.nj;
     double e1 = -1.0, e2 = -1.0;
     long long i1 = LLONG_MAX, i2 = LLONG_MAX;
+    double lbx = 0.0, lby = 0.0;
     if (i < ni && j < nj) {
         const long long o = (long long)j * ni + i;
         double U[4], Ub[4] = {0.0, 0.0, 0.0, 0.0};
@@ -239,12 +296,12 @@ __global__ void __launch_bounds__(128) k_rev(AdjParams a, const double* __restri
         {
             double gp[4] = {0, 0, 0, 0}, gm[4] = {0, 0, 0, 0};
             gather_line<REC>(tape, hb, a.xs, (long long)j * (ni + 1), 1, i, ni, gp, gm);
-            llf_vjp<0>(U, q, a.gamma, gp, gm, Ub);
+            lbx = llf_vjp<0, GLF>(U, q, a.gamma, gp, gm, GLF ? lamv[0] : 0.0, Ub);
         }
         {
             double gp[4] = {0, 0, 0, 0}, gm[4] = {0, 0, 0, 0};
             gather_line<REC>(tape + a.np * a.xs, hb + 4 * a.xs, a.ys, i, ni, j, nj, gp, gm);
-            llf_vjp<1>(U, q, a.gamma, gp, gm, Ub);
+            lby = llf_vjp<1, GLF>(U, q, a.gamma, gp, gm, GLF ? lamv[1] : 0.0, Ub);
         }
         const double dt = STAGE == 0 ? 0.0 : *dtp;
 #pragma unroll
@@ -273,30 +330,90 @@ __global__ void __launch_bounds__(128) k_rev(AdjParams a, const double* __restri
     }
     if (STAGE == 1 && mpart) {
         // block argmax, ties to the lowest cell index
-        auto better = [](double ea, long long ia, double eb, long long ib) {
-            return ea > eb || (ea == eb && ia < ib);
-        };
-#pragma unroll
-        for (int s = 16; s; s >>= 1) {
-            const double oe1 = __shfl_xor_sync(0xffffffffu, e1, s), oe2 = __shfl_xor_sync(0xffffffffu, e2, s);
-            const long long oi1 = __shfl_xor_sync(0xffffffffu, i1, s), oi2 = __shfl_xor_sync(0xffffffffu, i2, s);
-            if (better(oe1, oi1, e1, i1)) { e1 = oe1; i1 = oi1; }
-            if (better(oe2, oi2, e2, i2)) { e2 = oe2; i2 = oi2; }
-        }
-        __shared__ double se[2][4];
-        __shared__ long long si[2][4];
-        const int tid = threadIdx.x + threadIdx.y * blockDim.x;
-        if ((tid & 31) == 0) { se[0][tid >> 5] = e1; se[1][tid >> 5] = e2; si[0][tid >> 5] = i1; si[1][tid >> 5] = i2; }
-        __syncthreads();
-        if (tid == 0) {
-            const int nw = (blockDim.x * blockDim.y + 31) / 32;
-            for (int k = 1; k < nw; ++k) {
-                if (better(se[0][k], si[0][k], e1, i1)) { e1 = se[0][k]; i1 = si[0][k]; }
-                if (better(se[1][k], si[1][k], e2, i2)) { e2 = se[1][k]; i2 = si[1][k]; }
-            }
+        block_argmax(e1, i1, e2, i2);
+        if (threadIdx.x == 0 && threadIdx.y == 0) {
             double* mp = mpart + 4 * (blockIdx.y * gridDim.x + blockIdx.x);
             mp[0] = e1; mp[1] = (double)i1; mp[2] = e2; mp[3] = (double)i2;
         }
+    }
+    if (GLF) {
+        __syncthreads();  // the argmax reduction's shared arrays are read before the next sum
+        block_sum2(lbx, lby);
+        if (threadIdx.x == 0 && threadIdx.y == 0) {
+            double* lp = lpart + 2 * (blockIdx.y * gridDim.x + blockIdx.x);
+            lp[0] = lbx;
+            lp[1] = lby;
+        }
+    }
+}
+
+// GLF: per block, the maxima of |u|+alpha and |v|+alpha over the stage input's cells and their
+// cells (the stage's global lambda, max_eig_i/j of get_primary.f90:69-73).
+__global__ void __launch_bounds__(128) k_maxarg(AdjParams a, const double* __restrict__ u,
+                                                double* __restrict__ mpart) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    double e1 = -1.0, e2 = -1.0;
+    long long i1 = LLONG_MAX, i2 = LLONG_MAX;
+    if (i < a.ni && j < a.nj) {
+        const long long o = (long long)j * a.ni + i;
+        double U[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) U[v] = u[v * a.plane + o];
+        const Prim q = prim_of(U, a.gamma);
+        e1 = fabs(q.u) + q.a;
+        e2 = fabs(q.v) + q.a;
+        i1 = i2 = o;
+    }
+    block_argmax(e1, i1, e2, i2);
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        double* mp = mpart + 4 * (blockIdx.y * gridDim.x + blockIdx.x);
+        mp[0] = e1; mp[1] = (double)i1; mp[2] = e2; mp[3] = (double)i2;
+    }
+}
+
+// GLF: the block maxima reduced to lamv = (lambda_x, lambda_y, cell of lambda_x, cell of
+// lambda_y), ties to the lowest cell. One block of 256 threads.
+__global__ void __launch_bounds__(256) k_maxred(const double* __restrict__ mpart, int nm, double* __restrict__ lamv) {
+    const int t = threadIdx.x;
+    double e1 = -1.0, e2 = -1.0;
+    long long i1 = LLONG_MAX, i2 = LLONG_MAX;
+    for (int k = t; k < nm; k += blockDim.x) {
+        const double* mp = mpart + 4 * k;
+        if (argmax_better(mp[0], (long long)mp[1], e1, i1)) { e1 = mp[0]; i1 = (long long)mp[1]; }
+        if (argmax_better(mp[2], (long long)mp[3], e2, i2)) { e2 = mp[2]; i2 = (long long)mp[3]; }
+    }
+    block_argmax(e1, i1, e2, i2);
+    if (t == 0) { lamv[0] = e1; lamv[1] = e2; lamv[2] = (double)i1; lamv[3] = (double)i2; }
+}
+
+// GLF: the stage's total sensitivity of lambda_x and lambda_y (the block sums of k_rev, in a
+// fixed order) sent through |u_n| + alpha at the cells of the maxima into the stage's output,
+// with the stage's coefficient of L(u) (1 for STAGE 0, dt, dt/4, 2 dt/3 for stages 1, 2, 3).
+template <int STAGE>
+__global__ void __launch_bounds__(256) k_lamg(AdjParams a, const double* __restrict__ lpart, int nb,
+                                              const double* __restrict__ lamv, const double* __restrict__ u,
+                                              const double* __restrict__ dtp, double* __restrict__ out) {
+    const int t = threadIdx.x;
+    double sx = 0.0, sy = 0.0;
+    for (int k = t; k < nb; k += blockDim.x) { sx += lpart[2 * k]; sy += lpart[2 * k + 1]; }
+    block_sum2(sx, sy);
+    if (t != 0) return;
+    const double dt = STAGE == 0 ? 1.0 : *dtp;
+    const double c = STAGE == 0 ? 1.0 : STAGE == 1 ? dt : STAGE == 2 ? 0.25 * dt : 2.0 / 3.0 * dt;
+    const double cell[2] = {lamv[2], lamv[3]};
+    const double sens[2] = {sx, sy};
+#pragma unroll
+    for (int d = 0; d < 2; ++d) {
+        // no cell holds a finite maximum (a NaN state): nothing to differentiate
+        if (!(cell[d] >= 0.0 && cell[d] < (double)a.plane)) continue;
+        const long long o = (long long)cell[d];
+        double U[4], Ub[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+        for (int v = 0; v < 4; ++v) U[v] = u[v * a.plane + o];
+        if (d == 0) wave_speed_vjp<0>(U, a.gamma, c * sens[d], Ub);
+        else        wave_speed_vjp<1>(U, a.gamma, c * sens[d], Ub);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) out[v * a.plane + o] += Ub[v];
     }
 }
 
@@ -392,6 +509,9 @@ struct dense_adjoint {
     double *g = nullptr, *g1 = nullptr, *g2 = nullptr, *acc = nullptr, *hb = nullptr;
     double* part = nullptr;  int npart = 0;       // per stage: k_hbar blocks
     double* mpart = nullptr; int nm = 0;
+    // GLF: the stage's (lambda_x, lambda_y, their cells), block maxima, block sums of lambda's
+    // sensitivity
+    double *lamv = nullptr, *lmp = nullptr, *lpart = nullptr;
     dim3 gh, gc;
     int nsteps = -1;                              // steps of the last forward
     cudaEvent_t ev_in = nullptr, ev_out = nullptr;
@@ -479,31 +599,56 @@ int taped_stage(dense_adjoint* a, int irk, double* tape) {
     return DENSE_OK;
 }
 
-template <int REC>
+template <int REC, bool GLF>
 void launch_rev(dense_adjoint* a, int stage, const double* u, const double* tape, const double* w, double* out,
                 const double* dtp, cudaStream_t s) {
     using namespace dense::adj;
     const dim3 bc(kCX, kCY);
+    double* const lv = a->lamv;
+    double* const lp = a->lpart;
     switch (stage) {
-    case 3: k_rev<3, REC><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, a->hb, a->acc, out, dtp, nullptr); break;
-    case 2: k_rev<2, REC><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, a->hb, a->acc, out, dtp, nullptr); break;
-    case 1: k_rev<1, REC><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, a->hb, a->acc, out, dtp, a->mpart); break;
-    default: k_rev<0, REC><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, a->hb, nullptr, out, nullptr, nullptr); break;
+    case 3: k_rev<3, REC, GLF><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, a->hb, a->acc, out, dtp, nullptr, lv, lp); break;
+    case 2: k_rev<2, REC, GLF><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, a->hb, a->acc, out, dtp, nullptr, lv, lp); break;
+    case 1: k_rev<1, REC, GLF><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, a->hb, a->acc, out, dtp, a->mpart, lv, lp); break;
+    default: k_rev<0, REC, GLF><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, a->hb, nullptr, out, nullptr, nullptr, lv, lp); break;
+    }
+}
+template <bool GLF>
+void launch_rev_recon(dense_adjoint* a, int stage, const double* u, const double* tape, const double* w,
+                      double* out, const double* dtp, cudaStream_t s) {
+    switch (a->cfg.recon) {
+    case DENSE_RECON_UPWIND5: launch_rev<DENSE_RECON_UPWIND5, GLF>(a, stage, u, tape, w, out, dtp, s); break;
+    case DENSE_RECON_WENOJS5: launch_rev<DENSE_RECON_WENOJS5, GLF>(a, stage, u, tape, w, out, dtp, s); break;
+    default:                  launch_rev<DENSE_RECON_WENOZ5, GLF>(a, stage, u, tape, w, out, dtp, s); break;
     }
 }
 
 // the reverse of one stage: hbar of w on every face (and w . L(u) per block into part), then
-// the cells
+// the cells; GLF first finds the stage's global lambda and its cells, and last sends lambda's
+// sensitivity to those cells
 void vjp(dense_adjoint* a, int stage, const double* u, const double* tape, const double* w, double* out,
          double* part, const double* dtp) {
+    using namespace dense::adj;
     cudaStream_t s = a->h->stream;
-    dense::adj::k_hbar<<<a->gh, dim3(kHX, kHY), 0, s>>>(a->ap, w, tape, a->hb, part);
-    switch (a->cfg.recon) {
-    case DENSE_RECON_UPWIND5: launch_rev<DENSE_RECON_UPWIND5>(a, stage, u, tape, w, out, dtp, s); break;
-    case DENSE_RECON_WENOJS5: launch_rev<DENSE_RECON_WENOJS5>(a, stage, u, tape, w, out, dtp, s); break;
-    default:                  launch_rev<DENSE_RECON_WENOZ5>(a, stage, u, tape, w, out, dtp, s); break;
+    const bool glf = a->cfg.splitting == DENSE_SPLIT_GLF;
+    if (glf) {
+        k_maxarg<<<a->gc, dim3(kCX, kCY), 0, s>>>(a->ap, u, a->lmp);
+        k_maxred<<<1, 256, 0, s>>>(a->lmp, a->nm, a->lamv);
+        a->launches += 2;
     }
+    k_hbar<<<a->gh, dim3(kHX, kHY), 0, s>>>(a->ap, w, tape, a->hb, part);
+    if (glf) launch_rev_recon<true>(a, stage, u, tape, w, out, dtp, s);
+    else     launch_rev_recon<false>(a, stage, u, tape, w, out, dtp, s);
     a->launches += 2;
+    if (glf) {
+        switch (stage) {
+        case 3: k_lamg<3><<<1, 256, 0, s>>>(a->ap, a->lpart, a->nm, a->lamv, u, dtp, out); break;
+        case 2: k_lamg<2><<<1, 256, 0, s>>>(a->ap, a->lpart, a->nm, a->lamv, u, dtp, out); break;
+        case 1: k_lamg<1><<<1, 256, 0, s>>>(a->ap, a->lpart, a->nm, a->lamv, u, dtp, out); break;
+        default: k_lamg<0><<<1, 256, 0, s>>>(a->ap, a->lpart, a->nm, a->lamv, u, dtp, out); break;
+        }
+        a->launches += 1;
+    }
 }
 
 // reverse of one step from its three recorded stage states and tapes; g holds dJ/du(n+1) on
@@ -550,7 +695,8 @@ int dense_adjoint_get_solver(dense_adjoint_t* a, dense_handle_t** h) {
 void dense_adjoint_destroy(dense_adjoint_t* a) {
     if (!a) return;
     if (a->h) cudaStreamSynchronize(a->h->stream);
-    double* bufs[] = {a->ckpt, a->dts, a->rec, a->tape, a->g, a->g1, a->g2, a->acc, a->hb, a->part, a->mpart};
+    double* bufs[] = {a->ckpt, a->dts, a->rec, a->tape, a->g, a->g1, a->g2, a->acc, a->hb, a->part, a->mpart,
+                      a->lamv, a->lmp, a->lpart};
     for (double* b : bufs) if (b) cudaFree(b);
     if (a->argmax) cudaFree(a->argmax);
     if (a->ev_in) cudaEventDestroy(a->ev_in);
@@ -562,8 +708,8 @@ void dense_adjoint_destroy(dense_adjoint_t* a) {
 int dense_adjoint_create(const dense_config_t* cfg, int checkpoint_every, dense_adjoint_t** out) {
     if (!out || !cfg) return aerr(nullptr, DENSE_ERR_ARG, "null argument");
     *out = nullptr;
-    if (cfg->splitting != DENSE_SPLIT_LLF)
-        return aerr(nullptr, DENSE_ERR_ARG, "the adjoint covers the LLF splitting (101) only");
+    if (cfg->splitting != DENSE_SPLIT_LLF && cfg->splitting != DENSE_SPLIT_GLF)
+        return aerr(nullptr, DENSE_ERR_ARG, "the adjoint covers the LLF and GLF splittings (101, 102)");
     if (cfg->recon != DENSE_RECON_UPWIND5 && cfg->recon != DENSE_RECON_WENOJS5 && cfg->recon != DENSE_RECON_WENOZ5)
         return aerr(nullptr, DENSE_ERR_ARG, "the adjoint covers reconstructions 251, 253 and 255");
     if (cfg->benchmark != DENSE_BENCH_IVC_PERIODIC && cfg->benchmark != DENSE_BENCH_RM_PERIODIC)
@@ -603,6 +749,7 @@ int dense_adjoint_create(const dense_config_t* cfg, int checkpoint_every, dense_
         {&a->g, a->state}, {&a->g1, a->state}, {&a->g2, a->state}, {&a->acc, a->state},
         {&a->hb, (size_t)4 * (p.xs + p.ys)}, {&a->part, (size_t)3 * a->npart}, {&a->mpart, (size_t)4 * a->nm},
         {&a->rec, (size_t)3 * a->k * a->state}, {&a->tape, (size_t)3 * a->k * a->tape_stage},
+        {&a->lamv, 4}, {&a->lmp, (size_t)4 * a->nm}, {&a->lpart, (size_t)2 * a->nm},
     };
     for (auto& b : bufs) {
         cudaError_t e = cudaMalloc((void**)b.p, b.n * sizeof(double));

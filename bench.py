@@ -529,8 +529,9 @@ def main():
         return run_batched(args, dense, dense.load_library())
     wl = WORKLOADS[args.workload]
     if args.ni and args.nj:
-        wl = wl[:3] + (args.ni, args.nj, wl[5].split(" ")[0] + f" {args.ni}x{args.nj} (reduced) "
-                       + " ".join(wl[5].split(" ")[2:]), wl[6])
+        full = f"{wl[3]}x{wl[4]}"
+        wl = wl[:3] + (args.ni, args.nj, wl[5].replace(full, f"{args.ni}x{args.nj} (the {full} workload's "
+                                                               f"scheme on a reduced grid)"), wl[6])
     if args.impl == "reference":
         return run_reference_arm(args, wl)
 

@@ -29,15 +29,16 @@ def perturbed_state(dense, cfg, seed=0, amp=1e-3):
     return c, U.contiguous()
 
 
-@pytest.mark.parametrize("recon", [251, 253, 255])
-def test_rhs_vjp_matches_autograd(dense, adjoint, recon):
-    cfg = vortex_cfg(dense, recon, ni=24, nj=20, var_eps=4.0, var_xc=4.6, var_yc=5.3)
+@pytest.mark.parametrize("split,recon", [(101, 251), (101, 253), (101, 255), (102, 251), (102, 253),
+                                         (102, 255)])
+def test_rhs_vjp_matches_autograd(dense, adjoint, split, recon):
+    cfg = vortex_cfg(dense, recon, ni=24, nj=20, var_eps=4.0, var_xc=4.6, var_yc=5.3, splitting=split)
     c, U = perturbed_state(dense, cfg)
     v = torch.randn(U.shape, generator=torch.Generator().manual_seed(1), dtype=torch.float64).cuda()
     with adjoint.Adjoint(c) as adj:
         out, vdotl = adj.rhs_vjp(U, v)
     Ut = U.clone().requires_grad_(True)
-    L = torch_step.rhs(Ut, c.gamma, c.dx, c.dy, recon)
+    L = torch_step.rhs(Ut, c.gamma, c.dx, c.dy, recon, split)
     (ref,) = torch.autograd.grad(L, Ut, v)
     L = L.detach()
     # two evaluation orders of derivatives whose WENO weights scale like 1/(1e-6 + beta)^3
@@ -45,11 +46,12 @@ def test_rhs_vjp_matches_autograd(dense, adjoint, recon):
     assert abs(vdotl - float((v * L).sum())) < 1e-12 * float((v * L).abs().sum())
 
 
-@pytest.mark.parametrize("recon,const_dt", [(253, 0), (255, 0), (251, 0), (253, 1)])
-def test_steps_gradient_matches_autograd(dense, adjoint, recon, const_dt):
+@pytest.mark.parametrize("split,recon,const_dt", [(101, 253, 0), (101, 255, 0), (101, 251, 0), (101, 253, 1),
+                                                  (102, 253, 0), (102, 255, 0), (102, 251, 1)])
+def test_steps_gradient_matches_autograd(dense, adjoint, split, recon, const_dt):
     """7 steps with checkpoints every 3: two full segments and a partial one."""
     cfg = vortex_cfg(dense, recon, ni=24, nj=20, var_eps=4.0, var_xc=4.6, var_yc=5.3,
-                     if_const_dt=const_dt, dt=0.02)
+                     if_const_dt=const_dt, dt=0.02, splitting=split)
     c, U = perturbed_state(dense, cfg)
     gT = torch.randn(U.shape, generator=torch.Generator().manual_seed(2), dtype=torch.float64).cuda()
     with adjoint.Adjoint(c, checkpoint_every=3) as adj:
@@ -57,7 +59,7 @@ def test_steps_gradient_matches_autograd(dense, adjoint, recon, const_dt):
         g0 = adj.backward(gT)
         dts = adj.dts()
     Ut = U.clone().requires_grad_(True)
-    ref_T = torch_step.run(Ut, 7, c.gamma, c.dx, c.dy, recon, c.cfl, c.dt if const_dt else None)
+    ref_T = torch_step.run(Ut, 7, c.gamma, c.dx, c.dy, recon, c.cfl, c.dt if const_dt else None, split)
     assert rel(uT, ref_T.detach()) < 1e-12
     (ref,) = torch.autograd.grad(ref_T, Ut, gT)
     assert rel(g0, ref) < 1e-10
@@ -72,12 +74,12 @@ def padded(U):
     return cons
 
 
-@pytest.mark.parametrize("recon", [251, 253, 255])
-def test_taped_recompute_reproduces_the_forward(dense, adjoint, recon):
+@pytest.mark.parametrize("split,recon", [(101, 251), (101, 253), (101, 255), (102, 255)])
+def test_taped_recompute_reproduces_the_forward(dense, adjoint, split, recon):
     """The taping sweeps of the reverse pass recompute each segment bit for bit: after a
     backward the solver holds the state after the first segment, equal to a plain solve, and the
     fluxes of a taped stage equal the plain sweep's."""
-    cfg = vortex_cfg(dense, recon, ni=40, nj=32)
+    cfg = vortex_cfg(dense, recon, ni=40, nj=32, splitting=split)
     c, U = perturbed_state(dense, cfg)
     with adjoint.Adjoint(c, checkpoint_every=5) as adj:
         adj.forward(U, 12)
@@ -108,12 +110,13 @@ def test_backward_is_deterministic_and_repeatable(dense, adjoint):
     assert torch.equal(a, b)
 
 
-def test_autograd_function_in_a_graph(dense, adjoint):
+@pytest.mark.parametrize("split", [101, 102])
+def test_autograd_function_in_a_graph(dense, adjoint, split):
     """Loss 1/2 ||rho(T) - rho_target||^2 of a vortex built from (eps, xc, yc) by torch ops:
     autograd chains the vortex's derivatives with the adjoint; checked against central
     differences of the CUDA forward, which must not change the cells of the wave-speed maxima
-    (the time step is not differentiable where they switch)."""
-    cfg = vortex_cfg(dense, 253, ni=48, nj=48, cfl=0.4)
+    (the time step, and GLF's wave speed, are not differentiable where they switch)."""
+    cfg = vortex_cfg(dense, 253, ni=48, nj=48, cfl=0.4, splitting=split)
     c = dense.init_general(cfg)[0]
     n, h = 30, 1e-6
     with adjoint.Adjoint(c, checkpoint_every=8) as adj:

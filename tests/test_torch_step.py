@@ -23,15 +23,15 @@ def vortex_cfg(dense, recon, ni=24, nj=20, **kw):
     return dense.config_default(**base)
 
 
-@pytest.mark.parametrize("recon", [251, 253, 255])
-def test_torch_step_matches_oracle(dense, orc, recon):
-    cfg = vortex_cfg(dense, recon, var_eps=4.0, var_xc=4.6, var_yc=5.3)
+@pytest.mark.parametrize("split,recon", [(101, 251), (101, 253), (101, 255), (102, 253), (102, 255)])
+def test_torch_step_matches_oracle(dense, orc, split, recon):
+    cfg = vortex_cfg(dense, recon, var_eps=4.0, var_xc=4.6, var_yc=5.3, splitting=split)
     c, cons, prim, x, y = dense.init_general(cfg)
     o = orc.OracleSolver(c)
     o.steps(3)
     ref = to_state(o.get_state()[0])
     U = torch.from_numpy(to_state(cons))
-    got = torch_step.run(U, 3, c.gamma, c.dx, c.dy, recon, c.cfl).numpy()
+    got = torch_step.run(U, 3, c.gamma, c.dx, c.dy, recon, c.cfl, split=split).numpy()
     scale = np.abs(ref).max(axis=(1, 2), keepdims=True)
     assert (np.abs(got - ref) / scale).max() < 1e-12
 

@@ -2,7 +2,9 @@
 adjoint kernels against autograd (test infrastructure; never used by the library).
 
 Same scheme as the plain solver: get_primary (get_primary.f90:53-60), LLF splitting with
-lambda = |u_n| + alpha per cell (flux_splitting_LLF.f90:67-81), upwind5 / WENO-JS5 / WENO-Z5
+lambda = |u_n| + alpha per cell (flux_splitting_LLF.f90:67-81) or GLF splitting with lambda the
+maximum of |u_n| + alpha over the stage's input (flux_splitting_GLF.f90:13-70, the max_eig_i/j of
+get_primary.f90:69-73), upwind5 / WENO-JS5 / WENO-Z5
 reconstruction of F+ and F- at each face (scheme_*_general.f90, weno_mod.f90), the flux
 difference, and TVD-RK3 (time_advance_general.f90:9-267) with dt = cfl/(max(|u|+alpha)/dx +
 max(|v|+alpha)/dy) of the step's input (or a constant dt). States are (4, nj, ni) tensors of the
@@ -48,12 +50,14 @@ def primitives(U, gamma):
     return rho, u, v, p, a
 
 
-def rhs(U, gamma, dx, dy, rec):
+def rhs(U, gamma, dx, dy, rec, split=101):
     """L(U) = -(h_{i+1/2} - h_{i-1/2})/dx - (g_{j+1/2} - g_{j-1/2})/dy."""
     rho, u, v, p, a = primitives(U, gamma)
     out = torch.zeros_like(U)
     for d, (un, h, axis) in enumerate(((u, dx, 2), (v, dy, 1))):
         lam = un.abs() + a
+        if split == 102:
+            lam = lam.max()
         P = torch.stack([torch.zeros_like(p), p if d == 0 else torch.zeros_like(p),
                          p if d == 1 else torch.zeros_like(p), un * p])
         Fp = 0.5 * ((un + lam) * U + P)
@@ -67,7 +71,7 @@ def rhs(U, gamma, dx, dy, rec):
     return out
 
 
-def time_step(U, gamma, dx, dy, rec, cfl, dt_const=None):
+def time_step(U, gamma, dx, dy, rec, cfl, dt_const=None, split=101):
     """One TVD-RK3 step; returns (U_next, dt)."""
     if dt_const is None:
         _, u, v, _, a = primitives(U, gamma)
@@ -77,13 +81,13 @@ def time_step(U, gamma, dx, dy, rec, cfl, dt_const=None):
         dt = cfl * dt_x * dt_y / (dt_x + dt_y)
     else:
         dt = torch.tensor(dt_const, dtype=U.dtype, device=U.device)
-    u1 = U + dt * rhs(U, gamma, dx, dy, rec)
-    u2 = 3.0 / 4.0 * U + 1.0 / 4.0 * u1 + 1.0 / 4.0 * dt * rhs(u1, gamma, dx, dy, rec)
-    u3 = 1.0 / 3.0 * U + 2.0 / 3.0 * u2 + 2.0 / 3.0 * dt * rhs(u2, gamma, dx, dy, rec)
+    u1 = U + dt * rhs(U, gamma, dx, dy, rec, split)
+    u2 = 3.0 / 4.0 * U + 1.0 / 4.0 * u1 + 1.0 / 4.0 * dt * rhs(u1, gamma, dx, dy, rec, split)
+    u3 = 1.0 / 3.0 * U + 2.0 / 3.0 * u2 + 2.0 / 3.0 * dt * rhs(u2, gamma, dx, dy, rec, split)
     return u3, dt
 
 
-def run(U, n, gamma, dx, dy, rec, cfl, dt_const=None):
+def run(U, n, gamma, dx, dy, rec, cfl, dt_const=None, split=101):
     for _ in range(n):
-        U, _ = time_step(U, gamma, dx, dy, rec, cfl, dt_const)
+        U, _ = time_step(U, gamma, dx, dy, rec, cfl, dt_const, split)
     return U
