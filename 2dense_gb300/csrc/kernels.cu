@@ -1595,8 +1595,14 @@ __global__ void k_step_end(Scalars* sc) { k_step_end_body(sc); }
 
 // ---------------------------------------------------------------------------------------------
 // Launchers
-constexpr int kXTX = 32, kXTY = 4;   // xi tile
-constexpr int kETX = 32, kETY = 8;   // eta tile
+// Component-wise sweeps. xi tile: 32 interfaces x 4 rows (32 x 2 on small grids): a tile
+// stages (32 + 5)/32 = 1.16 cells per interface whatever its height. eta tile: 8 columns x 32
+// interfaces (8 x 8 on small grids): the halo runs along the sweep, so a tall narrow tile stages
+// (32 + 5)/32 = 1.16 cells per interface where 32 x 8 staged 1.63 and 32 x 4 2.25 (each staged
+// cell costs its split fluxes and eight indicator terms); 8-wide rows still read whole 64-byte
+// segments, and the smem rows of a warp (4 rows x 8 columns) stay free of bank conflicts.
+constexpr int kXTX = 32, kXTY = 4, kXSTY = 2;   // xi tile; small-grid height
+constexpr int kETX = 8, kETY = 32, kESTY = 8;   // eta tile; small-grid height
 // characteristic sweeps: eta tiles of 4 columns x 64 interfaces, AdaWENO xi tiles of one row of
 // 256 threads (251 interfaces, 256 cells; long lines along the sweep stage fewer halo cells per
 // interface: 1.02 in xi and 1.08 in eta against 1.16 and 1.63 for 32 x 4 and 32 x 8; measured on
@@ -1637,18 +1643,18 @@ static void cw_launch(dim3 g, const Params& p, int irk, cudaStream_t s) {
 
 // On small grids the standard tiles give a sweep only one or two blocks per SM, and the SMs that
 // get one more block than the others set the launch's time. Below four blocks per SM the sweep
-// runs with tiles of half the height, which doubles the block count (same arithmetic per
-// interface: the results do not depend on the tile).
+// runs with shorter tiles, which multiplies the block count (same arithmetic per interface: the
+// results do not depend on the tile).
 template <int SPL, int REC, bool TAPE = false>
 static void launch_cw(const Params& p, int irk, int dir, cudaStream_t s) {
     const unsigned few = 4u * sm_count();
     if (dir == 0) {
         const dim3 g = grid_xi(p, kXTX, kXTY);
-        if (g.x * g.y < few) cw_launch<0, SPL, REC, kXTX, kXTY / 2, TAPE>(grid_xi(p, kXTX, kXTY / 2), p, irk, s);
+        if (g.x * g.y < few) cw_launch<0, SPL, REC, kXTX, kXSTY, TAPE>(grid_xi(p, kXTX, kXSTY), p, irk, s);
         else                 cw_launch<0, SPL, REC, kXTX, kXTY, TAPE>(g, p, irk, s);
     } else {
         const dim3 g = grid_eta(p, kETX, kETY);
-        if (g.x * g.y < few) cw_launch<1, SPL, REC, kETX, kETY / 2, TAPE>(grid_eta(p, kETX, kETY / 2), p, irk, s);
+        if (g.x * g.y < few) cw_launch<1, SPL, REC, kETX, kESTY, TAPE>(grid_eta(p, kETX, kESTY), p, irk, s);
         else                 cw_launch<1, SPL, REC, kETX, kETY, TAPE>(g, p, irk, s);
     }
 }
@@ -1741,27 +1747,23 @@ __global__ void kb_step_end(const Params* tab, int n) {
 
 static inline const int3* as_map(const void* m) { return (const int3*)m; }
 
-template <int SPL, int REC, int XTX, int XTY, int ETX, int ETY>
-static void batch_cw(const BatchLaunch& b, int irk, int dir, cudaStream_t s) {
-    if (dir == 0)
-        kb_flux_cw<0, SPL, REC, XTX, XTY><<<b.nb_xi, dim3(XTX, XTY), CwTile<0, REC, XTX, XTY>::bytes, s>>>(
-            b.tab, as_map(b.map_xi), irk);
-    else
-        kb_flux_cw<1, SPL, REC, ETX, ETY><<<b.nb_eta, dim3(ETX, ETY), CwTile<1, REC, ETX, ETY>::bytes, s>>>(
-            b.tab, as_map(b.map_eta), irk);
+template <int DIR, int SPL, int REC, int TX, int TY>
+static void batch_cw(const BatchLaunch& b, int irk, cudaStream_t s) {
+    kb_flux_cw<DIR, SPL, REC, TX, TY><<<DIR == 0 ? b.nb_xi : b.nb_eta, dim3(TX, TY), CwTile<DIR, REC, TX, TY>::bytes, s>>>(
+        b.tab, as_map(DIR == 0 ? b.map_xi : b.map_eta), irk);
 }
-// xi tiles: (32,4) (64,2) (32,8); eta tiles: (32,8) (32,4) (64,4)
+// xi tiles: (32,4) (64,2) (32,8); eta tiles: (8,32) (8,16) (32,8)
 template <int SPL, int REC>
 static void batch_cw_variant(const BatchLaunch& b, int irk, int dir, cudaStream_t s) {
     const int v = dir == 0 ? b.xi_variant : b.eta_variant;
     if (dir == 0) {
-        if (v == 1) batch_cw<SPL, REC, 64, 2, 32, 8>(b, irk, 0, s);
-        else if (v == 2) batch_cw<SPL, REC, 32, 8, 32, 8>(b, irk, 0, s);
-        else batch_cw<SPL, REC, 32, 4, 32, 8>(b, irk, 0, s);
+        if (v == 1) batch_cw<0, SPL, REC, 64, 2>(b, irk, s);
+        else if (v == 2) batch_cw<0, SPL, REC, 32, 8>(b, irk, s);
+        else batch_cw<0, SPL, REC, 32, 4>(b, irk, s);
     } else {
-        if (v == 1) batch_cw<SPL, REC, 32, 4, 32, 4>(b, irk, 1, s);
-        else if (v == 2) batch_cw<SPL, REC, 32, 4, 64, 4>(b, irk, 1, s);
-        else batch_cw<SPL, REC, 32, 4, 32, 8>(b, irk, 1, s);
+        if (v == 1) batch_cw<1, SPL, REC, 8, 16>(b, irk, s);
+        else if (v == 2) batch_cw<1, SPL, REC, 32, 8>(b, irk, s);
+        else batch_cw<1, SPL, REC, 8, 32>(b, irk, s);
     }
 }
 
@@ -1817,22 +1819,22 @@ static void allow_smem(K kernel, size_t bytes) {
 template <int SPL, int REC>
 static void allow_cw_smem() {
     allow_smem(k_flux_cw<0, SPL, REC, kXTX, kXTY>, CwTile<0, REC, kXTX, kXTY>::bytes);
-    allow_smem(k_flux_cw<0, SPL, REC, kXTX, kXTY / 2>, CwTile<0, REC, kXTX, kXTY / 2>::bytes);
+    allow_smem(k_flux_cw<0, SPL, REC, kXTX, kXSTY>, CwTile<0, REC, kXTX, kXSTY>::bytes);
     allow_smem(k_flux_cw<1, SPL, REC, kETX, kETY>, CwTile<1, REC, kETX, kETY>::bytes);
-    allow_smem(k_flux_cw<1, SPL, REC, kETX, kETY / 2>, CwTile<1, REC, kETX, kETY / 2>::bytes);
+    allow_smem(k_flux_cw<1, SPL, REC, kETX, kESTY>, CwTile<1, REC, kETX, kESTY>::bytes);
     if (SPL == 0) {  // the adjoint's taping sweeps
         allow_smem(k_flux_cw<0, 0, REC, kXTX, kXTY, true>, CwTile<0, REC, kXTX, kXTY>::bytes);
-        allow_smem(k_flux_cw<0, 0, REC, kXTX, kXTY / 2, true>, CwTile<0, REC, kXTX, kXTY / 2>::bytes);
+        allow_smem(k_flux_cw<0, 0, REC, kXTX, kXSTY, true>, CwTile<0, REC, kXTX, kXSTY>::bytes);
         allow_smem(k_flux_cw<1, 0, REC, kETX, kETY, true>, CwTile<1, REC, kETX, kETY>::bytes);
-        allow_smem(k_flux_cw<1, 0, REC, kETX, kETY / 2, true>, CwTile<1, REC, kETX, kETY / 2>::bytes);
+        allow_smem(k_flux_cw<1, 0, REC, kETX, kESTY, true>, CwTile<1, REC, kETX, kESTY>::bytes);
     }
     // the batched tile variants of batch_cw_variant
     allow_smem(kb_flux_cw<0, SPL, REC, 32, 4>, CwTile<0, REC, 32, 4>::bytes);
     allow_smem(kb_flux_cw<0, SPL, REC, 64, 2>, CwTile<0, REC, 64, 2>::bytes);
     allow_smem(kb_flux_cw<0, SPL, REC, 32, 8>, CwTile<0, REC, 32, 8>::bytes);
+    allow_smem(kb_flux_cw<1, SPL, REC, 8, 32>, CwTile<1, REC, 8, 32>::bytes);
+    allow_smem(kb_flux_cw<1, SPL, REC, 8, 16>, CwTile<1, REC, 8, 16>::bytes);
     allow_smem(kb_flux_cw<1, SPL, REC, 32, 8>, CwTile<1, REC, 32, 8>::bytes);
-    allow_smem(kb_flux_cw<1, SPL, REC, 32, 4>, CwTile<1, REC, 32, 4>::bytes);
-    allow_smem(kb_flux_cw<1, SPL, REC, 64, 4>, CwTile<1, REC, 64, 4>::bytes);
 }
 static bool allow_tile_smem() {
     allow_cw_smem<0, 251>();
@@ -1892,7 +1894,7 @@ void batch_tile_shape(int splitting, int dir, int variant, int* tx, int* ty) {
         return;
     }
     static const int xi[kTileVariants][2] = {{32, 4}, {64, 2}, {32, 8}};
-    static const int eta[kTileVariants][2] = {{32, 8}, {32, 4}, {64, 4}};
+    static const int eta[kTileVariants][2] = {{8, 32}, {8, 16}, {32, 8}};
     const int v = variant < 0 || variant >= kTileVariants ? 0 : variant;
     *tx = dir == 0 ? xi[v][0] : eta[v][0];
     *ty = dir == 0 ? xi[v][1] : eta[v][1];

@@ -178,7 +178,8 @@ def test_free_stream_preserved(dense):
 # ---- parity across tile seams and at the headline configurations' own sizes ------------------
 #
 # The AdaWENO (105) sweeps cover 251 interfaces per xi tile and 123 per eta tile, the
-# characteristic WENO-Z (104) eta sweep 64, the component-wise sweeps 32 x 4 / 32 x 8. The grids
+# characteristic WENO-Z (104) eta sweep 64, the component-wise sweeps 32 interfaces along xi and
+# 32 (8 on small grids) along eta. The grids
 # below give every sweep at least three tiles along its direction, so every seam between tiles
 # (halo cells staged by both neighbours, characteristic items queued on either side) is compared
 # with the oracle.
@@ -222,7 +223,7 @@ def step_from(dense, orc, cfg, cons, prim, x, y, t=0.0, step=0, dt=None, nsteps=
 @pytest.mark.parametrize("split,recon,ni,nj", [
     (105, 0, 760, 380),     # AdaWENO: 4 xi tiles of 251 interfaces, 4 eta tiles of 123
     (104, 0, 160, 200),     # characteristic WENO-Z: 4 eta tiles of 64
-    (101, 253, 136, 40),    # component-wise: 5 xi tiles of 32, 5 eta tiles of 8
+    (101, 253, 136, 40),    # component-wise: 5 xi tiles of 32, 6 eta tiles of 8
 ])
 def test_random_state_across_tile_seams(dense, orc, split, recon, ni, nj):
     for strict in (1, 0):
