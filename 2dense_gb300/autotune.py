@@ -1,29 +1,40 @@
 """Autotuner of the batched form's launch schedule.
 
 A schedule is (xi tile variant, eta tile variant, block order): the thread-block shape of each
-direction sweep (``batch_tile_shape`` in csrc/kernels.cu) and the order in which the instances'
-blocks are laid out in each launch (instance-major, largest instance first, or round-robin).
-None of them changes any result -- every interface's arithmetic is the same -- so the tuner is
-free to pick whichever is fastest for the batch at hand.
+direction sweep (``batch_tile_shape`` in csrc/kernels.cu: 4 xi and 5 eta shapes, from short wide
+tiles that give small instances more blocks to tall narrow ones that stage fewer halo cells per
+interface) and the order in which the instances' blocks are laid out in each launch
+(instance-major, largest instance first, or round-robin) -- 60 schedules, counted by the library
+(``dense_batch_schedule_space``). None of them changes any result -- every interface's arithmetic
+is the same -- so the tuner is free to pick whichever is fastest for the batch at hand.
 
-The search is a coordinate descent (order, then xi tile, then eta tile), each candidate timed on a
-scratch copy of the batch (same configurations, same initial states) so the caller's solution is
-untouched. The winner is cached in a JSON file keyed by device, scheme and the histogram of
-instance sizes, so a second batch of the same shape reuses it without timing.
+The search is a coordinate descent (order, then xi tile, then eta tile, repeated until a pass
+changes nothing, at most three passes), each candidate timed on a scratch copy of the batch (same
+configurations, same initial states) so the caller's solution is untouched. The winner is cached
+in a JSON file keyed by device, scheme and the histogram of instance sizes, so a second batch of
+the same shape reuses it without timing.
 """
 from __future__ import annotations
 
+import ctypes
 import hashlib
 import json
 import os
 import time
 
+from . import _abi
 from .solver import BatchSolver, init_general
 
 CACHE = os.environ.get("DENSE2D_AUTOTUNE_CACHE",
                        os.path.join(os.path.expanduser("~"), ".cache", "dense2d_gb300", "autotune.json"))
-N_VARIANTS = 3
-ORDERS = 3
+
+
+def schedule_space() -> tuple[int, int, int]:
+    """(xi tile variants, eta tile variants, block orders) of dense_batch_set_schedule."""
+    lib = _abi.load_library()
+    n = [ctypes.c_int() for _ in range(3)]
+    lib.dense_batch_schedule_space(*[ctypes.byref(x) for x in n])
+    return n[0].value, n[1].value, n[2].value
 
 
 def _device_key() -> str:
@@ -96,15 +107,20 @@ def tune(cfgs, setups=None, steps: int = 2, reps: int = 2, use_cache: bool = Tru
                 trials[sched] = _time_schedule(scratch, sched, steps, reps)
             return trials[sched]
 
-        for o in range(ORDERS):
-            if run((best[0], best[1], o)) < run(best):
-                best = (best[0], best[1], o)
-        for v in range(N_VARIANTS):
-            if run((v, best[1], best[2])) < run(best):
-                best = (v, best[1], best[2])
-        for v in range(N_VARIANTS):
-            if run((best[0], v, best[2])) < run(best):
-                best = (best[0], v, best[2])
+        n_xi, n_eta, n_order = schedule_space()
+        for _ in range(3):
+            start = best
+            for o in range(n_order):
+                if run((best[0], best[1], o)) < run(best):
+                    best = (best[0], best[1], o)
+            for v in range(n_xi):
+                if run((v, best[1], best[2])) < run(best):
+                    best = (v, best[1], best[2])
+            for v in range(n_eta):
+                if run((best[0], v, best[2])) < run(best):
+                    best = (best[0], v, best[2])
+            if best == start:
+                break
     finally:
         scratch.close()
     named = {f"{k[0]},{k[1]},{k[2]}": v for k, v in trials.items()}

@@ -375,9 +375,16 @@ int dense_batch_download(dense_batch_t* b, int i, double* cons, double* prim) {
     return DENSE_OK;
 }
 
+int dense_batch_schedule_space(int* n_xi, int* n_eta, int* n_order) {
+    if (n_xi) *n_xi = dense::kXiVariants;
+    if (n_eta) *n_eta = dense::kEtaVariants;
+    if (n_order) *n_order = dense::kOrders;
+    return DENSE_OK;
+}
+
 int dense_batch_set_schedule(dense_batch_t* b, int xi_variant, int eta_variant, int order) {
-    if (!b || xi_variant < 0 || xi_variant >= dense::kTileVariants || eta_variant < 0 ||
-        eta_variant >= dense::kTileVariants || order < 0 || order > 2)
+    if (!b || xi_variant < 0 || xi_variant >= dense::kXiVariants || eta_variant < 0 ||
+        eta_variant >= dense::kEtaVariants || order < 0 || order >= dense::kOrders)
         return bset(b, DENSE_ERR_ARG, "bad schedule");
     BCK(b, cudaStreamSynchronize(b->stream));
     b->order = order;

@@ -122,7 +122,7 @@ struct int3_ { int x, y, z; };  // host mirror of CUDA's int3 (instance, block x
 
 // Tile shapes (threads x, threads y) the batched flux sweeps can run with; an autotuner picks
 // one per direction. Variant 0 is the single-instance shape.
-constexpr int kTileVariants = 3;
+constexpr int kXiVariants = 4, kEtaVariants = 5, kOrders = 3;
 void batch_tile_shape(int splitting, int dir, int variant, int* tx, int* ty);
 
 struct BatchLaunch {

@@ -1752,18 +1752,25 @@ static void batch_cw(const BatchLaunch& b, int irk, cudaStream_t s) {
     kb_flux_cw<DIR, SPL, REC, TX, TY><<<DIR == 0 ? b.nb_xi : b.nb_eta, dim3(TX, TY), CwTile<DIR, REC, TX, TY>::bytes, s>>>(
         b.tab, as_map(DIR == 0 ? b.map_xi : b.map_eta), irk);
 }
-// xi tiles: (32,4) (64,2) (32,8); eta tiles: (8,32) (8,16) (32,8)
+// xi tiles: (32,4) (64,2) (32,8) (32,2); eta tiles: (8,32) (8,16) (32,8) (16,16) (4,64)
 template <int SPL, int REC>
 static void batch_cw_variant(const BatchLaunch& b, int irk, int dir, cudaStream_t s) {
     const int v = dir == 0 ? b.xi_variant : b.eta_variant;
     if (dir == 0) {
-        if (v == 1) batch_cw<0, SPL, REC, 64, 2>(b, irk, s);
-        else if (v == 2) batch_cw<0, SPL, REC, 32, 8>(b, irk, s);
-        else batch_cw<0, SPL, REC, 32, 4>(b, irk, s);
+        switch (v) {
+        case 1: batch_cw<0, SPL, REC, 64, 2>(b, irk, s); break;
+        case 2: batch_cw<0, SPL, REC, 32, 8>(b, irk, s); break;
+        case 3: batch_cw<0, SPL, REC, 32, 2>(b, irk, s); break;
+        default: batch_cw<0, SPL, REC, 32, 4>(b, irk, s); break;
+        }
     } else {
-        if (v == 1) batch_cw<1, SPL, REC, 8, 16>(b, irk, s);
-        else if (v == 2) batch_cw<1, SPL, REC, 32, 8>(b, irk, s);
-        else batch_cw<1, SPL, REC, 8, 32>(b, irk, s);
+        switch (v) {
+        case 1: batch_cw<1, SPL, REC, 8, 16>(b, irk, s); break;
+        case 2: batch_cw<1, SPL, REC, 32, 8>(b, irk, s); break;
+        case 3: batch_cw<1, SPL, REC, 16, 16>(b, irk, s); break;
+        case 4: batch_cw<1, SPL, REC, 4, 64>(b, irk, s); break;
+        default: batch_cw<1, SPL, REC, 8, 32>(b, irk, s); break;
+        }
     }
 }
 
@@ -1832,9 +1839,12 @@ static void allow_cw_smem() {
     allow_smem(kb_flux_cw<0, SPL, REC, 32, 4>, CwTile<0, REC, 32, 4>::bytes);
     allow_smem(kb_flux_cw<0, SPL, REC, 64, 2>, CwTile<0, REC, 64, 2>::bytes);
     allow_smem(kb_flux_cw<0, SPL, REC, 32, 8>, CwTile<0, REC, 32, 8>::bytes);
+    allow_smem(kb_flux_cw<0, SPL, REC, 32, 2>, CwTile<0, REC, 32, 2>::bytes);
     allow_smem(kb_flux_cw<1, SPL, REC, 8, 32>, CwTile<1, REC, 8, 32>::bytes);
     allow_smem(kb_flux_cw<1, SPL, REC, 8, 16>, CwTile<1, REC, 8, 16>::bytes);
     allow_smem(kb_flux_cw<1, SPL, REC, 32, 8>, CwTile<1, REC, 32, 8>::bytes);
+    allow_smem(kb_flux_cw<1, SPL, REC, 16, 16>, CwTile<1, REC, 16, 16>::bytes);
+    allow_smem(kb_flux_cw<1, SPL, REC, 4, 64>, CwTile<1, REC, 4, 64>::bytes);
 }
 static bool allow_tile_smem() {
     allow_cw_smem<0, 251>();
@@ -1893,9 +1903,10 @@ void batch_tile_shape(int splitting, int dir, int variant, int* tx, int* ty) {
                              : VNS::CharTile<1, false, VNS::kCETX, VNS::kCETY>::KW);
         return;
     }
-    static const int xi[kTileVariants][2] = {{32, 4}, {64, 2}, {32, 8}};
-    static const int eta[kTileVariants][2] = {{8, 32}, {8, 16}, {32, 8}};
-    const int v = variant < 0 || variant >= kTileVariants ? 0 : variant;
+    static const int xi[kXiVariants][2] = {{32, 4}, {64, 2}, {32, 8}, {32, 2}};
+    static const int eta[kEtaVariants][2] = {{8, 32}, {8, 16}, {32, 8}, {16, 16}, {4, 64}};
+    const int n = dir == 0 ? kXiVariants : kEtaVariants;
+    const int v = variant < 0 || variant >= n ? 0 : variant;
     *tx = dir == 0 ? xi[v][0] : eta[v][0];
     *ty = dir == 0 ? xi[v][1] : eta[v][1];
 }

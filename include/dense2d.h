@@ -327,9 +327,13 @@ int dense_batch_get_time(dense_batch_t* b, int i, double* t, int* step, double* 
    the _async form does not wait */
 int dense_batch_steps(dense_batch_t* b, int nsteps, double t_end, int total_step);
 int dense_batch_steps_async(dense_batch_t* b, int nsteps, double t_end, int total_step);
-/* launch schedule (picked by the autotuner): tile shape variants of the xi and eta sweeps
-   (0..2) and the block order (0 instance-major, 1 largest instance first, 2 round-robin) */
+/* launch schedule (picked by the autotuner): tile shape variants of the component-wise xi and
+   eta sweeps and the block order (0 instance-major, 1 largest instance first, 2 round-robin);
+   the characteristic sweeps (104, 105) keep their one shape. Variant 0 is the single-instance
+   tile: xi (32,4) (64,2) (32,8) (32,2); eta (8,32) (8,16) (32,8) (16,16) (4,64) threads. */
 int dense_batch_set_schedule(dense_batch_t* b, int xi_variant, int eta_variant, int order);
+/* the number of xi variants, eta variants and block orders dense_batch_set_schedule accepts */
+int dense_batch_schedule_space(int* n_xi, int* n_eta, int* n_order);
 int dense_batch_get_stream(dense_batch_t* b, void** stream);
 int dense_batch_status(dense_batch_t* b, unsigned* flags);
 long long dense_batch_launch_count(dense_batch_t* b);

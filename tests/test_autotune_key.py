@@ -40,3 +40,8 @@ def test_cache_round_trip(autotune, tmp_path, monkeypatch):
     assert autotune._load_cache() == {"k": [1, 2, 0]}
     path.write_text("not json")
     assert autotune._load_cache() == {}
+
+
+def test_schedule_space_from_the_library(autotune):
+    n_xi, n_eta, n_order = autotune.schedule_space()
+    assert (n_xi, n_eta, n_order) == (4, 5, 3)

@@ -53,7 +53,7 @@ def test_batch_equals_plain_solves(dense, split, recon):
 def test_every_schedule_gives_the_same_bits(dense):
     cfgs = batch_cfgs(dense, 101, 255, SIZES, seed=9)
     ref = None
-    for sched in [(0, 0, 0), (1, 2, 1), (2, 1, 2), (1, 1, 0), (2, 2, 1)]:
+    for sched in [(0, 0, 0), (1, 2, 1), (2, 1, 2), (1, 1, 0), (2, 2, 1), (3, 3, 0), (0, 4, 2), (3, 4, 1)]:
         with dense.BatchSolver.from_setups(cfgs) as b:
             b.set_schedule(*sched)
             b.steps(2)

@@ -68,7 +68,7 @@ def test_checked_batch_every_tile_variant(dense, split, recon):
     with dense.BatchSolver.from_setups(batch_cfgs(dense, split, recon, SIZES, strict=0)) as b:
         b.steps(2)
         ref = [b.download(i) for i in range(len(SIZES))]
-    for sched in [(0, 0, 0), (1, 1, 1), (2, 2, 2)]:
+    for sched in [(0, 0, 0), (1, 1, 1), (2, 2, 2), (3, 3, 0), (0, 4, 1)]:
         with dense.BatchSolver.from_setups(batch_cfgs(dense, split, recon, SIZES, strict=2)) as b:
             b.set_schedule(*sched)
             b.steps(2)
