@@ -268,9 +268,7 @@ int dense_batch_create(int n, const dense_config_t* cfgs, dense_batch_t** out) {
         p.sc = (Scalars*)q;
         p.ni = c.ni; p.nj = c.nj; p.P = P; p.plane = (long long)plane;
         p.gamma = c.gamma; p.cfl = c.cfl; p.delta = c.delta; p.dx = c.dx; p.dy = c.dy; p.dt_const = c.dt;
-        if (c.delta < 0.0) p.theta_kk = 0.0;
-        else if (c.delta >= 1.0) p.theta_kk = __builtin_huge_val();
-        else p.theta_kk = std::sqrt(c.delta / (1.0 - c.delta));
+        p.theta_c = dense::theta_c_of(c.delta);
         p.if_const_dt = c.if_const_dt;
         p.bodyforce = c.if_bodyforce && (c.benchmark == DENSE_BENCH_RT || c.benchmark == DENSE_BENCH_RT_REFLECT);
         p.benchmark = c.benchmark; p.splitting = c.splitting; p.recon = c.recon;

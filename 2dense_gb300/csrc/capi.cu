@@ -85,11 +85,7 @@ void fill_params(dense_handle* h) {
     p.ni = c.ni; p.nj = c.nj; p.P = h->P;
     p.plane = (long long)h->NJp * h->P;
     p.gamma = c.gamma; p.cfl = c.cfl; p.delta = c.delta; p.dx = c.dx; p.dy = c.dy; p.dt_const = c.dt;
-    // theta = D^2 / (D^2 + (N-D)^2) > delta  <=>  D > sqrt(delta/(1-delta)) (N-D)  for
-    // 0 <= delta < 1; delta < 0 always selects the smooth branch, delta >= 1 never does
-    if (c.delta < 0.0) p.theta_kk = 0.0;
-    else if (c.delta >= 1.0) p.theta_kk = __builtin_huge_val();
-    else p.theta_kk = std::sqrt(c.delta / (1.0 - c.delta));
+    p.theta_c = dense::theta_c_of(c.delta);
     p.if_const_dt = c.if_const_dt;
     // the body force is nonzero only where boundary_rt_general refreshes it (:154-155)
     p.bodyforce = c.if_bodyforce && (c.benchmark == DENSE_BENCH_RT || c.benchmark == DENSE_BENCH_RT_REFLECT);

@@ -56,10 +56,11 @@ struct Params {
     long long plane; // doubles per variable plane = NJp * P
     double gamma, cfl, delta, dx, dy, dt_const;
     // AdaWENO switch theta > delta written without a divide (fast kernels): with
-    // theta = 1/(1 + (sum alpha - 1)^2) and sum alpha - 1 = tau^2 Q / D >= 0 (common denominator D),
-    // theta > delta <=> D > theta_kk tau^2 Q, theta_kk = sqrt(delta/(1-delta)) for 0 <= delta < 1;
-    // 0 for delta < 0 (always smooth), +inf for delta >= 1 (never smooth)
-    double theta_kk;
+    // theta = 1/(1 + (sum alpha - 1)^2), N = (sum alpha) D and N - D = tau^2 Q >= 0 (common
+    // denominator D), theta > delta <=> D > k (N - D) with k = sqrt(delta/(1-delta))
+    // <=> D > theta_c N with theta_c = k/(1+k), for 0 <= delta < 1; theta_c = 0 for delta < 0
+    // (always smooth), 1 for delta >= 1 (never smooth: N >= D)
+    double theta_c;
     int if_const_dt, bodyforce, benchmark, splitting, recon;
     // periodic in x and y with at least 2 kB cells each way (benchmarks 11 and 14): the update
     // also writes each boundary cell's periodic images into the ghost layers, which is the whole
@@ -75,6 +76,14 @@ struct Params {
     // (if_save_theta): xi [2][nj][ni+1], then eta [2][nj+1][ni] (sign 0 = "+"); else null
     double* theta;
 };
+
+// Params::theta_c of an AdaWENO threshold delta.
+inline double theta_c_of(double delta) {
+    if (delta < 0.0) return 0.0;
+    if (delta >= 1.0) return 1.0;
+    const double k = __builtin_sqrt(delta / (1.0 - delta));
+    return k / (1.0 + k);
+}
 
 // Whether the update of a configuration writes the periodic ghost images (Params::periodic_ghosts).
 inline int periodic_ghosts(int benchmark, int ni, int nj) {

@@ -983,15 +983,17 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
                 const double d1 = fma(0.25 * B1, B1, A2[atk(cm + (s == 0 ? 0 : 1), tx, ty)]);
                 const double d2 = fma(B2h, B2h, A2[atk(c2, tx, ty)]);
                 // WENO-Z over the common denominator D = prod d_k^2, P_k = D/d_k^2, T = tau^2:
-                // alpha_k D = c_k (D + T P_k); since sum c_k = 1, (sum alpha - 1) D = T Q with
-                // Q = sum c_k P_k, and theta > delta <=> D > theta_kk T Q
+                // alpha_k D = c_k (D + T P_k); since sum c_k = 1, N = (sum alpha) D = D + T Q with
+                // Q = sum c_k P_k, and theta > delta <=> D > theta_c N. Both sides are positive,
+                // so the test compares their bit patterns on the integer pipe.
                 const double e0 = d0 * d0, e1 = d1 * d1, e2 = d2 * d2;
                 const double P0 = e1 * e2, P1 = e0 * e2, P2 = e0 * e1;
                 const double D = e0 * P0;
                 const double dd = d2 - d0, T = dd * dd;
                 const double Q = fma(c31, P1, c30 * P0) + c32 * P2;
-                smooth[s] = fma(-p.theta_kk * T, Q, D) > 0.0;
-                const double r = rcp_nr(fma(T, Q, D));
+                const double N = fma(T, Q, D);
+                smooth[s] = __double_as_longlong(D) > __double_as_longlong(p.theta_c * N);
+                const double r = rcp_nr(N);
                 // u_k = alpha_k / (c_k sum alpha); the weights are w_k = c_k u_k, w1 = 1 - w0 - w2
                 wsur[s][0] = fma(T, P0, D) * r;
                 wsur[s][2] = fma(T, P2, D) * r;

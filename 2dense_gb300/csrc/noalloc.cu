@@ -159,9 +159,7 @@ extern "C" int dense_stage_noalloc(const dense_config_t* cfg, int irk, double cu
     p.plane = (long long)NJp * p.P;
     p.gamma = cfg->gamma; p.cfl = cfg->cfl; p.delta = cfg->delta; p.dx = cfg->dx; p.dy = cfg->dy;
     p.dt_const = cfg->dt;
-    if (cfg->delta < 0.0) p.theta_kk = 0.0;
-    else if (cfg->delta >= 1.0) p.theta_kk = __builtin_huge_val();
-    else p.theta_kk = sqrt(cfg->delta / (1.0 - cfg->delta));
+    p.theta_c = dense::theta_c_of(cfg->delta);
     p.if_const_dt = cfg->if_const_dt;
     p.bodyforce = cfg->if_bodyforce && (b == DENSE_BENCH_RT || b == DENSE_BENCH_RT_REFLECT);
     p.benchmark = b; p.splitting = cfg->splitting; p.recon = cfg->recon;
