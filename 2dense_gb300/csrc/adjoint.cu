@@ -1,6 +1,6 @@
-// adjoint.cu — the discrete adjoint of the plain solver's time step: LLF or GLF splitting
-// (101, 102) with upwind5 / WENO-JS5 / WENO-Z5 reconstruction (251/253/255) and TVD-RK3 with the
-// CFL time step, on grids periodic in x and y (benchmarks 11 and 14).
+// adjoint.cu — the discrete adjoint of the plain solver's time step: LLF, GLF or Steger-Warming
+// splitting (101, 102, 103) with upwind5 / WENO-JS5 / WENO-Z5 reconstruction (251/253/255) and
+// TVD-RK3 with the CFL time step, on grids periodic in x and y (benchmarks 11 and 14).
 //
 // The forward step (time_rk3_general, time_advance_general.f90:9-267) applies per stage
 //     L(u)_c = -(h_{f+1} - h_f)/dx - (g_{f'+1} - g_{f'})/dy,     cell c between faces f, f+1,
@@ -30,6 +30,10 @@
 // maximum and its cell before the stage's reverse, k_rev uses it as a constant and sums the
 // sensitivity of lambda over all cells per block, and k_lamg sends the total through lambda to
 // the cell of the maximum (the gradient of a max flows to its argmax, ties to the lowest cell).
+// Steger-Warming (flux_splitting_SW.f90:14-168) splits each cell's flux with the three eigenvalues
+// u_n, u_n -+ alpha of the cell alone; its transposed Jacobian is taken exactly in forward mode:
+// the split, written once over a dual-number type, is evaluated with each conserved variable of
+// the cell seeded in turn (four passes), and the sensitivities of F+ and F- contract the columns.
 // No atomics: every sum has a fixed order, so the gradient is deterministic.
 #include <cuda_runtime.h>
 
@@ -128,6 +132,80 @@ __device__ __forceinline__ double llf_vjp(const double U[4], const Prim& q, doub
     const double pb = 0.5 * (gp[1 + DIR] + gm[1 + DIR]) + 0.5 * un * g3;
     prim_pullback<DIR>(U, q, gamma, unb, GLF ? 0.0 : lamb, pb, Ub);
     return lamb;
+}
+
+// ---- Steger-Warming: exact Jacobian columns in forward mode ---------------------------------
+// A value and its derivative along one seed direction.
+struct Dual {
+    double v, d;
+};
+__device__ __forceinline__ Dual operator+(Dual a, Dual b) { return {a.v + b.v, a.d + b.d}; }
+__device__ __forceinline__ Dual operator-(Dual a, Dual b) { return {a.v - b.v, a.d - b.d}; }
+__device__ __forceinline__ Dual operator*(Dual a, Dual b) { return {a.v * b.v, fma(a.d, b.v, a.v * b.d)}; }
+__device__ __forceinline__ Dual operator*(double c, Dual a) { return {c * a.v, c * a.d}; }
+__device__ __forceinline__ Dual operator/(Dual a, Dual b) {
+    const double r = rcp_nr(b.v), q = a.v * r;
+    return {q, (a.d - q * b.d) * r};
+}
+__device__ __forceinline__ Dual operator/(Dual a, double c) { return {a.v / c, a.d / c}; }
+__device__ __forceinline__ Dual dsqrt(Dual a) {
+    const double rs = rsqrt_nr(a.v), s = a.v * rs;
+    return {s, 0.5 * a.d * rs};
+}
+
+// The Steger-Warming split of one cell in direction DIR from its conserved variables: get_primary
+// (get_primary.f90:53-60, with the pressure floor of :58), then flux_splitting_SW.f90:42-91 (xi)
+// / :110-160 (eta) -- eigenvalues l1 = u_n, l2 = u_n - alpha, l3 = u_n + alpha split as
+// (l +- sqrt(l^2 + eps^2))/2 with eps = 0.125.
+template <int DIR>
+__device__ __forceinline__ void sw_split_dual(const Dual U[4], double gamma, Dual fp[4], Dual fm[4]) {
+    const Dual rho = U[0];
+    const Dual u = U[1] / rho, v = U[2] / rho;
+    const Dual uu2 = u * u + v * v;
+    Dual p = (gamma - 1.0) * (U[3] - 0.5 * (rho * uu2));
+    if (p.v < 0.0) p = Dual{kPFloor, 0.0};
+    const Dual a = dsqrt((gamma * p) / rho);
+    const double eps2 = 0.125 * 0.125, g1 = gamma - 1.0, c2g = 1.0 / (2.0 * gamma);
+    const Dual un = DIR == 0 ? u : v, ut = DIR == 0 ? v : u;
+    const Dual l1 = un, l2 = un - a, l3 = un + a;
+    const Dual e{eps2, 0.0};
+    const Dual s1 = dsqrt(l1 * l1 + e), s2 = dsqrt(l2 * l2 + e), s3 = dsqrt(l3 * l3 + e);
+    const Dual q2 = l2 * l2 + ut * ut, q3 = l3 * l3 + ut * ut;
+    const Dual crho = c2g * rho;
+#pragma unroll
+    for (int sg = 0; sg < 2; ++sg) {
+        const Dual p1 = 0.5 * (sg == 0 ? l1 + s1 : l1 - s1);
+        const Dual p2 = 0.5 * (sg == 0 ? l2 + s2 : l2 - s2);
+        const Dual p3 = 0.5 * (sg == 0 ? l3 + s3 : l3 - s3);
+        const Dual wii = ((3.0 - gamma) / (2.0 * g1)) * ((p2 + p3) * (a * a));
+        const Dual A = (2.0 * g1) * p1;
+        Dual* f = sg == 0 ? fp : fm;
+        f[0] = (A + p2 + p3) * crho;
+        f[1 + DIR] = (A * un + p2 * l2 + p3 * l3) * crho;
+        f[2 - DIR] = ((A + p2 + p3) * ut) * crho;
+        f[3] = (g1 * (p1 * uu2) + 0.5 * (p2 * q2) + 0.5 * (p3 * q3) + wii) * crho;
+    }
+}
+
+// Ub += (dF+/dU)^T gp + (dF-/dU)^T gm of the Steger-Warming split in both directions at one cell
+// (g[d] the sensitivities of direction d's F+ then F-): one forward pass per conserved variable.
+__device__ __forceinline__ void sw_vjp(const double U[4], double gamma, const double gpx[4], const double gmx[4],
+                                       const double gpy[4], const double gmy[4], double Ub[4]) {
+#pragma unroll 1
+    for (int k = 0; k < 4; ++k) {
+        Dual Ud[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) Ud[c] = Dual{U[c], c == k ? 1.0 : 0.0};
+        Dual fp[4], fm[4];
+        double acc = 0.0;
+        sw_split_dual<0>(Ud, gamma, fp, fm);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc = fma(gpx[c], fp[c].d, fma(gmx[c], fm[c].d, acc));
+        sw_split_dual<1>(Ud, gamma, fp, fm);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc = fma(gpy[c], fp[c].d, fma(gmy[c], fm[c].d, acc));
+        Ub[k] += acc;
+    }
 }
 
 // Ub += scale * d(|u_n| + alpha)/dU at one cell.
@@ -273,9 +351,10 @@ __device__ __forceinline__ void gather_line(const double* __restrict__ T, const 
 
 // Cell kernel: Ub = (dL/du)^T w at the cell from the stage's tape and hbar, then the reverse of
 // RK stage STAGE (3, 2, 1; 0 = Ub alone). Stage 1 also reduces the wave-speed maxima of its
-// state u0 (the time step's input) per block, with their cells. GLF: lamv holds the stage's
-// global lambda of both directions; the sensitivities of lambda are summed per block into lpart.
-template <int STAGE, int REC, bool GLF>
+// state u0 (the time step's input) per block, with their cells. SPL: 0 LLF, 1 GLF, 2 SW. GLF:
+// lamv holds the stage's global lambda of both directions; the sensitivities of lambda are summed
+// per block into lpart.
+template <int STAGE, int REC, int SPL>
 __global__ void __launch_bounds__(128) k_rev(AdjParams a, const double* __restrict__ u,
                                              const double* __restrict__ w, const double* __restrict__ tape,
                                              const double* __restrict__ hb, double* __restrict__ acc,
@@ -292,16 +371,16 @@ __global__ void __launch_bounds__(128) k_rev(AdjParams a, const double* __restri
         double U[4], Ub[4] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll
         for (int v = 0; v < 4; ++v) U[v] = u[v * a.plane + o];
+        constexpr bool GLF = SPL == 1;
         const Prim q = prim_of(U, a.gamma);
-        {
-            double gp[4] = {0, 0, 0, 0}, gm[4] = {0, 0, 0, 0};
-            gather_line<REC>(tape, hb, a.xs, (long long)j * (ni + 1), 1, i, ni, gp, gm);
-            lbx = llf_vjp<0, GLF>(U, q, a.gamma, gp, gm, GLF ? lamv[0] : 0.0, Ub);
-        }
-        {
-            double gp[4] = {0, 0, 0, 0}, gm[4] = {0, 0, 0, 0};
-            gather_line<REC>(tape + a.np * a.xs, hb + 4 * a.xs, a.ys, i, ni, j, nj, gp, gm);
-            lby = llf_vjp<1, GLF>(U, q, a.gamma, gp, gm, GLF ? lamv[1] : 0.0, Ub);
+        double gpx[4] = {0, 0, 0, 0}, gmx[4] = {0, 0, 0, 0}, gpy[4] = {0, 0, 0, 0}, gmy[4] = {0, 0, 0, 0};
+        gather_line<REC>(tape, hb, a.xs, (long long)j * (ni + 1), 1, i, ni, gpx, gmx);
+        gather_line<REC>(tape + a.np * a.xs, hb + 4 * a.xs, a.ys, i, ni, j, nj, gpy, gmy);
+        if (SPL == 2) {
+            sw_vjp(U, a.gamma, gpx, gmx, gpy, gmy, Ub);
+        } else {
+            lbx = llf_vjp<0, GLF>(U, q, a.gamma, gpx, gmx, GLF ? lamv[0] : 0.0, Ub);
+            lby = llf_vjp<1, GLF>(U, q, a.gamma, gpy, gmy, GLF ? lamv[1] : 0.0, Ub);
         }
         const double dt = STAGE == 0 ? 0.0 : *dtp;
 #pragma unroll
@@ -336,7 +415,7 @@ __global__ void __launch_bounds__(128) k_rev(AdjParams a, const double* __restri
             mp[0] = e1; mp[1] = (double)i1; mp[2] = e2; mp[3] = (double)i2;
         }
     }
-    if (GLF) {
+    if (SPL == 1) {
         __syncthreads();  // the argmax reduction's shared arrays are read before the next sum
         block_sum2(lbx, lby);
         if (threadIdx.x == 0 && threadIdx.y == 0) {
@@ -599,7 +678,7 @@ int taped_stage(dense_adjoint* a, int irk, double* tape) {
     return DENSE_OK;
 }
 
-template <int REC, bool GLF>
+template <int REC, int SPL>
 void launch_rev(dense_adjoint* a, int stage, const double* u, const double* tape, const double* w, double* out,
                 const double* dtp, cudaStream_t s) {
     using namespace dense::adj;
@@ -607,19 +686,19 @@ void launch_rev(dense_adjoint* a, int stage, const double* u, const double* tape
     double* const lv = a->lamv;
     double* const lp = a->lpart;
     switch (stage) {
-    case 3: k_rev<3, REC, GLF><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, a->hb, a->acc, out, dtp, nullptr, lv, lp); break;
-    case 2: k_rev<2, REC, GLF><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, a->hb, a->acc, out, dtp, nullptr, lv, lp); break;
-    case 1: k_rev<1, REC, GLF><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, a->hb, a->acc, out, dtp, a->mpart, lv, lp); break;
-    default: k_rev<0, REC, GLF><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, a->hb, nullptr, out, nullptr, nullptr, lv, lp); break;
+    case 3: k_rev<3, REC, SPL><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, a->hb, a->acc, out, dtp, nullptr, lv, lp); break;
+    case 2: k_rev<2, REC, SPL><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, a->hb, a->acc, out, dtp, nullptr, lv, lp); break;
+    case 1: k_rev<1, REC, SPL><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, a->hb, a->acc, out, dtp, a->mpart, lv, lp); break;
+    default: k_rev<0, REC, SPL><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, a->hb, nullptr, out, nullptr, nullptr, lv, lp); break;
     }
 }
-template <bool GLF>
+template <int SPL>
 void launch_rev_recon(dense_adjoint* a, int stage, const double* u, const double* tape, const double* w,
                       double* out, const double* dtp, cudaStream_t s) {
     switch (a->cfg.recon) {
-    case DENSE_RECON_UPWIND5: launch_rev<DENSE_RECON_UPWIND5, GLF>(a, stage, u, tape, w, out, dtp, s); break;
-    case DENSE_RECON_WENOJS5: launch_rev<DENSE_RECON_WENOJS5, GLF>(a, stage, u, tape, w, out, dtp, s); break;
-    default:                  launch_rev<DENSE_RECON_WENOZ5, GLF>(a, stage, u, tape, w, out, dtp, s); break;
+    case DENSE_RECON_UPWIND5: launch_rev<DENSE_RECON_UPWIND5, SPL>(a, stage, u, tape, w, out, dtp, s); break;
+    case DENSE_RECON_WENOJS5: launch_rev<DENSE_RECON_WENOJS5, SPL>(a, stage, u, tape, w, out, dtp, s); break;
+    default:                  launch_rev<DENSE_RECON_WENOZ5, SPL>(a, stage, u, tape, w, out, dtp, s); break;
     }
 }
 
@@ -637,8 +716,9 @@ void vjp(dense_adjoint* a, int stage, const double* u, const double* tape, const
         a->launches += 2;
     }
     k_hbar<<<a->gh, dim3(kHX, kHY), 0, s>>>(a->ap, w, tape, a->hb, part);
-    if (glf) launch_rev_recon<true>(a, stage, u, tape, w, out, dtp, s);
-    else     launch_rev_recon<false>(a, stage, u, tape, w, out, dtp, s);
+    if (glf) launch_rev_recon<1>(a, stage, u, tape, w, out, dtp, s);
+    else if (a->cfg.splitting == DENSE_SPLIT_SW) launch_rev_recon<2>(a, stage, u, tape, w, out, dtp, s);
+    else launch_rev_recon<0>(a, stage, u, tape, w, out, dtp, s);
     a->launches += 2;
     if (glf) {
         switch (stage) {
@@ -708,8 +788,8 @@ void dense_adjoint_destroy(dense_adjoint_t* a) {
 int dense_adjoint_create(const dense_config_t* cfg, int checkpoint_every, dense_adjoint_t** out) {
     if (!out || !cfg) return aerr(nullptr, DENSE_ERR_ARG, "null argument");
     *out = nullptr;
-    if (cfg->splitting != DENSE_SPLIT_LLF && cfg->splitting != DENSE_SPLIT_GLF)
-        return aerr(nullptr, DENSE_ERR_ARG, "the adjoint covers the LLF and GLF splittings (101, 102)");
+    if (cfg->splitting != DENSE_SPLIT_LLF && cfg->splitting != DENSE_SPLIT_GLF && cfg->splitting != DENSE_SPLIT_SW)
+        return aerr(nullptr, DENSE_ERR_ARG, "the adjoint covers the LLF, GLF and Steger-Warming splittings (101-103)");
     if (cfg->recon != DENSE_RECON_UPWIND5 && cfg->recon != DENSE_RECON_WENOJS5 && cfg->recon != DENSE_RECON_WENOZ5)
         return aerr(nullptr, DENSE_ERR_ARG, "the adjoint covers reconstructions 251, 253 and 255");
     if (cfg->benchmark != DENSE_BENCH_IVC_PERIODIC && cfg->benchmark != DENSE_BENCH_RM_PERIODIC)

@@ -67,7 +67,7 @@ struct Params {
     // of the next stage's boundary fill (set by periodic_ghosts() below)
     int periodic_ghosts;
     int count_branches;  // accumulate Scalars::branch_count in the AdaWENO sweeps
-    // Tape of the component-wise LLF sweeps for the discrete adjoint (flux_tape launches only):
+    // Tape of the component-wise LLF/GLF/SW sweeps for the discrete adjoint (flux_tape launches only):
     // per direction tape_planes(recon) planes of the direction's face array (xi [nj][ni+1], eta
     // [nj+1][ni], eta after xi): the reconstructions' stencil gradients g[(s*5 + m)*4 + v] (s = 0
     // for F+, 1 for F-; none for upwind5, whose gradient is constant), then the fluxes h[v].
@@ -108,8 +108,8 @@ struct KernelTable {
     void (*step_end)(const Params&, void* stream);
     // kernel launches issued by flux(dir) for this configuration
     int (*flux_launches)(const Params&, int dir);
-    // flux(dir) of the component-wise LLF/GLF sweeps with reconstruction 251/253/255 that also
-    // writes Params::tape; identical fluxes and state updates
+    // flux(dir) of the component-wise LLF/GLF/Steger-Warming sweeps with reconstruction
+    // 251/253/255 that also writes Params::tape; identical fluxes and state updates
     void (*flux_tape)(const Params&, int irk, int dir, void* stream);
 };
 

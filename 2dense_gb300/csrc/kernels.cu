@@ -1692,11 +1692,12 @@ static void launch_flux(const Params& p, int irk, int dir, void* stream) {
 // flux(dir) plus the adjoint tape: LLF/GLF with reconstruction 251, 253 or 255 only
 static void launch_flux_tape(const Params& p, int irk, int dir, void* stream) {
     cudaStream_t s = (cudaStream_t)stream;
-    if (p.splitting != DENSE_SPLIT_LLF && p.splitting != DENSE_SPLIT_GLF) return;
+    if (p.splitting != DENSE_SPLIT_LLF && p.splitting != DENSE_SPLIT_GLF && p.splitting != DENSE_SPLIT_SW) return;
+    const bool sw = p.splitting == DENSE_SPLIT_SW;
     switch (p.recon) {
-    case DENSE_RECON_UPWIND5: launch_cw<0, 251, true>(p, irk, dir, s); break;
-    case DENSE_RECON_WENOJS5: launch_cw<0, 253, true>(p, irk, dir, s); break;
-    case DENSE_RECON_WENOZ5:  launch_cw<0, 255, true>(p, irk, dir, s); break;
+    case DENSE_RECON_UPWIND5: sw ? launch_cw<1, 251, true>(p, irk, dir, s) : launch_cw<0, 251, true>(p, irk, dir, s); break;
+    case DENSE_RECON_WENOJS5: sw ? launch_cw<1, 253, true>(p, irk, dir, s) : launch_cw<0, 253, true>(p, irk, dir, s); break;
+    case DENSE_RECON_WENOZ5:  sw ? launch_cw<1, 255, true>(p, irk, dir, s) : launch_cw<0, 255, true>(p, irk, dir, s); break;
     default:
         break;
     }
@@ -1831,12 +1832,11 @@ static void allow_cw_smem() {
     allow_smem(k_flux_cw<0, SPL, REC, kXTX, kXSTY>, CwTile<0, REC, kXTX, kXSTY>::bytes);
     allow_smem(k_flux_cw<1, SPL, REC, kETX, kETY>, CwTile<1, REC, kETX, kETY>::bytes);
     allow_smem(k_flux_cw<1, SPL, REC, kETX, kESTY>, CwTile<1, REC, kETX, kESTY>::bytes);
-    if (SPL == 0) {  // the adjoint's taping sweeps
-        allow_smem(k_flux_cw<0, 0, REC, kXTX, kXTY, true>, CwTile<0, REC, kXTX, kXTY>::bytes);
-        allow_smem(k_flux_cw<0, 0, REC, kXTX, kXSTY, true>, CwTile<0, REC, kXTX, kXSTY>::bytes);
-        allow_smem(k_flux_cw<1, 0, REC, kETX, kETY, true>, CwTile<1, REC, kETX, kETY>::bytes);
-        allow_smem(k_flux_cw<1, 0, REC, kETX, kESTY, true>, CwTile<1, REC, kETX, kESTY>::bytes);
-    }
+    // the adjoint's taping sweeps
+    allow_smem(k_flux_cw<0, SPL, REC, kXTX, kXTY, true>, CwTile<0, REC, kXTX, kXTY>::bytes);
+    allow_smem(k_flux_cw<0, SPL, REC, kXTX, kXSTY, true>, CwTile<0, REC, kXTX, kXSTY>::bytes);
+    allow_smem(k_flux_cw<1, SPL, REC, kETX, kETY, true>, CwTile<1, REC, kETX, kETY>::bytes);
+    allow_smem(k_flux_cw<1, SPL, REC, kETX, kESTY, true>, CwTile<1, REC, kETX, kESTY>::bytes);
     // the batched tile variants of batch_cw_variant
     allow_smem(kb_flux_cw<0, SPL, REC, 32, 4>, CwTile<0, REC, 32, 4>::bytes);
     allow_smem(kb_flux_cw<0, SPL, REC, 64, 2>, CwTile<0, REC, 64, 2>::bytes);

@@ -30,7 +30,7 @@ def perturbed_state(dense, cfg, seed=0, amp=1e-3):
 
 
 @pytest.mark.parametrize("split,recon", [(101, 251), (101, 253), (101, 255), (102, 251), (102, 253),
-                                         (102, 255)])
+                                         (102, 255), (103, 251), (103, 253), (103, 255)])
 def test_rhs_vjp_matches_autograd(dense, adjoint, split, recon):
     cfg = vortex_cfg(dense, recon, ni=24, nj=20, var_eps=4.0, var_xc=4.6, var_yc=5.3, splitting=split)
     c, U = perturbed_state(dense, cfg)
@@ -47,7 +47,8 @@ def test_rhs_vjp_matches_autograd(dense, adjoint, split, recon):
 
 
 @pytest.mark.parametrize("split,recon,const_dt", [(101, 253, 0), (101, 255, 0), (101, 251, 0), (101, 253, 1),
-                                                  (102, 253, 0), (102, 255, 0), (102, 251, 1)])
+                                                  (102, 253, 0), (102, 255, 0), (102, 251, 1),
+                                                  (103, 253, 0), (103, 255, 0)])
 def test_steps_gradient_matches_autograd(dense, adjoint, split, recon, const_dt):
     """7 steps with checkpoints every 3: two full segments and a partial one."""
     cfg = vortex_cfg(dense, recon, ni=24, nj=20, var_eps=4.0, var_xc=4.6, var_yc=5.3,
@@ -74,7 +75,7 @@ def padded(U):
     return cons
 
 
-@pytest.mark.parametrize("split,recon", [(101, 251), (101, 253), (101, 255), (102, 255)])
+@pytest.mark.parametrize("split,recon", [(101, 251), (101, 253), (101, 255), (102, 255), (103, 253)])
 def test_taped_recompute_reproduces_the_forward(dense, adjoint, split, recon):
     """The taping sweeps of the reverse pass recompute each segment bit for bit: after a
     backward the solver holds the state after the first segment, equal to a plain solve, and the
@@ -110,7 +111,7 @@ def test_backward_is_deterministic_and_repeatable(dense, adjoint):
     assert torch.equal(a, b)
 
 
-@pytest.mark.parametrize("split", [101, 102])
+@pytest.mark.parametrize("split", [101, 102, 103])
 def test_autograd_function_in_a_graph(dense, adjoint, split):
     """Loss 1/2 ||rho(T) - rho_target||^2 of a vortex built from (eps, xc, yc) by torch ops:
     autograd chains the vortex's derivatives with the adjoint; checked against central

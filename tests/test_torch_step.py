@@ -23,7 +23,8 @@ def vortex_cfg(dense, recon, ni=24, nj=20, **kw):
     return dense.config_default(**base)
 
 
-@pytest.mark.parametrize("split,recon", [(101, 251), (101, 253), (101, 255), (102, 253), (102, 255)])
+@pytest.mark.parametrize("split,recon", [(101, 251), (101, 253), (101, 255), (102, 253), (102, 255),
+                                         (103, 251), (103, 255)])
 def test_torch_step_matches_oracle(dense, orc, split, recon):
     cfg = vortex_cfg(dense, recon, var_eps=4.0, var_xc=4.6, var_yc=5.3, splitting=split)
     c, cons, prim, x, y = dense.init_general(cfg)

@@ -4,7 +4,9 @@ adjoint kernels against autograd (test infrastructure; never used by the library
 Same scheme as the plain solver: get_primary (get_primary.f90:53-60), LLF splitting with
 lambda = |u_n| + alpha per cell (flux_splitting_LLF.f90:67-81) or GLF splitting with lambda the
 maximum of |u_n| + alpha over the stage's input (flux_splitting_GLF.f90:13-70, the max_eig_i/j of
-get_primary.f90:69-73), upwind5 / WENO-JS5 / WENO-Z5
+get_primary.f90:69-73), or Steger-Warming splitting with the three eigenvalues u_n, u_n -+ alpha
+split as (l +- sqrt(l^2 + eps^2))/2, eps = 0.125 (flux_splitting_SW.f90:14-168), upwind5 /
+WENO-JS5 / WENO-Z5
 reconstruction of F+ and F- at each face (scheme_*_general.f90, weno_mod.f90), the flux
 difference, and TVD-RK3 (time_advance_general.f90:9-267) with dt = cfl/(max(|u|+alpha)/dx +
 max(|v|+alpha)/dy) of the step's input (or a constant dt). States are (4, nj, ni) tensors of the
@@ -50,18 +52,44 @@ def primitives(U, gamma):
     return rho, u, v, p, a
 
 
+def steger_warming(rho, u, v, a, gamma, d):
+    """(F+, F-) of the Steger-Warming splitting in direction d (0: x, 1: y)."""
+    eps2 = 0.125 ** 2
+    g1 = gamma - 1.0
+    un, ut = (u, v) if d == 0 else (v, u)
+    l1, l2, l3 = un, un - a, un + a
+    s1, s2, s3 = (torch.sqrt(l * l + eps2) for l in (l1, l2, l3))
+    uu2 = u * u + v * v
+    q2, q3 = l2 * l2 + ut * ut, l3 * l3 + ut * ut
+    out = []
+    for sg in (1.0, -1.0):
+        p1, p2, p3 = (l1 + sg * s1) / 2.0, (l2 + sg * s2) / 2.0, (l3 + sg * s3) / 2.0
+        wii = (3.0 - gamma) * (p2 + p3) * a * a / (2.0 * g1)
+        A = p1 * 2.0 * g1
+        c = rho / (2.0 * gamma)
+        f0 = (A + p2 + p3) * c
+        fn = (A * un + p2 * l2 + p3 * l3) * c
+        ft = (A * ut + p2 * ut + p3 * ut) * c
+        f3 = (p1 * g1 * uu2 + p2 * 0.5 * q2 + p3 * 0.5 * q3 + wii) * c
+        out.append(torch.stack([f0, fn, ft, f3] if d == 0 else [f0, ft, fn, f3]))
+    return out
+
+
 def rhs(U, gamma, dx, dy, rec, split=101):
     """L(U) = -(h_{i+1/2} - h_{i-1/2})/dx - (g_{j+1/2} - g_{j-1/2})/dy."""
     rho, u, v, p, a = primitives(U, gamma)
     out = torch.zeros_like(U)
     for d, (un, h, axis) in enumerate(((u, dx, 2), (v, dy, 1))):
-        lam = un.abs() + a
-        if split == 102:
-            lam = lam.max()
-        P = torch.stack([torch.zeros_like(p), p if d == 0 else torch.zeros_like(p),
-                         p if d == 1 else torch.zeros_like(p), un * p])
-        Fp = 0.5 * ((un + lam) * U + P)
-        Fm = 0.5 * ((un - lam) * U + P)
+        if split == 103:
+            Fp, Fm = steger_warming(rho, u, v, a, gamma, d)
+        else:
+            lam = un.abs() + a
+            if split == 102:
+                lam = lam.max()
+            P = torch.stack([torch.zeros_like(p), p if d == 0 else torch.zeros_like(p),
+                             p if d == 1 else torch.zeros_like(p), un * p])
+            Fp = 0.5 * ((un + lam) * U + P)
+            Fm = 0.5 * ((un - lam) * U + P)
         sh = lambda F, k: torch.roll(F, shifts=-k, dims=axis)  # element f holds F[f + k]
         # face f (left of cell f): F+ of cells f-3..f+1, F- of cells f+2..f-2
         hp = _recon([sh(Fp, k) for k in (-3, -2, -1, 0, 1)], rec)
