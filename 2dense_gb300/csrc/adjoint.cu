@@ -375,13 +375,12 @@ __global__ void __launch_bounds__(128) k_rev(AdjParams a, const double* __restri
         const Prim q = prim_of(U, a.gamma);
         double gpx[4] = {0, 0, 0, 0}, gmx[4] = {0, 0, 0, 0}, gpy[4] = {0, 0, 0, 0}, gmy[4] = {0, 0, 0, 0};
         gather_line<REC>(tape, hb, a.xs, (long long)j * (ni + 1), 1, i, ni, gpx, gmx);
+        // LF splittings pull each direction back before gathering the next (fewer live
+        // registers); Steger-Warming seeds each variable once for both directions
+        if (SPL != 2) lbx = llf_vjp<0, GLF>(U, q, a.gamma, gpx, gmx, GLF ? lamv[0] : 0.0, Ub);
         gather_line<REC>(tape + a.np * a.xs, hb + 4 * a.xs, a.ys, i, ni, j, nj, gpy, gmy);
-        if (SPL == 2) {
-            sw_vjp(U, a.gamma, gpx, gmx, gpy, gmy, Ub);
-        } else {
-            lbx = llf_vjp<0, GLF>(U, q, a.gamma, gpx, gmx, GLF ? lamv[0] : 0.0, Ub);
-            lby = llf_vjp<1, GLF>(U, q, a.gamma, gpy, gmy, GLF ? lamv[1] : 0.0, Ub);
-        }
+        if (SPL != 2) lby = llf_vjp<1, GLF>(U, q, a.gamma, gpy, gmy, GLF ? lamv[1] : 0.0, Ub);
+        else          sw_vjp(U, a.gamma, gpx, gmx, gpy, gmy, Ub);
         const double dt = STAGE == 0 ? 0.0 : *dtp;
 #pragma unroll
         for (int v = 0; v < 4; ++v) {

@@ -174,34 +174,6 @@ __device__ __forceinline__ void betas_fast(const double lf[5], double& d0, doubl
     tau = fabs(d2 - d0);
 }
 
-// Weight numerators n_k = alpha_k D and their sum N = (sum alpha) D, from d_k = ss + beta_k.
-template <bool Z>
-__device__ __forceinline__ void weno_num_from_d(double d0, double d1, double d2, double tau, double& n0,
-                                                double& n1, double& n2, double& N, double& D) {
-    const double e0 = d0 * d0, e1 = d1 * d1, e2 = d2 * d2;
-    const double P0 = e1 * e2, P1 = e0 * e2, P2 = e0 * e1;
-    D = e0 * P0;
-    if (Z) {
-        const double T = tau * tau;
-        n0 = c30 * fma(T, P0, D);
-        n1 = c31 * fma(T, P1, D);
-        n2 = c32 * fma(T, P2, D);
-    } else {
-        n0 = c30 * P0;
-        n1 = c31 * P1;
-        n2 = c32 * P2;
-    }
-    // written as rounded adds: with FMA contraction on, n_k (products) and this sum could fuse
-    // differently in different kernels, and the plain and taping sweeps must agree bit for bit
-    N = __dadd_rn(__dadd_rn(n0, n1), n2);
-}
-
-__device__ __forceinline__ void candidates_fast(const double lf[5], double& q0, double& q1, double& q2) {
-    q0 = fma(a302, lf[2], fma(a301, lf[1], a300 * lf[0]));
-    q1 = fma(a312, lf[3], fma(a311, lf[2], a310 * lf[1]));
-    q2 = fma(a322, lf[4], fma(a321, lf[3], a320 * lf[2]));
-}
-
 // The candidates scaled by the linear weights, c_k q_k (the constants folded together).
 __device__ __forceinline__ void candidates_c(const double lf[5], double& q0, double& q1, double& q2) {
     q0 = fma(c30 * a302, lf[2], fma(c30 * a301, lf[1], (c30 * a300) * lf[0]));
@@ -209,25 +181,39 @@ __device__ __forceinline__ void candidates_c(const double lf[5], double& q0, dou
     q2 = fma(c32 * a322, lf[4], fma(c32 * a321, lf[3], (c32 * a320) * lf[2]));
 }
 
-// WENO reconstruction from d_k = ss + beta_k: h = sum_k v_k (c_k q_k) / sum_k c_k v_k with
-// v_k = alpha_k D / c_k, i.e. P_k (JS) or D + tau^2 P_k (Z), over the common denominator D.
-// Every operation is an explicit FMA or a product feeding one, so no kernel contracts it
-// differently from another (the plain and taping sweeps agree bit for bit); the result is a
-// rounded product, which the caller's sum of the two signs must not fuse with.
+// Terms of a WENO reconstruction from d_k = ss + beta_k that its value and, in the adjoint's
+// taping sweeps, its gradient share: the scaled candidates c_k q_k, e_k = d_k^2, P_k =
+// prod_{j != k} e_j, D = prod e_j, tau = |d_2 - d_0| (= |beta_2 - beta_0|), v_k = alpha_k D / c_k
+// -- P_k (JS) or D + tau^2 P_k (Z) -- and N = sum_k c_k v_k = (sum alpha) D.
+struct WenoTerms {
+    double q[3], P[3], v[3], D, tau, N;
+};
+template <bool Z>
+__device__ __forceinline__ void weno_terms(const double lf[5], double d0, double d1, double d2, WenoTerms& t) {
+    candidates_c(lf, t.q[0], t.q[1], t.q[2]);
+    const double e0 = d0 * d0, e1 = d1 * d1, e2 = d2 * d2;
+    t.P[0] = e1 * e2; t.P[1] = e0 * e2; t.P[2] = e0 * e1;
+    t.D = e0 * t.P[0];
+    const double dd = d2 - d0;
+    t.tau = fabs(dd);
+    const double T = dd * dd;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) t.v[k] = Z ? fma(T, t.P[k], t.D) : t.P[k];
+    t.N = fma(c32, t.v[2], fma(c31, t.v[1], c30 * t.v[0]));
+}
+// h = sum_k v_k (c_k q_k) / N with iN = 1/N. Every operation is an explicit FMA or a product
+// feeding one, so no kernel contracts it differently from another (the plain and taping sweeps
+// agree bit for bit); the result is a rounded product, which the caller's sum of the two signs
+// must not fuse with.
+__device__ __forceinline__ double weno_value(const WenoTerms& t, double iN) {
+    return __dmul_rn(fma(t.v[2], t.q[2], fma(t.v[1], t.q[1], t.v[0] * t.q[0])), iN);
+}
+// WENO reconstruction from d_k = ss + beta_k.
 template <bool Z>
 __device__ __forceinline__ double weno_from_d(const double lf[5], double d0, double d1, double d2) {
-    double q0, q1, q2;
-    candidates_c(lf, q0, q1, q2);
-    const double e0 = d0 * d0, e1 = d1 * d1, e2 = d2 * d2;
-    double v0 = e1 * e2, v1 = e0 * e2, v2 = e0 * e1;
-    if (Z) {
-        const double D = e0 * v0, dd = d2 - d0, T = dd * dd;
-        v0 = fma(T, v0, D);
-        v1 = fma(T, v1, D);
-        v2 = fma(T, v2, D);
-    }
-    const double N = fma(c32, v2, fma(c31, v1, c30 * v0));
-    return __dmul_rn(fma(v2, q2, fma(v1, q1, v0 * q0)), rcp_nr(N));
+    WenoTerms t;
+    weno_terms<Z>(lf, d0, d1, d2, t);
+    return weno_value(t, rcp_nr(t.N));
 }
 
 template <bool Z> __device__ __forceinline__ double weno_fast(const double lf[5]) {
@@ -281,28 +267,22 @@ __device__ __forceinline__ void stencil_from_u(double u0, double u2, double W[5]
 // da_k/dbeta_k = -2 a_k/d_k; Z: a_k = c_k (1 + tau^2/d_k^2), so da_k/dbeta_k = -2 c_k tau^2/d_k^3
 // and da_k/dtau = 2 c_k tau/d_k^2, tau = |beta_2 - beta_0|; d_k = ss + beta_k), and beta_k =
 // 13/12 A_k^2 + 1/4 B_k^2 on the second differences A_k and the first-order combinations B_k.
-// Written over the common denominators of weno_num_from_d (n_k = a_k D, N = sum(a) D, D = prod
-// d_k^2, P_k = D/d_k^2), with the quantities W itself needs computed by the same expressions.
-// The caller passes d_k = ss + beta_k as its own reconstruction computed them, so that the two
-// share every common term.
-template <int REC>
-__device__ __forceinline__ void recon_grad(const double lf[5], double d0, double d1, double d2, double g[5]) {
-    if (REC == DENSE_RECON_UPWIND5) {
-        g[0] = 2.0 / 60.0; g[1] = -13.0 / 60.0; g[2] = 47.0 / 60.0; g[3] = 27.0 / 60.0; g[4] = -3.0 / 60.0;
-        return;
+// Written over the terms the value itself uses (weno_terms: w_k = c_k v_k / N, and
+// (q_k - W) c_k = c_k q_k - c_k W), with h and iN = 1/N as the value computed them, so that the
+// taping sweep evaluates every shared term once.
+template <bool Z>
+__device__ __forceinline__ void weno_grad(const double lf[5], double d0, double d1, double d2, const WenoTerms& t,
+                                          double h, double iN, double g[5]) {
+    constexpr double cs[3] = {c30, c31, c32};
+    double E[3], u[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        E[k] = fma(-cs[k], h, t.q[k]);  // (q_k - h) c_k
+        u[k] = t.v[k] * iN;             // w_k / c_k
     }
-    constexpr bool Z = REC == DENSE_RECON_WENOZ5;
-    double q0, q1, q2, n0, n1, n2, N, D;
-    const double tau = fabs(d2 - d0);
-    candidates_fast(lf, q0, q1, q2);
-    weno_num_from_d<Z>(d0, d1, d2, tau, n0, n1, n2, N, D);
-    const double iN = rcp_nr(N);
-    const double h = fma(n2, q2, fma(n1, q1, n0 * q0)) * iN;
-    const double w0 = n0 * iN, w1 = n1 * iN, w2 = n2 * iN;
-    const double e0 = d0 * d0, e1 = d1 * d1, e2 = d2 * d2;
-    const double P0 = e1 * e2, P1 = e0 * e2, P2 = e0 * e1;
-    const double iD = rcp_nr(D);
-    const double id0 = d0 * (P0 * iD), id1 = d1 * (P1 * iD), id2 = d2 * (P2 * iD);  // 1/d_k
+    const double w0 = c30 * u[0], w1 = c31 * u[1], w2 = c32 * u[2];
+    const double iD = rcp_nr(t.D);
+    const double id0 = d0 * (t.P[0] * iD), id1 = d1 * (t.P[1] * iD), id2 = d2 * (t.P[2] * iD);  // 1/d_k
     const double A0 = fma(-2.0, lf[1], lf[0]) + lf[2], B0 = fma(3.0, lf[2], fma(-4.0, lf[1], lf[0]));
     const double A1 = fma(-2.0, lf[2], lf[1]) + lf[3], B1 = lf[1] - lf[3];
     const double A2 = fma(-2.0, lf[3], lf[2]) + lf[4], B2 = fma(3.0, lf[2], fma(-4.0, lf[3], lf[4]));
@@ -310,14 +290,16 @@ __device__ __forceinline__ void recon_grad(const double lf[5], double d0, double
     // share of dW/dlf is -13/3 r_k A_k dA_k/dlf - r_k B_k dB_k/dlf.
     double r0, r1, r2;
     if (!Z) {
-        r0 = (q0 - h) * (w0 * id0);
-        r1 = (q1 - h) * (w1 * id1);
-        r2 = (q2 - h) * (w2 * id2);
+        // (q_k - W) w_k / d_k = E_k u_k / d_k
+        r0 = (E[0] * u[0]) * id0;
+        r1 = (E[1] * u[1]) * id1;
+        r2 = (E[2] * u[2]) * id2;
     } else {
-        // s_k = (q_k - W)/sum(a) * c_k tau / d_k^2 = (q_k - W) c_k tau P_k / N
-        const double s0 = (q0 - h) * (c30 * tau) * (P0 * iN);
-        const double s1 = (q1 - h) * (c31 * tau) * (P1 * iN);
-        const double s2 = (q2 - h) * (c32 * tau) * (P2 * iN);
+        // s_k = (q_k - W)/sum(a) * c_k tau / d_k^2 = E_k tau P_k / N
+        const double tau = t.tau;
+        const double s0 = (E[0] * tau) * (t.P[0] * iN);
+        const double s1 = (E[1] * tau) * (t.P[1] * iN);
+        const double s2 = (E[2] * tau) * (t.P[2] * iN);
         // dW/dtau = 2 (s0 + s1 + s2); dtau/dbeta_2 = -dtau/dbeta_0 = sign(beta_2 - beta_0)
         const double sh = d2 >= d0 ? s0 + s1 + s2 : -(s0 + s1 + s2);
         r0 = fma(s0 * tau, id0, sh);
@@ -333,6 +315,19 @@ __device__ __forceinline__ void recon_grad(const double lf[5], double d0, double
     g[2] = fma(a302, w0, fma(a311, w1, fma(a320, w2, fma(k, PA0, fma(-2.0 * k, PA1, fma(k, PA2, -3.0 * (NB0 + NB2)))))));
     g[3] = fma(a312, w1, fma(a321, w2, fma(k, PA1, fma(-2.0 * k, PA2, fma(4.0, NB2, NB1)))));
     g[4] = fma(a322, w2, fma(k, PA2, -NB2));
+}
+// The gradient alone (upwind5's is constant): the terms and value recomputed.
+template <int REC>
+__device__ __forceinline__ void recon_grad(const double lf[5], double d0, double d1, double d2, double g[5]) {
+    if (REC == DENSE_RECON_UPWIND5) {
+        g[0] = 2.0 / 60.0; g[1] = -13.0 / 60.0; g[2] = 47.0 / 60.0; g[3] = 27.0 / 60.0; g[4] = -3.0 / 60.0;
+        return;
+    }
+    constexpr bool Z = REC == DENSE_RECON_WENOZ5;
+    WenoTerms t;
+    weno_terms<Z>(lf, d0, d1, d2, t);
+    const double iN = rcp_nr(t.N);
+    weno_grad<Z>(lf, d0, d1, d2, t, weno_value(t, iN), iN, g);
 }
 
 template <int REC> __device__ __forceinline__ double recon5(const double lf[5]) {
@@ -700,13 +695,29 @@ __device__ __forceinline__ void flux_cw_block(const Params& p, int irk, int bx, 
             constexpr bool Z = REC == DENSE_RECON_WENOZ5;
             const double* Sp = sS + v * NCELL;
             const double* Sm = sS + (4 + v) * NCELL;
+            // the value, and for the tape its gradient from the same terms
+            auto recon_taped = [&](const double lf[5], double d0, double d1, double d2, int m0) -> double {
+                if constexpr (TAPE) {
+                    WenoTerms tt;
+                    weno_terms<Z>(lf, d0, d1, d2, tt);
+                    const double iN = rcp_nr(tt.N);
+                    const double hv = weno_value(tt, iN);
+                    const long long ts = DIR == 0 ? (long long)p.nj * (p.ni + 1) : (long long)(p.nj + 1) * p.ni;
+                    double g[5];
+                    weno_grad<Z>(lf, d0, d1, d2, tt, hv, iN, g);
+#pragma unroll
+                    for (int m = 0; m < 5; ++m) tape_at[((m0 + m) * 4 + v) * ts] = g[m];
+                    return hv;
+                } else {
+                    (void)m0;
+                    return weno_from_d<Z>(lf, d0, d1, d2);
+                }
+            };
             double d0, d1, d2;
             betas_staged(lp, Sp[atk(t + 1)], Sp[atk(t + 2)], Sp[atk(t + 3)], d0, d1, d2);
-            const double hp = weno_from_d<Z>(lp, d0, d1, d2);
-            tape_grad(lp, d0, d1, d2, 0);
+            const double hp = recon_taped(lp, d0, d1, d2, 0);
             betas_staged(lm, Sm[atk(t + 4)], Sm[atk(t + 3)], Sm[atk(t + 2)], d0, d1, d2);
-            const double hm = weno_from_d<Z>(lm, d0, d1, d2);
-            tape_grad(lm, d0, d1, d2, 5);
+            const double hm = recon_taped(lm, d0, d1, d2, 5);
             h = hp + hm;
         } else {
             h = recon5<REC>(lp) + recon5<REC>(lm);
@@ -1169,11 +1180,15 @@ __device__ __forceinline__ void prim_cell(const Params& p, long long o, const do
 #else
     double pr = (p.gamma - 1.0) * (q[3] - 0.5 * rho * (u * u + v * v));
 #endif
-    if (pr < 0.0) { pr = kPFloor; flags |= DENSE_FLAG_P_FLOOR; }
 #if FAST
+    // pr < 0 and a2 > 0 tested on the bit patterns (integer pipe, not an FP64 compare): pr < 0
+    // is a set sign bit on a nonzero, non-NaN value; a NaN a2 takes either branch to NaN
+    const long long pb = __double_as_longlong(pr), pm = pb & 0x7fffffffffffffffLL;
+    if (pb < 0 && pm != 0 && pm <= 0x7ff0000000000000LL) { pr = kPFloor; flags |= DENSE_FLAG_P_FLOOR; }
     const double a2 = p.gamma * pr * ir;
-    const double alpha = a2 > 0.0 ? a2 * rsqrt_nr(a2) : sqrt(a2);
+    const double alpha = __double_as_longlong(a2) > 0 ? a2 * rsqrt_nr(a2) : sqrt(a2);
 #else
+    if (pr < 0.0) { pr = kPFloor; flags |= DENSE_FLAG_P_FLOOR; }
     const double alpha = sqrt(p.gamma * pr / rho);
 #endif
     p.prim[o] = rho;
