@@ -55,6 +55,15 @@ __global__ void k_set_time(Scalars* sc, double t, long long step) {
 }
 __global__ void k_set_active(Scalars* sc) { sc->active = 1; }
 
+// A stack of rows between the padded device layout (row pitch P) and the caller's Fortran
+// layout (rows of NIp doubles): one contiguous copy when the pitches agree (NIp even), a pitched
+// copy otherwise.
+cudaError_t copy_rows(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t rows,
+                      cudaMemcpyKind kind, cudaStream_t s) {
+    if (dpitch == width && spitch == width) return cudaMemcpyAsync(dst, src, width * rows, kind, s);
+    return cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, rows, kind, s);
+}
+
 bool valid_split(int s) { return s >= DENSE_SPLIT_LLF && s <= DENSE_SPLIT_SC; }
 bool valid_bench(int b) {
     return b == 0 || (b >= 1 && b <= 9) || b == DENSE_BENCH_IVC_PERIODIC || b == DENSE_BENCH_RT_REFLECT ||
@@ -299,9 +308,9 @@ int dense_upload(dense_handle_t* h, const double* cons, const double* prim, cons
     const dense_config_t& c = h->cfg;
     const size_t row = (size_t)h->NIp * sizeof(double), pitch = (size_t)h->P * sizeof(double);
     // Fortran cons(NIp,NJp,4) is a stack of 4*NJp rows of NIp doubles: one pitched copy
-    CK(h, cudaMemcpy2DAsync(h->cons, pitch, cons, row, row, (size_t)h->NJp * 4, cudaMemcpyHostToDevice, h->stream));
+    CK(h, copy_rows(h->cons, pitch, cons, row, row, (size_t)h->NJp * 4, cudaMemcpyHostToDevice, h->stream));
     if (prim) {
-        CK(h, cudaMemcpy2DAsync(h->prim, pitch, prim, row, row, (size_t)h->NJp * 5, cudaMemcpyHostToDevice, h->stream));
+        CK(h, copy_rows(h->prim, pitch, prim, row, row, (size_t)h->NJp * 5, cudaMemcpyHostToDevice, h->stream));
     } else {
         CK(h, cudaMemsetAsync(h->prim, 0, (size_t)h->NJp * h->P * 5 * sizeof(double), h->stream));
     }
@@ -371,9 +380,9 @@ int dense_download(dense_handle_t* h, double* cons, double* prim) {
     if (!h->uploaded) return seterr(h, DENSE_ERR_STATE, "dense_download before dense_upload");
     const size_t row = (size_t)h->NIp * sizeof(double), pitch = (size_t)h->P * sizeof(double);
     if (cons)
-        CK(h, cudaMemcpy2DAsync(cons, row, h->cons, pitch, row, (size_t)h->NJp * 4, cudaMemcpyDeviceToHost, h->stream));
+        CK(h, copy_rows(cons, row, h->cons, pitch, row, (size_t)h->NJp * 4, cudaMemcpyDeviceToHost, h->stream));
     if (prim)
-        CK(h, cudaMemcpy2DAsync(prim, row, h->prim, pitch, row, (size_t)h->NJp * 5, cudaMemcpyDeviceToHost, h->stream));
+        CK(h, copy_rows(prim, row, h->prim, pitch, row, (size_t)h->NJp * 5, cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
     if (prim) {
         // entropy log(p)-log(rho) of the interior (get_primary.f90:67); ghosts hold 0
@@ -547,9 +556,9 @@ int dense_upload_device(dense_handle_t* h, const double* cons, const double* pri
     int rc = wait_for(h, stream);
     if (rc) return rc;
     const size_t row = (size_t)h->NIp * sizeof(double), pitch = (size_t)h->P * sizeof(double);
-    CK(h, cudaMemcpy2DAsync(h->cons, pitch, cons, row, row, (size_t)h->NJp * 4, cudaMemcpyDeviceToDevice, h->stream));
+    CK(h, copy_rows(h->cons, pitch, cons, row, row, (size_t)h->NJp * 4, cudaMemcpyDeviceToDevice, h->stream));
     if (prim)
-        CK(h, cudaMemcpy2DAsync(h->prim, pitch, prim, row, row, (size_t)h->NJp * 5, cudaMemcpyDeviceToDevice, h->stream));
+        CK(h, copy_rows(h->prim, pitch, prim, row, row, (size_t)h->NJp * 5, cudaMemcpyDeviceToDevice, h->stream));
     h->uploaded = true;
     h->prim_slot = -1;
     rc = ensure_prim(h, 0);
@@ -565,9 +574,9 @@ int dense_download_device(dense_handle_t* h, double* cons, double* prim, void* s
     if (rc) return rc;
     const size_t row = (size_t)h->NIp * sizeof(double), pitch = (size_t)h->P * sizeof(double);
     if (cons)
-        CK(h, cudaMemcpy2DAsync(cons, row, h->cons, pitch, row, (size_t)h->NJp * 4, cudaMemcpyDeviceToDevice, h->stream));
+        CK(h, copy_rows(cons, row, h->cons, pitch, row, (size_t)h->NJp * 4, cudaMemcpyDeviceToDevice, h->stream));
     if (prim)
-        CK(h, cudaMemcpy2DAsync(prim, row, h->prim, pitch, row, (size_t)h->NJp * 5, cudaMemcpyDeviceToDevice, h->stream));
+        CK(h, copy_rows(prim, row, h->prim, pitch, row, (size_t)h->NJp * 5, cudaMemcpyDeviceToDevice, h->stream));
     return signal_to(h, stream);
 }
 
@@ -608,7 +617,7 @@ int dense_stage_device(dense_handle_t* h, int irk, const double* cons0, double* 
     if (rc) return rc;
     if (irk > 1) {
         const size_t row = (size_t)h->NIp * sizeof(double), pitch = (size_t)h->P * sizeof(double);
-        CK(h, cudaMemcpy2DAsync(h->cons0, pitch, cons0, row, row, (size_t)h->NJp * 4, cudaMemcpyDeviceToDevice,
+        CK(h, copy_rows(h->cons0, pitch, cons0, row, row, (size_t)h->NJp * 4, cudaMemcpyDeviceToDevice,
                                 h->stream));
     }
     rc = ensure_prim(h, irk - 1);
