@@ -1,12 +1,14 @@
 // adjoint.cu — the discrete adjoint of the plain solver's time step: LLF, GLF or Steger-Warming
 // splitting (101, 102, 103) with upwind5 / WENO-JS5 / WENO-Z5 reconstruction (251/253/255) and
-// TVD-RK3 with the CFL time step, on grids periodic in x and y (benchmarks 11 and 14).
+// TVD-RK3 with the CFL time step, on grids periodic in x and y (benchmarks 11 and 14) or with
+// extrapolated and mirror sides (benchmarks 1, 2, 4, 9; wall_terms).
 //
 // The forward step (time_rk3_general, time_advance_general.f90:9-267) applies per stage
 //     L(u)_c = -(h_{f+1} - h_f)/dx - (g_{f'+1} - g_{f'})/dy,     cell c between faces f, f+1,
 //     h_f = W(F+ of cells f-3..f+1) + W(F- of cells f+2..f-2)    (cells in interior indices,
-// ghosts are periodic images), F+- = 0.5((u_n +- lambda) U + P), lambda = |u_n| + alpha of the
-// cell (flux_splitting_LLF.f90:67-81), W one of the 5-point reconstructions
+// ghosts are periodic images or built by a wall rule), F+- = 0.5((u_n +- lambda) U + P),
+// lambda = |u_n| + alpha of the cell (flux_splitting_LLF.f90:67-81), W one of the 5-point
+// reconstructions
 // (scheme_weno5js_general.f90, scheme_weno5z_general.f90, scheme_upwind5_general.f90), and
 //     u1 = u0 + dt L(u0),  u2 = 3/4 u0 + 1/4 u1 + 1/4 dt L(u1),  u3 = 1/3 u0 + 2/3 u2 + 2/3 dt L(u2)
 // with dt = cfl / (max(|u|+alpha)/dx + max(|v|+alpha)/dy) of u0.
@@ -62,7 +64,13 @@ struct AdjParams {
     long long xs, ys; // face planes: xi nj (ni+1), eta (nj+1) ni
     int np;           // tape planes per direction (tape_planes)
     double gamma, dx, dy, inv_dx, inv_dy, cfl;
+    int rule[4];      // ghost rule of each side (bottom, top, left, right): kRulePeriodic, ...
 };
+// Ghost rules of the benchmarks the adjoint covers (boundary_*_general.f90): a periodic copy,
+// the recursive 4/3, -1/3 extrapolation of the two cells next to the side, or the mirror of the
+// four cells next to it with the normal velocity negated -- applied to the conserved variables
+// and, separately, to the primitives.
+constexpr int kRulePeriodic = 0, kRuleExtrap = 1, kRuleReflect = 2;
 
 // get_primary of one cell (get_primary.f90:53-60), with the pressure floor of :58; rs = 1/alpha'
 // with alpha'^2 = gamma p / rho, so that alpha = alpha'^2 rs and dalpha/dp = gamma/(2 rho) rs.
@@ -82,6 +90,24 @@ __device__ __forceinline__ Prim prim_of(const double U[4], double gamma) {
     q.rs = rsqrt_nr(a2);
     q.a = a2 * q.rs;
     return q;
+}
+
+// Sensitivities of all primitives (rho, u, v, p, alpha) pulled back to the conserved variables.
+__device__ __forceinline__ void prim_pullback_all(const double U[4], const Prim& q, double gamma, double rhob,
+                                                  double ub, double vb, double pb, double ab, double Ub[4]) {
+    double rb = rhob - ab * 0.5 * q.a * q.ir;
+    if (!q.floored) pb += ab * (0.5 * gamma) * q.ir * q.rs;
+    Ub[1] += ub * q.ir;
+    Ub[2] += vb * q.ir;
+    rb -= (ub * q.u + vb * q.v) * q.ir;
+    if (!q.floored) {
+        const double g1 = gamma - 1.0;
+        Ub[3] += g1 * pb;
+        Ub[1] -= g1 * q.u * pb;
+        Ub[2] -= g1 * q.v * pb;
+        rb += g1 * 0.5 * (q.u * q.u + q.v * q.v) * pb;
+    }
+    Ub[0] += rb;
 }
 
 // Sensitivities of (u_n, alpha, p) pulled back to the conserved variables of the cell.
@@ -110,6 +136,33 @@ __device__ __forceinline__ void prim_pullback(const double U[4], const Prim& q, 
 // U + P): LLF's lambda = |u_n| + alpha of the cell is pulled back here; GLF's lambda (lam_g, the
 // global maximum) is a constant at the cell, and its sensitivity is returned for the caller to
 // send to the cell of the maximum.
+// The split's sensitivities at one cell in terms of its own U and primitives (u_n, p, alpha),
+// as a ghost cell holds them (its primitives come from the ghost rule, not from its U): Ub +=
+// dF/dU^T g, and unb, pb, ab; returns lambda's sensitivity (GLF).
+template <int DIR, bool GLF>
+__device__ __forceinline__ double llf_bar(const double U[4], double un, double p, double alpha, const double gp[4],
+                                          const double gm[4], double lam_g, double Ub[4], double& unb, double& pb,
+                                          double& ab) {
+    const double s = un >= 0.0 ? 1.0 : -1.0;
+    const double lam = GLF ? lam_g : s * un + alpha;
+    const double up = un + lam, um = un - lam;
+    double Sp = 0.0, Sm = 0.0;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        Ub[c] += 0.5 * (up * gp[c] + um * gm[c]);
+        Sp += gp[c] * U[c];
+        Sm += gm[c] * U[c];
+    }
+    Sp *= 0.5;
+    Sm *= 0.5;
+    const double g3 = gp[3] + gm[3];
+    const double lamb = Sp - Sm;
+    unb = Sp + Sm + 0.5 * p * g3 + (GLF ? 0.0 : s * lamb);
+    pb = 0.5 * (gp[1 + DIR] + gm[1 + DIR]) + 0.5 * un * g3;
+    ab = GLF ? 0.0 : lamb;
+    return lamb;
+}
+
 template <int DIR, bool GLF>
 __device__ __forceinline__ double llf_vjp(const double U[4], const Prim& q, double gamma, const double gp[4],
                                           const double gm[4], double lam_g, double Ub[4]) {
@@ -158,13 +211,9 @@ __device__ __forceinline__ Dual dsqrt(Dual a) {
 // / :110-160 (eta) -- eigenvalues l1 = u_n, l2 = u_n - alpha, l3 = u_n + alpha split as
 // (l +- sqrt(l^2 + eps^2))/2 with eps = 0.125.
 template <int DIR>
-__device__ __forceinline__ void sw_split_dual(const Dual U[4], double gamma, Dual fp[4], Dual fm[4]) {
-    const Dual rho = U[0];
-    const Dual u = U[1] / rho, v = U[2] / rho;
+__device__ __forceinline__ void sw_split_prim_dual(Dual rho, Dual u, Dual v, Dual a, double gamma, Dual fp[4],
+                                                   Dual fm[4]) {
     const Dual uu2 = u * u + v * v;
-    Dual p = (gamma - 1.0) * (U[3] - 0.5 * (rho * uu2));
-    if (p.v < 0.0) p = Dual{kPFloor, 0.0};
-    const Dual a = dsqrt((gamma * p) / rho);
     const double eps2 = 0.125 * 0.125, g1 = gamma - 1.0, c2g = 1.0 / (2.0 * gamma);
     const Dual un = DIR == 0 ? u : v, ut = DIR == 0 ? v : u;
     const Dual l1 = un, l2 = un - a, l3 = un + a;
@@ -184,6 +233,34 @@ __device__ __forceinline__ void sw_split_dual(const Dual U[4], double gamma, Dua
         f[1 + DIR] = (A * un + p2 * l2 + p3 * l3) * crho;
         f[2 - DIR] = ((A + p2 + p3) * ut) * crho;
         f[3] = (g1 * (p1 * uu2) + 0.5 * (p2 * q2) + 0.5 * (p3 * q3) + wii) * crho;
+    }
+}
+template <int DIR>
+__device__ __forceinline__ void sw_split_dual(const Dual U[4], double gamma, Dual fp[4], Dual fm[4]) {
+    const Dual rho = U[0];
+    const Dual u = U[1] / rho, v = U[2] / rho;
+    Dual p = (gamma - 1.0) * (U[3] - 0.5 * (rho * (u * u + v * v)));
+    if (p.v < 0.0) p = Dual{kPFloor, 0.0};
+    const Dual a = dsqrt((gamma * p) / rho);
+    sw_split_prim_dual<DIR>(rho, u, v, a, gamma, fp, fm);
+}
+
+// The Steger-Warming split's sensitivities at a ghost cell with respect to its primitives
+// (rho, u, v, alpha; the split does not read U): pr += dF/dprim^T g, one forward pass each.
+template <int DIR>
+__device__ __forceinline__ void sw_prim_bar(const double pv[4], double gamma, const double gp[4], const double gm[4],
+                                            double pr[4]) {
+#pragma unroll 1
+    for (int k = 0; k < 4; ++k) {
+        Dual q[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) q[c] = Dual{pv[c], c == k ? 1.0 : 0.0};
+        Dual fp[4], fm[4];
+        sw_split_prim_dual<DIR>(q[0], q[1], q[2], q[3], gamma, fp, fm);
+        double acc = 0.0;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc = fma(gp[c], fp[c].d, fma(gm[c], fm[c].d, acc));
+        pr[k] += acc;
     }
 }
 
@@ -326,8 +403,8 @@ __device__ __forceinline__ void add_face(const double* __restrict__ T, const dou
 }
 template <int REC>
 __device__ __forceinline__ void gather_line(const double* __restrict__ T, const double* __restrict__ H, long long ts,
-                                            long long base, long long stride, int x, int n, double gp[4],
-                                            double gm[4]) {
+                                            long long base, long long stride, int x, int n, bool periodic,
+                                            double gp[4], double gm[4]) {
     if (x >= 3 && x <= n - 4) {  // every reading face inside 1..n-1: no images
 #pragma unroll
         for (int m = 0; m < 5; ++m) {
@@ -343,24 +420,124 @@ __device__ __forceinline__ void gather_line(const double* __restrict__ T, const 
             const int f = s == 0 ? x + 3 - m : x - 2 + m;
             double* acc = s == 0 ? gp : gm;
             if (f >= 0 && f <= n) add_face<REC>(T, H, ts, base + (long long)f * stride, s, m, acc);
+            if (!periodic) continue;
             if (f >= n) add_face<REC>(T, H, ts, base + (long long)(f - n) * stride, s, m, acc);  // image x - n
             if (f <= 0) add_face<REC>(T, H, ts, base + (long long)(f + n) * stride, s, m, acc);  // image x + n
         }
     }
 }
 
+// The ghost cells of a side with a wall rule that the interior cell (i, j) feeds, in direction
+// DIR (0: the left and right sides of row j, 1: the bottom and top of column i): for each such
+// ghost, its state rebuilt from the interior state by the rule, the sensitivities of its F+ and
+// F- gathered from the faces whose stencils read it, the split's sensitivities in terms of the
+// ghost's U and primitives (a ghost's primitives come from the rule, not from its U), and these
+// sent back through the rule: into Ub directly, into pbar (rho, u, v, p, alpha of the cell) for
+// the caller to pull back through get_primary. A mirror ghost k copies the cell k+1 in from the
+// side (normal velocity negated); an extrapolated ghost k is w1_k c1 + w2_k c2 of the two cells
+// next to the side (the recursion g = 4/3 near - 1/3 far unrolled), so both of those cells
+// rebuild all four ghosts and take their shares. GLF: a ghost's lambda sensitivity goes to the
+// global lambda once (lb, by the cell next to the side or the mirrored cell).
+template <int DIR, int SPL, int REC>
+__device__ __forceinline__ void wall_terms(const AdjParams& a, const double* __restrict__ u,
+                                           const double* __restrict__ tape, const double* __restrict__ hb, int i,
+                                           int j, const Prim& q, const double U[4], double lam_g, double Ub[4],
+                                           double pbar[5], double& lb) {
+    const int n = DIR == 0 ? a.ni : a.nj, x = DIR == 0 ? i : j;
+    const long long ts = DIR == 0 ? a.xs : a.ys;
+    const double* T = DIR == 0 ? tape : tape + a.np * a.xs;
+    const double* H = DIR == 0 ? hb : hb + 4 * a.xs;
+    const long long base = DIR == 0 ? (long long)j * (a.ni + 1) : i;
+    const long long stride = DIR == 0 ? 1 : a.ni;
+    constexpr double we[2][4] = {{4.0 / 3.0, 13.0 / 9.0, 40.0 / 27.0, 121.0 / 81.0},
+                                 {-1.0 / 3.0, -4.0 / 9.0, -13.0 / 27.0, -40.0 / 81.0}};
+#pragma unroll 1
+    for (int side = 0; side < 2; ++side) {
+        const int rule = a.rule[DIR == 0 ? 2 + side : side];
+        if (rule == kRulePeriodic) continue;
+        const int dist = side == 0 ? x + 1 : n - x;  // 1 = next to the side
+        if (dist > (rule == kRuleReflect ? 4 : 2)) continue;
+        // extrapolation: conserved variables and primitives (rho, u, v, p, alpha) of the two
+        // cells next to the side
+        double c1[9], c2[9];
+        if (rule == kRuleExtrap) {
+#pragma unroll
+            for (int d = 0; d < 2; ++d) {
+                const int xx = side == 0 ? d : n - 1 - d;
+                const long long o = DIR == 0 ? (long long)j * a.ni + xx : (long long)xx * a.ni + i;
+                double* c = d == 0 ? c1 : c2;
+#pragma unroll
+                for (int v = 0; v < 4; ++v) c[v] = u[v * a.plane + o];
+                const Prim qq = prim_of(c, a.gamma);
+                c[4] = c[0]; c[5] = qq.u; c[6] = qq.v; c[7] = qq.p; c[8] = qq.a;
+            }
+        }
+#pragma unroll 1
+        for (int k = 0; k < 4; ++k) {
+            double w;
+            if (rule == kRuleReflect) {
+                if (dist != k + 1) continue;
+                w = 1.0;
+            } else {
+                w = we[dist - 1][k];
+            }
+            double g[9];  // the ghost's U (0..3) and primitives (4..8)
+            if (rule == kRuleReflect) {
+#pragma unroll
+                for (int v = 0; v < 4; ++v) g[v] = U[v];
+                g[4] = U[0]; g[5] = q.u; g[6] = q.v; g[7] = q.p; g[8] = q.a;
+                g[1 + DIR] = -g[1 + DIR];
+                g[5 + DIR] = -g[5 + DIR];
+            } else {
+#pragma unroll
+                for (int v = 0; v < 9; ++v) {
+                    double na = c1[v], fa = c2[v], gv = 0.0;
+                    for (int l = 0; l <= k; ++l) {
+                        gv = fma(na, 4.0 / 3.0, -(fa * (1.0 / 3.0)));
+                        fa = na;
+                        na = gv;
+                    }
+                    g[v] = gv;
+                }
+            }
+            double gp[4] = {0, 0, 0, 0}, gm[4] = {0, 0, 0, 0};
+            gather_line<REC>(T, H, ts, base, stride, side == 0 ? -1 - k : n + k, n, false, gp, gm);
+            double Ubg[4] = {0, 0, 0, 0}, prb[5] = {0, 0, 0, 0, 0};
+            if (SPL == 2) {
+                const double pv[4] = {g[4], g[5], g[6], g[8]};
+                double pr4[4] = {0, 0, 0, 0};
+                sw_prim_bar<DIR>(pv, a.gamma, gp, gm, pr4);
+                prb[0] = pr4[0]; prb[1] = pr4[1]; prb[2] = pr4[2]; prb[4] = pr4[3];
+            } else {
+                double unb, pb, ab;
+                const double lamb = llf_bar<DIR, SPL == 1>(g, g[5 + DIR], g[7], g[8], gp, gm, lam_g, Ubg, unb, pb, ab);
+                prb[1 + DIR] = unb;
+                prb[3] = pb;
+                prb[4] = ab;
+                if (SPL == 1 && (rule == kRuleReflect || dist == 1)) lb += lamb;
+            }
+            const double sn = rule == kRuleReflect ? -1.0 : 1.0;
+#pragma unroll
+            for (int v = 0; v < 4; ++v) Ub[v] += (v == 1 + DIR ? sn * w : w) * Ubg[v];
+#pragma unroll
+            for (int v = 0; v < 5; ++v) pbar[v] += (v == 1 + DIR ? sn * w : w) * prb[v];
+        }
+    }
+}
+
 // Cell kernel: Ub = (dL/du)^T w at the cell from the stage's tape and hbar, then the reverse of
-// RK stage STAGE (3, 2, 1; 0 = Ub alone). Stage 1 also reduces the wave-speed maxima of its
-// state u0 (the time step's input) per block, with their cells. SPL: 0 LLF, 1 GLF, 2 SW. GLF:
+// RK stage STAGE (3, 2, 1; 0 = Ub alone; a kernel argument, uniform over the grid). Stage 1
+// also reduces the wave-speed maxima of its state u0 (the time step's input) per block, with
+// their cells. WALLS: the grid has wall sides (wall_terms). SPL: 0 LLF, 1 GLF, 2 SW. GLF:
 // lamv holds the stage's global lambda of both directions; the sensitivities of lambda are summed
 // per block into lpart.
-template <int STAGE, int REC, int SPL>
+template <int REC, int SPL, bool WALLS>
 __global__ void __launch_bounds__(128) k_rev(AdjParams a, const double* __restrict__ u,
                                              const double* __restrict__ w, const double* __restrict__ tape,
                                              const double* __restrict__ hb, double* __restrict__ acc,
                                              double* __restrict__ out, const double* __restrict__ dtp,
                                              double* __restrict__ mpart, const double* __restrict__ lamv,
-                                             double* __restrict__ lpart) {
+                                             double* __restrict__ lpart, int STAGE) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     const int ni = a.ni, nj = a.nj;
     double e1 = -1.0, e2 = -1.0;
@@ -374,13 +551,21 @@ __global__ void __launch_bounds__(128) k_rev(AdjParams a, const double* __restri
         constexpr bool GLF = SPL == 1;
         const Prim q = prim_of(U, a.gamma);
         double gpx[4] = {0, 0, 0, 0}, gmx[4] = {0, 0, 0, 0}, gpy[4] = {0, 0, 0, 0}, gmy[4] = {0, 0, 0, 0};
-        gather_line<REC>(tape, hb, a.xs, (long long)j * (ni + 1), 1, i, ni, gpx, gmx);
+        const bool px = a.rule[2] == kRulePeriodic, py = a.rule[0] == kRulePeriodic;
+        gather_line<REC>(tape, hb, a.xs, (long long)j * (ni + 1), 1, i, ni, px, gpx, gmx);
         // LF splittings pull each direction back before gathering the next (fewer live
         // registers); Steger-Warming seeds each variable once for both directions
         if (SPL != 2) lbx = llf_vjp<0, GLF>(U, q, a.gamma, gpx, gmx, GLF ? lamv[0] : 0.0, Ub);
-        gather_line<REC>(tape + a.np * a.xs, hb + 4 * a.xs, a.ys, i, ni, j, nj, gpy, gmy);
+        gather_line<REC>(tape + a.np * a.xs, hb + 4 * a.xs, a.ys, i, ni, j, nj, py, gpy, gmy);
         if (SPL != 2) lby = llf_vjp<1, GLF>(U, q, a.gamma, gpy, gmy, GLF ? lamv[1] : 0.0, Ub);
         else          sw_vjp(U, a.gamma, gpx, gmx, gpy, gmy, Ub);
+        if (WALLS && (!px || !py)) {  // the ghost cells of wall sides that this cell feeds
+            // (a separate instantiation: the periodic kernels keep their registers)
+            double pbar[5] = {0, 0, 0, 0, 0};
+            if (!px) wall_terms<0, SPL, REC>(a, u, tape, hb, i, j, q, U, GLF ? lamv[0] : 0.0, Ub, pbar, lbx);
+            if (!py) wall_terms<1, SPL, REC>(a, u, tape, hb, i, j, q, U, GLF ? lamv[1] : 0.0, Ub, pbar, lby);
+            prim_pullback_all(U, q, a.gamma, pbar[0], pbar[1], pbar[2], pbar[3], pbar[4], Ub);
+        }
         const double dt = STAGE == 0 ? 0.0 : *dtp;
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
@@ -677,19 +862,26 @@ int taped_stage(dense_adjoint* a, int irk, double* tape) {
     return DENSE_OK;
 }
 
-template <int REC, int SPL>
-void launch_rev(dense_adjoint* a, int stage, const double* u, const double* tape, const double* w, double* out,
-                const double* dtp, cudaStream_t s) {
+template <int REC, int SPL, bool WALLS>
+void launch_rev_w(dense_adjoint* a, int stage, const double* u, const double* tape, const double* w, double* out,
+                  const double* dtp, cudaStream_t s) {
     using namespace dense::adj;
     const dim3 bc(kCX, kCY);
     double* const lv = a->lamv;
     double* const lp = a->lpart;
-    switch (stage) {
-    case 3: k_rev<3, REC, SPL><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, a->hb, a->acc, out, dtp, nullptr, lv, lp); break;
-    case 2: k_rev<2, REC, SPL><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, a->hb, a->acc, out, dtp, nullptr, lv, lp); break;
-    case 1: k_rev<1, REC, SPL><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, a->hb, a->acc, out, dtp, a->mpart, lv, lp); break;
-    default: k_rev<0, REC, SPL><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, a->hb, nullptr, out, nullptr, nullptr, lv, lp); break;
-    }
+    if (stage == 0)
+        k_rev<REC, SPL, WALLS><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, a->hb, nullptr, out, nullptr, nullptr, lv, lp, 0);
+    else
+        k_rev<REC, SPL, WALLS><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, a->hb, a->acc, out, dtp,
+                                                    stage == 1 ? a->mpart : nullptr, lv, lp, stage);
+}
+template <int REC, int SPL>
+void launch_rev(dense_adjoint* a, int stage, const double* u, const double* tape, const double* w, double* out,
+                const double* dtp, cudaStream_t s) {
+    const int* r = a->ap.rule;
+    const bool walls = r[0] != dense::adj::kRulePeriodic || r[2] != dense::adj::kRulePeriodic;
+    if (walls) launch_rev_w<REC, SPL, true>(a, stage, u, tape, w, out, dtp, s);
+    else       launch_rev_w<REC, SPL, false>(a, stage, u, tape, w, out, dtp, s);
 }
 template <int SPL>
 void launch_rev_recon(dense_adjoint* a, int stage, const double* u, const double* tape, const double* w,
@@ -791,8 +983,23 @@ int dense_adjoint_create(const dense_config_t* cfg, int checkpoint_every, dense_
         return aerr(nullptr, DENSE_ERR_ARG, "the adjoint covers the LLF, GLF and Steger-Warming splittings (101-103)");
     if (cfg->recon != DENSE_RECON_UPWIND5 && cfg->recon != DENSE_RECON_WENOJS5 && cfg->recon != DENSE_RECON_WENOZ5)
         return aerr(nullptr, DENSE_ERR_ARG, "the adjoint covers reconstructions 251, 253 and 255");
-    if (cfg->benchmark != DENSE_BENCH_IVC_PERIODIC && cfg->benchmark != DENSE_BENCH_RM_PERIODIC)
-        return aerr(nullptr, DENSE_ERR_ARG, "the adjoint needs a grid periodic in x and y (benchmarks 11, 14)");
+    // ghost rules (bottom, top, left, right) of the benchmarks covered: periodic, the
+    // extrapolation and the mirror (boundary_ivc/sedov/rm/shockvortex_general.f90)
+    int rules[4];
+    switch (cfg->benchmark) {
+    case DENSE_BENCH_IVC_PERIODIC: case DENSE_BENCH_RM_PERIODIC:
+        rules[0] = rules[1] = rules[2] = rules[3] = dense::adj::kRulePeriodic; break;
+    case DENSE_BENCH_IVC:  // y periodic, x extrapolated
+        rules[0] = rules[1] = dense::adj::kRulePeriodic; rules[2] = rules[3] = dense::adj::kRuleExtrap; break;
+    case DENSE_BENCH_SEDOV:  // mirror bottom and left, extrapolation top and right
+        rules[0] = rules[2] = dense::adj::kRuleReflect; rules[1] = rules[3] = dense::adj::kRuleExtrap; break;
+    case DENSE_BENCH_RM: case DENSE_BENCH_SHOCKVORTEX:  // mirror bottom and top, extrapolated sides
+        rules[0] = rules[1] = dense::adj::kRuleReflect; rules[2] = rules[3] = dense::adj::kRuleExtrap; break;
+    default:
+        return aerr(nullptr, DENSE_ERR_ARG,
+                    "the adjoint covers the benchmarks with periodic, extrapolated or mirror sides "
+                    "(1, 2, 4, 9, 11, 14); not the Dirichlet, time-dependent or body-force ones");
+    }
     if (cfg->ni < 8 || cfg->nj < 8) return aerr(nullptr, DENSE_ERR_ARG, "the adjoint needs ni, nj >= 8");
     if (checkpoint_every < 1) return aerr(nullptr, DENSE_ERR_ARG, "checkpoint_every must be >= 1");
     auto* a = new dense_adjoint();
@@ -819,6 +1026,7 @@ int dense_adjoint_create(const dense_config_t* cfg, int checkpoint_every, dense_
     p.np = dense::tape_planes(cfg->recon);
     p.gamma = cfg->gamma; p.dx = cfg->dx; p.dy = cfg->dy; p.inv_dx = 1.0 / cfg->dx; p.inv_dy = 1.0 / cfg->dy;
     p.cfl = cfg->cfl;
+    for (int k = 0; k < 4; ++k) p.rule[k] = rules[k];
     a->tape_stage = (size_t)p.np * (size_t)(p.xs + p.ys);
     a->gh = dim3((cfg->ni + 1 + kHX - 1) / kHX, (cfg->nj + 1 + kHY - 1) / kHY, 2);
     a->gc = dim3((cfg->ni + kCX - 1) / kCX, (cfg->nj + kCY - 1) / kCY);

@@ -147,8 +147,54 @@ def test_autograd_function_in_a_graph(dense, adjoint, split):
             assert abs(fd - grad[k]) <= 1e-6 * abs(grad[k]), (k, fd, grad[k])
 
 
+def rough_state(dense, cfg, seed):
+    """A seeded positive state of cfg's grid, smooth on the scale of a few cells."""
+    c = dense.init_general(cfg)[0]
+    g = torch.Generator().manual_seed(seed)
+    sm = lambda: torch.nn.functional.avg_pool2d(torch.rand(1, 1, c.nj + 4, c.ni + 4, generator=g,
+                                                           dtype=torch.float64), 5, 1)[0, 0]
+    rho, u, v, p = 0.5 + 1.5 * sm(), 2.0 * sm() - 1.0, 2.0 * sm() - 1.0, 0.5 + 1.5 * sm()
+    U = torch.stack([rho, rho * u, rho * v, p / (c.gamma - 1.0) + 0.5 * rho * (u * u + v * v)])
+    return c, U.contiguous().cuda()
+
+
+@pytest.mark.parametrize("bench,split,recon", [(1, 101, 253), (2, 101, 255), (4, 102, 253), (9, 103, 255),
+                                               (2, 103, 251), (1, 102, 255)])
+def test_rhs_vjp_with_walls_matches_autograd(dense, adjoint, bench, split, recon):
+    """The reference's benchmarks with walls -- extrapolated (1: x; 2: top, right; 4, 9: sides)
+    and mirror sides (2: bottom, left; 4, 9: bottom, top): the ghost cells' split sensitivities
+    sent back through the rules, against autograd through the PyTorch step's ghost layers."""
+    cfg = dense.config_default(ni=24, nj=20, benchmark=bench, splitting=split, recon=recon, cfl=0.4)
+    c, U = rough_state(dense, cfg, seed=bench * 10 + split % 10)
+    v = torch.randn(U.shape, generator=torch.Generator().manual_seed(3), dtype=torch.float64).cuda()
+    with adjoint.Adjoint(c) as adj:
+        out, vdotl = adj.rhs_vjp(U, v)
+    Ut = U.clone().requires_grad_(True)
+    L = torch_step.rhs(Ut, c.gamma, c.dx, c.dy, recon, split, bench)
+    (ref,) = torch.autograd.grad(L, Ut, v)
+    assert rel(out, ref) < 1e-10
+    assert abs(vdotl - float((v * L.detach()).sum())) < 1e-12 * float((v * L.detach()).abs().sum())
+
+
+@pytest.mark.parametrize("bench,split,recon", [(4, 101, 253), (2, 102, 255), (1, 103, 253)])
+def test_steps_gradient_with_walls_matches_autograd(dense, adjoint, bench, split, recon):
+    """5 steps with checkpoints every 2 on grids with wall sides, CFL time step."""
+    cfg = dense.config_default(ni=24, nj=20, benchmark=bench, splitting=split, recon=recon, cfl=0.4)
+    c, U = rough_state(dense, cfg, seed=7 + bench)
+    gT = torch.randn(U.shape, generator=torch.Generator().manual_seed(5), dtype=torch.float64).cuda()
+    with adjoint.Adjoint(c, checkpoint_every=2) as adj:
+        uT = adj.forward(U, 5)
+        g0 = adj.backward(gT)
+    Ut = U.clone().requires_grad_(True)
+    ref_T = torch_step.run(Ut, 5, c.gamma, c.dx, c.dy, recon, c.cfl, None, split, bench)
+    assert rel(uT, ref_T.detach()) < 1e-12
+    (ref,) = torch.autograd.grad(ref_T, Ut, gT)
+    assert rel(g0, ref) < 1e-10
+
+
 def test_rejects_unsupported_configurations(dense, adjoint):
-    for kw in (dict(splitting=104), dict(recon=0, splitting=105), dict(benchmark=5), dict(ni=6)):
+    for kw in (dict(splitting=104), dict(recon=0, splitting=105), dict(benchmark=5), dict(benchmark=3),
+               dict(benchmark=13), dict(ni=6)):
         cfg = dense.init_general(vortex_cfg(dense, 253))[0]
         for k, v in kw.items():
             setattr(cfg, k, v)

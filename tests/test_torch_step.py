@@ -37,6 +37,30 @@ def test_torch_step_matches_oracle(dense, orc, split, recon):
     assert (np.abs(got - ref) / scale).max() < 1e-12
 
 
+@pytest.mark.parametrize("bench,split,recon", [(1, 101, 253), (2, 102, 255), (4, 103, 253), (9, 101, 255),
+                                               (1, 103, 251)])
+def test_torch_step_with_walls_matches_oracle(dense, orc, bench, split, recon):
+    """The ghost rules of the reference's benchmarks with walls (extrapolation, mirror) from
+    a rough seeded state: three steps within 1e-12 of the oracle."""
+    cfg = dense.config_default(ni=24, nj=20, benchmark=bench, splitting=split, recon=recon, cfl=0.4)
+    c, cons, prim, x, y = dense.init_general(cfg)
+    rng = np.random.default_rng(bench * 1000 + split + recon)
+    shape = (c.ni + 8, c.nj + 8)
+    rho, u, v, p = (rng.uniform(0.5, 2.0, shape), rng.uniform(-1, 1, shape), rng.uniform(-1, 1, shape),
+                    rng.uniform(0.5, 2.0, shape))
+    cons = np.zeros(shape + (4,), order="F")
+    cons[..., 0], cons[..., 1], cons[..., 2] = rho, rho * u, rho * v
+    cons[..., 3] = p / (c.gamma - 1.0) + 0.5 * rho * (u * u + v * v)
+    o = orc.OracleSolver(c)
+    o.set_state(cons, None)
+    o.steps(3)
+    ref = to_state(o.get_state()[0])
+    got = torch_step.run(torch.from_numpy(to_state(cons)), 3, c.gamma, c.dx, c.dy, recon, c.cfl,
+                         split=split, bench=bench).numpy()
+    scale = np.abs(ref).max(axis=(1, 2), keepdims=True)
+    assert (np.abs(got - ref) / scale).max() < 1e-12
+
+
 def test_vortex_state_matches_setup(dense):
     adjoint = importlib.import_module("2dense_gb300.adjoint")
     cfg = vortex_cfg(dense, 253, var_eps=3.5, var_xc=4.2, var_yc=5.9)

@@ -10,7 +10,8 @@ WENO-JS5 / WENO-Z5
 reconstruction of F+ and F- at each face (scheme_*_general.f90, weno_mod.f90), the flux
 difference, and TVD-RK3 (time_advance_general.f90:9-267) with dt = cfl/(max(|u|+alpha)/dx +
 max(|v|+alpha)/dy) of the step's input (or a constant dt). States are (4, nj, ni) tensors of the
-interior; periodic neighbours come from torch.roll.
+interior; periodic neighbours come from torch.roll, and the ghost layers of the benchmarks with
+walls from the reference's rules (RULES).
 """
 from __future__ import annotations
 
@@ -75,8 +76,49 @@ def steger_warming(rho, u, v, a, gamma, d):
     return out
 
 
-def rhs(U, gamma, dx, dy, rec, split=101):
+# Ghost rules of the reference's benchmarks with fixed walls (boundary_ivc_general.f90,
+# boundary_sedov_general.f90, boundary_rm_general.f90, boundary_shockvortex_general.f90), per side
+# (bottom, top, left, right): "P" periodic, "E" the recursive 4/3, -1/3 extrapolation, "R" the
+# mirror with the normal velocity negated. Ghost primitives come from the rule applied to the
+# interior primitives, not from the ghost conserved variables.
+RULES = {1: "PPEE", 2: "RERE", 4: "RREE", 9: "RREE", 11: "PPPP", 14: "PPPP"}
+
+
+def _pad_axis(A, axis, lo, hi, flip):
+    """A (nv, nj, ni) padded by 4 ghost layers along axis (2: x, 1: y); flip is the component
+    negated by a mirror (the normal momentum, or the normal velocity of the primitives)."""
+    n = A.shape[axis]
+    take = lambda k: A.narrow(axis, k, 1)
+    sign = torch.ones(A.shape[0], dtype=A.dtype, device=A.device)
+    sign[flip] = -1.0
+    sign = sign.view(-1, 1, 1)
+
+    def side(rule, inner):  # inner(d): the interior slice at distance d (1 = adjacent)
+        if rule == "P":
+            return None
+        if rule == "R":
+            return [sign * inner(k + 1) for k in range(4)]
+        a, b = inner(1), inner(2)
+        out = []
+        for _ in range(4):
+            g = 4.0 / 3.0 * a - 1.0 / 3.0 * b
+            out.append(g)
+            b, a = a, g
+        return out
+
+    low = side(lo, lambda d: take(d - 1))
+    high = side(hi, lambda d: take(n - d))
+    if low is None:
+        low = [take(n - 1 - k) for k in range(4)]
+    if high is None:
+        high = [take(k) for k in range(4)]
+    return torch.cat(list(reversed(low)) + [A] + high, dim=axis)
+
+
+def rhs(U, gamma, dx, dy, rec, split=101, bench=11):
     """L(U) = -(h_{i+1/2} - h_{i-1/2})/dx - (g_{j+1/2} - g_{j-1/2})/dy."""
+    if bench not in (11, 14):
+        return _rhs_padded(U, gamma, dx, dy, rec, split, RULES[bench])
     rho, u, v, p, a = primitives(U, gamma)
     out = torch.zeros_like(U)
     for d, (un, h, axis) in enumerate(((u, dx, 2), (v, dy, 1))):
@@ -99,7 +141,37 @@ def rhs(U, gamma, dx, dy, rec, split=101):
     return out
 
 
-def time_step(U, gamma, dx, dy, rec, cfl, dt_const=None, split=101):
+def _rhs_padded(U, gamma, dx, dy, rec, split, rules):
+    """L(U) on a grid with ghost layers filled by the given rules (bottom, top, left, right)."""
+    rho, u, v, p, a = primitives(U, gamma)
+    Pr = torch.stack([rho, u, v, p, a])
+    out = torch.zeros_like(U)
+    for d, (h, axis) in enumerate(((dx, 2), (dy, 1))):
+        lo, hi = (rules[2], rules[3]) if d == 0 else (rules[0], rules[1])
+        Ug = _pad_axis(U, axis, lo, hi, 1 + d)
+        Pg = _pad_axis(Pr, axis, lo, hi, 1 + d)
+        r_, u_, v_, p_, a_ = Pg
+        un = u_ if d == 0 else v_
+        if split == 103:
+            Fp, Fm = steger_warming(r_, u_, v_, a_, gamma, d)
+        else:
+            lam = un.abs() + a_
+            if split == 102:  # the maximum over the interior cells (get_primary.f90:69-73)
+                lam = ((u if d == 0 else v).abs() + a).max()
+            zero = torch.zeros_like(p_)
+            P = torch.stack([zero, p_ if d == 0 else zero, p_ if d == 1 else zero, un * p_])
+            Fp = 0.5 * ((un + lam) * Ug + P)
+            Fm = 0.5 * ((un - lam) * Ug + P)
+        n = U.shape[axis]
+        sl = lambda F, k: F.narrow(axis, k, n + 1)  # padded index k + f for faces f = 0..n
+        hp = _recon([sl(Fp, k) for k in (1, 2, 3, 4, 5)], rec)
+        hm = _recon([sl(Fm, k) for k in (6, 5, 4, 3, 2)], rec)
+        hf = hp + hm
+        out = out - (hf.narrow(axis, 1, n) - hf.narrow(axis, 0, n)) / h
+    return out
+
+
+def time_step(U, gamma, dx, dy, rec, cfl, dt_const=None, split=101, bench=11):
     """One TVD-RK3 step; returns (U_next, dt)."""
     if dt_const is None:
         _, u, v, _, a = primitives(U, gamma)
@@ -109,13 +181,13 @@ def time_step(U, gamma, dx, dy, rec, cfl, dt_const=None, split=101):
         dt = cfl * dt_x * dt_y / (dt_x + dt_y)
     else:
         dt = torch.tensor(dt_const, dtype=U.dtype, device=U.device)
-    u1 = U + dt * rhs(U, gamma, dx, dy, rec, split)
-    u2 = 3.0 / 4.0 * U + 1.0 / 4.0 * u1 + 1.0 / 4.0 * dt * rhs(u1, gamma, dx, dy, rec, split)
-    u3 = 1.0 / 3.0 * U + 2.0 / 3.0 * u2 + 2.0 / 3.0 * dt * rhs(u2, gamma, dx, dy, rec, split)
+    u1 = U + dt * rhs(U, gamma, dx, dy, rec, split, bench)
+    u2 = 3.0 / 4.0 * U + 1.0 / 4.0 * u1 + 1.0 / 4.0 * dt * rhs(u1, gamma, dx, dy, rec, split, bench)
+    u3 = 1.0 / 3.0 * U + 2.0 / 3.0 * u2 + 2.0 / 3.0 * dt * rhs(u2, gamma, dx, dy, rec, split, bench)
     return u3, dt
 
 
-def run(U, n, gamma, dx, dy, rec, cfl, dt_const=None, split=101):
+def run(U, n, gamma, dx, dy, rec, cfl, dt_const=None, split=101, bench=11):
     for _ in range(n):
-        U, _ = time_step(U, gamma, dx, dy, rec, cfl, dt_const, split)
+        U, _ = time_step(U, gamma, dx, dy, rec, cfl, dt_const, split, bench)
     return U
