@@ -141,9 +141,10 @@ __device__ __forceinline__ double upwind5(const double lf[5]) {
 // FAST arithmetic. On GB300 an IEEE double divide costs about ten FMA slots of the FP64 pipe,
 // and the reference's WENO weights spend seven divides per stencil. The fast variant
 //  * takes reciprocals and inverse square roots from the hardware seeds (rcp.approx.ftz.f64,
-//    rsqrt.approx.ftz.f64) refined by two Newton-Raphson steps each (Newton's iteration for
-//    1/d: r <- r + r(1 - d r); for 1/sqrt(x): y <- y + y(1 - x y^2)/2), which lands within
-//    an ulp of the correctly rounded result for the positive normal arguments used here;
+//    rsqrt.approx.ftz.f64) refined by one third-order step each (with e = 1 - d r, 1/d =
+//    r (1 + e + e^2 + ...); with e = 1 - x y^2, 1/sqrt(x) = y (1 + e/2 + 3e^2/8 + ...)), which
+//    lands within 2 ulp of the correctly rounded result for the positive normal arguments
+//    used here;
 //  * writes the WENO weights over a common denominator: with d_k = ss + beta_k,
 //    P_k = prod_{j != k} d_j^2 and D = prod_j d_j^2,
 //      WENO-JS: alpha_k D = c_k P_k,   WENO-Z: alpha_k D = c_k (D + tau^2 P_k),
@@ -153,44 +154,51 @@ __device__ __forceinline__ double upwind5(const double lf[5]) {
 // Products of squared d_k stay far inside the double range for d_k in [1e-6, 1e40].
 // (rcp_nr and rsqrt_nr: fastmath.cuh)
 
-constexpr double k1312 = 13.0 / 12.0;
 
-// d_k = ss + beta_k and tau = |beta_2 - beta_0| with beta_k = 13/12 a_k^2 + 1/4 b_k^2. For the
-// outer substencils the halves a_k/2, b_k/2 are formed directly (b_0 = a_0 + 2 (lf2 - lf1),
-// b_2 = a_2 + 2 (lf2 - lf3)), so that 13/12 a^2 + 1/4 b^2 = 13/3 (a/2)^2 + (b/2)^2 needs no 1/4.
-__device__ __forceinline__ void betas_fast(const double lf[5], double& d0, double& d1, double& d2,
-                                           double& tau) {
-    constexpr double k133 = 13.0 / 3.0;
-    const double a0h = fma(0.5, lf[0] + lf[2], -lf[1]);
-    const double b0h = a0h + (lf[2] - lf[1]);
-    const double a1 = fma(-2.0, lf[2], lf[1]) + lf[3];
-    const double b1 = lf[1] - lf[3];
-    const double a2h = fma(0.5, lf[2] + lf[4], -lf[3]);
-    const double b2h = a2h + (lf[2] - lf[3]);
-    // d_k = ss + beta_k with ss added inside the last FMA; tau = |beta_2 - beta_0| = |d_2 - d_0|
-    d0 = fma(k133 * a0h, a0h, fma(b0h, b0h, kSS));
-    d1 = fma(k1312 * a1, a1, fma(0.25 * b1, b1, kSS));
-    d2 = fma(k133 * a2h, a2h, fma(b2h, b2h, kSS));
-    tau = fabs(d2 - d0);
+// The fast WENO reconstructions work from a stencil's centre value lf[2] and its first
+// differences g_m = lf[m] - lf[m+1] (m = 0..3): the indicators' second differences A_k =
+// g_k - g_{k+1} and first-order combinations B_0 = g_0 - 3 g_1, B_1 = g_1 + g_2, B_2 = 3 g_2 - g_3,
+// and the candidates relative to the centre, q_0 - lf2 = g_0/3 - 5 g_1/6, q_1 - lf2 = -g_1/6 -
+// g_2/3, q_2 - lf2 = -2 g_2/3 + g_3/6, so that h = lf[2] + sum_k w_k (q_k - lf[2]) (the weights
+// sum to one). The indicators are formed four times over, d_k = 4 (ss + beta_k) = 4 ss +
+// 13/3 A_k^2 + B_k^2, with no 1/4 products; the weights are ratios of homogeneous products of the
+// d_k, which that exact binary scale leaves unchanged.
+constexpr double k133 = 13.0 / 3.0;   // 4 x 13/12 (exactly, in binary)
+
+// d_k = 4 (ss + beta_k) from the first differences and the terms s_k = 4 ss + 13/3 A_k^2 (staged
+// once per cell by the component-wise sweeps, whose neighbouring interfaces share them).
+__device__ __forceinline__ void betas_staged(const double g[4], double s0, double s1, double s2, double& d0,
+                                             double& d1, double& d2) {
+    const double B0 = fma(-3.0, g[1], g[0]), B1 = g[1] + g[2], B2 = fma(3.0, g[2], -g[3]);
+    d0 = fma(B0, B0, s0);
+    d1 = fma(B1, B1, s1);
+    d2 = fma(B2, B2, s2);
+}
+// The same from the first differences alone (a stencil no other interface shares).
+__device__ __forceinline__ void betas_g(const double g[4], double& d0, double& d1, double& d2) {
+    const double A0 = g[0] - g[1], A1 = g[1] - g[2], A2 = g[2] - g[3];
+    const double B0 = fma(-3.0, g[1], g[0]), B1 = g[1] + g[2], B2 = fma(3.0, g[2], -g[3]);
+    d0 = fma(k133 * A0, A0, fma(B0, B0, 4.0 * kSS));
+    d1 = fma(k133 * A1, A1, fma(B1, B1, 4.0 * kSS));
+    d2 = fma(k133 * A2, A2, fma(B2, B2, 4.0 * kSS));
+}
+__device__ __forceinline__ void first_differences(const double lf[5], double g[4]) {
+#pragma unroll
+    for (int m = 0; m < 4; ++m) g[m] = lf[m] - lf[m + 1];
 }
 
-// The candidates scaled by the linear weights, c_k q_k (the constants folded together).
-__device__ __forceinline__ void candidates_c(const double lf[5], double& q0, double& q1, double& q2) {
-    q0 = fma(c30 * a302, lf[2], fma(c30 * a301, lf[1], (c30 * a300) * lf[0]));
-    q1 = fma(c31 * a312, lf[3], fma(c31 * a311, lf[2], (c31 * a310) * lf[1]));
-    q2 = fma(c32 * a322, lf[4], fma(c32 * a321, lf[3], (c32 * a320) * lf[2]));
-}
-
-// Terms of a WENO reconstruction from d_k = ss + beta_k that its value and, in the adjoint's
-// taping sweeps, its gradient share: the scaled candidates c_k q_k, e_k = d_k^2, P_k =
-// prod_{j != k} e_j, D = prod e_j, tau = |d_2 - d_0| (= |beta_2 - beta_0|), v_k = alpha_k D / c_k
-// -- P_k (JS) or D + tau^2 P_k (Z) -- and N = sum_k c_k v_k = (sum alpha) D.
+// Terms of a WENO reconstruction that its value and, in the adjoint's taping sweeps, its gradient
+// share: the relative candidates scaled by the linear weights, r_k = c_k (q_k - lf2), e_k = d_k^2,
+// P_k = prod_{j != k} e_j, D = prod e_j, tau = |d_2 - d_0| (4 |beta_2 - beta_0|), v_k = alpha_k
+// D / c_k -- P_k (JS) or D + tau^2 P_k (Z) -- and N = sum_k c_k v_k = (sum alpha) D.
 struct WenoTerms {
-    double q[3], P[3], v[3], D, tau, N;
+    double r[3], P[3], v[3], D, tau, N;
 };
 template <bool Z>
-__device__ __forceinline__ void weno_terms(const double lf[5], double d0, double d1, double d2, WenoTerms& t) {
-    candidates_c(lf, t.q[0], t.q[1], t.q[2]);
+__device__ __forceinline__ void weno_terms(const double g[4], double d0, double d1, double d2, WenoTerms& t) {
+    t.r[0] = fma(c30 / 3.0, g[0], (-5.0 * c30 / 6.0) * g[1]);
+    t.r[1] = fma(-c31 / 3.0, g[2], (-c31 / 6.0) * g[1]);
+    t.r[2] = fma(c32 / 6.0, g[3], (-2.0 * c32 / 3.0) * g[2]);
     const double e0 = d0 * d0, e1 = d1 * d1, e2 = d2 * d2;
     t.P[0] = e1 * e2; t.P[1] = e0 * e2; t.P[2] = e0 * e1;
     t.D = e0 * t.P[0];
@@ -201,45 +209,39 @@ __device__ __forceinline__ void weno_terms(const double lf[5], double d0, double
     for (int k = 0; k < 3; ++k) t.v[k] = Z ? fma(T, t.P[k], t.D) : t.P[k];
     t.N = fma(c32, t.v[2], fma(c31, t.v[1], c30 * t.v[0]));
 }
-// h = sum_k v_k (c_k q_k) / N with iN = 1/N. Every operation is an explicit FMA or a product
+// sum_k v_k r_k, the numerator of h - lf2
+__device__ __forceinline__ double weno_num(const WenoTerms& t) {
+    return fma(t.v[2], t.r[2], fma(t.v[1], t.r[1], t.v[0] * t.r[0]));
+}
+// h = lf2 + sum_k v_k r_k / N with iN = 1/N. Every operation is an explicit FMA or a product
 // feeding one, so no kernel contracts it differently from another (the plain and taping sweeps
-// agree bit for bit); the result is a rounded product, which the caller's sum of the two signs
-// must not fuse with.
-__device__ __forceinline__ double weno_value(const WenoTerms& t, double iN) {
-    return __dmul_rn(fma(t.v[2], t.q[2], fma(t.v[1], t.q[1], t.v[0] * t.q[0])), iN);
+// agree bit for bit).
+__device__ __forceinline__ double weno_value(const WenoTerms& t, double iN, double lf2) {
+    return fma(weno_num(t), iN, lf2);
 }
-// WENO reconstruction from d_k = ss + beta_k.
+// WENO reconstruction from its centre value, first differences and d_k.
 template <bool Z>
-__device__ __forceinline__ double weno_from_d(const double lf[5], double d0, double d1, double d2) {
+__device__ __forceinline__ double weno_from_d(double lf2, const double g[4], double d0, double d1, double d2) {
     WenoTerms t;
-    weno_terms<Z>(lf, d0, d1, d2, t);
-    return weno_value(t, rcp_nr(t.N));
+    weno_terms<Z>(g, d0, d1, d2, t);
+    return weno_value(t, rcp_nr(t.N), lf2);
 }
 
+// WENO reconstruction of a stencil no other interface shares (the characteristic fields).
 template <bool Z> __device__ __forceinline__ double weno_fast(const double lf[5]) {
-    double d0, d1, d2, tau;
-    betas_fast(lf, d0, d1, d2, tau);
-    return weno_from_d<Z>(lf, d0, d1, d2);
+    double g[4], d0, d1, d2;
+    first_differences(lf, g);
+    betas_g(g, d0, d1, d2);
+    return weno_from_d<Z>(lf[2], g, d0, d1, d2);
 }
 
-// Second-difference term of a smoothness indicator, ss + 13/12 A^2 with A = lm - 2 lc + lr: it
-// depends on one cell and its two neighbours only, so a sweep computes it once per cell and sign
-// and each of the three interfaces that use it reads it (the "-" sign passes its neighbours in
-// mirrored order, as its stencil reads them).
+// Second-difference term of a smoothness indicator, s = 4 ss + 13/3 A^2 (four times ss + 13/12
+// A^2) with A = lm - 2 lc + lr: it depends on one cell and its two neighbours only, so a sweep
+// computes it once per cell and sign and each of the three interfaces that use it reads it (the
+// "-" sign passes its neighbours in mirrored order, as its stencil reads them).
 __device__ __forceinline__ double ind_second(double lm, double lc, double lr) {
     const double a = fma(-2.0, lc, lm) + lr;
-    return fma(k1312 * a, a, kSS);
-}
-// d_k = ss + beta_k from the staged terms s_k = ss + 13/12 A_k^2 of the three substencils
-// (centred on lf[1], lf[2], lf[3]): beta_k adds the first-order term 1/4 B_k^2.
-__device__ __forceinline__ void betas_staged(const double lf[5], double s0, double s1, double s2, double& d0,
-                                             double& d1, double& d2) {
-    const double b0 = fma(3.0, lf[2], fma(-4.0, lf[1], lf[0]));
-    const double b1 = lf[1] - lf[3];
-    const double b2 = fma(3.0, lf[2], fma(-4.0, lf[3], lf[4]));
-    d0 = fma(0.25 * b0, b0, s0);
-    d1 = fma(0.25 * b1, b1, s1);
-    d2 = fma(0.25 * b2, b2, s2);
+    return fma(k133 * a, a, 4.0 * kSS);
 }
 
 // The five coefficients of h = sum_k w_k q_k as one 5-point stencil: W[m] lf[m].
@@ -267,25 +269,26 @@ __device__ __forceinline__ void stencil_from_u(double u0, double u2, double W[5]
 // da_k/dbeta_k = -2 a_k/d_k; Z: a_k = c_k (1 + tau^2/d_k^2), so da_k/dbeta_k = -2 c_k tau^2/d_k^3
 // and da_k/dtau = 2 c_k tau/d_k^2, tau = |beta_2 - beta_0|; d_k = ss + beta_k), and beta_k =
 // 13/12 A_k^2 + 1/4 B_k^2 on the second differences A_k and the first-order combinations B_k.
-// Written over the terms the value itself uses (weno_terms: w_k = c_k v_k / N, and
-// (q_k - W) c_k = c_k q_k - c_k W), with h and iN = 1/N as the value computed them, so that the
-// taping sweep evaluates every shared term once.
+// Written over the terms the value itself uses (weno_terms: w_k = c_k v_k / N, and c_k (q_k - W)
+// = r_k - c_k (W - lf2)), with corr = W - lf2 and iN = 1/N as the value computed them, so that
+// the taping sweep evaluates every shared term once. The d_k arrive four times ss + beta_k,
+// which scales 1/d_k and the tau terms by 1/4; two exact factors of 4 undo it.
 template <bool Z>
-__device__ __forceinline__ void weno_grad(const double lf[5], double d0, double d1, double d2, const WenoTerms& t,
-                                          double h, double iN, double g[5]) {
+__device__ __forceinline__ void weno_grad(const double gd[4], double d0, double d1, double d2, const WenoTerms& t,
+                                          double corr, double iN, double g[5]) {
     constexpr double cs[3] = {c30, c31, c32};
     double E[3], u[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        E[k] = fma(-cs[k], h, t.q[k]);  // (q_k - h) c_k
-        u[k] = t.v[k] * iN;             // w_k / c_k
+        E[k] = fma(-cs[k], corr, t.r[k]);  // (q_k - W) c_k
+        u[k] = t.v[k] * iN;                // w_k / c_k
     }
     const double w0 = c30 * u[0], w1 = c31 * u[1], w2 = c32 * u[2];
-    const double iD = rcp_nr(t.D);
-    const double id0 = d0 * (t.P[0] * iD), id1 = d1 * (t.P[1] * iD), id2 = d2 * (t.P[2] * iD);  // 1/d_k
-    const double A0 = fma(-2.0, lf[1], lf[0]) + lf[2], B0 = fma(3.0, lf[2], fma(-4.0, lf[1], lf[0]));
-    const double A1 = fma(-2.0, lf[2], lf[1]) + lf[3], B1 = lf[1] - lf[3];
-    const double A2 = fma(-2.0, lf[3], lf[2]) + lf[4], B2 = fma(3.0, lf[2], fma(-4.0, lf[3], lf[4]));
+    const double iD = 4.0 * rcp_nr(t.D);
+    const double id0 = d0 * (t.P[0] * iD), id1 = d1 * (t.P[1] * iD), id2 = d2 * (t.P[2] * iD);  // 1/(ss + beta_k)
+    const double A0 = gd[0] - gd[1], B0 = fma(-3.0, gd[1], gd[0]);
+    const double A1 = gd[1] - gd[2], B1 = gd[1] + gd[2];
+    const double A2 = gd[2] - gd[3], B2 = fma(3.0, gd[2], -gd[3]);
     // r_k = -1/2 dW/dbeta_k. With dbeta_k/dlf = 13/6 A_k dA_k/dlf + 1/2 B_k dB_k/dlf, beta_k's
     // share of dW/dlf is -13/3 r_k A_k dA_k/dlf - r_k B_k dB_k/dlf.
     double r0, r1, r2;
@@ -295,13 +298,14 @@ __device__ __forceinline__ void weno_grad(const double lf[5], double d0, double 
         r1 = (E[1] * u[1]) * id1;
         r2 = (E[2] * u[2]) * id2;
     } else {
-        // s_k = (q_k - W)/sum(a) * c_k tau / d_k^2 = E_k tau P_k / N
+        // s_k = (q_k - W)/sum(a) * c_k tau / d_k^2 = E_k tau P_k / N (a quarter of it here)
         const double tau = t.tau;
         const double s0 = (E[0] * tau) * (t.P[0] * iN);
         const double s1 = (E[1] * tau) * (t.P[1] * iN);
         const double s2 = (E[2] * tau) * (t.P[2] * iN);
         // dW/dtau = 2 (s0 + s1 + s2); dtau/dbeta_2 = -dtau/dbeta_0 = sign(beta_2 - beta_0)
-        const double sh = d2 >= d0 ? s0 + s1 + s2 : -(s0 + s1 + s2);
+        const double st = 4.0 * (s0 + s1 + s2);
+        const double sh = d2 >= d0 ? st : -st;
         r0 = fma(s0 * tau, id0, sh);
         r1 = s1 * tau * id1;
         r2 = fma(s2 * tau, id2, -sh);
@@ -316,18 +320,21 @@ __device__ __forceinline__ void weno_grad(const double lf[5], double d0, double 
     g[3] = fma(a312, w1, fma(a321, w2, fma(k, PA1, fma(-2.0 * k, PA2, fma(4.0, NB2, NB1)))));
     g[4] = fma(a322, w2, fma(k, PA2, -NB2));
 }
-// The gradient alone (upwind5's is constant): the terms and value recomputed.
+// The gradient of a stencil's reconstruction alone (upwind5's is constant), its terms recomputed.
 template <int REC>
-__device__ __forceinline__ void recon_grad(const double lf[5], double d0, double d1, double d2, double g[5]) {
+__device__ __forceinline__ void recon_grad(const double lf[5], double g[5]) {
     if (REC == DENSE_RECON_UPWIND5) {
         g[0] = 2.0 / 60.0; g[1] = -13.0 / 60.0; g[2] = 47.0 / 60.0; g[3] = 27.0 / 60.0; g[4] = -3.0 / 60.0;
         return;
     }
     constexpr bool Z = REC == DENSE_RECON_WENOZ5;
+    double gd[4], d0, d1, d2;
+    first_differences(lf, gd);
+    betas_g(gd, d0, d1, d2);
     WenoTerms t;
-    weno_terms<Z>(lf, d0, d1, d2, t);
+    weno_terms<Z>(gd, d0, d1, d2, t);
     const double iN = rcp_nr(t.N);
-    weno_grad<Z>(lf, d0, d1, d2, t, weno_value(t, iN), iN, g);
+    weno_grad<Z>(gd, d0, d1, d2, t, weno_num(t) * iN, iN, g);
 }
 
 template <int REC> __device__ __forceinline__ double recon5(const double lf[5]) {
@@ -519,26 +526,52 @@ __device__ __forceinline__ bool roe_eig_fast(double g1, double sl, double sr, do
     return c2 > 0.0;
 }
 
+// Characteristic-wise WENO-Z at one interface and one sign from the stencil's centre split flux
+// Fc and its first differences dF[m] = F[m] - F[m+1] (m = 0..3): the projection is linear, so the
+// characteristic fields' first differences are the projected differences, and each field's
+// reconstruction works from them directly (weno_from_d).
 template <int DIR>
-__device__ __forceinline__ void char_weno_fast(const EigFast& e, const double F[5][4], double h[4]) {
-    double l0[5], l1[5], l2[5], l3[5];
+__device__ __forceinline__ void char_weno_fast_g(const EigFast& e, const double Fc[4], const double dF[4][4],
+                                                 double h[4]) {
+    auto proj = [&](const double f[4], double l[4]) {
+        l[0] = fma(e.l00, f[0], fma(e.l10, f[1], fma(e.l20, f[2], e.l30 * f[3])));
+        l[1] = fma(e.l01, f[0], fma(e.l11, f[1], fma(e.l21, f[2], e.l31 * f[3])));
+        l[2] = fma(-e.ut0, f[0], DIR == 0 ? f[2] : f[1]);
+        l[3] = fma(e.l03, f[0], fma(e.l13, f[1], fma(e.l23, f[2], e.l30 * f[3])));
+    };
+    double lc[4], gd[4][4];
+    proj(Fc, lc);
 #pragma unroll
-    for (int m = 0; m < 5; ++m) {
-        const double f0 = F[m][0], f1 = F[m][1], f2 = F[m][2], f3 = F[m][3];
-        l0[m] = fma(e.l00, f0, fma(e.l10, f1, fma(e.l20, f2, e.l30 * f3)));
-        l1[m] = fma(e.l01, f0, fma(e.l11, f1, fma(e.l21, f2, e.l31 * f3)));
-        l2[m] = fma(-e.ut0, f0, DIR == 0 ? f2 : f1);
-        l3[m] = fma(e.l03, f0, fma(e.l13, f1, fma(e.l23, f2, e.l30 * f3)));
+    for (int m = 0; m < 4; ++m) {
+        double l[4];
+        proj(dF[m], l);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) gd[k][m] = l[k];
     }
-    const double c0 = weno_fast<true>(l0), c1 = weno_fast<true>(l1);
-    const double c2 = weno_fast<true>(l2), c3 = weno_fast<true>(l3);
-    const double s = c0 + c1 + c3, d = c3 - c0;
+    double c[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        double d0, d1, d2;
+        betas_g(gd[k], d0, d1, d2);
+        c[k] = weno_from_d<true>(lc[k], gd[k], d0, d1, d2);
+    }
+    const double s = c[0] + c[1] + c[3], d = c[3] - c[0];
     const double hn = fma(e.un0, s, e.a0 * d);
-    const double ht = fma(e.ut0, s, c2);
+    const double ht = fma(e.ut0, s, c[2]);
     h[0] = s;
     h[1 + DIR] = hn;
     h[2 - DIR] = ht;
-    h[3] = fma(e.h0, c0 + c3, fma(e.a0un0, d, fma(e.uu0, c1, e.ut0 * c2)));
+    h[3] = fma(e.h0, c[0] + c[3], fma(e.a0un0, d, fma(e.uu0, c[1], e.ut0 * c[2])));
+}
+// The same from the stencil's five split fluxes F[m][c].
+template <int DIR>
+__device__ __forceinline__ void char_weno_fast(const EigFast& e, const double F[5][4], double h[4]) {
+    double dF[4][4];
+#pragma unroll
+    for (int m = 0; m < 4; ++m)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) dF[m][c] = F[m][c] - F[m + 1][c];
+    char_weno_fast_g<DIR>(e, F[2], dF, h);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -577,18 +610,23 @@ __device__ __forceinline__ void stage_scalars(const Params& p, int irk) {
 // xi tile: TX interfaces x TY rows, cells f0+1 .. f0+TX+5; eta tile: TX columns x TY interfaces.
 // Dynamic shared memory of one block, in doubles: the split fluxes sF[8][NL][NC] (F+ of the four
 // components, then F-) and, for the WENO reconstructions of the fast variant, the indicators'
-// second-difference terms sS[8][NL][NC] of the same cells (F+ then F-).
+// second-difference terms sS[8][NL][NC] and the forward differences sG[8][NL][NC] = F(k) - F(k+1)
+// along the sweep of the same cells (F+ then F-): a cell's terms serve up to four interfaces.
 template <int DIR, int REC, int TX, int TY>
 struct CwTile {
     static constexpr int NL = DIR == 0 ? TY : TY + 5;   // smem rows
     static constexpr int NC = DIR == 0 ? TX + 5 : TX;   // smem columns
     static constexpr int NCELL = NL * NC;
     static constexpr bool kStageS = FAST && REC != DENSE_RECON_UPWIND5;
-    static constexpr size_t bytes = sizeof(double) * (size_t)NCELL * (kStageS ? 16 : 8);
+    static constexpr size_t bytes = sizeof(double) * (size_t)NCELL * (kStageS ? 24 : 8);
 };
 
-template <int DIR, int SPL, int REC, int TX, int TY, bool TAPE = false>
+// TZ threads share an interface (threadIdx.z): they stage the tile's cells together and each
+// reconstructs the components tz, tz + TZ, ...; the arithmetic of every component is the same
+// whatever TZ, so the results do not depend on it.
+template <int DIR, int SPL, int REC, int TX, int TY, bool TAPE = false, int TZ = 1>
 __device__ __forceinline__ void flux_cw_block(const Params& p, int irk, int bx, int by) {
+    static_assert(TZ == 1 || TZ == 2 || TZ == 4, "TZ divides the four components");
     if (!p.sc->active) return;
     using L = CwTile<DIR, REC, TX, TY>;
     constexpr int NL = L::NL, NC = L::NC, NCELL = L::NCELL;
@@ -596,11 +634,12 @@ __device__ __forceinline__ void flux_cw_block(const Params& p, int irk, int bx, 
     extern __shared__ __align__(16) double dsm[];
     double* const sF = dsm;
     double* const sS = dsm + 8 * NCELL;
-    (void)sS; (void)NL;
+    double* const sG = dsm + 16 * NCELL;
+    (void)sS; (void)sG; (void)NL;
     auto at = [&](int r, int c) { return chk(p, r, NL) * NC + chk(p, c, NC); };
-    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int tx = threadIdx.x, ty = threadIdx.y, tz = TZ == 1 ? 0 : (int)threadIdx.z;
     const int slot = irk - 1;
-    if (DIR == 0 && bx == 0 && by == 0 && tx == 0 && ty == 0) stage_scalars(p, irk);
+    if (DIR == 0 && bx == 0 && by == 0 && tx == 0 && ty == 0 && tz == 0) stage_scalars(p, irk);
     const double lam_g = p.sc->maxeig[slot][DIR];
     const int NIp = p.ni + 2 * kB, NJp = p.nj + 2 * kB;
 
@@ -625,14 +664,14 @@ __device__ __forceinline__ void flux_cw_block(const Params& p, int irk, int bx, 
     if (DIR == 0) {
         const int f0 = bx * TX, j = by * TY + ty;
         if (j < p.nj)
-            for (int k = tx; k < TX + 5; k += TX) {
+            for (int k = tx + TX * tz; k < TX + 5; k += TX * TZ) {
                 const int I = f0 + 1 + k;
                 if (I < NIp) cell(I, j + kB, ty, k);
             }
     } else {
         const int g0 = by * TY, i = bx * TX + tx;
         if (i < p.ni)
-            for (int k = ty; k < TY + 5; k += TY) {
+            for (int k = ty + TY * tz; k < TY + 5; k += TY * TZ) {
                 const int J = g0 + 1 + k;
                 if (J < NJp) cell(i + kB, J, k, tx);
             }
@@ -641,16 +680,18 @@ __device__ __forceinline__ void flux_cw_block(const Params& p, int irk, int bx, 
 
     // phase 1b (fast WENO): the indicators' second-difference terms, once per cell and sign for
     // the cells with both neighbours in the tile ("+" reads a cell's neighbours as k-1, k, k+1,
-    // "-" as k+1, k, k-1)
+    // "-" as k+1, k, k-1), and the forward differences of the cells with a next neighbour
     if constexpr (kStageS) {
         constexpr int KN = DIR == 0 ? TX + 5 : TY + 5;   // cells along the sweep
-        const int tid = tx + ty * TX;
-        for (int e = tid; e < 8 * NCELL; e += TX * TY) {
+        const int tid = tx + ty * TX + tz * TX * TY;
+        for (int e = tid; e < 8 * NCELL; e += TX * TY * TZ) {
             const int q = e / NCELL, o = e - q * NCELL;
             const int k = DIR == 0 ? o % NC : o / NC;
-            if (k == 0 || k == KN - 1) continue;
+            if (k == KN - 1) continue;
             const int st = DIR == 0 ? 1 : NC;             // neighbour along the sweep
             const double* F = sF + q * NCELL + o;
+            sG[e] = F[0] - F[st];
+            if (k == 0) continue;
             sS[e] = q < 4 ? ind_second(F[-st], F[0], F[st]) : ind_second(F[st], F[0], F[-st]);
         }
         __syncthreads();
@@ -670,70 +711,74 @@ __device__ __forceinline__ void flux_cw_block(const Params& p, int irk, int bx, 
                             : p.tape + (DIR == 0 ? 0 : tape_planes(REC) * (long long)p.nj * (p.ni + 1)) +
                                   fidx<DIR>(p, 0, line, f);
     (void)tape_at;
+    [[maybe_unused]] const long long ts = DIR == 0 ? (long long)p.nj * (p.ni + 1) : (long long)(p.nj + 1) * p.ni;
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {
-        double lp[5], lm[5];
-#pragma unroll
-        for (int m = 0; m < 5; ++m) {
-            // "+": lf(m) = F+(cell f+3+m), smem index t+2+m; "-": lf(m) = F-(cell f+4-m), index t+3-m
-            lp[m] = sF[v * NCELL + atk(t + m)];
-            lm[m] = sF[(4 + v) * NCELL + atk(t + 5 - m)];
-        }
-        // the adjoint's tape: the reconstruction's gradient for stencil slot m0 (0 "+", 5 "-")
-        [[maybe_unused]] auto tape_grad = [&](const double lf[5], double d0, double d1, double d2, int m0) {
-            if constexpr (TAPE && REC != DENSE_RECON_UPWIND5) {
-                const long long ts = DIR == 0 ? (long long)p.nj * (p.ni + 1) : (long long)(p.nj + 1) * p.ni;
-                double g[5];
-                recon_grad<REC>(lf, d0, d1, d2, g);
-#pragma unroll
-                for (int m = 0; m < 5; ++m) tape_at[((m0 + m) * 4 + v) * ts] = g[m];
-            }
-        };
+    for (int vz = 0; vz < 4 / TZ; ++vz) {
+        const int v = tz + vz * TZ;
         double h;
         if constexpr (kStageS) {
-            // "+" substencils centred on tile cells t+1, t+2, t+3; "-" on t+4, t+3, t+2
+            // "+": lf(m) = F+(tile cell t+m), g_m = G+(t+m), substencils centred on t+1, t+2, t+3;
+            // "-": lf(m) = F-(tile cell t+5-m), g_m = F-(t+5-m) - F-(t+4-m) = -G-(t+4-m),
+            // substencils centred on t+4, t+3, t+2
             constexpr bool Z = REC == DENSE_RECON_WENOZ5;
             const double* Sp = sS + v * NCELL;
             const double* Sm = sS + (4 + v) * NCELL;
-            // the value, and for the tape its gradient from the same terms
-            auto recon_taped = [&](const double lf[5], double d0, double d1, double d2, int m0) -> double {
+            const double* Gp = sG + v * NCELL;
+            const double* Gm = sG + (4 + v) * NCELL;
+            double gp[4], gm[4];
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                gp[m] = Gp[atk(t + m)];
+                gm[m] = -Gm[atk(t + 4 - m)];
+            }
+            const double lp2 = sF[v * NCELL + atk(t + 2)], lm2 = sF[(4 + v) * NCELL + atk(t + 3)];
+            // the value, and for the tape its gradient from the same terms (stencil slot m0:
+            // 0 "+", 5 "-")
+            auto recon_taped = [&](double lf2, const double gd[4], double d0, double d1, double d2,
+                                   int m0) -> double {
                 if constexpr (TAPE) {
                     WenoTerms tt;
-                    weno_terms<Z>(lf, d0, d1, d2, tt);
+                    weno_terms<Z>(gd, d0, d1, d2, tt);
                     const double iN = rcp_nr(tt.N);
-                    const double hv = weno_value(tt, iN);
-                    const long long ts = DIR == 0 ? (long long)p.nj * (p.ni + 1) : (long long)(p.nj + 1) * p.ni;
+                    const double num = weno_num(tt);
                     double g[5];
-                    weno_grad<Z>(lf, d0, d1, d2, tt, hv, iN, g);
+                    weno_grad<Z>(gd, d0, d1, d2, tt, num * iN, iN, g);
 #pragma unroll
                     for (int m = 0; m < 5; ++m) tape_at[((m0 + m) * 4 + v) * ts] = g[m];
-                    return hv;
+                    return fma(num, iN, lf2);
                 } else {
                     (void)m0;
-                    return weno_from_d<Z>(lf, d0, d1, d2);
+                    return weno_from_d<Z>(lf2, gd, d0, d1, d2);
                 }
             };
             double d0, d1, d2;
-            betas_staged(lp, Sp[atk(t + 1)], Sp[atk(t + 2)], Sp[atk(t + 3)], d0, d1, d2);
-            const double hp = recon_taped(lp, d0, d1, d2, 0);
-            betas_staged(lm, Sm[atk(t + 4)], Sm[atk(t + 3)], Sm[atk(t + 2)], d0, d1, d2);
-            const double hm = recon_taped(lm, d0, d1, d2, 5);
+            betas_staged(gp, Sp[atk(t + 1)], Sp[atk(t + 2)], Sp[atk(t + 3)], d0, d1, d2);
+            const double hp = recon_taped(lp2, gp, d0, d1, d2, 0);
+            betas_staged(gm, Sm[atk(t + 4)], Sm[atk(t + 3)], Sm[atk(t + 2)], d0, d1, d2);
+            const double hm = recon_taped(lm2, gm, d0, d1, d2, 5);
             h = hp + hm;
         } else {
+            double lp[5], lm[5];
+#pragma unroll
+            for (int m = 0; m < 5; ++m) {
+                // "+": lf(m) = F+(cell f+3+m), smem index t+2+m; "-": lf(m) = F-(cell f+4-m), index t+3-m
+                lp[m] = sF[v * NCELL + atk(t + m)];
+                lm[m] = sF[(4 + v) * NCELL + atk(t + 5 - m)];
+            }
             h = recon5<REC>(lp) + recon5<REC>(lm);
             if constexpr (TAPE && REC != DENSE_RECON_UPWIND5) {
-                double d0, d1, d2, tau;
-                betas_fast(lp, d0, d1, d2, tau);
-                tape_grad(lp, d0, d1, d2, 0);
-                betas_fast(lm, d0, d1, d2, tau);
-                tape_grad(lm, d0, d1, d2, 5);
+                // the adjoint's tape: the reconstructions' gradients for stencil slots 0 ("+") and 5 ("-")
+                double g[5];
+                recon_grad<REC>(lp, g);
+#pragma unroll
+                for (int m = 0; m < 5; ++m) tape_at[(m * 4 + v) * ts] = g[m];
+                recon_grad<REC>(lm, g);
+#pragma unroll
+                for (int m = 0; m < 5; ++m) tape_at[((5 + m) * 4 + v) * ts] = g[m];
             }
         }
         (DIR == 0 ? p.hx : p.he)[fidx<DIR>(p, v, line, f)] = h;
-        if constexpr (TAPE) {
-            const long long ts = DIR == 0 ? (long long)p.nj * (p.ni + 1) : (long long)(p.nj + 1) * p.ni;
-            tape_at[(tape_planes(REC) - 4 + v) * ts] = h;
-        }
+        if constexpr (TAPE) tape_at[(tape_planes(REC) - 4 + v) * ts] = h;
     }
 }
 
@@ -778,7 +823,9 @@ struct CharTile {
     static constexpr bool kStageHS = FAST && !ADAPT;
     static constexpr bool kStageInd = FAST && ADAPT;
     static constexpr int kF = 0, kQ = kF + 8 * NCELL, kS = kQ + 4 * NCELL;
-    static constexpr int kR = kS + (kStageHS ? NCELL : 0);
+    // 104, fast: the forward differences of the split fluxes along the sweep, F(k) - F(k+1)
+    static constexpr int kDF = kS + (kStageHS ? NCELL : 0);
+    static constexpr int kR = kDF + (kStageHS ? 8 * NCELL : 0);
     static constexpr int kRSize = !ADAPT ? 0
                                   : (kStageInd ? (8 * NCELL > 8 * NT ? 8 * NCELL : 8 * NT)
                                                : (2 * NCELL > 8 * NT ? 2 * NCELL : 8 * NT));
@@ -852,14 +899,29 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
     }
     __syncthreads();
 
-    // phase 1b (AdaWENO, fast): per cell and sign, half the surrogate's second difference
-    // A/2 = (sur(k-1) + sur(k+1))/2 - sur(k) (symmetric, so the same for both stencil
-    // directions), the squared-difference term ss + 13/12 A^2 = ss + 13/3 (A/2)^2 of the
-    // smoothness indicators, and the first difference sur(k+1) - sur(k); an interface's
-    // indicators then need only their first-order terms. Halving A lets the interfaces form
-    // B_k/2 with an add and square it in the indicator's FMA, with no 1/4 factor.
-    double* const sD2 = sR + 2 * NCELL;   // [2][NCELL]: A/2
-    double* const sA2 = sR + 4 * NCELL;   // [2][NCELL]: ss + 13/12 A^2
+    // phase 1b (104, fast): the split fluxes' forward differences along the sweep, once per cell
+    // and sign for the cells with a next neighbour in the tile (each serves four interfaces)
+    double* const sDF = dsm + L::kDF;
+    if constexpr (kStageHS) {
+        constexpr int KN = L::KW + 5;
+        constexpr int st = DIR == 0 ? 1 : NC;            // neighbour along the sweep
+        for (int e = tid; e < 8 * NCELL; e += NT) {
+            const int o = e % NCELL;
+            const int k = DIR == 0 ? o % NC : o / NC;
+            if (k < KN - 1) sDF[e] = sF[e] - sF[e + st];
+        }
+        __syncthreads();
+    }
+
+    // phase 1b (AdaWENO, fast): per cell and sign, the surrogate's second difference
+    // A = sur(k-1) + sur(k+1) - 2 sur(k) (symmetric, so the same for both stencil directions),
+    // four times the squared-difference term ss + 13/12 A^2 of the smoothness indicators, and
+    // the first difference sur(k+1) - sur(k); an interface's indicators then need only their
+    // first-order terms. With the factor 4 (exact in binary) the interfaces add B_k^2 in the
+    // indicator's FMA with no 1/4 product; the weights and the switch compare homogeneous
+    // products of the d_k, which that scale leaves unchanged.
+    double* const sD2 = sR + 2 * NCELL;   // [2][NCELL]: A
+    double* const sA2 = sR + 4 * NCELL;   // [2][NCELL]: 4 (ss + 13/12 A^2)
     double* const sDl = sR + 6 * NCELL;   // [2][NCELL]: sur(k+1) - sur(k)
     if constexpr (kStageInd) {
         constexpr int KN = L::KW + 5;                    // cells along the sweep
@@ -873,9 +935,9 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
 #pragma unroll
             for (int sg = 0; sg < 2; ++sg) {
                 const double* su = sR + sg * NCELL;
-                const double ah = fma(0.5, su[om] + su[op], -su[o]);
-                sD2[sg * NCELL + o] = ah;
-                sA2[sg * NCELL + o] = fma(k133 * ah, ah, kSS);
+                const double a = fma(-2.0, su[o], su[om] + su[op]);
+                sD2[sg * NCELL + o] = a;
+                sA2[sg * NCELL + o] = fma(k133 * a, a, 4.0 * kSS);
                 sDl[sg * NCELL + o] = su[op] - su[o];
             }
         }
@@ -959,9 +1021,26 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
         double hsum[4];
 #pragma unroll
         for (int s = 0; s < 2; ++s) {
-            double F[5][4], h[4];
+            double h[4];
+#if FAST
+            // "+": centre F+(t+2), differences F+(t+m) - F+(t+m+1) = DF+(t+m); "-": centre
+            // F-(t+3), differences F-(t+5-m) - F-(t+4-m) = -DF-(t+4-m)
+            const int t = DIR == 0 ? tx : ty;
+            double Fc[4], dF[4][4];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                Fc[c] = s == 0 ? SF(c, t + 2, tx, ty) : SF(4 + c, t + 3, tx, ty);
+#pragma unroll
+                for (int m = 0; m < 4; ++m)
+                    dF[m][c] = s == 0 ? sDF[c * NCELL + atk(t + m, tx, ty)]
+                                      : -sDF[(4 + c) * NCELL + atk(t + 4 - m, tx, ty)];
+            }
+            char_weno_fast_g<DIR>(e, Fc, dF, h);
+#else
+            double F[5][4];
             stencil(tx, ty, s, F);
             char_recon(e, F, h);
+#endif
 #pragma unroll
             for (int c = 0; c < 4; ++c) hsum[c] = s == 0 ? h[c] : hsum[c] + h[c];
         }
@@ -982,17 +1061,18 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
                 const double* D2 = sD2 + s * NCELL;
                 const double* A2 = sA2 + s * NCELL;
                 const double* Dl = sDl + s * NCELL;
-                const double A0h = D2[atk(c0, tx, ty)], A2h = D2[atk(c2, tx, ty)];
+                const double A0 = D2[atk(c0, tx, ty)], A2c = D2[atk(c2, tx, ty)];
                 const double dl1 = Dl[atk(s == 0 ? t + 1 : t + 3, tx, ty)];
                 const double dl2 = Dl[atk(t + 2, tx, ty)];
                 // B0 = lf0 - 4 lf1 + 3 lf2 = A0 +- 2 dl1, B1 = lf1 - lf3 = -+(dl1 + dl2),
-                // B2 = 3 lf2 - 4 lf3 + lf4 = A2 -+ 2 dl2 (upper signs "+", lower "-"), halved
-                const double B0h = s == 0 ? A0h + dl1 : A0h - dl1;
+                // B2 = 3 lf2 - 4 lf3 + lf4 = A2 -+ 2 dl2 (upper signs "+", lower "-"); d_k here
+                // is 4 (ss + beta_k)
+                const double B0 = fma(s == 0 ? 2.0 : -2.0, dl1, A0);
                 const double B1 = dl1 + dl2;
-                const double B2h = s == 0 ? A2h - dl2 : A2h + dl2;
-                const double d0 = fma(B0h, B0h, A2[atk(c0, tx, ty)]);
-                const double d1 = fma(0.25 * B1, B1, A2[atk(cm + (s == 0 ? 0 : 1), tx, ty)]);
-                const double d2 = fma(B2h, B2h, A2[atk(c2, tx, ty)]);
+                const double B2 = fma(s == 0 ? -2.0 : 2.0, dl2, A2c);
+                const double d0 = fma(B0, B0, A2[atk(c0, tx, ty)]);
+                const double d1 = fma(B1, B1, A2[atk(cm + (s == 0 ? 0 : 1), tx, ty)]);
+                const double d2 = fma(B2, B2, A2[atk(c2, tx, ty)]);
                 // WENO-Z over the common denominator D = prod d_k^2, P_k = D/d_k^2, T = tau^2:
                 // alpha_k D = c_k (D + T P_k); since sum c_k = 1, N = (sum alpha) D = D + T Q with
                 // Q = sum c_k P_k, and theta > delta <=> D > theta_c N. Both sides are positive,
@@ -1543,9 +1623,9 @@ __device__ __forceinline__ void bc_block(const Params& p, int bx) {
 // registers instead of 94, a few bytes spilled: the xi sweep 2 % faster on the 1920 x 480 double
 // Mach reflection); the 104 eta sweep lost 4 % that way and keeps its natural 96 registers.
 constexpr int char_min_blocks(bool adapt) { return adapt ? 3 : 1; }
-template <int DIR, int SPL, int REC, int TX, int TY, bool TAPE = false>
-__global__ void __launch_bounds__(TX* TY) k_flux_cw(Params p, int irk) {
-    flux_cw_block<DIR, SPL, REC, TX, TY, TAPE>(p, irk, blockIdx.x, blockIdx.y);
+template <int DIR, int SPL, int REC, int TX, int TY, bool TAPE = false, int TZ = 1>
+__global__ void __launch_bounds__(TX* TY* TZ) k_flux_cw(Params p, int irk) {
+    flux_cw_block<DIR, SPL, REC, TX, TY, TAPE, TZ>(p, irk, blockIdx.x, blockIdx.y);
 }
 template <int DIR, bool ADAPT, int TX, int TY>
 __global__ void __launch_bounds__(TX* TY, char_min_blocks(ADAPT)) k_flux_char(Params p, int irk) {
@@ -1653,25 +1733,30 @@ static int sm_count() {
 }
 
 // A component-wise sweep on its tile's dynamic shared memory.
-template <int DIR, int SPL, int REC, int TX, int TY, bool TAPE = false>
+template <int DIR, int SPL, int REC, int TX, int TY, bool TAPE = false, int TZ = 1>
 static void cw_launch(dim3 g, const Params& p, int irk, cudaStream_t s) {
-    k_flux_cw<DIR, SPL, REC, TX, TY, TAPE><<<g, dim3(TX, TY), CwTile<DIR, REC, TX, TY>::bytes, s>>>(p, irk);
+    k_flux_cw<DIR, SPL, REC, TX, TY, TAPE, TZ><<<g, dim3(TX, TY, TZ), CwTile<DIR, REC, TX, TY>::bytes, s>>>(p, irk);
 }
 
 // On small grids the standard tiles give a sweep only one or two blocks per SM, and the SMs that
 // get one more block than the others set the launch's time. Below four blocks per SM the sweep
-// runs with shorter tiles, which multiplies the block count (same arithmetic per interface: the
-// results do not depend on the tile).
+// runs with shorter tiles, which multiplies the block count, and with four threads per
+// interface (one per component: four times the warps to hide the dependent FP64 chains of a
+// sweep that is only one wave deep); same arithmetic per interface, so the results do not
+// depend on the tile. Measured on the 200 x 200 vortex: 1.925e8 -> 1.976e8 cell-updates/s for
+// the four threads; on 512 x 512 and larger grids the standard tiles gain nothing from them.
+// The adjoint's taping sweeps keep one thread per interface (no gain measured).
+constexpr int cw_small_tz(bool tape) { return tape ? 1 : 4; }
 template <int SPL, int REC, bool TAPE = false>
 static void launch_cw(const Params& p, int irk, int dir, cudaStream_t s) {
     const unsigned few = 4u * sm_count();
     if (dir == 0) {
         const dim3 g = grid_xi(p, kXTX, kXTY);
-        if (g.x * g.y < few) cw_launch<0, SPL, REC, kXTX, kXSTY, TAPE>(grid_xi(p, kXTX, kXSTY), p, irk, s);
+        if (g.x * g.y < few) cw_launch<0, SPL, REC, kXTX, kXSTY, TAPE, cw_small_tz(TAPE)>(grid_xi(p, kXTX, kXSTY), p, irk, s);
         else                 cw_launch<0, SPL, REC, kXTX, kXTY, TAPE>(g, p, irk, s);
     } else {
         const dim3 g = grid_eta(p, kETX, kETY);
-        if (g.x * g.y < few) cw_launch<1, SPL, REC, kETX, kESTY, TAPE>(grid_eta(p, kETX, kESTY), p, irk, s);
+        if (g.x * g.y < few) cw_launch<1, SPL, REC, kETX, kESTY, TAPE, cw_small_tz(TAPE)>(grid_eta(p, kETX, kESTY), p, irk, s);
         else                 cw_launch<1, SPL, REC, kETX, kETY, TAPE>(g, p, irk, s);
     }
 }
@@ -1844,14 +1929,14 @@ static void allow_smem(K kernel, size_t bytes) {
 template <int SPL, int REC>
 static void allow_cw_smem() {
     allow_smem(k_flux_cw<0, SPL, REC, kXTX, kXTY>, CwTile<0, REC, kXTX, kXTY>::bytes);
-    allow_smem(k_flux_cw<0, SPL, REC, kXTX, kXSTY>, CwTile<0, REC, kXTX, kXSTY>::bytes);
+    allow_smem(k_flux_cw<0, SPL, REC, kXTX, kXSTY, false, cw_small_tz(false)>, CwTile<0, REC, kXTX, kXSTY>::bytes);
     allow_smem(k_flux_cw<1, SPL, REC, kETX, kETY>, CwTile<1, REC, kETX, kETY>::bytes);
-    allow_smem(k_flux_cw<1, SPL, REC, kETX, kESTY>, CwTile<1, REC, kETX, kESTY>::bytes);
+    allow_smem(k_flux_cw<1, SPL, REC, kETX, kESTY, false, cw_small_tz(false)>, CwTile<1, REC, kETX, kESTY>::bytes);
     // the adjoint's taping sweeps
     allow_smem(k_flux_cw<0, SPL, REC, kXTX, kXTY, true>, CwTile<0, REC, kXTX, kXTY>::bytes);
-    allow_smem(k_flux_cw<0, SPL, REC, kXTX, kXSTY, true>, CwTile<0, REC, kXTX, kXSTY>::bytes);
+    allow_smem(k_flux_cw<0, SPL, REC, kXTX, kXSTY, true, cw_small_tz(true)>, CwTile<0, REC, kXTX, kXSTY>::bytes);
     allow_smem(k_flux_cw<1, SPL, REC, kETX, kETY, true>, CwTile<1, REC, kETX, kETY>::bytes);
-    allow_smem(k_flux_cw<1, SPL, REC, kETX, kESTY, true>, CwTile<1, REC, kETX, kESTY>::bytes);
+    allow_smem(k_flux_cw<1, SPL, REC, kETX, kESTY, true, cw_small_tz(true)>, CwTile<1, REC, kETX, kESTY>::bytes);
     // the batched tile variants of batch_cw_variant
     allow_smem(kb_flux_cw<0, SPL, REC, 32, 4>, CwTile<0, REC, 32, 4>::bytes);
     allow_smem(kb_flux_cw<0, SPL, REC, 64, 2>, CwTile<0, REC, 64, 2>::bytes);
