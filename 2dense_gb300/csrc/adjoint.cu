@@ -41,6 +41,7 @@
 
 #include <climits>
 #include <cmath>
+#include <cstring>
 #include <string>
 #include <vector>
 
@@ -780,6 +781,14 @@ struct dense_adjoint {
     cudaEvent_t ev_in = nullptr, ev_out = nullptr;
     long long launches = 0;
     std::string err;
+    // A full segment's recompute and reverse as CUDA graphs, the same for every segment: they
+    // read and write the segment buffers (rec, tape) and the segment's slices of the time steps
+    // and maxima cells, copied into seg_dts / out of seg_argmax around the reverse.
+    cudaGraphExec_t rec_exec = nullptr, rev_exec = nullptr;
+    long long rec_nodes = 0, rev_nodes = 0;
+    dense::Params rec_prm{};                      // the solver parameters rec_exec was built with
+    double* seg_dts = nullptr;
+    int* seg_argmax = nullptr;
 };
 
 namespace {
@@ -848,8 +857,8 @@ int restart(dense_adjoint* a, const double* state) {
 }
 
 // one stage of the forward solver with taping sweeps: boundary, flux_tape xi and eta, update.
-// Launched directly on the solver's stream: forking the eta sweep onto a second stream, which
-// pays in the step graph, made the eagerly launched backward 34 % slower.
+// Launched eagerly, directly on the solver's stream: forking the eta sweep onto a second stream
+// made the eagerly launched backward 34 % slower (the fork pays inside a graph: graph_stage).
 int taped_stage(dense_adjoint* a, int irk, double* tape) {
     dense_handle* h = a->h;
     dense::Params p = h->prm;
@@ -860,6 +869,29 @@ int taped_stage(dense_adjoint* a, int irk, double* tape) {
     h->kt->update(h->prm, irk, h->stream);
     a->launches += 4;
     return DENSE_OK;
+}
+// The same stage as graph nodes (under stream capture), like the step graph's stage: the eta
+// taping sweep a branch beside the xi sweep, and on grids periodic in x and y no boundary fill
+// in stages 2 and 3 (the previous update wrote the ghost layers).
+cudaError_t graph_stage(dense_adjoint* a, int irk, double* tape) {
+    dense_handle* h = a->h;
+    dense::Params p = h->prm;
+    p.tape = tape;
+    if (irk == 1 || !h->prm.periodic_ghosts) {
+        h->kt->bc(h->prm, h->stream);
+        a->launches += 1;
+    }
+    cudaError_t e = cudaEventRecord(h->ev_fork, h->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(h->side, h->ev_fork, 0);
+    if (e != cudaSuccess) return e;
+    h->kt->flux_tape(p, irk, 1, h->side);
+    h->kt->flux_tape(p, irk, 0, h->stream);
+    e = cudaEventRecord(h->ev_join, h->side);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(h->stream, h->ev_join, 0);
+    if (e != cudaSuccess) return e;
+    h->kt->update(h->prm, irk, h->stream);
+    a->launches += 3;
+    return cudaSuccess;
 }
 
 template <int REC, int SPL, bool WALLS>
@@ -922,10 +954,10 @@ void vjp(dense_adjoint* a, int stage, const double* u, const double* tape, const
     }
 }
 
-// reverse of one step from its three recorded stage states and tapes; g holds dJ/du(n+1) on
-// entry and dJ/du(n) on return
-void reverse_step(dense_adjoint* a, const double* rec_step, const double* tape_step, int step) {
-    const double* dtp = a->dts + step;
+// reverse of one step from its three recorded stage states and tapes, its time step *dtp and
+// the slot of its maxima cells; g holds dJ/du(n+1) on entry and dJ/du(n) on return
+void reverse_step(dense_adjoint* a, const double* rec_step, const double* tape_step, const double* dtp,
+                  int* argmax) {
     const double* u[3] = {rec_step, rec_step + a->state, rec_step + 2 * a->state};
     const double* t[3] = {tape_step, tape_step + a->tape_stage, tape_step + 2 * a->tape_stage};
     vjp(a, 3, u[2], t[2], a->g, a->g2, a->part + 2 * a->npart, dtp);
@@ -933,9 +965,82 @@ void reverse_step(dense_adjoint* a, const double* rec_step, const double* tape_s
     vjp(a, 1, u[0], t[0], a->g1, a->g, a->part, dtp);
     if (!a->cfg.if_const_dt) {
         dense::adj::k_dt<<<1, 256, 0, a->h->stream>>>(a->ap, a->part, a->npart, a->mpart, a->nm, u[0], a->g, dtp,
-                                                      a->argmax + 2 * step);
+                                                      argmax);
         a->launches += 1;
     }
+}
+
+// record the stage inputs of a segment's step s and recompute it with taping sweeps
+int recompute_step(dense_adjoint* a, int s, bool graph) {
+    dense_handle* h = a->h;
+    h->kt->step_begin(h->prm, h->stream);
+    for (int irk = 1; irk <= 3; ++irk) {
+        int rc = from_solver(a, a->rec + ((size_t)s * 3 + irk - 1) * a->state);
+        if (rc) return rc;
+        double* tape = a->tape + ((size_t)s * 3 + irk - 1) * a->tape_stage;
+        if (graph) {
+            const cudaError_t e = graph_stage(a, irk, tape);
+            if (e != cudaSuccess) return aerr(a, DENSE_ERR_CUDA, std::string("segment graph: ") + cudaGetErrorString(e));
+        } else {
+            rc = taped_stage(a, irk, tape);
+            if (rc) return rc;
+        }
+    }
+    h->kt->step_end(h->prm, h->stream);
+    a->launches += 2;
+    return DENSE_OK;
+}
+
+// Capture `body` (launches on the solver's stream) as a graph; *nodes = the kernels it launched.
+template <class F>
+int capture(dense_adjoint* a, F body, cudaGraphExec_t* exec, long long* nodes) {
+    dense_handle* h = a->h;
+    if (*exec) cudaGraphExecDestroy(*exec);
+    *exec = nullptr;
+    const long long l0 = a->launches;
+    ACK(a, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    const int rc = body();
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+    *nodes = a->launches - l0;
+    a->launches = l0;
+    if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) return aerr(a, DENSE_ERR_CUDA, std::string("segment capture: ") + cudaGetErrorString(e));
+    const cudaError_t ie = cudaGraphInstantiate(exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) return aerr(a, DENSE_ERR_CUDA, std::string("segment graph: ") + cudaGetErrorString(ie));
+    return DENSE_OK;
+}
+
+// the graphs of a full segment (k steps), built on first use and again when the solver's
+// parameters have changed since
+int segment_graphs(dense_adjoint* a) {
+    dense_handle* h = a->h;
+    if (!a->rec_exec || std::memcmp(&a->rec_prm, &h->prm, sizeof(h->prm)) != 0) {
+        AH(a, dense::handle_ensure_side(h));
+        int rc = capture(a, [&] {
+            for (int s = 0; s < a->k; ++s) {
+                const int r = recompute_step(a, s, true);
+                if (r) return r;
+            }
+            return (int)DENSE_OK;
+        }, &a->rec_exec, &a->rec_nodes);
+        if (rc) return rc;
+        a->rec_prm = h->prm;
+    }
+    if (!a->rev_exec) {
+        int rc = capture(a, [&] {
+            for (int s = a->k - 1; s >= 0; --s)
+                reverse_step(a, a->rec + (size_t)s * 3 * a->state, a->tape + (size_t)s * 3 * a->tape_stage,
+                             a->seg_dts + s, a->seg_argmax + 2 * s);
+            return (int)DENSE_OK;
+        }, &a->rev_exec, &a->rev_nodes);
+        if (rc) return rc;
+    }
+    return DENSE_OK;
 }
 
 template <class T>
@@ -967,9 +1072,12 @@ void dense_adjoint_destroy(dense_adjoint_t* a) {
     if (!a) return;
     if (a->h) cudaStreamSynchronize(a->h->stream);
     double* bufs[] = {a->ckpt, a->dts, a->rec, a->tape, a->g, a->g1, a->g2, a->acc, a->hb, a->part, a->mpart,
-                      a->lamv, a->lmp, a->lpart};
+                      a->lamv, a->lmp, a->lpart, a->seg_dts};
     for (double* b : bufs) if (b) cudaFree(b);
     if (a->argmax) cudaFree(a->argmax);
+    if (a->seg_argmax) cudaFree(a->seg_argmax);
+    if (a->rec_exec) cudaGraphExecDestroy(a->rec_exec);
+    if (a->rev_exec) cudaGraphExecDestroy(a->rev_exec);
     if (a->ev_in) cudaEventDestroy(a->ev_in);
     if (a->ev_out) cudaEventDestroy(a->ev_out);
     if (a->h) dense_destroy(a->h);
@@ -1036,11 +1144,15 @@ int dense_adjoint_create(const dense_config_t* cfg, int checkpoint_every, dense_
         {&a->g, a->state}, {&a->g1, a->state}, {&a->g2, a->state}, {&a->acc, a->state},
         {&a->hb, (size_t)4 * (p.xs + p.ys)}, {&a->part, (size_t)3 * a->npart}, {&a->mpart, (size_t)4 * a->nm},
         {&a->rec, (size_t)3 * a->k * a->state}, {&a->tape, (size_t)3 * a->k * a->tape_stage},
-        {&a->lamv, 4}, {&a->lmp, (size_t)4 * a->nm}, {&a->lpart, (size_t)2 * a->nm},
+        {&a->lamv, 4}, {&a->lmp, (size_t)4 * a->nm}, {&a->lpart, (size_t)2 * a->nm}, {&a->seg_dts, (size_t)a->k},
     };
     for (auto& b : bufs) {
         cudaError_t e = cudaMalloc((void**)b.p, b.n * sizeof(double));
         if (e != cudaSuccess) { a->err = std::string("cudaMalloc: ") + cudaGetErrorString(e); return fail(DENSE_ERR_NOMEM); }
+    }
+    if (cudaMalloc((void**)&a->seg_argmax, (size_t)2 * a->k * sizeof(int)) != cudaSuccess) {
+        a->err = "cudaMalloc of the segment's maxima cells failed";
+        return fail(DENSE_ERR_NOMEM);
     }
     if (cudaEventCreateWithFlags(&a->ev_in, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&a->ev_out, cudaEventDisableTiming) != cudaSuccess) {
@@ -1092,23 +1204,33 @@ int dense_adjoint_backward(dense_adjoint_t* a, const double* gT, double* g0, voi
     dense_handle* h = a->h;
     ACK(a, cudaMemcpyAsync(a->g, gT, a->state * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
     const int nseg = (a->nsteps + a->k - 1) / a->k;
+    if (a->nsteps >= a->k) {
+        rc = segment_graphs(a);
+        if (rc) return rc;
+    }
     for (int seg = nseg - 1; seg >= 0; --seg) {
         const int s0 = seg * a->k, len = std::min(a->k, a->nsteps - s0);
         rc = restart(a, a->ckpt + (size_t)seg * a->state);
         if (rc) return rc;
-        // recompute the segment with taping sweeps, recording each stage's input state
+        if (len == a->k) {
+            // a full segment: its recompute (recording each stage's input state, taping the
+            // sweeps) and its reverse as the segment graphs
+            ACK(a, cudaGraphLaunch(a->rec_exec, h->stream));
+            ACK(a, cudaMemcpyAsync(a->seg_dts, a->dts + s0, (size_t)a->k * sizeof(double), cudaMemcpyDeviceToDevice,
+                                   h->stream));
+            ACK(a, cudaGraphLaunch(a->rev_exec, h->stream));
+            ACK(a, cudaMemcpyAsync(a->argmax + 2 * (size_t)s0, a->seg_argmax, (size_t)2 * a->k * sizeof(int),
+                                   cudaMemcpyDeviceToDevice, h->stream));
+            a->launches += a->rec_nodes + a->rev_nodes;
+            continue;
+        }
         for (int s = 0; s < len; ++s) {
-            h->kt->step_begin(h->prm, h->stream);
-            for (int irk = 1; irk <= 3; ++irk) {
-                rc = from_solver(a, a->rec + ((size_t)s * 3 + irk - 1) * a->state);
-                if (!rc) rc = taped_stage(a, irk, a->tape + ((size_t)s * 3 + irk - 1) * a->tape_stage);
-                if (rc) return rc;
-            }
-            h->kt->step_end(h->prm, h->stream);
-            a->launches += 2;
+            rc = recompute_step(a, s, false);
+            if (rc) return rc;
         }
         for (int s = len - 1; s >= 0; --s)
-            reverse_step(a, a->rec + (size_t)s * 3 * a->state, a->tape + (size_t)s * 3 * a->tape_stage, s0 + s);
+            reverse_step(a, a->rec + (size_t)s * 3 * a->state, a->tape + (size_t)s * 3 * a->tape_stage,
+                         a->dts + s0 + s, a->argmax + 2 * (s0 + s));
     }
     h->prim_slot = -1;
     ACK(a, cudaMemcpyAsync(g0, a->g, a->state * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));

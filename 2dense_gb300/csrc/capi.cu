@@ -237,6 +237,7 @@ int dense::handle_ensure_prim(dense_handle* h, int slot) { return ensure_prim(h,
 void dense::set_last_error(const char* msg) { g_err = msg ? msg : ""; }
 int dense::handle_step_graph(dense_handle* h) { return build_step_graph(h); }
 int dense::handle_stage_launches(dense_handle* h) { return stage_launches(h); }
+int dense::handle_ensure_side(dense_handle* h) { return ensure_side(h); }
 
 extern "C" {
 

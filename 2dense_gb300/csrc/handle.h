@@ -39,4 +39,6 @@ int handle_ensure_prim(dense_handle* h, int slot);
 int handle_step_graph(dense_handle* h);
 // kernel launches of one stage (boundary, two sweeps, update)
 int handle_stage_launches(dense_handle* h);
+// the side stream and the fork/join events of a stage's two sweeps, created on first use
+int handle_ensure_side(dense_handle* h);
 }  // namespace dense

@@ -166,13 +166,14 @@ __device__ __forceinline__ double upwind5(const double lf[5]) {
 constexpr double k133 = 13.0 / 3.0;   // 4 x 13/12 (exactly, in binary)
 
 // d_k = 4 (ss + beta_k) from the first differences and the terms s_k = 4 ss + 13/3 A_k^2 (staged
-// once per cell by the component-wise sweeps, whose neighbouring interfaces share them).
+// once per cell by the component-wise sweeps, whose neighbouring interfaces share them); B[k]
+// the first-order combinations.
 __device__ __forceinline__ void betas_staged(const double g[4], double s0, double s1, double s2, double& d0,
-                                             double& d1, double& d2) {
-    const double B0 = fma(-3.0, g[1], g[0]), B1 = g[1] + g[2], B2 = fma(3.0, g[2], -g[3]);
-    d0 = fma(B0, B0, s0);
-    d1 = fma(B1, B1, s1);
-    d2 = fma(B2, B2, s2);
+                                             double& d1, double& d2, double B[3]) {
+    B[0] = fma(-3.0, g[1], g[0]); B[1] = g[1] + g[2]; B[2] = fma(3.0, g[2], -g[3]);
+    d0 = fma(B[0], B[0], s0);
+    d1 = fma(B[1], B[1], s1);
+    d2 = fma(B[2], B[2], s2);
 }
 // The same from the first differences alone (a stencil no other interface shares).
 __device__ __forceinline__ void betas_g(const double g[4], double& d0, double& d1, double& d2) {
@@ -270,12 +271,15 @@ __device__ __forceinline__ void stencil_from_u(double u0, double u2, double W[5]
 // and da_k/dtau = 2 c_k tau/d_k^2, tau = |beta_2 - beta_0|; d_k = ss + beta_k), and beta_k =
 // 13/12 A_k^2 + 1/4 B_k^2 on the second differences A_k and the first-order combinations B_k.
 // Written over the terms the value itself uses (weno_terms: w_k = c_k v_k / N, and c_k (q_k - W)
-// = r_k - c_k (W - lf2)), with corr = W - lf2 and iN = 1/N as the value computed them, so that
-// the taping sweep evaluates every shared term once. The d_k arrive four times ss + beta_k,
-// which scales 1/d_k and the tau terms by 1/4; two exact factors of 4 undo it.
+// = r_k - c_k (W - lf2); the first-order combinations B_k of its indicators), with corr = W -
+// lf2 and iN = 1/N as the value computed them, so that the taping sweep evaluates every shared
+// term once. The d_k arrive four times ss + beta_k, which scales 1/d_k and the tau terms by 1/4;
+// two exact factors of 4 undo it. W(lf + c) = W(lf) + c (the weights see differences only, and
+// each candidate's coefficients sum to one), so the five entries sum to one: the centre entry is
+// taken as 1 minus the other four.
 template <bool Z>
-__device__ __forceinline__ void weno_grad(const double gd[4], double d0, double d1, double d2, const WenoTerms& t,
-                                          double corr, double iN, double g[5]) {
+__device__ __forceinline__ void weno_grad(const double gd[4], const double B[3], double d0, double d1, double d2,
+                                          const WenoTerms& t, double corr, double iN, double g[5]) {
     constexpr double cs[3] = {c30, c31, c32};
     double E[3], u[3];
 #pragma unroll
@@ -283,12 +287,11 @@ __device__ __forceinline__ void weno_grad(const double gd[4], double d0, double 
         E[k] = fma(-cs[k], corr, t.r[k]);  // (q_k - W) c_k
         u[k] = t.v[k] * iN;                // w_k / c_k
     }
-    const double w0 = c30 * u[0], w1 = c31 * u[1], w2 = c32 * u[2];
     const double iD = 4.0 * rcp_nr(t.D);
     const double id0 = d0 * (t.P[0] * iD), id1 = d1 * (t.P[1] * iD), id2 = d2 * (t.P[2] * iD);  // 1/(ss + beta_k)
-    const double A0 = gd[0] - gd[1], B0 = fma(-3.0, gd[1], gd[0]);
-    const double A1 = gd[1] - gd[2], B1 = gd[1] + gd[2];
-    const double A2 = gd[2] - gd[3], B2 = fma(3.0, gd[2], -gd[3]);
+    const double A0 = gd[0] - gd[1], B0 = B[0];
+    const double A1 = gd[1] - gd[2], B1 = B[1];
+    const double A2 = gd[2] - gd[3], B2 = B[2];
     // r_k = -1/2 dW/dbeta_k. With dbeta_k/dlf = 13/6 A_k dA_k/dlf + 1/2 B_k dB_k/dlf, beta_k's
     // share of dW/dlf is -13/3 r_k A_k dA_k/dlf - r_k B_k dB_k/dlf.
     double r0, r1, r2;
@@ -313,12 +316,13 @@ __device__ __forceinline__ void weno_grad(const double gd[4], double d0, double 
     const double PA0 = r0 * A0, PA1 = r1 * A1, PA2 = r2 * A2;
     const double NB0 = r0 * B0, NB1 = r1 * B1, NB2 = r2 * B2;
     constexpr double k = -13.0 / 3.0;
-    // g[m] = sum_k w_k dq_k/dlf[m] (the 5-point stencil of the weights) + the indicators' shares
-    g[0] = fma(a300, w0, fma(k, PA0, -NB0));
-    g[1] = fma(a301, w0, fma(a310, w1, fma(-2.0 * k, PA0, fma(k, PA1, fma(4.0, NB0, -NB1)))));
-    g[2] = fma(a302, w0, fma(a311, w1, fma(a320, w2, fma(k, PA0, fma(-2.0 * k, PA1, fma(k, PA2, -3.0 * (NB0 + NB2)))))));
-    g[3] = fma(a312, w1, fma(a321, w2, fma(k, PA1, fma(-2.0 * k, PA2, fma(4.0, NB2, NB1)))));
-    g[4] = fma(a322, w2, fma(k, PA2, -NB2));
+    // g[m] = sum_k w_k dq_k/dlf[m] (the 5-point stencil of the weights w_k = c_k u_k, the c_k
+    // folded into the stencil's constants) + the indicators' shares
+    g[0] = fma(c30 * a300, u[0], fma(k, PA0, -NB0));
+    g[1] = fma(c30 * a301, u[0], fma(c31 * a310, u[1], fma(-2.0 * k, PA0, fma(k, PA1, fma(4.0, NB0, -NB1)))));
+    g[3] = fma(c31 * a312, u[1], fma(c32 * a321, u[2], fma(k, PA1, fma(-2.0 * k, PA2, fma(4.0, NB2, NB1)))));
+    g[4] = fma(c32 * a322, u[2], fma(k, PA2, -NB2));
+    g[2] = 1.0 - ((g[0] + g[1]) + (g[3] + g[4]));
 }
 // The gradient of a stencil's reconstruction alone (upwind5's is constant), its terms recomputed.
 template <int REC>
@@ -331,10 +335,11 @@ __device__ __forceinline__ void recon_grad(const double lf[5], double g[5]) {
     double gd[4], d0, d1, d2;
     first_differences(lf, gd);
     betas_g(gd, d0, d1, d2);
+    const double B[3] = {fma(-3.0, gd[1], gd[0]), gd[1] + gd[2], fma(3.0, gd[2], -gd[3])};
     WenoTerms t;
     weno_terms<Z>(gd, d0, d1, d2, t);
     const double iN = rcp_nr(t.N);
-    weno_grad<Z>(gd, d0, d1, d2, t, weno_num(t) * iN, iN, g);
+    weno_grad<Z>(gd, B, d0, d1, d2, t, weno_num(t) * iN, iN, g);
 }
 
 template <int REC> __device__ __forceinline__ double recon5(const double lf[5]) {
@@ -734,28 +739,28 @@ __device__ __forceinline__ void flux_cw_block(const Params& p, int irk, int bx, 
             const double lp2 = sF[v * NCELL + atk(t + 2)], lm2 = sF[(4 + v) * NCELL + atk(t + 3)];
             // the value, and for the tape its gradient from the same terms (stencil slot m0:
             // 0 "+", 5 "-")
-            auto recon_taped = [&](double lf2, const double gd[4], double d0, double d1, double d2,
-                                   int m0) -> double {
+            auto recon_taped = [&](double lf2, const double gd[4], const double B[3], double d0, double d1,
+                                   double d2, int m0) -> double {
                 if constexpr (TAPE) {
                     WenoTerms tt;
                     weno_terms<Z>(gd, d0, d1, d2, tt);
                     const double iN = rcp_nr(tt.N);
                     const double num = weno_num(tt);
                     double g[5];
-                    weno_grad<Z>(gd, d0, d1, d2, tt, num * iN, iN, g);
+                    weno_grad<Z>(gd, B, d0, d1, d2, tt, num * iN, iN, g);
 #pragma unroll
                     for (int m = 0; m < 5; ++m) tape_at[((m0 + m) * 4 + v) * ts] = g[m];
                     return fma(num, iN, lf2);
                 } else {
-                    (void)m0;
+                    (void)m0; (void)B;
                     return weno_from_d<Z>(lf2, gd, d0, d1, d2);
                 }
             };
-            double d0, d1, d2;
-            betas_staged(gp, Sp[atk(t + 1)], Sp[atk(t + 2)], Sp[atk(t + 3)], d0, d1, d2);
-            const double hp = recon_taped(lp2, gp, d0, d1, d2, 0);
-            betas_staged(gm, Sm[atk(t + 4)], Sm[atk(t + 3)], Sm[atk(t + 2)], d0, d1, d2);
-            const double hm = recon_taped(lm2, gm, d0, d1, d2, 5);
+            double d0, d1, d2, B[3];
+            betas_staged(gp, Sp[atk(t + 1)], Sp[atk(t + 2)], Sp[atk(t + 3)], d0, d1, d2, B);
+            const double hp = recon_taped(lp2, gp, B, d0, d1, d2, 0);
+            betas_staged(gm, Sm[atk(t + 4)], Sm[atk(t + 3)], Sm[atk(t + 2)], d0, d1, d2, B);
+            const double hm = recon_taped(lm2, gm, B, d0, d1, d2, 5);
             h = hp + hm;
         } else {
             double lp[5], lm[5];
