@@ -185,6 +185,9 @@ def load_library(path: str | None = None):
         "dense_batch_steps_async": (_c_int, [vp, _c_int, _c_double, _c_int]),
         "dense_batch_set_schedule": (_c_int, [vp, _c_int, _c_int, _c_int]),
         "dense_batch_schedule_space": (_c_int, [ctypes.POINTER(_c_int)] * 3),
+        "dense_batch_set_launch_mode": (_c_int, [vp, _c_int]),
+        "dense_batch_get_launch_mode": (_c_int, [vp, ctypes.POINTER(_c_int)]),
+        "dense_batch_hold_instance": (_c_int, [vp, _c_int, ctypes.c_longlong]),
         "dense_batch_get_stream": (_c_int, [vp, ctypes.POINTER(vp)]),
         "dense_batch_status": (_c_int, [vp, ctypes.POINTER(ctypes.c_uint)]),
         "dense_batch_launch_count": (ctypes.c_longlong, [vp]),

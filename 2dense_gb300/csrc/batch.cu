@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
 #include <numeric>
@@ -41,6 +42,15 @@ struct dense_batch {
     bool prim_valid = false;
     long long launches = 0;
     std::string err;
+    // the persistent step (mode 1): its item list, the per-instance phase counts, the sync words
+    // (ticket, abort, items done per instance and phase; then the error word, kept across steps)
+    int mode = 0;                 // 0 one launch per phase, 1 one persistent launch per step
+    int* items = nullptr;         // int4 entries
+    size_t items_cap = 0;
+    unsigned* need = nullptr;
+    unsigned* sync = nullptr;
+    dense::PersistLaunch pl{};
+    int hold_instance = -1;       // failure injection: this instance's boundary phase never completes
 };
 
 namespace {
@@ -141,6 +151,110 @@ int build_maps(dense_batch* b, int xi_variant, int eta_variant) {
     return DENSE_OK;
 }
 
+// The persistent step's item list in phase order (dense::PersistLaunch): per phase, the
+// instances in the schedule's block order, each instance's items of that phase together (an
+// instance's items of one phase finish close together, so its next phase can start early).
+int build_items(dense_batch* b) {
+    using namespace dense;
+    const int n = b->n;
+    int xtx, xty, etx, ety;
+    batch_tile_shape(b->cfg[0].splitting, 0, b->bl.xi_variant, &xtx, &xty);
+    batch_tile_shape(b->cfg[0].splitting, 1, b->bl.eta_variant, &etx, &ety);
+    std::vector<int> inst(n);
+    std::iota(inst.begin(), inst.end(), 0);
+    if (b->order == 1)
+        std::stable_sort(inst.begin(), inst.end(), [&](int a, int c) {
+            return (long long)b->cfg[a].ni * b->cfg[a].nj > (long long)b->cfg[c].ni * b->cfg[c].nj;
+        });
+    std::vector<int> it;
+    std::vector<unsigned> need((size_t)n * kPhases, 0u);
+    auto push = [&](int kind, int stage, int phase, int dep, int i, int x, int y) {
+        it.push_back(persist_code(kind, stage, phase, dep)); it.push_back(i); it.push_back(x); it.push_back(y);
+        need[(size_t)i * kPhases + phase] += 1;
+    };
+    // one phase of every instance; blocks(i, emit) emits instance i's items of the phase
+    auto phase_items = [&](auto&& blocks) {
+        if (b->order != 2) {
+            for (int i : inst) blocks(i, -1);
+            return;
+        }
+        // round-robin: one item of each instance in turn
+        std::vector<int> k(n, 0);
+        for (bool more = true; more;) {
+            more = false;
+            for (int i = 0; i < n; ++i)
+                if (blocks(i, k[i])) { ++k[i]; more = true; }
+        }
+    };
+    // instance i's items of a phase as a list of (kind, x, y); with sel >= 0 only item sel
+    // (returns whether it exists)
+    auto emit = [&](int i, int sel, int kind, int stage, int phase, int dep,
+                    const std::vector<std::array<int, 3>>& list) {
+        if (sel < 0) {
+            for (const auto& e : list) push(e[0], stage, phase, dep, i, e[1], e[2]);
+            return true;
+        }
+        if (sel >= (int)list.size()) return false;
+        push(list[sel][0], stage, phase, dep, i, list[sel][1], list[sel][2]);
+        (void)kind;
+        return true;
+    };
+    std::vector<std::vector<std::array<int, 3>>> bc(n), sw(n), up(n);
+    for (int i = 0; i < n; ++i) {
+        const int ni = b->cfg[i].ni, nj = b->cfg[i].nj;
+        for (int x = 0; x < (2 * ni + 2 * nj + kPersistThreads - 1) / kPersistThreads; ++x) bc[i].push_back({kItemBc, x, 0});
+        for (int y = 0; y < (nj + xty - 1) / xty; ++y)
+            for (int x = 0; x < (ni + 1 + xtx - 1) / xtx; ++x) sw[i].push_back({kItemXi, x, y});
+        for (int y = 0; y < (nj + 1 + ety - 1) / ety; ++y)
+            for (int x = 0; x < (ni + etx - 1) / etx; ++x) sw[i].push_back({kItemEta, x, y});
+        for (int y = 0; y < (nj + 7) / 8; ++y)
+            for (int x = 0; x < (ni + 31) / 32; ++x) up[i].push_back({kItemUpdate, x, y});
+    }
+    const std::vector<std::array<int, 3>> one = {{0, 0, 0}};
+    phase_items([&](int i, int sel) {
+        return emit(i, sel, kItemBegin, 0, 0, -1, {{kItemBegin, 0, 0}});
+    });
+    for (int st = 1; st <= 3; ++st) {
+        const int pb = 3 * st - 2, ps = 3 * st - 1, pu = 3 * st, prev = st == 1 ? 0 : 3 * st - 3;
+        phase_items([&](int i, int sel) {
+            if (st > 1 && b->prm[i].periodic_ghosts) return false;  // the previous update wrote the ghosts
+            return emit(i, sel, kItemBc, st, pb, prev, bc[i]);
+        });
+        phase_items([&](int i, int sel) {
+            const bool has_bc = st == 1 || !b->prm[i].periodic_ghosts;
+            return emit(i, sel, kItemXi, st, ps, has_bc ? pb : prev, sw[i]);
+        });
+        phase_items([&](int i, int sel) { return emit(i, sel, kItemUpdate, st, pu, ps, up[i]); });
+    }
+    phase_items([&](int i, int sel) { return emit(i, sel, kItemEnd, 0, kPhases - 1, 9, {{kItemEnd, 0, 0}}); });
+    (void)one;
+    if (b->hold_instance >= 0 && b->hold_instance < n) need[(size_t)b->hold_instance * kPhases + 1] += 1;
+    const size_t total = it.size();
+    if (total > b->items_cap) {
+        if (b->items) cudaFree(b->items);
+        b->items = nullptr;
+        BCK(b, cudaMalloc((void**)&b->items, total * sizeof(int)));
+        b->items_cap = total;
+    }
+    BCK(b, cudaMemcpy(b->items, it.data(), total * sizeof(int), cudaMemcpyHostToDevice));
+    if (!b->need) BCK(b, cudaMalloc((void**)&b->need, need.size() * sizeof(unsigned)));
+    BCK(b, cudaMemcpy(b->need, need.data(), need.size() * sizeof(unsigned), cudaMemcpyHostToDevice));
+    if (!b->sync) {
+        BCK(b, cudaMalloc((void**)&b->sync, (2 + need.size() + 1) * sizeof(unsigned)));
+        BCK(b, cudaMemset(b->sync, 0, (2 + need.size() + 1) * sizeof(unsigned)));
+    }
+    PersistLaunch& L = b->pl;
+    L.items = b->items;
+    L.nitems = (int)(total / 4);
+    L.sync = b->sync;
+    L.need = b->need;
+    L.err = b->sync + 2 + need.size();
+    if (!L.spin_limit) L.spin_limit = 1ll << 22;
+    if (!b->kt->persist_shape || !b->kt->persist_shape(b->bl, &L))
+        return bset(b, DENSE_ERR_ARG, "no persistent launch for this scheme and variant");
+    return DENSE_OK;
+}
+
 void drop_graph(dense_batch* b) {
     if (b->graph) cudaGraphExecDestroy(b->graph);
     b->graph = nullptr;
@@ -164,6 +278,23 @@ int build_graph(dense_batch* b) {
         BCK(b, cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming));
     }
     cudaGraph_t g = nullptr;
+    if (b->mode == 1) {
+        // the persistent step: its sync words cleared, then the one launch
+        BCK(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t ce = cudaMemsetAsync(b->sync, 0, (2 + (size_t)b->n * dense::kPhases) * sizeof(unsigned), b->stream);
+        if (ce == cudaSuccess) b->kt->persist(b->bl, b->pl, b->stream);
+        cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+        if (e == cudaSuccess && ce != cudaSuccess) {
+            cudaGraphDestroy(g);
+            e = ce;
+        }
+        if (e != cudaSuccess) return bset(b, DENSE_ERR_CUDA, std::string("stream capture: ") + cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&b->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return bset(b, DENSE_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+        b->graph_nodes = 1;
+        return DENSE_OK;
+    }
     BCK(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     b->kt->step_begin(b->bl, b->stream);
     // per stage: boundary; the eta sweep as a branch beside the xi sweep (both read the stage
@@ -288,6 +419,9 @@ int dense_batch_create(int n, const dense_config_t* cfgs, dense_batch_t** out) {
 void dense_batch_destroy(dense_batch_t* b) {
     if (!b) return;
     drop_graph(b);
+    if (b->items) cudaFree(b->items);
+    if (b->need) cudaFree(b->need);
+    if (b->sync) cudaFree(b->sync);
     if (b->maps) cudaFree(b->maps);
     if (b->tab) cudaFree(b->tab);
     if (b->pool) cudaFree(b->pool);
@@ -345,6 +479,16 @@ int dense_batch_steps(dense_batch_t* b, int nsteps, double t_end, int total_step
     int rc = dense_batch_steps_async(b, nsteps, t_end, total_step);
     if (rc) return rc;
     BCK(b, cudaStreamSynchronize(b->stream));
+    if (b->mode == 1) {
+        unsigned e = 0;
+        BCK(b, cudaMemcpy(&e, b->pl.err, sizeof(unsigned), cudaMemcpyDeviceToHost));
+        if (e) {
+            BCK(b, cudaMemset(b->pl.err, 0, sizeof(unsigned)));
+            return bset(b, DENSE_ERR_TIMEOUT,
+                        "a wait of the persistent step gave up (DENSE_FLAG_TIMEOUT in the instances' status); the "
+                        "step's results are not valid");
+        }
+    }
     return DENSE_OK;
 }
 
@@ -387,7 +531,48 @@ int dense_batch_set_schedule(dense_batch_t* b, int xi_variant, int eta_variant, 
     BCK(b, cudaStreamSynchronize(b->stream));
     b->order = order;
     int rc = build_maps(b, xi_variant, eta_variant);
+    if (!rc && b->mode == 1) rc = build_items(b);
     if (rc) return rc;
+    drop_graph(b);
+    return DENSE_OK;
+}
+
+int dense_batch_set_launch_mode(dense_batch_t* b, int mode) {
+    if (!b || (mode != 0 && mode != 1)) return bset(b, DENSE_ERR_ARG, "launch mode must be 0 or 1");
+    if (mode == 1 && (!b->kt->persist || b->cfg[0].splitting > DENSE_SPLIT_SW))
+        return bset(b, DENSE_ERR_ARG,
+                    "the persistent step covers the component-wise schemes (101-103 with 251/253/255) of the "
+                    "fast variant");
+    BCK(b, cudaStreamSynchronize(b->stream));
+    const int old = b->mode;
+    b->mode = mode;
+    if (mode == 1) {
+        const int rc = build_items(b);
+        if (rc) {
+            b->mode = old;
+            return rc;
+        }
+    }
+    drop_graph(b);
+    return DENSE_OK;
+}
+
+int dense_batch_get_launch_mode(dense_batch_t* b, int* mode) {
+    if (!b || !mode) return bset(b, DENSE_ERR_ARG, "null argument");
+    *mode = b->mode;
+    return DENSE_OK;
+}
+
+int dense_batch_hold_instance(dense_batch_t* b, int instance, long long spin_limit) {
+    if (!b || instance < -1 || instance >= b->n || spin_limit < 0)
+        return bset(b, DENSE_ERR_ARG, "bad instance or spin limit");
+    BCK(b, cudaStreamSynchronize(b->stream));
+    b->hold_instance = instance;
+    b->pl.spin_limit = spin_limit ? spin_limit : (1ll << 22);
+    if (b->mode == 1) {
+        const int rc = build_items(b);
+        if (rc) return rc;
+    }
     drop_graph(b);
     return DENSE_OK;
 }
@@ -401,12 +586,13 @@ int dense_batch_get_stream(dense_batch_t* b, void** stream) {
 int dense_batch_status(dense_batch_t* b, unsigned* flags) {
     if (!b || !flags) return bset(b, DENSE_ERR_ARG, "null argument");
     unsigned f = 0;
+    std::vector<unsigned> fl(b->n, 0u);
     for (int i = 0; i < b->n; ++i) {
-        unsigned fi = 0;
-        BCK(b, cudaMemcpyAsync(&fi, &b->prm[i].sc->status, sizeof(unsigned), cudaMemcpyDeviceToHost, b->stream));
-        BCK(b, cudaStreamSynchronize(b->stream));
-        f |= fi;
+        BCK(b, cudaMemcpyAsync(&fl[i], &b->prm[i].sc->status, sizeof(unsigned), cudaMemcpyDeviceToHost, b->stream));
+        BCK(b, cudaMemsetAsync(&b->prm[i].sc->status, 0, sizeof(unsigned), b->stream));
     }
+    BCK(b, cudaStreamSynchronize(b->stream));
+    for (unsigned fi : fl) f |= fi;
     *flags = f;
     return DENSE_OK;
 }

@@ -145,6 +145,31 @@ struct BatchLaunch {
     int splitting, recon;  // common to the batch
 };
 
+// The persistent step of a batch (component-wise schemes, fast variant): one launch of resident
+// blocks of kPersistThreads threads works through a list of items, each a piece of one phase of
+// one instance. Phases of an instance, in order: 0 the loop predicate; per stage s = 1..3 the
+// boundary lines (3s - 2), the xi and eta tiles (3s - 1) and the update's cell blocks (3s); 10
+// the time advance. An item waits until every item of one earlier phase of its own instance
+// (its dependency) has finished.
+constexpr int kPersistThreads = 256;
+constexpr int kPhases = 11;
+enum PersistKind { kItemBegin = 0, kItemBc = 1, kItemXi = 2, kItemEta = 3, kItemUpdate = 4, kItemEnd = 5 };
+// item (x, y, z, w): x = kind | stage << 4 | phase << 8 | (dependency phase + 1) << 16, y the
+// instance, (z, w) the block coordinates within the instance (tile, boundary-line block of
+// kPersistThreads lines, or cell block of 32 x 8)
+inline int persist_code(int kind, int stage, int phase, int dep) {
+    return kind | stage << 4 | phase << 8 | (dep + 1) << 16;
+}
+struct PersistLaunch {
+    const void* items; int nitems;   // int4 items in list order
+    unsigned* sync;                  // [0] ticket, [1] abort word, [2 + kPhases i + ph] items done
+    const unsigned* need;            // [kPhases i + ph]: items of phase ph of instance i
+    unsigned* err;                   // set by a wait that gave up; kept across steps
+    long long spin_limit;            // polls before a wait gives up (DENSE_FLAG_TIMEOUT)
+    int grid;                        // resident blocks
+    size_t smem;                     // dynamic shared memory per block
+};
+
 struct BatchKernelTable {
     void (*prim)(const BatchLaunch&, int slot, void* stream);
     void (*bc)(const BatchLaunch&, void* stream);
@@ -152,6 +177,10 @@ struct BatchKernelTable {
     void (*update)(const BatchLaunch&, int irk, void* stream);
     void (*step_begin)(const BatchLaunch&, void* stream);
     void (*step_end)(const BatchLaunch&, void* stream);
+    // the persistent step (null where the variant has none); persist_shape fills the launch's
+    // grid and shared memory for the batch's scheme and tiles, false if it has none
+    void (*persist)(const BatchLaunch&, const PersistLaunch&, void* stream);
+    bool (*persist_shape)(const BatchLaunch&, PersistLaunch*);
 };
 const BatchKernelTable* batch_kernels_fast();
 const BatchKernelTable* batch_kernels_strict();

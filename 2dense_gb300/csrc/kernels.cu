@@ -642,9 +642,12 @@ __device__ __forceinline__ void flux_cw_block(const Params& p, int irk, int bx, 
     double* const sG = dsm + 16 * NCELL;
     (void)sS; (void)sG; (void)NL;
     auto at = [&](int r, int c) { return chk(p, r, NL) * NC + chk(p, c, NC); };
-    const int tx = threadIdx.x, ty = threadIdx.y, tz = TZ == 1 ? 0 : (int)threadIdx.z;
+    // the thread's place in the tile from its linear index (a TX x TY x TZ block, or the
+    // persistent kernel's one-dimensional block of as many threads)
+    const int lt = threadIdx.x + TX * (threadIdx.y + TY * threadIdx.z);
+    const int tx = lt % TX, ty = (lt / TX) % TY, tz = TZ == 1 ? 0 : lt / (TX * TY);
     const int slot = irk - 1;
-    if (DIR == 0 && bx == 0 && by == 0 && tx == 0 && ty == 0 && tz == 0) stage_scalars(p, irk);
+    if (DIR == 0 && bx == 0 && by == 0 && lt == 0) stage_scalars(p, irk);
     const double lam_g = p.sc->maxeig[slot][DIR];
     const int NIp = p.ni + 2 * kB, NJp = p.nj + 2 * kB;
 
@@ -1313,10 +1316,10 @@ __device__ __forceinline__ void prim_block(const Params& p, int slot, int bx, in
 // time_rk3_general(irk) (time_advance_general.f90:9-267) fused with get_primary of the updated
 // state for the next stage. Body force of Rayleigh-Taylor: S = (0, 0, rho, rho v) of the stage
 // input (boundary_rt_general.f90:154-155), added after the combine as a separate rounding.
+// (i, j): the thread's interior cell.
 template <int IRK>
-__device__ __forceinline__ void update_block(const Params& p, int bx, int by) {
+__device__ __forceinline__ void update_block(const Params& p, int i, int j) {
     if (!p.sc->active) return;
-    const int i = bx * blockDim.x + threadIdx.x, j = by * blockDim.y + threadIdx.y;
     double e1 = 0.0, e2 = 0.0;
     unsigned flags = 0;
     if (i < p.ni && j < p.nj) {
@@ -1638,17 +1641,27 @@ __global__ void __launch_bounds__(TX* TY, char_min_blocks(ADAPT)) k_flux_char(Pa
 }
 __global__ void k_prim(Params p, int slot) { prim_block(p, slot, blockIdx.x, blockIdx.y); }
 template <int IRK>
-__global__ void k_update(Params p) { update_block<IRK>(p, blockIdx.x, blockIdx.y); }
+__global__ void k_update(Params p) {
+    update_block<IRK>(p, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y);
+}
 __global__ void k_bc(Params p) { bc_block(p, blockIdx.x); }
 
 // Batched kernels: one launch covers every instance of a batch. Block b works on instance
 // map[b].x at block coordinates (map[b].y, map[b].z) of that instance's own grid, with the
 // instance's parameters staged in shared memory; the per-block code is the single-instance
 // code, so each instance's arithmetic -- and result -- is the same as a plain solve's.
+// The instance's parameters to shared memory, 8-byte words in parallel.
+__device__ __forceinline__ void load_params(Params& sp, const Params* src) {
+    static_assert(sizeof(Params) % sizeof(long long) == 0, "Params copies as 8-byte words");
+    const int lt = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    const int nt = blockDim.x * blockDim.y * blockDim.z;
+    for (int k = lt; k < (int)(sizeof(Params) / sizeof(long long)); k += nt)
+        ((long long*)&sp)[k] = ((const long long*)src)[k];
+}
 #define DENSE_BATCH_PROLOGUE                                                 \
     __shared__ Params sp;                                                    \
     const int3 m = map[blockIdx.x];                                          \
-    if (threadIdx.x == 0 && threadIdx.y == 0) sp = tab[m.x];                 \
+    load_params(sp, tab + m.x);                                              \
     __syncthreads();
 
 template <int DIR, int SPL, int REC, int TX, int TY>
@@ -1668,13 +1681,14 @@ __global__ void kb_prim(const Params* tab, const int3* map, int slot) {
 template <int IRK>
 __global__ void kb_update(const Params* tab, const int3* map) {
     DENSE_BATCH_PROLOGUE
-    update_block<IRK>(sp, m.y, m.z);
+    update_block<IRK>(sp, m.y * blockDim.x + threadIdx.x, m.z * blockDim.y + threadIdx.y);
 }
 __global__ void kb_bc(const Params* tab, const int3* map) {
     DENSE_BATCH_PROLOGUE
     bc_block(sp, m.y);
 }
 #undef DENSE_BATCH_PROLOGUE
+
 
 // ---------------------------------------------------------------------------------------------
 // Step bookkeeping (general_main.f90:23-37): the while-condition at the start of a step and the
@@ -1694,6 +1708,134 @@ __device__ __forceinline__ void k_step_end_body(Scalars* sc) {
 }
 __global__ void k_step_begin(Scalars* sc) { k_step_begin_body(sc); }
 __global__ void k_step_end(Scalars* sc) { k_step_end_body(sc); }
+
+#define DENSE_PERSIST (FAST && !DENSE_CHECK)
+#if DENSE_PERSIST
+// ---------------------------------------------------------------------------------------------
+// The persistent step of a batch (component-wise schemes). Resident blocks of kPersistThreads
+// threads take the step's items (PersistLaunch, internal.h) in list order from one ticket
+// counter. An item waits only for its dependency, the phase before it of its own instance (the
+// count of that phase's finished items), so one instance's next stage starts while others are
+// still in their sweeps: no grid-wide barrier between phases and no idle tail per phase. The list
+// is in phase order, so every item an item waits for was handed out before it, to a running
+// block: as that block's current item, which waits only for earlier items, or as its next one,
+// which it starts once its current, earlier, item is done. So the earliest unfinished item can
+// always proceed, and the waits end. They are bounded
+// all the same (spin_limit polls); a wait that gives up sets DENSE_FLAG_TIMEOUT in its instance's
+// status and the launch's abort word, and every wait after that gives up at once (the step's
+// results are then not valid; the host reports DENSE_ERR_TIMEOUT). A finished item publishes
+// with a release add after the block's barrier; a waiting block's first thread polls with
+// acquire loads before the barrier that releases the others, so the items' writes are visible
+// to every thread of the block.
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* a) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(a) : "memory");
+    return v;
+}
+__device__ __forceinline__ void add_release(unsigned* a, unsigned v) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(a), "r"(v) : "memory");
+}
+
+// one sweep tile of the item's variant: the batched tile shapes (batch_tile_shape) with
+// threads per interface added to make kPersistThreads
+template <int DIR, int SPL, int REC, int TX, int TY>
+__device__ __noinline__ void persist_tile(const Params& p, int irk, int bx, int by) {
+    constexpr int TZ = kPersistThreads / (TX * TY);
+    static_assert(TX * TY * TZ == kPersistThreads, "a persistent tile has kPersistThreads threads");
+    flux_cw_block<DIR, SPL, REC, TX, TY, false, TZ>(p, irk, bx, by);
+}
+template <int SPL, int REC>
+__device__ __forceinline__ void persist_sweep(const Params& p, int dir, int variant, int irk, int bx, int by) {
+    if (dir == 0) {
+        switch (variant) {
+        case 1: persist_tile<0, SPL, REC, 64, 2>(p, irk, bx, by); break;
+        case 2: persist_tile<0, SPL, REC, 32, 8>(p, irk, bx, by); break;
+        case 3: persist_tile<0, SPL, REC, 32, 2>(p, irk, bx, by); break;
+        default: persist_tile<0, SPL, REC, 32, 4>(p, irk, bx, by); break;
+        }
+    } else {
+        switch (variant) {
+        case 1: persist_tile<1, SPL, REC, 8, 16>(p, irk, bx, by); break;
+        case 2: persist_tile<1, SPL, REC, 32, 8>(p, irk, bx, by); break;
+        case 3: persist_tile<1, SPL, REC, 16, 16>(p, irk, bx, by); break;
+        case 4: persist_tile<1, SPL, REC, 4, 64>(p, irk, bx, by); break;
+        default: persist_tile<1, SPL, REC, 8, 32>(p, irk, bx, by); break;
+        }
+    }
+}
+__device__ __noinline__ void persist_bc(const Params& p, int bx) { bc_block(p, bx); }
+template <int IRK>
+__device__ __noinline__ void persist_update(const Params& p, int bx, int by) {
+    update_block<IRK>(p, bx * 32 + (int)threadIdx.x % 32, by * 8 + (int)threadIdx.x / 32);
+}
+
+template <int SPL, int REC>
+__global__ void __launch_bounds__(kPersistThreads, SPL == 0 ? 4 : 2)
+kb_persist(const Params* tab, PersistLaunch L, int xi_variant, int eta_variant) {
+    __shared__ Params sp;
+    __shared__ int s_item, s_skip;
+    const int lt = threadIdx.x;
+    unsigned* const ticket = L.sync;
+    unsigned* const abort_w = L.sync + 1;
+    unsigned* const done = L.sync + 2;
+    const int4* const items = (const int4*)L.items;
+    if (lt == 0) s_item = (int)atomicAdd(ticket, 1u);
+    __syncthreads();
+    int cur = s_item;
+    while (cur < L.nitems) {
+        // the next ticket is taken now, its value needed only after this item: the block holds
+        // two tickets, which keeps the waits finite (an item handed out as a block's next waits
+        // only for that block's current item, which is earlier)
+        unsigned nxt = 0;
+        if (lt == 0) nxt = atomicAdd(ticket, 1u);
+        const int4 w = items[cur];
+        const int kind = w.x & 15, irk = (w.x >> 4) & 15, ph = (w.x >> 8) & 255, dep = (w.x >> 16) - 1;
+        load_params(sp, tab + w.y);
+        if (lt == 0) {
+            int skip = 0;
+            if (dep >= 0) {
+                const unsigned* d = done + w.y * kPhases + dep;
+                const unsigned want = L.need[w.y * kPhases + dep];
+                long long n = 0;
+                while (ld_acquire(d) < want) {
+                    if (ld_acquire(abort_w)) { skip = 1; break; }
+                    if (++n > L.spin_limit) {
+                        atomicOr(abort_w, 1u);
+                        atomicOr(L.err, 1u);
+                        atomicOr(&tab[w.y].sc->status, DENSE_FLAG_TIMEOUT);
+                        skip = 1;
+                        break;
+                    }
+                    __nanosleep(64);
+                }
+            }
+            s_skip = skip;
+        }
+        __syncthreads();
+        if (!s_skip) {
+            switch (kind) {
+            case kItemBegin: if (lt == 0) k_step_begin_body(sp.sc); break;
+            case kItemEnd:   if (lt == 0) k_step_end_body(sp.sc); break;
+            case kItemBc:    persist_bc(sp, w.z); break;
+            case kItemXi:    persist_sweep<SPL, REC>(sp, 0, xi_variant, irk, w.z, w.w); break;
+            case kItemEta:   persist_sweep<SPL, REC>(sp, 1, eta_variant, irk, w.z, w.w); break;
+            default:
+                if (irk == 1) persist_update<1>(sp, w.z, w.w);
+                else if (irk == 2) persist_update<2>(sp, w.z, w.w);
+                else persist_update<3>(sp, w.z, w.w);
+                break;
+            }
+        }
+        __syncthreads();  // the item's writes precede its count; sp and s_item are free again
+        if (lt == 0) {
+            add_release(done + w.y * kPhases + ph, 1u);
+            s_item = (int)nxt;
+        }
+        __syncthreads();
+        cur = s_item;
+    }
+}
+#endif
 
 // ---------------------------------------------------------------------------------------------
 // Launchers
@@ -1923,6 +2065,70 @@ static void batch_step_end(const BatchLaunch& b, void* stream) {
     kb_step_end<<<(b.n + 127) / 128, 128, 0, (cudaStream_t)stream>>>(b.tab, b.n);
 }
 
+#if DENSE_PERSIST
+template <int SPL, int REC>
+static void persist_launch(const BatchLaunch& b, const PersistLaunch& L, cudaStream_t s) {
+    kb_persist<SPL, REC><<<L.grid, kPersistThreads, L.smem, s>>>(b.tab, L, b.xi_variant, b.eta_variant);
+}
+template <int SPL, int REC>
+static bool persist_dims(PersistLaunch* L, size_t smem) {
+    int per_sm = 0;
+    if (cudaFuncSetAttribute(kb_persist<SPL, REC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kb_persist<SPL, REC>, kPersistThreads, smem) !=
+            cudaSuccess ||
+        per_sm < 1)
+        return false;
+    L->grid = per_sm * sm_count();
+    L->smem = smem;
+    return true;
+}
+// dynamic shared memory of a batched tile variant
+template <int REC>
+static size_t cw_tile_bytes(int dir, int variant) {
+    if (dir == 0) {
+        switch (variant) {
+        case 1: return CwTile<0, REC, 64, 2>::bytes;
+        case 2: return CwTile<0, REC, 32, 8>::bytes;
+        case 3: return CwTile<0, REC, 32, 2>::bytes;
+        default: return CwTile<0, REC, 32, 4>::bytes;
+        }
+    }
+    switch (variant) {
+    case 1: return CwTile<1, REC, 8, 16>::bytes;
+    case 2: return CwTile<1, REC, 32, 8>::bytes;
+    case 3: return CwTile<1, REC, 16, 16>::bytes;
+    case 4: return CwTile<1, REC, 4, 64>::bytes;
+    default: return CwTile<1, REC, 8, 32>::bytes;
+    }
+}
+template <int SPL, int REC>
+static bool persist_shape_of(const BatchLaunch& b, PersistLaunch* L) {
+    const size_t sx = cw_tile_bytes<REC>(0, b.xi_variant), se = cw_tile_bytes<REC>(1, b.eta_variant);
+    const size_t smem = sx > se ? sx : se;
+    return persist_dims<SPL, REC>(L, smem);
+}
+static bool batch_persist_shape(const BatchLaunch& b, PersistLaunch* L) {
+    if (b.splitting != DENSE_SPLIT_LLF && b.splitting != DENSE_SPLIT_GLF && b.splitting != DENSE_SPLIT_SW) return false;
+    const bool sw = b.splitting == DENSE_SPLIT_SW;
+    switch (b.recon) {
+    case DENSE_RECON_UPWIND5: return sw ? persist_shape_of<1, 251>(b, L) : persist_shape_of<0, 251>(b, L);
+    case DENSE_RECON_WENOJS5: return sw ? persist_shape_of<1, 253>(b, L) : persist_shape_of<0, 253>(b, L);
+    case DENSE_RECON_WENOZ5:  return sw ? persist_shape_of<1, 255>(b, L) : persist_shape_of<0, 255>(b, L);
+    default: return false;
+    }
+}
+static void batch_persist(const BatchLaunch& b, const PersistLaunch& L, void* stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    const bool sw = b.splitting == DENSE_SPLIT_SW;
+    switch (b.recon) {
+    case DENSE_RECON_UPWIND5: sw ? persist_launch<1, 251>(b, L, s) : persist_launch<0, 251>(b, L, s); break;
+    case DENSE_RECON_WENOJS5: sw ? persist_launch<1, 253>(b, L, s) : persist_launch<0, 253>(b, L, s); break;
+    default:                  sw ? persist_launch<1, 255>(b, L, s) : persist_launch<0, 255>(b, L, s); break;
+    }
+}
+#endif
+
 // The sweeps take their tile from dynamic shared memory; with the static work queue of the
 // characteristic sweeps and the batched kernels' staged parameters, the larger tiles need more
 // than the default 48 KB a block may use, which a kernel has to be allowed once (set for every
@@ -1993,8 +2199,9 @@ const BatchKernelTable* batch_kernels_checked() {
 const BatchKernelTable* batch_kernels_fast() {
     static const bool smem_ok = VNS::allow_tile_smem();
     (void)smem_ok;
-    static const BatchKernelTable t = {VNS::batch_prim, VNS::batch_bc, VNS::batch_flux, VNS::batch_update,
-                                       VNS::batch_step_begin, VNS::batch_step_end};
+    static const BatchKernelTable t = {VNS::batch_prim,       VNS::batch_bc,       VNS::batch_flux,
+                                       VNS::batch_update,     VNS::batch_step_begin, VNS::batch_step_end,
+                                       VNS::batch_persist,    VNS::batch_persist_shape};
     return &t;
 }
 // Tile shapes of the batched sweeps (the shapes instantiated above).

@@ -312,8 +312,25 @@ class BatchSolver:
         """Every instance's initial state computed on the device (benchmarks 11, 13, 14)."""
         self._chk(self.lib.dense_batch_init_device(self.h))
 
-    def set_schedule(self, xi_variant: int, eta_variant: int, order: int):
+    def set_schedule(self, xi_variant: int, eta_variant: int, order: int, mode: int | None = None):
+        """Tile variants, block order and (when given) launch mode: 0 one launch per phase,
+        1 one persistent launch per step."""
         self._chk(self.lib.dense_batch_set_schedule(self.h, xi_variant, eta_variant, order))
+        if mode is not None:
+            self.set_launch_mode(mode)
+
+    def set_launch_mode(self, mode: int):
+        self._chk(self.lib.dense_batch_set_launch_mode(self.h, mode))
+
+    def launch_mode(self) -> int:
+        m = ctypes.c_int()
+        self._chk(self.lib.dense_batch_get_launch_mode(self.h, ctypes.byref(m)))
+        return m.value
+
+    def hold_instance(self, instance: int, spin_limit: int = 0):
+        """Failure injection: the persistent step's waits on ``instance`` give up after
+        ``spin_limit`` polls (-1 removes the hold)."""
+        self._chk(self.lib.dense_batch_hold_instance(self.h, instance, spin_limit))
 
     def stream(self) -> int:
         s = ctypes.c_void_p()

@@ -334,7 +334,25 @@ int dense_batch_steps_async(dense_batch_t* b, int nsteps, double t_end, int tota
 int dense_batch_set_schedule(dense_batch_t* b, int xi_variant, int eta_variant, int order);
 /* the number of xi variants, eta variants and block orders dense_batch_set_schedule accepts */
 int dense_batch_schedule_space(int* n_xi, int* n_eta, int* n_order);
+/* How a step is launched. Mode 0 (the default): one launch per phase (boundary, xi sweep, eta
+   sweep, update per stage) over every instance, a CUDA graph per step. Mode 1: one persistent
+   launch per step (captured in the step's CUDA graph) of resident 256-thread blocks that take the
+   step's pieces -- per instance its loop predicate, boundary lines, sweep tiles (the schedule's
+   tiles with threads per interface added to make 256) and update blocks per stage, and its time
+   advance -- in list order, each piece waiting only for the phase before it of its own instance,
+   so an instance's next stage overlaps other instances' sweeps. Results are bit-identical to
+   mode 0. Every wait is bounded; one that gives up sets DENSE_FLAG_TIMEOUT, the step's results
+   are not valid and dense_batch_steps returns DENSE_ERR_TIMEOUT. Mode 1 covers the
+   component-wise schemes (101-103 with 251/253/255) of the fast variant (strict = 0); anything
+   else returns DENSE_ERR_ARG. */
+int dense_batch_set_launch_mode(dense_batch_t* b, int mode);
+int dense_batch_get_launch_mode(dense_batch_t* b, int* mode);
+/* Failure injection for tests of the persistent step's bounded waits: the boundary phase of
+   stage 1 of `instance` is given one piece more than it has, so the pieces that wait for it give
+   up after spin_limit polls (0: the default limit of 2^22). instance = -1 removes the hold. */
+int dense_batch_hold_instance(dense_batch_t* b, int instance, long long spin_limit);
 int dense_batch_get_stream(dense_batch_t* b, void** stream);
+/* Read (and clear) every instance's device status word: DENSE_FLAG_* bits, OR-ed. Synchronises. */
 int dense_batch_status(dense_batch_t* b, unsigned* flags);
 long long dense_batch_launch_count(dense_batch_t* b);
 long long dense_batch_cells(dense_batch_t* b);
