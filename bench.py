@@ -272,6 +272,8 @@ def run_batched(args, dense, lib):
     cfgs = [s[0] for s in setups]
     cells = sum(c.ni * c.nj for c in cfgs)
     sched, info = at.tune(cfgs, setups=setups, steps=2, reps=2)
+    if args.batch_mode != "auto":
+        sched = tuple(sched[:3]) + (1 if args.batch_mode == "persistent" else 0,)
     b = dense.BatchSolver(cfgs)
     for i, (c, cons, prim, x, y) in enumerate(setups):
         b.upload(i, cons, prim, x, y)
@@ -505,6 +507,9 @@ def main():
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--batch-nmin", type=int, default=64, help="smallest instance size of the batched workload")
     ap.add_argument("--batch-nmax", type=int, default=512, help="largest instance size of the batched workload")
+    ap.add_argument("--batch-mode", choices=("auto", "phases", "persistent"), default="auto",
+                    help="launch mode of the batched workload: the autotuner's pick, one launch per "
+                         "phase, or one persistent launch per step (tiles and order tuned either way)")
     ap.add_argument("--adj-steps", type=int, default=400, help="time steps of the adjoint workload's run")
     args = ap.parse_args()
     if args.steps is None:
