@@ -66,12 +66,20 @@ struct AdjParams {
     int np;           // tape planes per direction (tape_planes)
     double gamma, dx, dy, inv_dx, inv_dy, cfl;
     int rule[4];      // ghost rule of each side (bottom, top, left, right): kRulePeriodic, ...
+    // Rayleigh-Taylor's body force: each stage adds f_s (0, 0, rho, rho v) of its input, f_s =
+    // dt, dt/4, (2/3 in single precision) dt (time_advance_general.f90:79,160,242); the
+    // stages' per-block sums of w . (0, 0, rho, rho v) for the time step's sensitivity go to
+    // bpart[(s - 1) nm + block]
+    int bodyforce;
+    double* bpart;
 };
 // Ghost rules of the benchmarks the adjoint covers (boundary_*_general.f90): a periodic copy,
-// the recursive 4/3, -1/3 extrapolation of the two cells next to the side, or the mirror of the
+// the recursive 4/3, -1/3 extrapolation of the two cells next to the side, the mirror of the
 // four cells next to it with the normal velocity negated -- applied to the conserved variables
-// and, separately, to the primitives.
-constexpr int kRulePeriodic = 0, kRuleExtrap = 1, kRuleReflect = 2;
+// and, separately, to the primitives -- or a fixed state (Rayleigh-Taylor's Dirichlet bottom and
+// top, boundary_rt_general.f90:14-57), which no interior cell feeds.
+constexpr int kRulePeriodic = 0, kRuleExtrap = 1, kRuleReflect = 2, kRuleFixed = 3;
+constexpr double kTwoThirdsSingle = (double)(2.0f / 3.0f);  // time_advance_general.f90:242
 
 // get_primary of one cell (get_primary.f90:53-60), with the pressure floor of :58; rs = 1/alpha'
 // with alpha'^2 = gamma p / rho, so that alpha = alpha'^2 rs and dalpha/dp = gamma/(2 rho) rs.
@@ -457,6 +465,26 @@ __device__ __forceinline__ void wall_terms(const AdjParams& a, const double* __r
         const int rule = a.rule[DIR == 0 ? 2 + side : side];
         if (rule == kRulePeriodic) continue;
         const int dist = side == 0 ? x + 1 : n - x;  // 1 = next to the side
+        if (rule == kRuleFixed) {
+            // a fixed ghost state (Rayleigh-Taylor's bottom and top, boundary_rt_general.f90:
+            // 14-57) depends on no cell; only GLF's global lambda enters its split,
+            // dF+-/dlambda = +-U/2, whose sensitivity the cell next to the side takes for the
+            // line's four ghosts
+            if (SPL != 1 || dist != 1) continue;
+            const bool bottom = DIR == 1 && side == 0;
+            const double rho = bottom ? 2.0 : 1.0, pr = bottom ? 1.0 : 2.5;
+            const double Ug[4] = {rho, 0.0, 0.0, pr / (a.gamma - 1.0)};
+#pragma unroll 1
+            for (int k = 0; k < 4; ++k) {
+                double gp[4] = {0, 0, 0, 0}, gm[4] = {0, 0, 0, 0};
+                gather_line<REC>(T, H, ts, base, stride, side == 0 ? -1 - k : n + k, n, false, gp, gm);
+                double s = 0.0;
+#pragma unroll
+                for (int c = 0; c < 4; ++c) s = fma(gp[c] - gm[c], Ug[c], s);
+                lb += 0.5 * s;
+            }
+            continue;
+        }
         if (dist > (rule == kRuleReflect ? 4 : 2)) continue;
         // extrapolation: conserved variables and primitives (rho, u, v, p, alpha) of the two
         // cells next to the side
@@ -544,6 +572,7 @@ __global__ void __launch_bounds__(128) k_rev(AdjParams a, const double* __restri
     double e1 = -1.0, e2 = -1.0;
     long long i1 = LLONG_MAX, i2 = LLONG_MAX;
     double lbx = 0.0, lby = 0.0;
+    double bsum = 0.0, Ub_bf0 = 0.0, Ub_bf2 = 0.0;  // the body force's terms (a.bodyforce)
     if (i < ni && j < nj) {
         const long long o = (long long)j * ni + i;
         double U[4], Ub[4] = {0.0, 0.0, 0.0, 0.0};
@@ -568,6 +597,15 @@ __global__ void __launch_bounds__(128) k_rev(AdjParams a, const double* __restri
             prim_pullback_all(U, q, a.gamma, pbar[0], pbar[1], pbar[2], pbar[3], pbar[4], Ub);
         }
         const double dt = STAGE == 0 ? 0.0 : *dtp;
+        if (STAGE != 0 && a.bodyforce) {
+            // the stage's body force f_s (0, 0, rho, rho v) of its input u: (df/du)^T w sends
+            // f_s w[2] to rho and f_s w[3] to rho v; its dt-part w . S for the time step
+            const double w2 = w[2 * a.plane + o], w3 = w[3 * a.plane + o];
+            const double f = (STAGE == 1 ? 1.0 : STAGE == 2 ? 0.25 : kTwoThirdsSingle) * dt;
+            bsum = fma(w2, U[0], w3 * U[2]);
+            Ub_bf0 = f * w2;
+            Ub_bf2 = f * w3;
+        }
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
             const long long ov = v * a.plane + o;
@@ -575,14 +613,15 @@ __global__ void __launch_bounds__(128) k_rev(AdjParams a, const double* __restri
                 out[ov] = Ub[v];
             } else {
                 const double wv = w[ov];
+                const double bf = v == 0 ? Ub_bf0 : v == 2 ? Ub_bf2 : 0.0;
                 if (STAGE == 3) {
                     acc[ov] = 1.0 / 3.0 * wv;
-                    out[ov] = 2.0 / 3.0 * wv + 2.0 / 3.0 * dt * Ub[v];
+                    out[ov] = 2.0 / 3.0 * wv + 2.0 / 3.0 * dt * Ub[v] + bf;
                 } else if (STAGE == 2) {
                     acc[ov] += 3.0 / 4.0 * wv;
-                    out[ov] = 1.0 / 4.0 * wv + 1.0 / 4.0 * dt * Ub[v];
+                    out[ov] = 1.0 / 4.0 * wv + 1.0 / 4.0 * dt * Ub[v] + bf;
                 } else {
-                    out[ov] = acc[ov] + wv + dt * Ub[v];
+                    out[ov] = acc[ov] + wv + dt * Ub[v] + bf;
                 }
             }
         }
@@ -608,6 +647,13 @@ __global__ void __launch_bounds__(128) k_rev(AdjParams a, const double* __restri
             lp[0] = lbx;
             lp[1] = lby;
         }
+    }
+    if (STAGE != 0 && a.bodyforce) {  // uniform over the grid
+        __syncthreads();  // the shared arrays of the reductions above are free again
+        double zero = 0.0;
+        block_sum2(bsum, zero);
+        if (threadIdx.x == 0 && threadIdx.y == 0)
+            a.bpart[(STAGE - 1) * (gridDim.x * gridDim.y) + blockIdx.y * gridDim.x + blockIdx.x] = bsum;
     }
 }
 
@@ -694,6 +740,11 @@ __global__ void __launch_bounds__(256) k_dt(AdjParams a, const double* __restric
         const int st = k / npart;
         s += (st == 0 ? 1.0 : st == 1 ? 0.25 : 2.0 / 3.0) * part[k];
     }
+    if (a.bodyforce)  // the stages' body-force terms w . S, with their own stage-3 factor
+        for (int k = t; k < 3 * nm; k += blockDim.x) {
+            const int st = k / nm;
+            s += (st == 0 ? 1.0 : st == 1 ? 0.25 : kTwoThirdsSingle) * a.bpart[k];
+        }
     double e1 = -1.0, e2 = -1.0, i1 = 1e300, i2 = 1e300;
     for (int k = t; k < nm; k += blockDim.x) {
         const double* mp = mpart + 4 * k;
@@ -1072,7 +1123,7 @@ void dense_adjoint_destroy(dense_adjoint_t* a) {
     if (!a) return;
     if (a->h) cudaStreamSynchronize(a->h->stream);
     double* bufs[] = {a->ckpt, a->dts, a->rec, a->tape, a->g, a->g1, a->g2, a->acc, a->hb, a->part, a->mpart,
-                      a->lamv, a->lmp, a->lpart, a->seg_dts};
+                      a->lamv, a->lmp, a->lpart, a->seg_dts, a->ap.bpart};
     for (double* b : bufs) if (b) cudaFree(b);
     if (a->argmax) cudaFree(a->argmax);
     if (a->seg_argmax) cudaFree(a->seg_argmax);
@@ -1092,7 +1143,7 @@ int dense_adjoint_create(const dense_config_t* cfg, int checkpoint_every, dense_
     if (cfg->recon != DENSE_RECON_UPWIND5 && cfg->recon != DENSE_RECON_WENOJS5 && cfg->recon != DENSE_RECON_WENOZ5)
         return aerr(nullptr, DENSE_ERR_ARG, "the adjoint covers reconstructions 251, 253 and 255");
     // ghost rules (bottom, top, left, right) of the benchmarks covered: periodic, the
-    // extrapolation and the mirror (boundary_ivc/sedov/rm/shockvortex_general.f90)
+    // extrapolation, the mirror and fixed states (boundary_ivc/sedov/rm/shockvortex/rt_general.f90)
     int rules[4];
     switch (cfg->benchmark) {
     case DENSE_BENCH_IVC_PERIODIC: case DENSE_BENCH_RM_PERIODIC:
@@ -1103,10 +1154,14 @@ int dense_adjoint_create(const dense_config_t* cfg, int checkpoint_every, dense_
         rules[0] = rules[2] = dense::adj::kRuleReflect; rules[1] = rules[3] = dense::adj::kRuleExtrap; break;
     case DENSE_BENCH_RM: case DENSE_BENCH_SHOCKVORTEX:  // mirror bottom and top, extrapolated sides
         rules[0] = rules[1] = dense::adj::kRuleReflect; rules[2] = rules[3] = dense::adj::kRuleExtrap; break;
+    case DENSE_BENCH_RT:  // fixed bottom and top states, periodic sides
+        rules[0] = rules[1] = dense::adj::kRuleFixed; rules[2] = rules[3] = dense::adj::kRulePeriodic; break;
+    case DENSE_BENCH_RT_REFLECT:  // fixed bottom and top states, mirror sides
+        rules[0] = rules[1] = dense::adj::kRuleFixed; rules[2] = rules[3] = dense::adj::kRuleReflect; break;
     default:
         return aerr(nullptr, DENSE_ERR_ARG,
-                    "the adjoint covers the benchmarks with periodic, extrapolated or mirror sides "
-                    "(1, 2, 4, 9, 11, 14); not the Dirichlet, time-dependent or body-force ones");
+                    "the adjoint covers the benchmarks with periodic, extrapolated, mirror or fixed-state sides "
+                    "(1, 2, 3, 4, 9, 11, 13, 14); not those with time-dependent or inflow rules (5, 6)");
     }
     if (cfg->ni < 8 || cfg->nj < 8) return aerr(nullptr, DENSE_ERR_ARG, "the adjoint needs ni, nj >= 8");
     if (checkpoint_every < 1) return aerr(nullptr, DENSE_ERR_ARG, "checkpoint_every must be >= 1");
@@ -1135,6 +1190,9 @@ int dense_adjoint_create(const dense_config_t* cfg, int checkpoint_every, dense_
     p.gamma = cfg->gamma; p.dx = cfg->dx; p.dy = cfg->dy; p.inv_dx = 1.0 / cfg->dx; p.inv_dy = 1.0 / cfg->dy;
     p.cfl = cfg->cfl;
     for (int k = 0; k < 4; ++k) p.rule[k] = rules[k];
+    // the forward solver applies the body force on the same condition (fill_params)
+    p.bodyforce = cfg->if_bodyforce &&
+                  (cfg->benchmark == DENSE_BENCH_RT || cfg->benchmark == DENSE_BENCH_RT_REFLECT);
     a->tape_stage = (size_t)p.np * (size_t)(p.xs + p.ys);
     a->gh = dim3((cfg->ni + 1 + kHX - 1) / kHX, (cfg->nj + 1 + kHY - 1) / kHY, 2);
     a->gc = dim3((cfg->ni + kCX - 1) / kCX, (cfg->nj + kCY - 1) / kCY);
@@ -1145,6 +1203,7 @@ int dense_adjoint_create(const dense_config_t* cfg, int checkpoint_every, dense_
         {&a->hb, (size_t)4 * (p.xs + p.ys)}, {&a->part, (size_t)3 * a->npart}, {&a->mpart, (size_t)4 * a->nm},
         {&a->rec, (size_t)3 * a->k * a->state}, {&a->tape, (size_t)3 * a->k * a->tape_stage},
         {&a->lamv, 4}, {&a->lmp, (size_t)4 * a->nm}, {&a->lpart, (size_t)2 * a->nm}, {&a->seg_dts, (size_t)a->k},
+        {&p.bpart, (size_t)3 * a->nm},
     };
     for (auto& b : bufs) {
         cudaError_t e = cudaMalloc((void**)b.p, b.n * sizeof(double));

@@ -159,11 +159,13 @@ def rough_state(dense, cfg, seed):
 
 
 @pytest.mark.parametrize("bench,split,recon", [(1, 101, 253), (2, 101, 255), (4, 102, 253), (9, 103, 255),
-                                               (2, 103, 251), (1, 102, 255)])
+                                               (2, 103, 251), (1, 102, 255), (3, 101, 253), (13, 102, 255),
+                                               (13, 103, 253)])
 def test_rhs_vjp_with_walls_matches_autograd(dense, adjoint, bench, split, recon):
-    """The reference's benchmarks with walls -- extrapolated (1: x; 2: top, right; 4, 9: sides)
-    and mirror sides (2: bottom, left; 4, 9: bottom, top): the ghost cells' split sensitivities
-    sent back through the rules, against autograd through the PyTorch step's ghost layers."""
+    """The reference's benchmarks with walls -- extrapolated (1: x; 2: top, right; 4, 9: sides),
+    mirror (2: bottom, left; 4, 9: bottom, top; 13: sides) and fixed-state sides (3, 13: bottom,
+    top): the ghost cells' split sensitivities sent back through the rules (none through a fixed
+    state), against autograd through the PyTorch step's ghost layers."""
     cfg = dense.config_default(ni=24, nj=20, benchmark=bench, splitting=split, recon=recon, cfl=0.4)
     c, U = rough_state(dense, cfg, seed=bench * 10 + split % 10)
     v = torch.randn(U.shape, generator=torch.Generator().manual_seed(3), dtype=torch.float64).cuda()
@@ -176,9 +178,12 @@ def test_rhs_vjp_with_walls_matches_autograd(dense, adjoint, bench, split, recon
     assert abs(vdotl - float((v * L.detach()).sum())) < 1e-12 * float((v * L.detach()).abs().sum())
 
 
-@pytest.mark.parametrize("bench,split,recon", [(4, 101, 253), (2, 102, 255), (1, 103, 253)])
+@pytest.mark.parametrize("bench,split,recon", [(4, 101, 253), (2, 102, 255), (1, 103, 253), (3, 101, 253),
+                                               (13, 102, 253), (13, 103, 255)])
 def test_steps_gradient_with_walls_matches_autograd(dense, adjoint, bench, split, recon):
-    """5 steps with checkpoints every 2 on grids with wall sides, CFL time step."""
+    """5 steps with checkpoints every 2 on grids with wall sides, CFL time step; on the
+    Rayleigh-Taylor grids (3, 13) with the body force of every stage, whose time-step factor
+    carries the step's sensitivity to dt as well."""
     cfg = dense.config_default(ni=24, nj=20, benchmark=bench, splitting=split, recon=recon, cfl=0.4)
     c, U = rough_state(dense, cfg, seed=7 + bench)
     gT = torch.randn(U.shape, generator=torch.Generator().manual_seed(5), dtype=torch.float64).cuda()
@@ -193,8 +198,8 @@ def test_steps_gradient_with_walls_matches_autograd(dense, adjoint, bench, split
 
 
 def test_rejects_unsupported_configurations(dense, adjoint):
-    for kw in (dict(splitting=104), dict(recon=0, splitting=105), dict(benchmark=5), dict(benchmark=3),
-               dict(benchmark=13), dict(ni=6)):
+    for kw in (dict(splitting=104), dict(recon=0, splitting=105), dict(benchmark=5), dict(benchmark=6),
+               dict(ni=6)):
         cfg = dense.init_general(vortex_cfg(dense, 253))[0]
         for k, v in kw.items():
             setattr(cfg, k, v)

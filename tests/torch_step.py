@@ -1,5 +1,5 @@
-"""Pure-PyTorch float64 reference of the time step on x- and y-periodic grids, for checking the
-adjoint kernels against autograd (test infrastructure; never used by the library).
+"""Pure-PyTorch float64 reference of the time step, for checking the adjoint kernels against
+autograd (test infrastructure; never used by the library).
 
 Same scheme as the plain solver: get_primary (get_primary.f90:53-60), LLF splitting with
 lambda = |u_n| + alpha per cell (flux_splitting_LLF.f90:67-81) or GLF splitting with lambda the
@@ -77,25 +77,41 @@ def steger_warming(rho, u, v, a, gamma, d):
 
 
 # Ghost rules of the reference's benchmarks with fixed walls (boundary_ivc_general.f90,
-# boundary_sedov_general.f90, boundary_rm_general.f90, boundary_shockvortex_general.f90), per side
-# (bottom, top, left, right): "P" periodic, "E" the recursive 4/3, -1/3 extrapolation, "R" the
-# mirror with the normal velocity negated. Ghost primitives come from the rule applied to the
-# interior primitives, not from the ghost conserved variables.
-RULES = {1: "PPEE", 2: "RERE", 4: "RREE", 9: "RREE", 11: "PPPP", 14: "PPPP"}
+# boundary_sedov_general.f90, boundary_rm_general.f90, boundary_shockvortex_general.f90,
+# boundary_rt_general.f90), per side (bottom, top, left, right): "P" periodic, "E" the recursive
+# 4/3, -1/3 extrapolation, "R" the mirror with the normal velocity negated, "F" a fixed state
+# (Rayleigh-Taylor's bottom and top, boundary_rt_general.f90:14-57). Ghost primitives come from
+# the rule applied to the interior primitives, not from the ghost conserved variables.
+RULES = {1: "PPEE", 2: "RERE", 3: "FFPP", 4: "RREE", 9: "RREE", 11: "PPPP", 13: "FFRR", 14: "PPPP"}
+# the fixed states (rho, u, v, p) of the "F" sides: bottom, top
+RT_STATES = ((2.0, 0.0, 0.0, 1.0), (1.0, 0.0, 0.0, 2.5))
+# the stage-3 body-force factor 2.0/3.0 is a default-real literal (time_advance_general.f90:242)
+TWO_THIRDS_SINGLE = float(torch.tensor(2.0 / 3.0, dtype=torch.float32))
 
 
-def _pad_axis(A, axis, lo, hi, flip):
+def fixed_state(gamma, rho, u, v, p):
+    """Conserved variables and primitives (rho, u, v, p, alpha) of a fixed ghost state."""
+    cons = (rho, rho * u, rho * v, p / (gamma - 1.0) + 0.5 * rho * (u * u + v * v))
+    prim = (rho, u, v, p, (gamma * p / rho) ** 0.5)
+    return cons, prim
+
+
+def _pad_axis(A, axis, lo, hi, flip, fixed=None):
     """A (nv, nj, ni) padded by 4 ghost layers along axis (2: x, 1: y); flip is the component
-    negated by a mirror (the normal momentum, or the normal velocity of the primitives)."""
+    negated by a mirror (the normal momentum, or the normal velocity of the primitives); fixed
+    the (low, high) side states of "F" rules as per-component values."""
     n = A.shape[axis]
     take = lambda k: A.narrow(axis, k, 1)
     sign = torch.ones(A.shape[0], dtype=A.dtype, device=A.device)
     sign[flip] = -1.0
     sign = sign.view(-1, 1, 1)
 
-    def side(rule, inner):  # inner(d): the interior slice at distance d (1 = adjacent)
+    def side(rule, inner, state=None):  # inner(d): the interior slice at distance d (1 = adjacent)
         if rule == "P":
             return None
+        if rule == "F":
+            g = torch.tensor(state, dtype=A.dtype, device=A.device).view(-1, 1, 1).expand_as(inner(1))
+            return [g for _ in range(4)]
         if rule == "R":
             return [sign * inner(k + 1) for k in range(4)]
         a, b = inner(1), inner(2)
@@ -106,8 +122,8 @@ def _pad_axis(A, axis, lo, hi, flip):
             b, a = a, g
         return out
 
-    low = side(lo, lambda d: take(d - 1))
-    high = side(hi, lambda d: take(n - d))
+    low = side(lo, lambda d: take(d - 1), fixed[0] if fixed else None)
+    high = side(hi, lambda d: take(n - d), fixed[1] if fixed else None)
     if low is None:
         low = [take(n - 1 - k) for k in range(4)]
     if high is None:
@@ -118,7 +134,8 @@ def _pad_axis(A, axis, lo, hi, flip):
 def rhs(U, gamma, dx, dy, rec, split=101, bench=11):
     """L(U) = -(h_{i+1/2} - h_{i-1/2})/dx - (g_{j+1/2} - g_{j-1/2})/dy."""
     if bench not in (11, 14):
-        return _rhs_padded(U, gamma, dx, dy, rec, split, RULES[bench])
+        fixed = [fixed_state(gamma, *st) for st in RT_STATES] if bench in (3, 13) else None
+        return _rhs_padded(U, gamma, dx, dy, rec, split, RULES[bench], fixed)
     rho, u, v, p, a = primitives(U, gamma)
     out = torch.zeros_like(U)
     for d, (un, h, axis) in enumerate(((u, dx, 2), (v, dy, 1))):
@@ -141,15 +158,18 @@ def rhs(U, gamma, dx, dy, rec, split=101, bench=11):
     return out
 
 
-def _rhs_padded(U, gamma, dx, dy, rec, split, rules):
-    """L(U) on a grid with ghost layers filled by the given rules (bottom, top, left, right)."""
+def _rhs_padded(U, gamma, dx, dy, rec, split, rules, fixed=None):
+    """L(U) on a grid with ghost layers filled by the given rules (bottom, top, left, right);
+    fixed: the (cons, prim) states of the bottom and top "F" sides."""
     rho, u, v, p, a = primitives(U, gamma)
     Pr = torch.stack([rho, u, v, p, a])
     out = torch.zeros_like(U)
     for d, (h, axis) in enumerate(((dx, 2), (dy, 1))):
         lo, hi = (rules[2], rules[3]) if d == 0 else (rules[0], rules[1])
-        Ug = _pad_axis(U, axis, lo, hi, 1 + d)
-        Pg = _pad_axis(Pr, axis, lo, hi, 1 + d)
+        fu = (fixed[0][0], fixed[1][0]) if fixed and d == 1 else None
+        fp = (fixed[0][1], fixed[1][1]) if fixed and d == 1 else None
+        Ug = _pad_axis(U, axis, lo, hi, 1 + d, fu)
+        Pg = _pad_axis(Pr, axis, lo, hi, 1 + d, fp)
         r_, u_, v_, p_, a_ = Pg
         un = u_ if d == 0 else v_
         if split == 103:
@@ -171,8 +191,19 @@ def _rhs_padded(U, gamma, dx, dy, rec, split, rules):
     return out
 
 
-def time_step(U, gamma, dx, dy, rec, cfl, dt_const=None, split=101, bench=11):
-    """One TVD-RK3 step; returns (U_next, dt)."""
+def body_force(U):
+    """The Rayleigh-Taylor source (0, 0, rho, rho v) of a state (boundary_rt_general.f90:154-155)."""
+    zero = torch.zeros_like(U[0])
+    return torch.stack([zero, zero, U[0], U[2]])
+
+
+def time_step(U, gamma, dx, dy, rec, cfl, dt_const=None, split=101, bench=11, bodyforce=None):
+    """One TVD-RK3 step; returns (U_next, dt). The body force (Rayleigh-Taylor, benchmarks 3
+    and 13 unless bodyforce says otherwise) is added to each stage after the combine, f_s times
+    the source of the stage's input with f_s = dt, dt/4 and 2/3 (single precision) dt
+    (time_advance_general.f90:79,160,242)."""
+    if bodyforce is None:
+        bodyforce = bench in (3, 13)
     if dt_const is None:
         _, u, v, _, a = primitives(U, gamma)
         mx = (u.abs() + a).max()
@@ -181,13 +212,16 @@ def time_step(U, gamma, dx, dy, rec, cfl, dt_const=None, split=101, bench=11):
         dt = cfl * dt_x * dt_y / (dt_x + dt_y)
     else:
         dt = torch.tensor(dt_const, dtype=U.dtype, device=U.device)
-    u1 = U + dt * rhs(U, gamma, dx, dy, rec, split, bench)
-    u2 = 3.0 / 4.0 * U + 1.0 / 4.0 * u1 + 1.0 / 4.0 * dt * rhs(u1, gamma, dx, dy, rec, split, bench)
-    u3 = 1.0 / 3.0 * U + 2.0 / 3.0 * u2 + 2.0 / 3.0 * dt * rhs(u2, gamma, dx, dy, rec, split, bench)
+    src = (lambda W, f: f * dt * body_force(W)) if bodyforce else (lambda W, f: 0.0)
+    u1 = U + dt * rhs(U, gamma, dx, dy, rec, split, bench) + src(U, 1.0)
+    u2 = (3.0 / 4.0 * U + 1.0 / 4.0 * u1 + 1.0 / 4.0 * dt * rhs(u1, gamma, dx, dy, rec, split, bench)
+          + src(u1, 0.25))
+    u3 = (1.0 / 3.0 * U + 2.0 / 3.0 * u2 + 2.0 / 3.0 * dt * rhs(u2, gamma, dx, dy, rec, split, bench)
+          + src(u2, TWO_THIRDS_SINGLE))
     return u3, dt
 
 
-def run(U, n, gamma, dx, dy, rec, cfl, dt_const=None, split=101, bench=11):
+def run(U, n, gamma, dx, dy, rec, cfl, dt_const=None, split=101, bench=11, bodyforce=None):
     for _ in range(n):
-        U, _ = time_step(U, gamma, dx, dy, rec, cfl, dt_const, split, bench)
+        U, _ = time_step(U, gamma, dx, dy, rec, cfl, dt_const, split, bench, bodyforce)
     return U
