@@ -2,8 +2,8 @@
 
 ``Adjoint`` owns a forward solver and the adjoint kernels of ``csrc/adjoint.cu`` (LLF, GLF or
 Steger-Warming splitting with upwind5 / WENO-JS5 / WENO-Z5 on x- and y-periodic grids or the
-reference's benchmarks with extrapolated, mirror and fixed-state sides (1, 2, 3, 4, 9, 13; the
-Rayleigh-Taylor ones with their body force), TVD-RK3, CFL or constant dt).
+reference's benchmarks with extrapolated, mirror and fixed-state sides (1, 2, 3, 4, 5, 9, 13;
+the Rayleigh-Taylor ones with their body force), TVD-RK3, CFL or constant dt).
 States are CUDA float64 tensors of the interior, shape (4, nj, ni): conserved variables
 (rho, rho u, rho v, E) with i fastest -- the reference's cons(i, j, v) without ghost layers.
 

@@ -72,6 +72,7 @@ struct AdjParams {
     // bpart[(s - 1) nm + block]
     int bodyforce;
     double* bpart;
+    int bench;        // the benchmark (its fixed ghost states: fixed_state)
 };
 // Ghost rules of the benchmarks the adjoint covers (boundary_*_general.f90): a periodic copy,
 // the recursive 4/3, -1/3 extrapolation of the two cells next to the side, the mirror of the
@@ -79,6 +80,9 @@ struct AdjParams {
 // and, separately, to the primitives -- or a fixed state (Rayleigh-Taylor's Dirichlet bottom and
 // top, boundary_rt_general.f90:14-57), which no interior cell feeds.
 constexpr int kRulePeriodic = 0, kRuleExtrap = 1, kRuleReflect = 2, kRuleFixed = 3;
+// the double Mach reflection's bottom: the mirror where the column's centre x >= 1/6, the fixed
+// post-shock state before it (boundary_doublemach_general.f90:14-48)
+constexpr int kRuleDMRBottom = 4;
 constexpr double kTwoThirdsSingle = (double)(2.0f / 3.0f);  // time_advance_general.f90:242
 
 // get_primary of one cell (get_primary.f90:53-60), with the pressure floor of :58; rs = 1/alpha'
@@ -447,11 +451,33 @@ __device__ __forceinline__ void gather_line(const double* __restrict__ T, const 
 // next to the side (the recursion g = 4/3 near - 1/3 far unrolled), so both of those cells
 // rebuild all four ghosts and take their shares. GLF: a ghost's lambda sensitivity goes to the
 // global lambda once (lb, by the cell next to the side or the mirrored cell).
+// Conserved variables of the fixed ghost state of side `side` of direction DIR at line `line`
+// (a column for the bottom and top, a row for the sides), at the step's start time t:
+// Rayleigh-Taylor's bottom (2, 0, 0, 1) and top (1, 0, 0, 2.5) (boundary_rt_general.f90:14-57);
+// the double Mach reflection's inflow and bottom-before-the-wall post-shock state, and its top,
+// post-shock ahead of the moving shock x < 1/6 + (1 + 20 t)/sqrt(3), pre-shock behind it
+// (boundary_doublemach_general.f90:51-99). Same formulas as the boundary fill's state_from.
+__device__ __forceinline__ void fixed_state(const AdjParams& a, int dir, int side, int line, double t, double Ug[4]) {
+    double rho, u = 0.0, v = 0.0, pr;
+    if (a.bench == DENSE_BENCH_DMR) {
+        const double x = ((double)(line + 1) - 0.5) * a.dx;  // the column's centre (init centres)
+        const bool post = !(dir == 1 && side == 1) || x < (1.0 / 6.0 + (1.0 + 20.0 * t) / sqrt(3.0));
+        if (post) { rho = 8.0; u = (double)8.25f * sqrt(3.0) * 0.5; v = -(double)8.25f * 0.5; pr = 116.5; }
+        else      { rho = 1.4; pr = 1.0; }
+    } else {
+        const bool bottom = side == 0;
+        rho = bottom ? 2.0 : 1.0;
+        pr = bottom ? 1.0 : 2.5;
+    }
+    Ug[0] = rho; Ug[1] = rho * u; Ug[2] = rho * v;
+    Ug[3] = pr / (a.gamma - 1.0) + 0.5 * rho * (u * u + v * v);
+}
+
 template <int DIR, int SPL, int REC>
 __device__ __forceinline__ void wall_terms(const AdjParams& a, const double* __restrict__ u,
                                            const double* __restrict__ tape, const double* __restrict__ hb, int i,
-                                           int j, const Prim& q, const double U[4], double lam_g, double Ub[4],
-                                           double pbar[5], double& lb) {
+                                           int j, const Prim& q, const double U[4], double lam_g, double t,
+                                           double Ub[4], double pbar[5], double& lb) {
     const int n = DIR == 0 ? a.ni : a.nj, x = DIR == 0 ? i : j;
     const long long ts = DIR == 0 ? a.xs : a.ys;
     const double* T = DIR == 0 ? tape : tape + a.np * a.xs;
@@ -462,18 +488,18 @@ __device__ __forceinline__ void wall_terms(const AdjParams& a, const double* __r
                                  {-1.0 / 3.0, -4.0 / 9.0, -13.0 / 27.0, -40.0 / 81.0}};
 #pragma unroll 1
     for (int side = 0; side < 2; ++side) {
-        const int rule = a.rule[DIR == 0 ? 2 + side : side];
+        int rule = a.rule[DIR == 0 ? 2 + side : side];
         if (rule == kRulePeriodic) continue;
+        const int line = DIR == 0 ? j : i;
+        if (rule == kRuleDMRBottom) rule = ((double)(i + 1) - 0.5) * a.dx >= 1.0 / 6.0 ? kRuleReflect : kRuleFixed;
         const int dist = side == 0 ? x + 1 : n - x;  // 1 = next to the side
         if (rule == kRuleFixed) {
-            // a fixed ghost state (Rayleigh-Taylor's bottom and top, boundary_rt_general.f90:
-            // 14-57) depends on no cell; only GLF's global lambda enters its split,
-            // dF+-/dlambda = +-U/2, whose sensitivity the cell next to the side takes for the
-            // line's four ghosts
+            // a fixed ghost state depends on no cell; only GLF's global lambda enters its
+            // split, dF+-/dlambda = +-U/2, whose sensitivity the cell next to the side takes for
+            // the line's four ghosts
             if (SPL != 1 || dist != 1) continue;
-            const bool bottom = DIR == 1 && side == 0;
-            const double rho = bottom ? 2.0 : 1.0, pr = bottom ? 1.0 : 2.5;
-            const double Ug[4] = {rho, 0.0, 0.0, pr / (a.gamma - 1.0)};
+            double Ug[4];
+            fixed_state(a, DIR, side, line, t, Ug);
 #pragma unroll 1
             for (int k = 0; k < 4; ++k) {
                 double gp[4] = {0, 0, 0, 0}, gm[4] = {0, 0, 0, 0};
@@ -565,8 +591,9 @@ __global__ void __launch_bounds__(128) k_rev(AdjParams a, const double* __restri
                                              const double* __restrict__ w, const double* __restrict__ tape,
                                              const double* __restrict__ hb, double* __restrict__ acc,
                                              double* __restrict__ out, const double* __restrict__ dtp,
-                                             double* __restrict__ mpart, const double* __restrict__ lamv,
-                                             double* __restrict__ lpart, int STAGE) {
+                                             const double* __restrict__ tp, double* __restrict__ mpart,
+                                             const double* __restrict__ lamv, double* __restrict__ lpart,
+                                             int STAGE) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     const int ni = a.ni, nj = a.nj;
     double e1 = -1.0, e2 = -1.0;
@@ -592,8 +619,9 @@ __global__ void __launch_bounds__(128) k_rev(AdjParams a, const double* __restri
         if (WALLS && (!px || !py)) {  // the ghost cells of wall sides that this cell feeds
             // (a separate instantiation: the periodic kernels keep their registers)
             double pbar[5] = {0, 0, 0, 0, 0};
-            if (!px) wall_terms<0, SPL, REC>(a, u, tape, hb, i, j, q, U, GLF ? lamv[0] : 0.0, Ub, pbar, lbx);
-            if (!py) wall_terms<1, SPL, REC>(a, u, tape, hb, i, j, q, U, GLF ? lamv[1] : 0.0, Ub, pbar, lby);
+            const double t = tp ? *tp : 0.0;  // the step's start time (the moving shock's ghosts)
+            if (!px) wall_terms<0, SPL, REC>(a, u, tape, hb, i, j, q, U, GLF ? lamv[0] : 0.0, t, Ub, pbar, lbx);
+            if (!py) wall_terms<1, SPL, REC>(a, u, tape, hb, i, j, q, U, GLF ? lamv[1] : 0.0, t, Ub, pbar, lby);
             prim_pullback_all(U, q, a.gamma, pbar[0], pbar[1], pbar[2], pbar[3], pbar[4], Ub);
         }
         const double dt = STAGE == 0 ? 0.0 : *dtp;
@@ -817,7 +845,8 @@ struct dense_adjoint {
     size_t tape_stage = 0;        // doubles of one stage's tape (both directions)
     AdjParams ap{};
     double* ckpt = nullptr;  int ckpt_cap = 0;    // states at steps 0, k, 2k, ...
-    double* dts = nullptr;   int dts_cap = 0;     // dt of every forward step
+    double* dts = nullptr;   int dts_cap = 0;     // dt of every forward step, then (from dts_cap
+                                                  // on) each step's start time
     int* argmax = nullptr;   int argmax_cap = 0;  // per step: cells of the two maxima
     double* rec = nullptr;                        // k steps x 3 stage states of one segment
     double* tape = nullptr;                       // k steps x 3 stage tapes of one segment
@@ -947,32 +976,33 @@ cudaError_t graph_stage(dense_adjoint* a, int irk, double* tape) {
 
 template <int REC, int SPL, bool WALLS>
 void launch_rev_w(dense_adjoint* a, int stage, const double* u, const double* tape, const double* w, double* out,
-                  const double* dtp, cudaStream_t s) {
+                  const double* dtp, const double* tp, cudaStream_t s) {
     using namespace dense::adj;
     const dim3 bc(kCX, kCY);
     double* const lv = a->lamv;
     double* const lp = a->lpart;
     if (stage == 0)
-        k_rev<REC, SPL, WALLS><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, a->hb, nullptr, out, nullptr, nullptr, lv, lp, 0);
+        k_rev<REC, SPL, WALLS><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, a->hb, nullptr, out, nullptr, tp, nullptr,
+                                                    lv, lp, 0);
     else
-        k_rev<REC, SPL, WALLS><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, a->hb, a->acc, out, dtp,
+        k_rev<REC, SPL, WALLS><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, a->hb, a->acc, out, dtp, tp,
                                                     stage == 1 ? a->mpart : nullptr, lv, lp, stage);
 }
 template <int REC, int SPL>
 void launch_rev(dense_adjoint* a, int stage, const double* u, const double* tape, const double* w, double* out,
-                const double* dtp, cudaStream_t s) {
+                const double* dtp, const double* tp, cudaStream_t s) {
     const int* r = a->ap.rule;
     const bool walls = r[0] != dense::adj::kRulePeriodic || r[2] != dense::adj::kRulePeriodic;
-    if (walls) launch_rev_w<REC, SPL, true>(a, stage, u, tape, w, out, dtp, s);
-    else       launch_rev_w<REC, SPL, false>(a, stage, u, tape, w, out, dtp, s);
+    if (walls) launch_rev_w<REC, SPL, true>(a, stage, u, tape, w, out, dtp, tp, s);
+    else       launch_rev_w<REC, SPL, false>(a, stage, u, tape, w, out, dtp, tp, s);
 }
 template <int SPL>
 void launch_rev_recon(dense_adjoint* a, int stage, const double* u, const double* tape, const double* w,
-                      double* out, const double* dtp, cudaStream_t s) {
+                      double* out, const double* dtp, const double* tp, cudaStream_t s) {
     switch (a->cfg.recon) {
-    case DENSE_RECON_UPWIND5: launch_rev<DENSE_RECON_UPWIND5, SPL>(a, stage, u, tape, w, out, dtp, s); break;
-    case DENSE_RECON_WENOJS5: launch_rev<DENSE_RECON_WENOJS5, SPL>(a, stage, u, tape, w, out, dtp, s); break;
-    default:                  launch_rev<DENSE_RECON_WENOZ5, SPL>(a, stage, u, tape, w, out, dtp, s); break;
+    case DENSE_RECON_UPWIND5: launch_rev<DENSE_RECON_UPWIND5, SPL>(a, stage, u, tape, w, out, dtp, tp, s); break;
+    case DENSE_RECON_WENOJS5: launch_rev<DENSE_RECON_WENOJS5, SPL>(a, stage, u, tape, w, out, dtp, tp, s); break;
+    default:                  launch_rev<DENSE_RECON_WENOZ5, SPL>(a, stage, u, tape, w, out, dtp, tp, s); break;
     }
 }
 
@@ -980,7 +1010,7 @@ void launch_rev_recon(dense_adjoint* a, int stage, const double* u, const double
 // the cells; GLF first finds the stage's global lambda and its cells, and last sends lambda's
 // sensitivity to those cells
 void vjp(dense_adjoint* a, int stage, const double* u, const double* tape, const double* w, double* out,
-         double* part, const double* dtp) {
+         double* part, const double* dtp, const double* tp) {
     using namespace dense::adj;
     cudaStream_t s = a->h->stream;
     const bool glf = a->cfg.splitting == DENSE_SPLIT_GLF;
@@ -990,9 +1020,9 @@ void vjp(dense_adjoint* a, int stage, const double* u, const double* tape, const
         a->launches += 2;
     }
     k_hbar<<<a->gh, dim3(kHX, kHY), 0, s>>>(a->ap, w, tape, a->hb, part);
-    if (glf) launch_rev_recon<1>(a, stage, u, tape, w, out, dtp, s);
-    else if (a->cfg.splitting == DENSE_SPLIT_SW) launch_rev_recon<2>(a, stage, u, tape, w, out, dtp, s);
-    else launch_rev_recon<0>(a, stage, u, tape, w, out, dtp, s);
+    if (glf) launch_rev_recon<1>(a, stage, u, tape, w, out, dtp, tp, s);
+    else if (a->cfg.splitting == DENSE_SPLIT_SW) launch_rev_recon<2>(a, stage, u, tape, w, out, dtp, tp, s);
+    else launch_rev_recon<0>(a, stage, u, tape, w, out, dtp, tp, s);
     a->launches += 2;
     if (glf) {
         switch (stage) {
@@ -1005,15 +1035,16 @@ void vjp(dense_adjoint* a, int stage, const double* u, const double* tape, const
     }
 }
 
-// reverse of one step from its three recorded stage states and tapes, its time step *dtp and
-// the slot of its maxima cells; g holds dJ/du(n+1) on entry and dJ/du(n) on return
+// reverse of one step from its three recorded stage states and tapes, its time step *dtp, its
+// start time *tp and the slot of its maxima cells; g holds dJ/du(n+1) on entry and dJ/du(n) on
+// return
 void reverse_step(dense_adjoint* a, const double* rec_step, const double* tape_step, const double* dtp,
-                  int* argmax) {
+                  const double* tp, int* argmax) {
     const double* u[3] = {rec_step, rec_step + a->state, rec_step + 2 * a->state};
     const double* t[3] = {tape_step, tape_step + a->tape_stage, tape_step + 2 * a->tape_stage};
-    vjp(a, 3, u[2], t[2], a->g, a->g2, a->part + 2 * a->npart, dtp);
-    vjp(a, 2, u[1], t[1], a->g2, a->g1, a->part + 1 * a->npart, dtp);
-    vjp(a, 1, u[0], t[0], a->g1, a->g, a->part, dtp);
+    vjp(a, 3, u[2], t[2], a->g, a->g2, a->part + 2 * a->npart, dtp, tp);
+    vjp(a, 2, u[1], t[1], a->g2, a->g1, a->part + 1 * a->npart, dtp, tp);
+    vjp(a, 1, u[0], t[0], a->g1, a->g, a->part, dtp, tp);
     if (!a->cfg.if_const_dt) {
         dense::adj::k_dt<<<1, 256, 0, a->h->stream>>>(a->ap, a->part, a->npart, a->mpart, a->nm, u[0], a->g, dtp,
                                                       argmax);
@@ -1086,7 +1117,7 @@ int segment_graphs(dense_adjoint* a) {
         int rc = capture(a, [&] {
             for (int s = a->k - 1; s >= 0; --s)
                 reverse_step(a, a->rec + (size_t)s * 3 * a->state, a->tape + (size_t)s * 3 * a->tape_stage,
-                             a->seg_dts + s, a->seg_argmax + 2 * s);
+                             a->seg_dts + s, a->seg_dts + a->k + s, a->seg_argmax + 2 * s);
             return (int)DENSE_OK;
         }, &a->rev_exec, &a->rev_nodes);
         if (rc) return rc;
@@ -1158,10 +1189,13 @@ int dense_adjoint_create(const dense_config_t* cfg, int checkpoint_every, dense_
         rules[0] = rules[1] = dense::adj::kRuleFixed; rules[2] = rules[3] = dense::adj::kRulePeriodic; break;
     case DENSE_BENCH_RT_REFLECT:  // fixed bottom and top states, mirror sides
         rules[0] = rules[1] = dense::adj::kRuleFixed; rules[2] = rules[3] = dense::adj::kRuleReflect; break;
+    case DENSE_BENCH_DMR:  // wall from x = 1/6 on, moving-shock top, inflow left, extrapolated right
+        rules[0] = dense::adj::kRuleDMRBottom; rules[1] = rules[2] = dense::adj::kRuleFixed;
+        rules[3] = dense::adj::kRuleExtrap; break;
     default:
         return aerr(nullptr, DENSE_ERR_ARG,
                     "the adjoint covers the benchmarks with periodic, extrapolated, mirror or fixed-state sides "
-                    "(1, 2, 3, 4, 9, 11, 13, 14); not those with time-dependent or inflow rules (5, 6)");
+                    "(1, 2, 3, 4, 5, 9, 11, 13, 14); not the shear layer's oscillating inflow (6)");
     }
     if (cfg->ni < 8 || cfg->nj < 8) return aerr(nullptr, DENSE_ERR_ARG, "the adjoint needs ni, nj >= 8");
     if (checkpoint_every < 1) return aerr(nullptr, DENSE_ERR_ARG, "checkpoint_every must be >= 1");
@@ -1182,6 +1216,17 @@ int dense_adjoint_create(const dense_config_t* cfg, int checkpoint_every, dense_
         dense_adjoint_destroy(a);
         return code;
     };
+    if (cfg->benchmark == DENSE_BENCH_DMR) {
+        // the forward solver's boundary rows of the cell centres x = (i - 1/2) dx (init centres):
+        // the bottom wall starts at x = 1/6, the top state follows the shock
+        std::vector<double> xs(cfg->ni);
+        for (int i = 0; i < cfg->ni; ++i) xs[i] = ((double)(i + 1) - 0.5) * cfg->dx;
+        if (cudaMemcpy(a->h->xbot, xs.data(), xs.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(a->h->xtop, xs.data(), xs.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
+            a->err = "cudaMemcpy of the boundary rows failed";
+            return fail(DENSE_ERR_CUDA);
+        }
+    }
     AdjParams& p = a->ap;
     p.ni = cfg->ni; p.nj = cfg->nj; p.plane = (long long)cfg->ni * cfg->nj;
     p.xs = (long long)cfg->nj * (cfg->ni + 1);
@@ -1193,6 +1238,7 @@ int dense_adjoint_create(const dense_config_t* cfg, int checkpoint_every, dense_
     // the forward solver applies the body force on the same condition (fill_params)
     p.bodyforce = cfg->if_bodyforce &&
                   (cfg->benchmark == DENSE_BENCH_RT || cfg->benchmark == DENSE_BENCH_RT_REFLECT);
+    p.bench = cfg->benchmark;
     a->tape_stage = (size_t)p.np * (size_t)(p.xs + p.ys);
     a->gh = dim3((cfg->ni + 1 + kHX - 1) / kHX, (cfg->nj + 1 + kHY - 1) / kHY, 2);
     a->gc = dim3((cfg->ni + kCX - 1) / kCX, (cfg->nj + kCY - 1) / kCY);
@@ -1202,7 +1248,7 @@ int dense_adjoint_create(const dense_config_t* cfg, int checkpoint_every, dense_
         {&a->g, a->state}, {&a->g1, a->state}, {&a->g2, a->state}, {&a->acc, a->state},
         {&a->hb, (size_t)4 * (p.xs + p.ys)}, {&a->part, (size_t)3 * a->npart}, {&a->mpart, (size_t)4 * a->nm},
         {&a->rec, (size_t)3 * a->k * a->state}, {&a->tape, (size_t)3 * a->k * a->tape_stage},
-        {&a->lamv, 4}, {&a->lmp, (size_t)4 * a->nm}, {&a->lpart, (size_t)2 * a->nm}, {&a->seg_dts, (size_t)a->k},
+        {&a->lamv, 4}, {&a->lmp, (size_t)4 * a->nm}, {&a->lpart, (size_t)2 * a->nm}, {&a->seg_dts, (size_t)2 * a->k},
         {&p.bpart, (size_t)3 * a->nm},
     };
     for (auto& b : bufs) {
@@ -1228,7 +1274,7 @@ int dense_adjoint_forward(dense_adjoint_t* a, const double* u0, int nsteps, doub
     if (nsteps < 0) return aerr(a, DENSE_ERR_ARG, "nsteps < 0");
     const int nseg = (nsteps + a->k - 1) / a->k;
     int rc = grow(a, &a->ckpt, &a->ckpt_cap, nseg > 0 ? nseg : 1, a->state);
-    if (!rc) rc = grow(a, &a->dts, &a->dts_cap, nsteps > 0 ? nsteps : 1, 1);
+    if (!rc) rc = grow(a, &a->dts, &a->dts_cap, nsteps > 0 ? nsteps : 1, 2);
     if (!rc) rc = grow(a, &a->argmax, &a->argmax_cap, nsteps > 0 ? nsteps : 1, 2);
     if (rc) return rc;
     a->nsteps = -1;
@@ -1244,6 +1290,8 @@ int dense_adjoint_forward(dense_adjoint_t* a, const double* u0, int nsteps, doub
             rc = from_solver(a, a->ckpt + (size_t)(s / a->k) * a->state);
             if (rc) return rc;
         }
+        ACK(a, cudaMemcpyAsync(a->dts + a->dts_cap + s, &h->sc->t, sizeof(double), cudaMemcpyDeviceToDevice,
+                               h->stream));
         ACK(a, cudaGraphLaunch(h->step_graph, h->stream));
         a->launches += h->graph_nodes;
         ACK(a, cudaMemcpyAsync(a->dts + s, &h->sc->dt, sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
@@ -1271,12 +1319,17 @@ int dense_adjoint_backward(dense_adjoint_t* a, const double* gT, double* g0, voi
         const int s0 = seg * a->k, len = std::min(a->k, a->nsteps - s0);
         rc = restart(a, a->ckpt + (size_t)seg * a->state);
         if (rc) return rc;
+        // the segment's start time (the double Mach reflection's top ghosts move with it)
+        ACK(a, cudaMemcpyAsync(&h->sc->t, a->dts + a->dts_cap + s0, sizeof(double), cudaMemcpyDeviceToDevice,
+                               h->stream));
         if (len == a->k) {
             // a full segment: its recompute (recording each stage's input state, taping the
             // sweeps) and its reverse as the segment graphs
             ACK(a, cudaGraphLaunch(a->rec_exec, h->stream));
             ACK(a, cudaMemcpyAsync(a->seg_dts, a->dts + s0, (size_t)a->k * sizeof(double), cudaMemcpyDeviceToDevice,
                                    h->stream));
+            ACK(a, cudaMemcpyAsync(a->seg_dts + a->k, a->dts + a->dts_cap + s0, (size_t)a->k * sizeof(double),
+                                   cudaMemcpyDeviceToDevice, h->stream));
             ACK(a, cudaGraphLaunch(a->rev_exec, h->stream));
             ACK(a, cudaMemcpyAsync(a->argmax + 2 * (size_t)s0, a->seg_argmax, (size_t)2 * a->k * sizeof(int),
                                    cudaMemcpyDeviceToDevice, h->stream));
@@ -1289,7 +1342,7 @@ int dense_adjoint_backward(dense_adjoint_t* a, const double* gT, double* g0, voi
         }
         for (int s = len - 1; s >= 0; --s)
             reverse_step(a, a->rec + (size_t)s * 3 * a->state, a->tape + (size_t)s * 3 * a->tape_stage,
-                         a->dts + s0 + s, a->argmax + 2 * (s0 + s));
+                         a->dts + s0 + s, a->dts + a->dts_cap + s0 + s, a->argmax + 2 * (s0 + s));
     }
     h->prim_slot = -1;
     ACK(a, cudaMemcpyAsync(g0, a->g, a->state * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
@@ -1310,7 +1363,7 @@ int dense_adjoint_rhs_vjp(dense_adjoint_t* a, const double* u, const double* v, 
     rc = taped_stage(a, 1, a->tape);
     if (rc) return rc;
     a->h->prim_slot = -1;
-    vjp(a, 0, u, a->tape, v, out, a->part, nullptr);
+    vjp(a, 0, u, a->tape, v, out, a->part, nullptr, nullptr);
     std::vector<double> part(a->npart);
     ACK(a, cudaMemcpyAsync(part.data(), a->part, a->npart * sizeof(double), cudaMemcpyDeviceToHost, a->h->stream));
     rc = finish(a, stream);

@@ -38,11 +38,13 @@ def test_torch_step_matches_oracle(dense, orc, split, recon):
 
 
 @pytest.mark.parametrize("bench,split,recon", [(1, 101, 253), (2, 102, 255), (4, 103, 253), (9, 101, 255),
-                                               (1, 103, 251), (3, 101, 253), (13, 102, 255), (13, 103, 251)])
+                                               (1, 103, 251), (3, 101, 253), (13, 102, 255), (13, 103, 251),
+                                               (5, 101, 253), (5, 102, 255), (5, 103, 253)])
 def test_torch_step_with_walls_matches_oracle(dense, orc, bench, split, recon):
-    """The ghost rules of the reference's benchmarks with walls (extrapolation, mirror, and
-    Rayleigh-Taylor's fixed states with its body force) from a rough seeded state: three steps
-    within 1e-12 of the oracle."""
+    """The ghost rules of the reference's benchmarks with walls (extrapolation, mirror,
+    Rayleigh-Taylor's fixed states with its body force, the double Mach reflection's wall,
+    moving-shock top and inflow) from a rough seeded state: three steps within 1e-12 of the
+    oracle."""
     cfg = dense.config_default(ni=24, nj=20, benchmark=bench, splitting=split, recon=recon, cfl=0.4)
     c, cons, prim, x, y = dense.init_general(cfg)
     rng = np.random.default_rng(bench * 1000 + split + recon)

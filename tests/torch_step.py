@@ -82,7 +82,12 @@ def steger_warming(rho, u, v, a, gamma, d):
 # 4/3, -1/3 extrapolation, "R" the mirror with the normal velocity negated, "F" a fixed state
 # (Rayleigh-Taylor's bottom and top, boundary_rt_general.f90:14-57). Ghost primitives come from
 # the rule applied to the interior primitives, not from the ghost conserved variables.
-RULES = {1: "PPEE", 2: "RERE", 3: "FFPP", 4: "RREE", 9: "RREE", 11: "PPPP", 13: "FFRR", 14: "PPPP"}
+# The double Mach reflection (5, boundary_doublemach_general.f90): "B" its bottom, the mirror
+# where the column's centre x >= 1/6 and the fixed post-shock state before it, "T" its top, the
+# post-shock state ahead of the moving shock x < 1/6 + (1 + 20 t)/sqrt(3) and the pre-shock
+# state behind it (t the step's start time), "F" its post-shock inflow on the left.
+RULES = {1: "PPEE", 2: "RERE", 3: "FFPP", 4: "RREE", 5: "BTFE", 9: "RREE", 11: "PPPP", 13: "FFRR",
+         14: "PPPP"}
 # the fixed states (rho, u, v, p) of the "F" sides: bottom, top
 RT_STATES = ((2.0, 0.0, 0.0, 1.0), (1.0, 0.0, 0.0, 2.5))
 # the stage-3 body-force factor 2.0/3.0 is a default-real literal (time_advance_general.f90:242)
@@ -106,12 +111,20 @@ def _pad_axis(A, axis, lo, hi, flip, fixed=None):
     sign[flip] = -1.0
     sign = sign.view(-1, 1, 1)
 
+    def as_layer(state, like):  # per-component constants, or a tensor of one ghost layer
+        if isinstance(state, torch.Tensor):
+            return state.expand_as(like)
+        return torch.tensor(state, dtype=A.dtype, device=A.device).view(-1, 1, 1).expand_as(like)
+
     def side(rule, inner, state=None):  # inner(d): the interior slice at distance d (1 = adjacent)
         if rule == "P":
             return None
-        if rule == "F":
-            g = torch.tensor(state, dtype=A.dtype, device=A.device).view(-1, 1, 1).expand_as(inner(1))
+        if rule in "FT":
+            g = as_layer(state, inner(1))
             return [g for _ in range(4)]
+        if rule == "B":  # state = (mirror mask, fixed state)
+            mask, fix = state
+            return [torch.where(mask, sign * inner(k + 1), as_layer(fix, inner(1))) for k in range(4)]
         if rule == "R":
             return [sign * inner(k + 1) for k in range(4)]
         a, b = inner(1), inner(2)
@@ -131,11 +144,32 @@ def _pad_axis(A, axis, lo, hi, flip, fixed=None):
     return torch.cat(list(reversed(low)) + [A] + high, dim=axis)
 
 
-def rhs(U, gamma, dx, dy, rec, split=101, bench=11):
-    """L(U) = -(h_{i+1/2} - h_{i-1/2})/dx - (g_{j+1/2} - g_{j-1/2})/dy."""
+def dmr_sides(U, gamma, dx, t):
+    """The double Mach reflection's side specifications for _rhs_padded: ((bottom, top) of the
+    conserved variables, (bottom, top) of the primitives, (left) of both)."""
+    ni = U.shape[2]
+    x = ((torch.arange(ni, dtype=U.dtype, device=U.device) + 1.0) - 0.5) * dx
+    post = fixed_state(gamma, 8.0, 8.25 * 3.0 ** 0.5 * 0.5, -8.25 * 0.5, 116.5)
+    pre = fixed_state(gamma, 1.4, 0.0, 0.0, 1.0)
+    wall = (x >= 1.0 / 6.0).view(1, 1, ni)
+    ahead = (x < (1.0 / 6.0 + (1.0 + 20.0 * t) / 3.0 ** 0.5)).view(1, 1, ni)
+    col = lambda st: torch.tensor(st, dtype=U.dtype, device=U.device).view(-1, 1, 1)
+    top = [torch.where(ahead, col(post[k]), col(pre[k])) for k in range(2)]
+    return ((wall, post[0]), top[0]), ((wall, post[1]), top[1]), post
+
+
+def rhs(U, gamma, dx, dy, rec, split=101, bench=11, t=0.0):
+    """L(U) = -(h_{i+1/2} - h_{i-1/2})/dx - (g_{j+1/2} - g_{j-1/2})/dy; t is the step's start
+    time (the double Mach reflection's top ghosts)."""
     if bench not in (11, 14):
-        fixed = [fixed_state(gamma, *st) for st in RT_STATES] if bench in (3, 13) else None
-        return _rhs_padded(U, gamma, dx, dy, rec, split, RULES[bench], fixed)
+        if bench in (3, 13):
+            fixed = [fixed_state(gamma, *st) for st in RT_STATES]
+            ys = ((fixed[0][0], fixed[1][0]), (fixed[0][1], fixed[1][1]))
+            return _rhs_padded(U, gamma, dx, dy, rec, split, RULES[bench], ys)
+        if bench == 5:
+            yu, yp, post = dmr_sides(U, gamma, dx, t)
+            return _rhs_padded(U, gamma, dx, dy, rec, split, RULES[bench], (yu, yp), ((post[0], None), (post[1], None)))
+        return _rhs_padded(U, gamma, dx, dy, rec, split, RULES[bench])
     rho, u, v, p, a = primitives(U, gamma)
     out = torch.zeros_like(U)
     for d, (un, h, axis) in enumerate(((u, dx, 2), (v, dy, 1))):
@@ -158,18 +192,18 @@ def rhs(U, gamma, dx, dy, rec, split=101, bench=11):
     return out
 
 
-def _rhs_padded(U, gamma, dx, dy, rec, split, rules, fixed=None):
+def _rhs_padded(U, gamma, dx, dy, rec, split, rules, ys=None, xs=None):
     """L(U) on a grid with ghost layers filled by the given rules (bottom, top, left, right);
-    fixed: the (cons, prim) states of the bottom and top "F" sides."""
+    ys, xs: the states of the y sides (bottom, top) and x sides (left, right) that need them, as
+    ((of the conserved variables), (of the primitives))."""
     rho, u, v, p, a = primitives(U, gamma)
     Pr = torch.stack([rho, u, v, p, a])
     out = torch.zeros_like(U)
     for d, (h, axis) in enumerate(((dx, 2), (dy, 1))):
         lo, hi = (rules[2], rules[3]) if d == 0 else (rules[0], rules[1])
-        fu = (fixed[0][0], fixed[1][0]) if fixed and d == 1 else None
-        fp = (fixed[0][1], fixed[1][1]) if fixed and d == 1 else None
-        Ug = _pad_axis(U, axis, lo, hi, 1 + d, fu)
-        Pg = _pad_axis(Pr, axis, lo, hi, 1 + d, fp)
+        spec = xs if d == 0 else ys
+        Ug = _pad_axis(U, axis, lo, hi, 1 + d, spec[0] if spec else None)
+        Pg = _pad_axis(Pr, axis, lo, hi, 1 + d, spec[1] if spec else None)
         r_, u_, v_, p_, a_ = Pg
         un = u_ if d == 0 else v_
         if split == 103:
@@ -197,7 +231,7 @@ def body_force(U):
     return torch.stack([zero, zero, U[0], U[2]])
 
 
-def time_step(U, gamma, dx, dy, rec, cfl, dt_const=None, split=101, bench=11, bodyforce=None):
+def time_step(U, gamma, dx, dy, rec, cfl, dt_const=None, split=101, bench=11, bodyforce=None, t=0.0):
     """One TVD-RK3 step; returns (U_next, dt). The body force (Rayleigh-Taylor, benchmarks 3
     and 13 unless bodyforce says otherwise) is added to each stage after the combine, f_s times
     the source of the stage's input with f_s = dt, dt/4 and 2/3 (single precision) dt
@@ -213,15 +247,16 @@ def time_step(U, gamma, dx, dy, rec, cfl, dt_const=None, split=101, bench=11, bo
     else:
         dt = torch.tensor(dt_const, dtype=U.dtype, device=U.device)
     src = (lambda W, f: f * dt * body_force(W)) if bodyforce else (lambda W, f: 0.0)
-    u1 = U + dt * rhs(U, gamma, dx, dy, rec, split, bench) + src(U, 1.0)
-    u2 = (3.0 / 4.0 * U + 1.0 / 4.0 * u1 + 1.0 / 4.0 * dt * rhs(u1, gamma, dx, dy, rec, split, bench)
-          + src(u1, 0.25))
-    u3 = (1.0 / 3.0 * U + 2.0 / 3.0 * u2 + 2.0 / 3.0 * dt * rhs(u2, gamma, dx, dy, rec, split, bench)
-          + src(u2, TWO_THIRDS_SINGLE))
+    L = lambda W: rhs(W, gamma, dx, dy, rec, split, bench, t)
+    u1 = U + dt * L(U) + src(U, 1.0)
+    u2 = 3.0 / 4.0 * U + 1.0 / 4.0 * u1 + 1.0 / 4.0 * dt * L(u1) + src(u1, 0.25)
+    u3 = 1.0 / 3.0 * U + 2.0 / 3.0 * u2 + 2.0 / 3.0 * dt * L(u2) + src(u2, TWO_THIRDS_SINGLE)
     return u3, dt
 
 
 def run(U, n, gamma, dx, dy, rec, cfl, dt_const=None, split=101, bench=11, bodyforce=None):
+    t = 0.0  # the steps' start times, accumulated as the solver does (general_main.f90:34)
     for _ in range(n):
-        U, _ = time_step(U, gamma, dx, dy, rec, cfl, dt_const, split, bench, bodyforce)
+        U, dt = time_step(U, gamma, dx, dy, rec, cfl, dt_const, split, bench, bodyforce, t)
+        t = t + float(dt.detach())
     return U
