@@ -1,7 +1,8 @@
 // adjoint.cu — the discrete adjoint of the plain solver's time step: LLF, GLF or Steger-Warming
-// splitting (101, 102, 103) with upwind5 / WENO-JS5 / WENO-Z5 reconstruction (251/253/255) and
-// TVD-RK3 with the CFL time step, on grids periodic in x and y (benchmarks 11 and 14) or with
-// extrapolated and mirror sides (benchmarks 1, 2, 4, 9; wall_terms).
+// splitting (101, 102, 103) with upwind5 / WENO-JS5 / WENO-Z5 reconstruction (251/253/255), or
+// the characteristic WENO-Z scheme (104, k_char_face), and TVD-RK3 with the CFL time step, on
+// grids periodic in x and y (benchmarks 11 and 14) or with extrapolated, mirror and fixed-state
+// sides (benchmarks 1, 2, 3, 4, 5, 9, 13; wall_terms).
 //
 // The forward step (time_rk3_general, time_advance_general.f90:9-267) applies per stage
 //     L(u)_c = -(h_{f+1} - h_f)/dx - (g_{f'+1} - g_{f'})/dy,     cell c between faces f, f+1,
@@ -52,10 +53,7 @@
 namespace dense {
 namespace adj {
 
-constexpr double a300 = 1.0 / 3.0, a301 = -7.0 / 6.0, a302 = 11.0 / 6.0;
-constexpr double a310 = -1.0 / 6.0, a311 = 5.0 / 6.0, a312 = 1.0 / 3.0;
-constexpr double a320 = 1.0 / 3.0, a321 = 5.0 / 6.0, a322 = -1.0 / 6.0;
-constexpr double kSS = (double)1.0e-6f;      // weno_mod.f90:37, a default-real literal
+#include "weno_fast.cuh"
 constexpr double kPFloor = (double)1.0e-6f;  // get_primary.f90:58
 constexpr double k1312 = 13.0 / 12.0;
 
@@ -63,7 +61,9 @@ struct AdjParams {
     int ni, nj;
     long long plane;  // ni * nj: one variable of a compact interior state
     long long xs, ys; // face planes: xi nj (ni+1), eta (nj+1) ni
-    int np;           // tape planes per direction (tape_planes)
+    int np;           // tape planes per direction (tape_planes; 4 for 104, the fluxes alone)
+    int gnp;          // planes per direction of what the cell kernel gathers: the tape (np), or
+                      // the characteristic scheme's face sensitivities of the split fluxes (40)
     double gamma, dx, dy, inv_dx, inv_dy, cfl;
     int rule[4];      // ghost rule of each side (bottom, top, left, right): kRulePeriodic, ...
     // Rayleigh-Taylor's body force: each stage adds f_s (0, 0, rho, rho v) of its input, f_s =
@@ -73,6 +73,12 @@ struct AdjParams {
     int bodyforce;
     double* bpart;
     int bench;        // the benchmark (its fixed ghost states: fixed_state)
+    // characteristic WENO-Z (104): k_char_face writes each face's split-flux sensitivities (the
+    // gather's "tape", read against unit face weights) and, per face, the sensitivities of the
+    // primitives (rho, u, v, p) of its left and right cells through the Roe eigenvectors:
+    // rbar[8][face plane] a direction (left cell 0..3, right cell 4..7), xi then eta
+    int charac;
+    double* rbar;
 };
 // Ghost rules of the benchmarks the adjoint covers (boundary_*_general.f90): a periodic copy,
 // the recursive 4/3, -1/3 extrapolation of the two cells next to the side, the mirror of the
@@ -457,7 +463,8 @@ __device__ __forceinline__ void gather_line(const double* __restrict__ T, const 
 // the double Mach reflection's inflow and bottom-before-the-wall post-shock state, and its top,
 // post-shock ahead of the moving shock x < 1/6 + (1 + 20 t)/sqrt(3), pre-shock behind it
 // (boundary_doublemach_general.f90:51-99). Same formulas as the boundary fill's state_from.
-__device__ __forceinline__ void fixed_state(const AdjParams& a, int dir, int side, int line, double t, double Ug[4]) {
+__device__ __forceinline__ void fixed_state(const AdjParams& a, int dir, int side, int line, double t, double Ug[4],
+                                            double* qg = nullptr) {
     double rho, u = 0.0, v = 0.0, pr;
     if (a.bench == DENSE_BENCH_DMR) {
         const double x = ((double)(line + 1) - 0.5) * a.dx;  // the column's centre (init centres)
@@ -471,6 +478,7 @@ __device__ __forceinline__ void fixed_state(const AdjParams& a, int dir, int sid
     }
     Ug[0] = rho; Ug[1] = rho * u; Ug[2] = rho * v;
     Ug[3] = pr / (a.gamma - 1.0) + 0.5 * rho * (u * u + v * v);
+    if (qg) { qg[0] = rho; qg[1] = u; qg[2] = v; qg[3] = pr; qg[4] = sqrt(a.gamma * pr / rho); }
 }
 
 template <int DIR, int SPL, int REC>
@@ -480,7 +488,7 @@ __device__ __forceinline__ void wall_terms(const AdjParams& a, const double* __r
                                            double Ub[4], double pbar[5], double& lb) {
     const int n = DIR == 0 ? a.ni : a.nj, x = DIR == 0 ? i : j;
     const long long ts = DIR == 0 ? a.xs : a.ys;
-    const double* T = DIR == 0 ? tape : tape + a.np * a.xs;
+    const double* T = DIR == 0 ? tape : tape + a.gnp * a.xs;
     const double* H = DIR == 0 ? hb : hb + 4 * a.xs;
     const long long base = DIR == 0 ? (long long)j * (a.ni + 1) : i;
     const long long stride = DIR == 0 ? 1 : a.ni;
@@ -571,6 +579,13 @@ __device__ __forceinline__ void wall_terms(const AdjParams& a, const double* __r
                 prb[4] = ab;
                 if (SPL == 1 && (rule == kRuleReflect || dist == 1)) lb += lamb;
             }
+            if (a.charac && k == 0) {
+                // the ghost next to the side is a Roe cell of the boundary face: the left cell of
+                // face 0, the right cell of face n
+                const double* RB = a.rbar + (DIR == 0 ? 0 : 8 * a.xs) + base + (long long)(side == 0 ? 0 : n) * stride;
+#pragma unroll
+                for (int v = 0; v < 4; ++v) prb[v] += RB[(side == 0 ? v : 4 + v) * ts];
+            }
             const double sn = rule == kRuleReflect ? -1.0 : 1.0;
 #pragma unroll
             for (int v = 0; v < 4; ++v) Ub[v] += (v == 1 + DIR ? sn * w : w) * Ubg[v];
@@ -578,6 +593,220 @@ __device__ __forceinline__ void wall_terms(const AdjParams& a, const double* __r
             for (int v = 0; v < 5; ++v) pbar[v] += (v == 1 + DIR ? sn * w : w) * prb[v];
         }
     }
+}
+
+// ---- characteristic WENO-Z (104): the face-level reverse ------------------------------------
+// Conserved variables (c[0..3]) and primitives (rho, u, v, p, alpha: c[4..8]) of cell x (interior
+// index along DIR, a ghost when outside 0..n-1) of line `line`, by the side rules as the forward's
+// boundary fill builds them: a periodic image, the mirror of cell k for ghost k (normal velocity
+// and momentum negated), the recursive extrapolation of the two cells next to the side (cons and
+// primitives each), or a fixed state.
+__device__ __forceinline__ void cell_state(const AdjParams& a, const double* __restrict__ u, long long o,
+                                           double c[9]) {
+#pragma unroll
+    for (int v = 0; v < 4; ++v) c[v] = u[v * a.plane + o];
+    const Prim q = prim_of(c, a.gamma);
+    c[4] = c[0]; c[5] = q.u; c[6] = q.v; c[7] = q.p; c[8] = q.a;
+}
+template <int DIR>
+__device__ __forceinline__ void fetch_cell(const AdjParams& a, const double* __restrict__ u, int line, int x,
+                                           double t, double c[9]) {
+    const int n = DIR == 0 ? a.ni : a.nj;
+    auto off = [&](int xx) { return DIR == 0 ? (long long)line * a.ni + xx : (long long)xx * a.ni + line; };
+    if (x >= 0 && x < n) { cell_state(a, u, off(x), c); return; }
+    const int side = x < 0 ? 0 : 1, k = x < 0 ? -1 - x : x - n;  // ghost layer k (0: next to the side)
+    int rule = a.rule[DIR == 0 ? 2 + side : side];
+    if (rule == kRuleDMRBottom) rule = ((double)(line + 1) - 0.5) * a.dx >= 1.0 / 6.0 ? kRuleReflect : kRuleFixed;
+    if (rule == kRulePeriodic) {
+        cell_state(a, u, off(side == 0 ? x + n : x - n), c);
+    } else if (rule == kRuleReflect) {
+        cell_state(a, u, off(side == 0 ? k : n - 1 - k), c);
+        c[1 + DIR] = -c[1 + DIR];
+        c[5 + DIR] = -c[5 + DIR];
+    } else if (rule == kRuleExtrap) {
+        double c1[9], c2[9];
+        cell_state(a, u, off(side == 0 ? 0 : n - 1), c1);
+        cell_state(a, u, off(side == 0 ? 1 : n - 2), c2);
+#pragma unroll
+        for (int v = 0; v < 9; ++v) {
+            double na = c1[v], fa = c2[v], gv = 0.0;
+            for (int l = 0; l <= k; ++l) {
+                gv = fma(na, 4.0 / 3.0, -(fa * (1.0 / 3.0)));
+                fa = na;
+                na = gv;
+            }
+            c[v] = gv;
+        }
+    } else {  // a fixed state at the step's start time t
+        fixed_state(a, DIR, side, line, t, c, c + 4);
+    }
+}
+
+// Per face of direction DIR (one thread): the characteristic reconstruction recomputed from the
+// stage input u -- the GLF split fluxes of the six stencil cells (the stage's global lambda),
+// the Roe average of the face's two cells and its eigenvectors (roe_eig_fast's formulas), per sign
+// the five split fluxes projected on the characteristic fields and WENO-Z per field with its
+// stencil gradient (weno_grad) -- and its reverse for the face's hbar: the back-projection's
+// transpose gives each field's value sensitivity, times the field's stencil gradient the
+// sensitivities of the projected values, the transposed projection those of the split fluxes,
+// written per (sign, stencil point, component) as the cell kernel's gather reads them (against
+// unit face weights); and the eigenvectors' sensitivities -- from the projections (sum over the
+// stencil of the projected-value sensitivities times the split fluxes) and the back-projection --
+// sent through the eigenvectors' formulas and the Roe average to the primitives (rho, u, v, p)
+// of the face's two cells (rbar).
+template <int DIR>
+__global__ void __launch_bounds__(128) k_char_face(AdjParams a, const double* __restrict__ u,
+                                                  const double* __restrict__ hb, const double* __restrict__ lamv,
+                                                  const double* __restrict__ tp, double* __restrict__ fbar) {
+    const int ni = a.ni, nj = a.nj;
+    // x runs along the face array's rows: the faces of a line (xi), the lines (eta)
+    const int tx = blockIdx.x * blockDim.x + threadIdx.x, ty = blockIdx.y * blockDim.y + threadIdx.y;
+    const int f = DIR == 0 ? tx : ty, line = DIR == 0 ? ty : tx;
+    const int n = DIR == 0 ? ni : nj, nline = DIR == 0 ? nj : ni;
+    if (line >= nline || f > n) return;
+    const double t = tp ? *tp : 0.0;
+    const long long ts = DIR == 0 ? a.xs : a.ys;
+    const long long to = DIR == 0 ? (long long)line * (ni + 1) + f : (long long)f * ni + line;
+    const double g1 = a.gamma - 1.0, kg = a.gamma / g1;
+    // the stencil cells f-3 .. f+2 and their GLF split fluxes
+    double c[6][9];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) fetch_cell<DIR>(a, u, line, f - 3 + q, t, c[q]);
+    const double lam = lamv[DIR];
+    double Fp[6][4], Fm[6][4];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+        const double un = c[q][5 + DIR], pr = c[q][7];
+        const double P[4] = {0.0, DIR == 0 ? pr : 0.0, DIR == 1 ? pr : 0.0, un * pr};
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            Fp[q][v] = 0.5 * fma(un + lam, c[q][v], P[v]);
+            Fm[q][v] = 0.5 * fma(un - lam, c[q][v], P[v]);
+        }
+    }
+    // Roe average of cells 2 (left) and 3 (right) and the eigenvector entries
+    const double rl = c[2][4], rr = c[3][4];
+    const double ul = c[2][5], ur = c[3][5], vl = c[2][6], vr = c[3][6], pl = c[2][7], pr = c[3][7];
+    const double sl = sqrt(rl), sr = sqrt(rr);
+    const double hl = kg * pl / rl + 0.5 * (ul * ul + vl * vl), hr = kg * pr / rr + 0.5 * (ur * ur + vr * vr);
+    const double r = 1.0 / (sl + sr);
+    const double u0 = (sr * ur + sl * ul) * r, v0 = (sr * vr + sl * vl) * r, h0 = (sr * hr + sl * hl) * r;
+    const double uu0 = 0.5 * (u0 * u0 + v0 * v0);
+    const double c2 = g1 * (h0 - uu0);
+    const double ia = 1.0 / sqrt(c2), a0 = c2 * ia, ihh = g1 * ia * ia;
+    const double un0 = DIR == 0 ? u0 : v0, ut0 = DIR == 0 ? v0 : u0, a0un0 = a0 * un0;
+    const double hu = 0.5 * uu0 * ihh, nu = 0.5 * un0 * ia, ia5 = 0.5 * ia;
+    const double pn = 0.5 * un0 * ihh, pt = 0.5 * ut0 * ihh, ih = 0.5 * ihh;
+    const double ln0 = -pn - ia5, ln3 = -pn + ia5;
+    // M[cc][k]: the coefficient of split-flux component cc in characteristic field k
+    double M[4][4];
+    M[0][0] = hu + nu; M[3][0] = ih;
+    M[0][3] = hu - nu; M[3][3] = ih;
+    if (DIR == 0) { M[1][0] = ln0; M[2][0] = -pt; M[1][3] = ln3; M[2][3] = -pt; }
+    else          { M[1][0] = -pt; M[2][0] = ln0; M[1][3] = -pt; M[2][3] = ln3; }
+    M[0][1] = 1.0 - uu0 * ihh; M[1][1] = u0 * ihh; M[2][1] = v0 * ihh; M[3][1] = -ihh;
+    M[0][2] = -ut0; M[1][2] = DIR == 1 ? 1.0 : 0.0; M[2][2] = DIR == 0 ? 1.0 : 0.0; M[3][2] = 0.0;
+    double HB[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) HB[v] = hb[(DIR == 0 ? 0 : 4 * a.xs) + v * ts + to];
+    const double hn = HB[1 + DIR], ht = HB[2 - DIR];
+    // sensitivities of the eigen quantities, summed over both signs
+    double un0b = 0, ut0b = 0, a0b = 0, h0b = 0, uu0b = 0, a0un0b = 0;
+    double A[4][4] = {};  // A[k][cc]: sensitivity of M[cc][k]
+    double* const FB = fbar + (DIR == 0 ? 0 : a.gnp * a.xs) + to;
+#pragma unroll
+    for (int sg = 0; sg < 2; ++sg) {
+        double F[5][4];
+#pragma unroll
+        for (int m = 0; m < 5; ++m)
+#pragma unroll
+            for (int v = 0; v < 4; ++v) F[m][v] = sg == 0 ? Fp[m][v] : Fm[5 - m][v];
+        double cv[4], G[4][5];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            double lf[5];
+#pragma unroll
+            for (int m = 0; m < 5; ++m)
+                lf[m] = fma(M[0][k], F[m][0], fma(M[1][k], F[m][1], fma(M[2][k], F[m][2], M[3][k] * F[m][3])));
+            double gd[4], d0, d1, d2;
+            first_differences(lf, gd);
+            betas_g(gd, d0, d1, d2);
+            const double B[3] = {fma(-3.0, gd[1], gd[0]), gd[1] + gd[2], fma(3.0, gd[2], -gd[3])};
+            WenoTerms t;
+            weno_terms<true>(gd, d0, d1, d2, t);
+            const double iN = rcp_nr(t.N), num = weno_num(t);
+            cv[k] = fma(num, iN, lf[2]);
+            weno_grad<true>(gd, B, d0, d1, d2, t, num * iN, iN, G[k]);
+        }
+        // the back-projection and its transpose
+        const double s = cv[0] + cv[1] + cv[3], d = cv[3] - cv[0];
+        const double sb = HB[0] + un0 * hn + ut0 * ht, db = a0 * hn + a0un0 * HB[3];
+        const double cb[4] = {sb - db + h0 * HB[3], sb + uu0 * HB[3], ht + ut0 * HB[3], sb + db + h0 * HB[3]};
+        un0b += s * hn;
+        a0b += d * hn;
+        ut0b += s * ht + cv[2] * HB[3];
+        h0b += (cv[0] + cv[3]) * HB[3];
+        a0un0b += d * HB[3];
+        uu0b += cv[1] * HB[3];
+        // the fields' projected-value sensitivities, the split fluxes', the eigenvectors'
+#pragma unroll
+        for (int m = 0; m < 5; ++m) {
+            double lb[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) lb[k] = cb[k] * G[k][m];
+#pragma unroll
+            for (int cc = 0; cc < 4; ++cc) {
+                FB[(long long)((sg * 5 + m) * 4 + cc) * ts] =
+                    fma(M[cc][0], lb[0], fma(M[cc][1], lb[1], fma(M[cc][2], lb[2], M[cc][3] * lb[3])));
+#pragma unroll
+                for (int k = 0; k < 4; ++k) A[k][cc] = fma(lb[k], F[m][cc], A[k][cc]);
+            }
+        }
+    }
+    // the eigenvector entries' sensitivities back to the Roe quantities
+    const double l00b = A[0][0], l03b = A[3][0];
+    const double l10b = A[0][1], l13b = A[3][1], l20b = A[0][2], l23b = A[3][2];
+    const double l30b = A[0][3] + A[3][3];
+    const double l01b = A[1][0], l11b = A[1][1], l21b = A[1][2], l31b = A[1][3];
+    ut0b -= A[2][0];
+    const double hub = l00b + l03b, nub = l00b - l03b;
+    const double nrm0 = DIR == 0 ? l10b : l20b, nrm3 = DIR == 0 ? l13b : l23b;  // the ln0, ln3 entries
+    const double tg0 = DIR == 0 ? l20b : l10b, tg3 = DIR == 0 ? l23b : l13b;    // the -pt entries
+    const double pnb = -nrm0 - nrm3, ia5b = -nrm0 + nrm3, ptb = -tg0 - tg3, ihb = l30b;
+    double ihhb = 0.0, iab = 0.0, u0b = 0.0, v0b = 0.0;
+    uu0b += -ihh * l01b + 0.5 * ihh * hub;
+    ihhb += -uu0 * l01b + u0 * l11b + v0 * l21b - l31b + 0.5 * uu0 * hub + 0.5 * un0 * pnb + 0.5 * ut0 * ptb +
+            0.5 * ihb;
+    u0b += ihh * l11b;
+    v0b += ihh * l21b;
+    un0b += 0.5 * ia * nub + 0.5 * ihh * pnb + a0 * a0un0b;
+    ut0b += 0.5 * ihh * ptb;
+    iab += 0.5 * un0 * nub + 0.5 * ia5b;
+    a0b += un0 * a0un0b;
+    if (DIR == 0) { u0b += un0b; v0b += ut0b; }
+    else          { v0b += un0b; u0b += ut0b; }
+    iab += 2.0 * g1 * ia * ihhb;  // ihh = g1 ia^2
+    double c2b = ia * a0b;        // a0 = c2 ia
+    iab += c2 * a0b;
+    c2b += -0.5 * ia * ia * ia * iab;  // ia = c2^-1/2
+    h0b += g1 * c2b;
+    uu0b += -g1 * c2b;
+    u0b += u0 * uu0b;
+    v0b += v0 * uu0b;
+    // the Roe average's inputs, then the two cells' primitives
+    const double slb = r * ((ul - u0) * u0b + (vl - v0) * v0b + (hl - h0) * h0b);
+    const double srb = r * ((ur - u0) * u0b + (vr - v0) * v0b + (hr - h0) * h0b);
+    const double ulb = sl * r * u0b, urb = sr * r * u0b, vlb = sl * r * v0b, vrb = sr * r * v0b;
+    const double hlb = sl * r * h0b, hrb = sr * r * h0b;
+    double* const RB = a.rbar + (DIR == 0 ? 0 : 8 * a.xs) + to;
+    RB[0 * ts] = 0.5 / sl * slb - kg * pl / (rl * rl) * hlb;
+    RB[1 * ts] = ulb + ul * hlb;
+    RB[2 * ts] = vlb + vl * hlb;
+    RB[3 * ts] = kg / rl * hlb;
+    RB[4 * ts] = 0.5 / sr * srb - kg * pr / (rr * rr) * hrb;
+    RB[5 * ts] = urb + ur * hrb;
+    RB[6 * ts] = vrb + vr * hrb;
+    RB[7 * ts] = kg / rr * hrb;
 }
 
 // Cell kernel: Ub = (dL/du)^T w at the cell from the stage's tape and hbar, then the reverse of
@@ -613,9 +842,33 @@ __global__ void __launch_bounds__(128) k_rev(AdjParams a, const double* __restri
         // LF splittings pull each direction back before gathering the next (fewer live
         // registers); Steger-Warming seeds each variable once for both directions
         if (SPL != 2) lbx = llf_vjp<0, GLF>(U, q, a.gamma, gpx, gmx, GLF ? lamv[0] : 0.0, Ub);
-        gather_line<REC>(tape + a.np * a.xs, hb + 4 * a.xs, a.ys, i, ni, j, nj, py, gpy, gmy);
+        gather_line<REC>(tape + a.gnp * a.xs, hb + 4 * a.xs, a.ys, i, ni, j, nj, py, gpy, gmy);
         if (SPL != 2) lby = llf_vjp<1, GLF>(U, q, a.gamma, gpy, gmy, GLF ? lamv[1] : 0.0, Ub);
         else          sw_vjp(U, a.gamma, gpx, gmx, gpy, gmy, Ub);
+        if (a.charac) {
+            // the Roe averages of the faces this cell is a side of: the left cell of face x+1 and
+            // the right cell of face x in each direction (and, on periodic lines, the right cell
+            // of face n from cell 0 and the left cell of face 0 from cell n-1, their images)
+            double rb[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+            for (int D = 0; D < 2; ++D) {
+                const int n = D == 0 ? ni : nj, x = D == 0 ? i : j;
+                const long long ts = D == 0 ? a.xs : a.ys;
+                const double* RB = a.rbar + (D == 0 ? 0 : 8 * a.xs);
+                auto face = [&](int f) { return D == 0 ? (long long)j * (ni + 1) + f : (long long)f * ni + i; };
+                auto add = [&](int f, int q0) {
+#pragma unroll
+                    for (int v = 0; v < 4; ++v) rb[v] += RB[(q0 + v) * ts + face(f)];
+                };
+                add(x + 1, 0);
+                add(x, 4);
+                if (D == 0 ? px : py) {
+                    if (x == n - 1) add(0, 0);
+                    if (x == 0) add(n, 4);
+                }
+            }
+            prim_pullback_all(U, q, a.gamma, rb[0], rb[1], rb[2], rb[3], 0.0, Ub);
+        }
         if (WALLS && (!px || !py)) {  // the ghost cells of wall sides that this cell feeds
             // (a separate instantiation: the periodic kernels keep their registers)
             double pbar[5] = {0, 0, 0, 0, 0};
@@ -856,7 +1109,10 @@ struct dense_adjoint {
     // GLF: the stage's (lambda_x, lambda_y, their cells), block maxima, block sums of lambda's
     // sensitivity
     double *lamv = nullptr, *lmp = nullptr, *lpart = nullptr;
-    dim3 gh, gc;
+    // characteristic WENO-Z (104): the faces' split-flux sensitivities (40 planes a direction)
+    // the cell kernel gathers against unit face weights (ones, 4 planes a direction)
+    double *fbar = nullptr, *ones = nullptr;
+    dim3 gh, gc, gfx, gfy;
     int nsteps = -1;                              // steps of the last forward
     cudaEvent_t ev_in = nullptr, ev_out = nullptr;
     long long launches = 0;
@@ -981,11 +1237,12 @@ void launch_rev_w(dense_adjoint* a, int stage, const double* u, const double* ta
     const dim3 bc(kCX, kCY);
     double* const lv = a->lamv;
     double* const lp = a->lpart;
+    const double* hb = a->ap.charac ? a->ones : a->hb;
     if (stage == 0)
-        k_rev<REC, SPL, WALLS><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, a->hb, nullptr, out, nullptr, tp, nullptr,
+        k_rev<REC, SPL, WALLS><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, hb, nullptr, out, nullptr, tp, nullptr,
                                                     lv, lp, 0);
     else
-        k_rev<REC, SPL, WALLS><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, a->hb, a->acc, out, dtp, tp,
+        k_rev<REC, SPL, WALLS><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, hb, a->acc, out, dtp, tp,
                                                     stage == 1 ? a->mpart : nullptr, lv, lp, stage);
 }
 template <int REC, int SPL>
@@ -1007,20 +1264,27 @@ void launch_rev_recon(dense_adjoint* a, int stage, const double* u, const double
 }
 
 // the reverse of one stage: hbar of w on every face (and w . L(u) per block into part), then
-// the cells; GLF first finds the stage's global lambda and its cells, and last sends lambda's
-// sensitivity to those cells
+// the cells; GLF (and the characteristic scheme, which splits by GLF) first finds the stage's
+// global lambda and its cells, and last sends lambda's sensitivity to those cells; the
+// characteristic scheme takes each face's reverse (k_char_face) before the cells gather it
 void vjp(dense_adjoint* a, int stage, const double* u, const double* tape, const double* w, double* out,
          double* part, const double* dtp, const double* tp) {
     using namespace dense::adj;
     cudaStream_t s = a->h->stream;
-    const bool glf = a->cfg.splitting == DENSE_SPLIT_GLF;
+    const bool charac = a->ap.charac != 0;
+    const bool glf = a->cfg.splitting == DENSE_SPLIT_GLF || charac;
     if (glf) {
         k_maxarg<<<a->gc, dim3(kCX, kCY), 0, s>>>(a->ap, u, a->lmp);
         k_maxred<<<1, 256, 0, s>>>(a->lmp, a->nm, a->lamv);
         a->launches += 2;
     }
     k_hbar<<<a->gh, dim3(kHX, kHY), 0, s>>>(a->ap, w, tape, a->hb, part);
-    if (glf) launch_rev_recon<1>(a, stage, u, tape, w, out, dtp, tp, s);
+    if (charac) {
+        k_char_face<0><<<a->gfx, dim3(kCX, kCY), 0, s>>>(a->ap, u, a->hb, a->lamv, tp, a->fbar);
+        k_char_face<1><<<a->gfy, dim3(kCX, kCY), 0, s>>>(a->ap, u, a->hb, a->lamv, tp, a->fbar);
+        a->launches += 2;
+        launch_rev<DENSE_RECON_WENOZ5, 1>(a, stage, u, a->fbar, w, out, dtp, tp, s);
+    } else if (glf) launch_rev_recon<1>(a, stage, u, tape, w, out, dtp, tp, s);
     else if (a->cfg.splitting == DENSE_SPLIT_SW) launch_rev_recon<2>(a, stage, u, tape, w, out, dtp, tp, s);
     else launch_rev_recon<0>(a, stage, u, tape, w, out, dtp, tp, s);
     a->launches += 2;
@@ -1154,7 +1418,7 @@ void dense_adjoint_destroy(dense_adjoint_t* a) {
     if (!a) return;
     if (a->h) cudaStreamSynchronize(a->h->stream);
     double* bufs[] = {a->ckpt, a->dts, a->rec, a->tape, a->g, a->g1, a->g2, a->acc, a->hb, a->part, a->mpart,
-                      a->lamv, a->lmp, a->lpart, a->seg_dts, a->ap.bpart};
+                      a->lamv, a->lmp, a->lpart, a->seg_dts, a->ap.bpart, a->fbar, a->ones, a->ap.rbar};
     for (double* b : bufs) if (b) cudaFree(b);
     if (a->argmax) cudaFree(a->argmax);
     if (a->seg_argmax) cudaFree(a->seg_argmax);
@@ -1169,9 +1433,15 @@ void dense_adjoint_destroy(dense_adjoint_t* a) {
 int dense_adjoint_create(const dense_config_t* cfg, int checkpoint_every, dense_adjoint_t** out) {
     if (!out || !cfg) return aerr(nullptr, DENSE_ERR_ARG, "null argument");
     *out = nullptr;
-    if (cfg->splitting != DENSE_SPLIT_LLF && cfg->splitting != DENSE_SPLIT_GLF && cfg->splitting != DENSE_SPLIT_SW)
-        return aerr(nullptr, DENSE_ERR_ARG, "the adjoint covers the LLF, GLF and Steger-Warming splittings (101-103)");
-    if (cfg->recon != DENSE_RECON_UPWIND5 && cfg->recon != DENSE_RECON_WENOJS5 && cfg->recon != DENSE_RECON_WENOZ5)
+    const bool charac = cfg->splitting == DENSE_SPLIT_CH;
+    if (cfg->splitting != DENSE_SPLIT_LLF && cfg->splitting != DENSE_SPLIT_GLF && cfg->splitting != DENSE_SPLIT_SW &&
+        !charac)
+        return aerr(nullptr, DENSE_ERR_ARG,
+                    "the adjoint covers the LLF, GLF and Steger-Warming splittings (101-103) and the characteristic "
+                    "WENO-Z (104); not the adaptive scheme (105)");
+    // the characteristic scheme reconstructs by its own WENO-Z; the recon field is not read
+    if (!charac && cfg->recon != DENSE_RECON_UPWIND5 && cfg->recon != DENSE_RECON_WENOJS5 &&
+        cfg->recon != DENSE_RECON_WENOZ5)
         return aerr(nullptr, DENSE_ERR_ARG, "the adjoint covers reconstructions 251, 253 and 255");
     // ghost rules (bottom, top, left, right) of the benchmarks covered: periodic, the
     // extrapolation, the mirror and fixed states (boundary_ivc/sedov/rm/shockvortex/rt_general.f90)
@@ -1231,7 +1501,9 @@ int dense_adjoint_create(const dense_config_t* cfg, int checkpoint_every, dense_
     p.ni = cfg->ni; p.nj = cfg->nj; p.plane = (long long)cfg->ni * cfg->nj;
     p.xs = (long long)cfg->nj * (cfg->ni + 1);
     p.ys = (long long)(cfg->nj + 1) * cfg->ni;
-    p.np = dense::tape_planes(cfg->recon);
+    p.np = charac ? 4 : dense::tape_planes(cfg->recon);
+    p.gnp = charac ? 40 : p.np;
+    p.charac = charac ? 1 : 0;
     p.gamma = cfg->gamma; p.dx = cfg->dx; p.dy = cfg->dy; p.inv_dx = 1.0 / cfg->dx; p.inv_dy = 1.0 / cfg->dy;
     p.cfl = cfg->cfl;
     for (int k = 0; k < 4; ++k) p.rule[k] = rules[k];
@@ -1242,6 +1514,8 @@ int dense_adjoint_create(const dense_config_t* cfg, int checkpoint_every, dense_
     a->tape_stage = (size_t)p.np * (size_t)(p.xs + p.ys);
     a->gh = dim3((cfg->ni + 1 + kHX - 1) / kHX, (cfg->nj + 1 + kHY - 1) / kHY, 2);
     a->gc = dim3((cfg->ni + kCX - 1) / kCX, (cfg->nj + kCY - 1) / kCY);
+    a->gfx = dim3((cfg->ni + 1 + kCX - 1) / kCX, (cfg->nj + kCY - 1) / kCY);  // xi faces (f, line)
+    a->gfy = dim3((cfg->ni + kCX - 1) / kCX, (cfg->nj + 1 + kCY - 1) / kCY);  // eta faces (line, f)
     a->npart = (int)(a->gh.x * a->gh.y * a->gh.z);
     a->nm = (int)(a->gc.x * a->gc.y);
     struct B { double** p; size_t n; } bufs[] = {
@@ -1254,6 +1528,19 @@ int dense_adjoint_create(const dense_config_t* cfg, int checkpoint_every, dense_
     for (auto& b : bufs) {
         cudaError_t e = cudaMalloc((void**)b.p, b.n * sizeof(double));
         if (e != cudaSuccess) { a->err = std::string("cudaMalloc: ") + cudaGetErrorString(e); return fail(DENSE_ERR_NOMEM); }
+    }
+    if (charac) {
+        const size_t fp = (size_t)(p.xs + p.ys);
+        struct B2 { double** p; size_t n; } cb[] = {{&a->fbar, 40 * fp}, {&p.rbar, 8 * fp}, {&a->ones, 4 * fp}};
+        for (auto& b : cb) {
+            cudaError_t e = cudaMalloc((void**)b.p, b.n * sizeof(double));
+            if (e != cudaSuccess) { a->err = std::string("cudaMalloc: ") + cudaGetErrorString(e); return fail(DENSE_ERR_NOMEM); }
+        }
+        const std::vector<double> one(4 * fp, 1.0);
+        if (cudaMemcpy(a->ones, one.data(), one.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
+            a->err = "cudaMemcpy of the unit face weights failed";
+            return fail(DENSE_ERR_CUDA);
+        }
     }
     if (cudaMalloc((void**)&a->seg_argmax, (size_t)2 * a->k * sizeof(int)) != cudaSuccess) {
         a->err = "cudaMalloc of the segment's maxima cells failed";

@@ -67,7 +67,8 @@ struct Params {
     // of the next stage's boundary fill (set by periodic_ghosts() below)
     int periodic_ghosts;
     int count_branches;  // accumulate Scalars::branch_count in the AdaWENO sweeps
-    // Tape of the component-wise LLF/GLF/SW sweeps for the discrete adjoint (flux_tape launches only):
+    // Tape of the sweeps for the discrete adjoint (flux_tape launches only; for the characteristic
+    // sweeps (104) only the fluxes, 4 planes a direction). The component-wise LLF/GLF/SW sweeps':
     // per direction tape_planes(recon) planes of the direction's face array (xi [nj][ni+1], eta
     // [nj+1][ni], eta after xi): the reconstructions' stencil gradients g[(s*5 + m)*4 + v] (s = 0
     // for F+, 1 for F-; none for upwind5, whose gradient is constant), then the fluxes h[v].

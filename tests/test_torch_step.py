@@ -39,7 +39,9 @@ def test_torch_step_matches_oracle(dense, orc, split, recon):
 
 @pytest.mark.parametrize("bench,split,recon", [(1, 101, 253), (2, 102, 255), (4, 103, 253), (9, 101, 255),
                                                (1, 103, 251), (3, 101, 253), (13, 102, 255), (13, 103, 251),
-                                               (5, 101, 253), (5, 102, 255), (5, 103, 253)])
+                                               (5, 101, 253), (5, 102, 255), (5, 103, 253), (11, 104, 0),
+                                               (3, 104, 0), (13, 104, 0), (4, 104, 0), (1, 104, 0),
+                                               (2, 104, 0), (5, 104, 0), (9, 104, 0)])
 def test_torch_step_with_walls_matches_oracle(dense, orc, bench, split, recon):
     """The ghost rules of the reference's benchmarks with walls (extrapolation, mirror,
     Rayleigh-Taylor's fixed states with its body force, the double Mach reflection's wall,

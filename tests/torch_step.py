@@ -161,7 +161,7 @@ def dmr_sides(U, gamma, dx, t):
 def rhs(U, gamma, dx, dy, rec, split=101, bench=11, t=0.0):
     """L(U) = -(h_{i+1/2} - h_{i-1/2})/dx - (g_{j+1/2} - g_{j-1/2})/dy; t is the step's start
     time (the double Mach reflection's top ghosts)."""
-    if bench not in (11, 14):
+    if bench not in (11, 14) or split == 104:
         if bench in (3, 13):
             fixed = [fixed_state(gamma, *st) for st in RT_STATES]
             ys = ((fixed[0][0], fixed[1][0]), (fixed[0][1], fixed[1][1]))
@@ -192,6 +192,67 @@ def rhs(U, gamma, dx, dy, rec, split=101, bench=11, t=0.0):
     return out
 
 
+def roe_eigen(gamma, rl, rr, ul, ur, vl, vr, pl, pr, d):
+    """Left and right eigenvectors of the Roe average of two cells (scheme_weno5th_CH.f90:44-62,
+    get_l_r_vec_xi/_eta of scheme_weno5th_SC.f90:277-328, 607-658): L[c][k] = l(c+1, k+1) (column
+    k the k-th left eigenvector), R[k][e] = r(k+1, e+1) (row k the k-th right eigenvector), as
+    nested lists of tensors."""
+    hl = pl / (gamma - 1.0) / rl + 0.5 * (ul * ul + vl * vl) + pl / rl
+    hr = pr / (gamma - 1.0) / rr + 0.5 * (ur * ur + vr * vr) + pr / rr
+    sr, sl = torch.sqrt(rr), torch.sqrt(rl)
+    den = sr + sl
+    u0 = (sr * ur + sl * ul) / den
+    v0 = (sr * vr + sl * vl) / den
+    h0 = (sr * hr + sl * hl) / den
+    c2 = (gamma - 1.0) * (h0 - 0.5 * (u0 * u0 + v0 * v0))
+    a0 = torch.sqrt(c2)
+    uu0 = 0.5 * (u0 * u0 + v0 * v0)
+    hh0 = a0 * a0 / (gamma - 1.0)
+    one, zero = torch.ones_like(u0), torch.zeros_like(u0)
+    un = u0 if d == 0 else v0
+    if d == 0:
+        R = [[one, u0 - a0, v0, h0 - a0 * u0], [one, u0, v0, uu0], [zero, zero, one, v0],
+             [one, u0 + a0, v0, h0 + a0 * u0]]
+    else:
+        R = [[one, u0, v0 - a0, h0 - a0 * v0], [one, u0, v0, uu0], [zero, one, zero, u0],
+             [one, u0, v0 + a0, h0 + a0 * v0]]
+    hu, nu, ia = 0.5 * uu0 / hh0, 0.5 * un / a0, 0.5 / a0
+    pu, pv, ih = 0.5 * u0 / hh0, 0.5 * v0 / hh0, 0.5 / hh0
+    L = [[None] * 4 for _ in range(4)]
+    if d == 0:
+        L[0][0], L[1][0], L[2][0], L[3][0] = hu + nu, -pu - ia, -pv, ih
+        L[0][3], L[1][3], L[2][3], L[3][3] = hu - nu, -pu + ia, -pv, ih
+        L[0][2], L[1][2], L[2][2], L[3][2] = -v0, zero, one, zero
+    else:
+        L[0][0], L[1][0], L[2][0], L[3][0] = hu + nu, -pu, -pv - ia, ih
+        L[0][3], L[1][3], L[2][3], L[3][3] = hu - nu, -pu, -pv + ia, ih
+        L[0][2], L[1][2], L[2][2], L[3][2] = -u0, one, zero, zero
+    L[0][1], L[1][1], L[2][1], L[3][1] = -uu0 / hh0 + 1.0, u0 / hh0, v0 / hh0, -1.0 / hh0
+    return L, R
+
+
+def _char_faces(Fp, Fm, Pg, gamma, axis, n, d):
+    """h at the faces 0..n of the characteristic WENO-Z scheme (104, flux_splitting_CH.f90:24-110,
+    scheme_weno5th_CH.f90): per face the Roe eigenvectors of its two cells (padded 3 + f and
+    4 + f), each sign's five split fluxes projected on them, WENO-Z per characteristic field, and
+    the back-projection."""
+    sl = lambda F, k: F.narrow(axis, k, n + 1)
+    sp = lambda F, k: F.narrow(axis - 1, k, n + 1)  # one primitive's plane
+    r_, u_, v_, p_, _ = Pg
+    L, R = roe_eigen(gamma, sp(r_, 3), sp(r_, 4), sp(u_, 3), sp(u_, 4), sp(v_, 3), sp(v_, 4),
+                     sp(p_, 3), sp(p_, 4), d)
+    h = 0.0
+    for F, ks in ((Fp, (1, 2, 3, 4, 5)), (Fm, (6, 5, 4, 3, 2))):
+        st = [sl(F, k) for k in ks]  # (4, ...) each
+        cv = []
+        for k in range(4):
+            lf = [L[0][k] * f[0] + L[1][k] * f[1] + L[2][k] * f[2] + L[3][k] * f[3] for f in st]
+            cv.append(_recon(lf, 255))
+        h = h + torch.stack([R[0][q] * cv[0] + R[1][q] * cv[1] + R[2][q] * cv[2] + R[3][q] * cv[3]
+                             for q in range(4)])
+    return h
+
+
 def _rhs_padded(U, gamma, dx, dy, rec, split, rules, ys=None, xs=None):
     """L(U) on a grid with ghost layers filled by the given rules (bottom, top, left, right);
     ys, xs: the states of the y sides (bottom, top) and x sides (left, right) that need them, as
@@ -206,6 +267,16 @@ def _rhs_padded(U, gamma, dx, dy, rec, split, rules, ys=None, xs=None):
         Pg = _pad_axis(Pr, axis, lo, hi, 1 + d, spec[1] if spec else None)
         r_, u_, v_, p_, a_ = Pg
         un = u_ if d == 0 else v_
+        if split == 104:  # GLF split, then the characteristic reconstruction
+            lam = ((u if d == 0 else v).abs() + a).max()
+            zero = torch.zeros_like(p_)
+            P = torch.stack([zero, p_ if d == 0 else zero, p_ if d == 1 else zero, un * p_])
+            Fp = 0.5 * ((un + lam) * Ug + P)
+            Fm = 0.5 * ((un - lam) * Ug + P)
+            n = U.shape[axis]
+            hf = _char_faces(Fp, Fm, Pg, gamma, axis, n, d)
+            out = out - (hf.narrow(axis, 1, n) - hf.narrow(axis, 0, n)) / h
+            continue
         if split == 103:
             Fp, Fm = steger_warming(r_, u_, v_, a_, gamma, d)
         else:
