@@ -55,7 +55,6 @@ namespace adj {
 
 #include "weno_fast.cuh"
 constexpr double kPFloor = (double)1.0e-6f;  // get_primary.f90:58
-constexpr double k1312 = 13.0 / 12.0;
 
 struct AdjParams {
     int ni, nj;
@@ -642,133 +641,166 @@ __device__ __forceinline__ void fetch_cell(const AdjParams& a, const double* __r
     }
 }
 
-// Per face of direction DIR (one thread): the characteristic reconstruction recomputed from the
-// stage input u -- the GLF split fluxes of the six stencil cells (the stage's global lambda),
-// the Roe average of the face's two cells and its eigenvectors (roe_eig_fast's formulas), per sign
-// the five split fluxes projected on the characteristic fields and WENO-Z per field with its
-// stencil gradient (weno_grad) -- and its reverse for the face's hbar: the back-projection's
-// transpose gives each field's value sensitivity, times the field's stencil gradient the
-// sensitivities of the projected values, the transposed projection those of the split fluxes,
-// written per (sign, stencil point, component) as the cell kernel's gather reads them (against
-// unit face weights); and the eigenvectors' sensitivities -- from the projections (sum over the
-// stencil of the projected-value sensitivities times the split fluxes) and the back-projection --
-// sent through the eigenvectors' formulas and the Roe average to the primitives (rho, u, v, p)
-// of the face's two cells (rbar).
+// Per face of direction DIR, two threads (adjacent lanes, one per sign): the characteristic
+// reconstruction recomputed from the stage input u -- the GLF split fluxes of the stencil cells
+// (the stage's global lambda), the Roe average of the face's two cells and its eigenvectors
+// (roe_eig_fast's formulas), the sign's five split fluxes projected on the characteristic
+// fields and WENO-Z per field with its stencil gradient (weno_grad) -- and its reverse for the
+// face's hbar: the back-projection's transpose gives each field's value sensitivity, times the
+// field's stencil gradient the sensitivities of the projected values, the transposed
+// projection those of the split fluxes, written per (sign, stencil point, component) as the
+// cell kernel's gather reads them (against unit face weights); and the eigenvectors'
+// sensitivities -- from the projections (sum over the stencil of the projected-value
+// sensitivities times the split fluxes) and the back-projection, the two signs' shares summed
+// across the lane pair -- sent through the eigenvectors' formulas and the Roe average to the
+// primitives (rho, u, v, p) of the face's two cells (rbar: the "+" lane writes the left cell's,
+// the "-" lane the right cell's).
+// A block of 32 x 4 threads takes 16 faces x 4 lines (xi) or 16 lines x 4 faces (eta); its
+// cells' split fluxes and primitives are staged once in shared memory (each cell's get_primary
+// and split computed once, not once per reading face), and each thread parks its projected-value
+// sensitivities there too, which keeps the field loop's live registers down.
 template <int DIR>
-__global__ void __launch_bounds__(128) k_char_face(AdjParams a, const double* __restrict__ u,
+__global__ void __launch_bounds__(128, 3) k_char_face(AdjParams a, const double* __restrict__ u,
                                                   const double* __restrict__ hb, const double* __restrict__ lamv,
                                                   const double* __restrict__ tp, double* __restrict__ fbar) {
+    constexpr int FA = DIR == 0 ? 16 : 4;  // faces of a block along the direction
+    constexpr int NB = DIR == 0 ? 4 : 16;  // lines of a block
+    constexpr int NA = FA + 5;             // cells staged along a line: f0-3 .. f0+FA+1
+    __shared__ double sC[12][NB][NA];      // F+ (0..3), F- (4..7), rho, u, v, p (8..11)
+    __shared__ double sL[20][128];         // per thread: cb[k] g_k[m] of its sign, row k*5+m
     const int ni = a.ni, nj = a.nj;
-    // x runs along the face array's rows: the faces of a line (xi), the lines (eta)
-    const int tx = blockIdx.x * blockDim.x + threadIdx.x, ty = blockIdx.y * blockDim.y + threadIdx.y;
-    const int f = DIR == 0 ? tx : ty, line = DIR == 0 ? ty : tx;
     const int n = DIR == 0 ? ni : nj, nline = DIR == 0 ? nj : ni;
-    if (line >= nline || f > n) return;
-    const double t = tp ? *tp : 0.0;
+    const int tid = threadIdx.x + 32 * threadIdx.y;
+    const int f0 = (DIR == 0 ? blockIdx.x : blockIdx.y) * FA, l0 = (DIR == 0 ? blockIdx.y : blockIdx.x) * NB;
+    const double lam = lamv[DIR];
+    {
+        const double t = tp ? *tp : 0.0;
+        for (int idx = tid; idx < NA * NB; idx += 128) {
+            const int ai = idx % NA, bi = idx / NA;
+            const int x = f0 - 3 + ai, line = l0 + bi;  // x >= -3; faces <= n read cells <= n+2
+            if (line >= nline || x > n + 2) continue;
+            double c[9];
+            fetch_cell<DIR>(a, u, line, x, t, c);
+            const double un = c[5 + DIR], pr = c[7];
+            const double P[4] = {0.0, DIR == 0 ? pr : 0.0, DIR == 1 ? pr : 0.0, un * pr};
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {
+                sC[v][bi][ai] = 0.5 * fma(un + lam, c[v], P[v]);
+                sC[4 + v][bi][ai] = 0.5 * fma(un - lam, c[v], P[v]);
+                sC[8 + v][bi][ai] = c[4 + v];
+            }
+        }
+    }
+    __syncthreads();
+    const int sg = threadIdx.x & 1, fl = threadIdx.x >> 1;
+    const int fa = DIR == 0 ? fl : (int)threadIdx.y, bi = DIR == 0 ? (int)threadIdx.y : fl;
+    const int f = f0 + fa, line = l0 + bi;
+    const bool valid = f <= n && line < nline;  // the same for both lanes of a face
     const long long ts = DIR == 0 ? a.xs : a.ys;
     const long long to = DIR == 0 ? (long long)line * (ni + 1) + f : (long long)f * ni + line;
     const double g1 = a.gamma - 1.0, kg = a.gamma / g1;
-    // the stencil cells f-3 .. f+2 and their GLF split fluxes
-    double c[6][9];
-#pragma unroll
-    for (int q = 0; q < 6; ++q) fetch_cell<DIR>(a, u, line, f - 3 + q, t, c[q]);
-    const double lam = lamv[DIR];
-    double Fp[6][4], Fm[6][4];
-#pragma unroll
-    for (int q = 0; q < 6; ++q) {
-        const double un = c[q][5 + DIR], pr = c[q][7];
-        const double P[4] = {0.0, DIR == 0 ? pr : 0.0, DIR == 1 ? pr : 0.0, un * pr};
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-            Fp[q][v] = 0.5 * fma(un + lam, c[q][v], P[v]);
-            Fm[q][v] = 0.5 * fma(un - lam, c[q][v], P[v]);
-        }
-    }
-    // Roe average of cells 2 (left) and 3 (right) and the eigenvector entries
-    const double rl = c[2][4], rr = c[3][4];
-    const double ul = c[2][5], ur = c[3][5], vl = c[2][6], vr = c[3][6], pl = c[2][7], pr = c[3][7];
-    const double sl = sqrt(rl), sr = sqrt(rr);
-    const double hl = kg * pl / rl + 0.5 * (ul * ul + vl * vl), hr = kg * pr / rr + 0.5 * (ur * ur + vr * vr);
-    const double r = 1.0 / (sl + sr);
-    const double u0 = (sr * ur + sl * ul) * r, v0 = (sr * vr + sl * vl) * r, h0 = (sr * hr + sl * hl) * r;
-    const double uu0 = 0.5 * (u0 * u0 + v0 * v0);
-    const double c2 = g1 * (h0 - uu0);
-    const double ia = 1.0 / sqrt(c2), a0 = c2 * ia, ihh = g1 * ia * ia;
-    const double un0 = DIR == 0 ? u0 : v0, ut0 = DIR == 0 ? v0 : u0, a0un0 = a0 * un0;
-    const double hu = 0.5 * uu0 * ihh, nu = 0.5 * un0 * ia, ia5 = 0.5 * ia;
-    const double pn = 0.5 * un0 * ihh, pt = 0.5 * ut0 * ihh, ih = 0.5 * ihh;
-    const double ln0 = -pn - ia5, ln3 = -pn + ia5;
-    // M[cc][k]: the coefficient of split-flux component cc in characteristic field k
-    double M[4][4];
-    M[0][0] = hu + nu; M[3][0] = ih;
-    M[0][3] = hu - nu; M[3][3] = ih;
-    if (DIR == 0) { M[1][0] = ln0; M[2][0] = -pt; M[1][3] = ln3; M[2][3] = -pt; }
-    else          { M[1][0] = -pt; M[2][0] = ln0; M[1][3] = -pt; M[2][3] = ln3; }
-    M[0][1] = 1.0 - uu0 * ihh; M[1][1] = u0 * ihh; M[2][1] = v0 * ihh; M[3][1] = -ihh;
-    M[0][2] = -ut0; M[1][2] = DIR == 1 ? 1.0 : 0.0; M[2][2] = DIR == 0 ? 1.0 : 0.0; M[3][2] = 0.0;
-    double HB[4];
-#pragma unroll
-    for (int v = 0; v < 4; ++v) HB[v] = hb[(DIR == 0 ? 0 : 4 * a.xs) + v * ts + to];
-    const double hn = HB[1 + DIR], ht = HB[2 - DIR];
-    // sensitivities of the eigen quantities, summed over both signs
+    // this sign's split flux of stencil point m, component cc (F+ of cells f-3..f+1, F- of
+    // cells f+2..f-2)
+    auto F = [&](int m, int cc) { return sC[sg * 4 + cc][bi][fa + (sg ? 5 - m : m)]; };
+    // the eigen quantities' sensitivities (this lane's sign; summed across the pair below)
     double un0b = 0, ut0b = 0, a0b = 0, h0b = 0, uu0b = 0, a0un0b = 0;
-    double A[4][4] = {};  // A[k][cc]: sensitivity of M[cc][k]
-    double* const FB = fbar + (DIR == 0 ? 0 : a.gnp * a.xs) + to;
+    double A0[4] = {0, 0, 0, 0}, A1[4] = {0, 0, 0, 0}, A3[4] = {0, 0, 0, 0}, A20 = 0;  // A[k][cc]
+    // the Roe average's inputs of this lane's cell (the "+" lane the left cell, the "-" lane the
+    // right), exchanged across the pair: sqrt(rho) and the total enthalpy
+    const int ac = fa + 2 + sg;
+    const double rs = valid ? sC[8][bi][ac] : 1.0, us = valid ? sC[9][bi][ac] : 0.0;
+    const double vs = valid ? sC[10][bi][ac] : 0.0, ps = valid ? sC[11][bi][ac] : 1.0;
+    const double irs = 1.0 / rs, ss = sqrt(rs), hs = fma(kg * ps, irs, 0.5 * (us * us + vs * vs));
+    const double ss_o = __shfl_xor_sync(0xffffffffu, ss, 1), hs_o = __shfl_xor_sync(0xffffffffu, hs, 1);
+    const double us_o = __shfl_xor_sync(0xffffffffu, us, 1), vs_o = __shfl_xor_sync(0xffffffffu, vs, 1);
+    const double sl = sg ? ss_o : ss, sr = sg ? ss : ss_o, hl = sg ? hs_o : hs, hr = sg ? hs : hs_o;
+    const double ul = sg ? us_o : us, ur = sg ? us : us_o, vl = sg ? vs_o : vs, vr = sg ? vs : vs_o;
+    double r = 0.5, u0 = 0, v0 = 0, h0 = 0, uu0 = 0, c2 = 1, ia = 1, a0 = 1;
+    double ihh = 0, un0 = 0, ut0 = 0;
+    if (valid) {
+        r = 1.0 / (sl + sr);
+        u0 = (sr * ur + sl * ul) * r; v0 = (sr * vr + sl * vl) * r; h0 = (sr * hr + sl * hl) * r;
+        uu0 = 0.5 * (u0 * u0 + v0 * v0);
+        c2 = g1 * (h0 - uu0);
+        ia = 1.0 / sqrt(c2); a0 = c2 * ia; ihh = g1 * ia * ia;
+        un0 = DIR == 0 ? u0 : v0; ut0 = DIR == 0 ? v0 : u0;
+        const double a0un0 = a0 * un0;
+        const double hu = 0.5 * uu0 * ihh, nu = 0.5 * un0 * ia, ia5 = 0.5 * ia;
+        const double pn = 0.5 * un0 * ihh, pt = 0.5 * ut0 * ihh, ih = 0.5 * ihh;
+        const double ln0 = -pn - ia5, ln3 = -pn + ia5;
+        // M[cc][k]: the coefficient of split-flux component cc in characteristic field k
+        double M[4][4];
+        M[0][0] = hu + nu; M[3][0] = ih;
+        M[0][3] = hu - nu; M[3][3] = ih;
+        if (DIR == 0) { M[1][0] = ln0; M[2][0] = -pt; M[1][3] = ln3; M[2][3] = -pt; }
+        else          { M[1][0] = -pt; M[2][0] = ln0; M[1][3] = -pt; M[2][3] = ln3; }
+        M[0][1] = 1.0 - uu0 * ihh; M[1][1] = u0 * ihh; M[2][1] = v0 * ihh; M[3][1] = -ihh;
+        M[0][2] = -ut0; M[1][2] = DIR == 1 ? 1.0 : 0.0; M[2][2] = DIR == 0 ? 1.0 : 0.0; M[3][2] = 0.0;
+        double HB[4];
 #pragma unroll
-    for (int sg = 0; sg < 2; ++sg) {
-        double F[5][4];
-#pragma unroll
-        for (int m = 0; m < 5; ++m)
-#pragma unroll
-            for (int v = 0; v < 4; ++v) F[m][v] = sg == 0 ? Fp[m][v] : Fm[5 - m][v];
-        double cv[4], G[4][5];
+        for (int v = 0; v < 4; ++v) HB[v] = hb[(DIR == 0 ? 0 : 4 * a.xs) + v * ts + to];
+        const double hn = HB[1 + DIR], ht = HB[2 - DIR];
+        // the back-projection's transpose: each field value's sensitivity
+        const double sb = HB[0] + un0 * hn + ut0 * ht, db = a0 * hn + a0un0 * HB[3];
+        const double cb[4] = {sb - db + h0 * HB[3], sb + uu0 * HB[3], ht + ut0 * HB[3], sb + db + h0 * HB[3]};
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             double lf[5];
 #pragma unroll
             for (int m = 0; m < 5; ++m)
-                lf[m] = fma(M[0][k], F[m][0], fma(M[1][k], F[m][1], fma(M[2][k], F[m][2], M[3][k] * F[m][3])));
+                lf[m] = fma(M[0][k], F(m, 0), fma(M[1][k], F(m, 1), fma(M[2][k], F(m, 2), M[3][k] * F(m, 3))));
             double gd[4], d0, d1, d2;
             first_differences(lf, gd);
             betas_g(gd, d0, d1, d2);
             const double B[3] = {fma(-3.0, gd[1], gd[0]), gd[1] + gd[2], fma(3.0, gd[2], -gd[3])};
-            WenoTerms t;
-            weno_terms<true>(gd, d0, d1, d2, t);
-            const double iN = rcp_nr(t.N), num = weno_num(t);
-            cv[k] = fma(num, iN, lf[2]);
-            weno_grad<true>(gd, B, d0, d1, d2, t, num * iN, iN, G[k]);
+            WenoTerms wt;
+            weno_terms<true>(gd, d0, d1, d2, wt);
+            const double iN = rcp_nr(wt.N), num = weno_num(wt);
+            const double cv = fma(num, iN, lf[2]);
+            double G[5];
+            weno_grad<true>(gd, B, d0, d1, d2, wt, num * iN, iN, G);
+#pragma unroll
+            for (int m = 0; m < 5; ++m) sL[k * 5 + m][tid] = cb[k] * G[m];
+            // the back-projection's own sensitivities, linear in the field values: with
+            // s = cv0 + cv1 + cv3 and d = cv3 - cv0, un0 takes s hn, a0 d hn, ut0 s ht + cv2 h3,
+            // h0 (cv0 + cv3) h3, a0 un0 d h3, uu0 cv1 h3
+            if (k != 2) { un0b = fma(cv, hn, un0b); ut0b = fma(cv, ht, ut0b); }
+            if (k == 0) { a0b = fma(-cv, hn, a0b); h0b = fma(cv, HB[3], h0b); a0un0b = fma(-cv, HB[3], a0un0b); }
+            if (k == 3) { a0b = fma(cv, hn, a0b); h0b = fma(cv, HB[3], h0b); a0un0b = fma(cv, HB[3], a0un0b); }
+            if (k == 1) uu0b = fma(cv, HB[3], uu0b);
+            if (k == 2) ut0b = fma(cv, HB[3], ut0b);
         }
-        // the back-projection and its transpose
-        const double s = cv[0] + cv[1] + cv[3], d = cv[3] - cv[0];
-        const double sb = HB[0] + un0 * hn + ut0 * ht, db = a0 * hn + a0un0 * HB[3];
-        const double cb[4] = {sb - db + h0 * HB[3], sb + uu0 * HB[3], ht + ut0 * HB[3], sb + db + h0 * HB[3]};
-        un0b += s * hn;
-        a0b += d * hn;
-        ut0b += s * ht + cv[2] * HB[3];
-        h0b += (cv[0] + cv[3]) * HB[3];
-        a0un0b += d * HB[3];
-        uu0b += cv[1] * HB[3];
-        // the fields' projected-value sensitivities, the split fluxes', the eigenvectors'
+        // the split fluxes' sensitivities (the transposed projection) and the projection
+        // coefficients' (sum over the stencil of the projected values' times the split fluxes)
+        double* const FB = fbar + (DIR == 0 ? 0 : a.gnp * a.xs) + to;
 #pragma unroll
         for (int m = 0; m < 5; ++m) {
-            double lb[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) lb[k] = cb[k] * G[k][m];
+            const double l0_ = sL[m][tid], l1_ = sL[5 + m][tid], l2_ = sL[10 + m][tid], l3_ = sL[15 + m][tid];
 #pragma unroll
             for (int cc = 0; cc < 4; ++cc) {
+                const double Fm = F(m, cc);
                 FB[(long long)((sg * 5 + m) * 4 + cc) * ts] =
-                    fma(M[cc][0], lb[0], fma(M[cc][1], lb[1], fma(M[cc][2], lb[2], M[cc][3] * lb[3])));
-#pragma unroll
-                for (int k = 0; k < 4; ++k) A[k][cc] = fma(lb[k], F[m][cc], A[k][cc]);
+                    fma(M[cc][0], l0_, fma(M[cc][1], l1_, fma(M[cc][2], l2_, M[cc][3] * l3_)));
+                A0[cc] = fma(l0_, Fm, A0[cc]);
+                A1[cc] = fma(l1_, Fm, A1[cc]);
+                A3[cc] = fma(l3_, Fm, A3[cc]);
+                if (cc == 0) A20 = fma(l2_, Fm, A20);
             }
         }
     }
+    // the two signs' shares (both lanes of a pair are valid or neither; every lane shuffles)
+    auto pair_sum = [](double& v) { v += __shfl_xor_sync(0xffffffffu, v, 1); };
+    pair_sum(un0b); pair_sum(ut0b); pair_sum(a0b); pair_sum(h0b); pair_sum(uu0b); pair_sum(a0un0b);
+#pragma unroll
+    for (int cc = 0; cc < 4; ++cc) { pair_sum(A0[cc]); pair_sum(A1[cc]); pair_sum(A3[cc]); }
+    pair_sum(A20);
+    if (!valid) return;
     // the eigenvector entries' sensitivities back to the Roe quantities
-    const double l00b = A[0][0], l03b = A[3][0];
-    const double l10b = A[0][1], l13b = A[3][1], l20b = A[0][2], l23b = A[3][2];
-    const double l30b = A[0][3] + A[3][3];
-    const double l01b = A[1][0], l11b = A[1][1], l21b = A[1][2], l31b = A[1][3];
-    ut0b -= A[2][0];
+    const double l00b = A0[0], l03b = A3[0];
+    const double l10b = A0[1], l13b = A3[1], l20b = A0[2], l23b = A3[2];
+    const double l30b = A0[3] + A3[3];
+    const double l01b = A1[0], l11b = A1[1], l21b = A1[2], l31b = A1[3];
+    ut0b -= A20;
     const double hub = l00b + l03b, nub = l00b - l03b;
     const double nrm0 = DIR == 0 ? l10b : l20b, nrm3 = DIR == 0 ? l13b : l23b;  // the ln0, ln3 entries
     const double tg0 = DIR == 0 ? l20b : l10b, tg3 = DIR == 0 ? l23b : l13b;    // the -pt entries
@@ -793,20 +825,17 @@ __global__ void __launch_bounds__(128) k_char_face(AdjParams a, const double* __
     uu0b += -g1 * c2b;
     u0b += u0 * uu0b;
     v0b += v0 * uu0b;
-    // the Roe average's inputs, then the two cells' primitives
-    const double slb = r * ((ul - u0) * u0b + (vl - v0) * v0b + (hl - h0) * h0b);
-    const double srb = r * ((ur - u0) * u0b + (vr - v0) * v0b + (hr - h0) * h0b);
-    const double ulb = sl * r * u0b, urb = sr * r * u0b, vlb = sl * r * v0b, vrb = sr * r * v0b;
-    const double hlb = sl * r * h0b, hrb = sr * r * h0b;
-    double* const RB = a.rbar + (DIR == 0 ? 0 : 8 * a.xs) + to;
-    RB[0 * ts] = 0.5 / sl * slb - kg * pl / (rl * rl) * hlb;
-    RB[1 * ts] = ulb + ul * hlb;
-    RB[2 * ts] = vlb + vl * hlb;
-    RB[3 * ts] = kg / rl * hlb;
-    RB[4 * ts] = 0.5 / sr * srb - kg * pr / (rr * rr) * hrb;
-    RB[5 * ts] = urb + ur * hrb;
-    RB[6 * ts] = vrb + vr * hrb;
-    RB[7 * ts] = kg / rr * hrb;
+    // the Roe average's inputs, then this lane's cell's primitives (the "+" lane the left cell's,
+    // rbar planes 0..3; the "-" lane the right cell's, 4..7): d sqrt(rho), d h, d u, d v of the
+    // average, then rho and p through sqrt(rho) and h = kg p / rho + (u^2 + v^2)/2
+    const double sbar = r * ((us - u0) * u0b + (vs - v0) * v0b + (hs - h0) * h0b);
+    const double sr_ = ss * r, kgir = kg * irs;
+    const double hbar = sr_ * h0b;
+    double* const RB = a.rbar + (DIR == 0 ? 0 : 8 * a.xs) + to + (long long)(4 * sg) * ts;
+    RB[0 * ts] = fma(0.5 * ss * irs, sbar, -(kgir * ps * irs * hbar));  // d sqrt(rho)/d rho = 1/(2 sqrt(rho))
+    RB[1 * ts] = fma(us, hbar, sr_ * u0b);
+    RB[2 * ts] = fma(vs, hbar, sr_ * v0b);
+    RB[3 * ts] = kgir * hbar;
 }
 
 // Cell kernel: Ub = (dL/du)^T w at the cell from the stage's tape and hbar, then the reverse of
@@ -1514,8 +1543,9 @@ int dense_adjoint_create(const dense_config_t* cfg, int checkpoint_every, dense_
     a->tape_stage = (size_t)p.np * (size_t)(p.xs + p.ys);
     a->gh = dim3((cfg->ni + 1 + kHX - 1) / kHX, (cfg->nj + 1 + kHY - 1) / kHY, 2);
     a->gc = dim3((cfg->ni + kCX - 1) / kCX, (cfg->nj + kCY - 1) / kCY);
-    a->gfx = dim3((cfg->ni + 1 + kCX - 1) / kCX, (cfg->nj + kCY - 1) / kCY);  // xi faces (f, line)
-    a->gfy = dim3((cfg->ni + kCX - 1) / kCX, (cfg->nj + 1 + kCY - 1) / kCY);  // eta faces (line, f)
+    // k_char_face blocks: 16 faces x 4 lines (xi), 16 lines x 4 faces (eta), two threads a face
+    a->gfx = dim3((cfg->ni + 1 + 15) / 16, (cfg->nj + 3) / 4);
+    a->gfy = dim3((cfg->ni + 15) / 16, (cfg->nj + 1 + 3) / 4);
     a->npart = (int)(a->gh.x * a->gh.y * a->gh.z);
     a->nm = (int)(a->gc.x * a->gc.y);
     struct B { double** p; size_t n; } bufs[] = {

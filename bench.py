@@ -343,9 +343,15 @@ def run_batched(args, dense, lib):
     print(json.dumps(line), flush=True)
 
 
+# the adjoint workload's schemes: (splitting, recon, name, FLOP-count key)
+ADJ_SCHEMES = {"llf-js": (101, 253, "LLF + WENO-JS5", "LLF+WENO-JS5"),
+               "char": (104, 0, "characteristic WENO-Z + GLF (104)", "CH (104)")}
+
+
 def run_adjoint(args, dense, lib):
     """Gradient of a vortex run through the discrete adjoint: 256x256 periodic vortex, LLF +
-    WENO-JS5, CFL 0.4, 400 steps, checkpoints every 20. Loss 1/2 ||rho(T) - rho_target||^2, the
+    WENO-JS5 (or the characteristic scheme 104: --adj-scheme char), CFL 0.4, 400 steps,
+    checkpoints every 20. Loss 1/2 ||rho(T) - rho_target||^2, the
     target from the unperturbed vortex (eps 5, centre (5,5)); the run starts from that vortex plus
     a seeded Gaussian density perturbation of amplitude 1e-3. Gradients w.r.t. the perturbation
     field and (eps, xc, yc), checked against central differences (h = 1e-6) of the CUDA forward."""
@@ -354,7 +360,8 @@ def run_adjoint(args, dense, lib):
     ni = args.ni or 256
     nj = args.nj or 256
     n, k = args.adj_steps, 20
-    cfg = dense.init_general(dense.config_default(ni=ni, nj=nj, benchmark=11, splitting=101, recon=253,
+    split, recon, scheme, fl_key = ADJ_SCHEMES[args.adj_scheme]
+    cfg = dense.init_general(dense.config_default(ni=ni, nj=nj, benchmark=11, splitting=split, recon=recon,
                                                   cfl=0.4, var_eps=5.0, var_xc=5.0, var_yc=5.0))[0]
     adj = adjm.Adjoint(cfg, checkpoint_every=k)
     Step = adjm.AdjointStep
@@ -452,14 +459,14 @@ def run_adjoint(args, dense, lib):
                     "max_cells_unchanged": bool(same)}
     status = 0
     cells = ni * nj
-    fl = json.load(open(os.path.join(ROOT, "tests", "golden", "flop_counts.json")))["schemes"]["LLF+WENO-JS5"]
+    fl = json.load(open(os.path.join(ROOT, "tests", "golden", "flop_counts.json")))["schemes"][fl_key]
     peak = ctypes.c_double()
     lib.dense_measure_fp64(0, ctypes.byref(peak))
     value = cells * n / ((fwd + bwd) * 1e-3)
     line = {"metric": METRIC + " (forward + adjoint)", "value": value, "unit": UNIT, "n_gpus": 1, "steps": reps,
             "warmup": args.warmup, "ms_per_step": (fwd + bwd) / n, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"adjoint: vortex {ni}x{nj} periodic, LLF + WENO-JS5, CFL 0.4, {n} steps, "
+            "config": {"workload": f"adjoint: vortex {ni}x{nj} periodic, {scheme}, CFL 0.4, {n} steps, "
                                    f"checkpoint every {k}; loss 1/2||rho(T)-rho_target||^2",
                        "ni": ni, "nj": nj, "nsteps": n, "checkpoint_every": k,
                        "l2": "state (2 MB) fits in L2; no flush: each timed rep is a 400-step chain"},
@@ -511,6 +518,8 @@ def main():
                     help="launch mode of the batched workload: the autotuner's pick, one launch per "
                          "phase, or one persistent launch per step (tiles and order tuned either way)")
     ap.add_argument("--adj-steps", type=int, default=400, help="time steps of the adjoint workload's run")
+    ap.add_argument("--adj-scheme", default="llf-js", choices=sorted(ADJ_SCHEMES),
+                    help="the adjoint workload's scheme: LLF + WENO-JS5 (101 + 253) or characteristic (104)")
     args = ap.parse_args()
     if args.steps is None:
         args.steps = 200 if args.workload == "batched" else 100
