@@ -1,8 +1,8 @@
 """Differentiable form: the discrete adjoint of n time steps behind ``torch.autograd.Function``.
 
 ``Adjoint`` owns a forward solver and the adjoint kernels of ``csrc/adjoint.cu`` (LLF, GLF or
-Steger-Warming splitting with upwind5 / WENO-JS5 / WENO-Z5, or the characteristic WENO-Z scheme
-104, on x- and y-periodic grids or the
+Steger-Warming splitting with upwind5 / WENO-JS5 / WENO-Z5, the characteristic WENO-Z scheme
+104 or AdaWENO 105, on x- and y-periodic grids or the
 reference's benchmarks with extrapolated, mirror and fixed-state sides (1, 2, 3, 4, 5, 9, 13;
 the Rayleigh-Taylor ones with their body force), TVD-RK3, CFL or constant dt).
 States are CUDA float64 tensors of the interior, shape (4, nj, ni): conserved variables

@@ -1,6 +1,7 @@
 // adjoint.cu — the discrete adjoint of the plain solver's time step: LLF, GLF or Steger-Warming
 // splitting (101, 102, 103) with upwind5 / WENO-JS5 / WENO-Z5 reconstruction (251/253/255), or
-// the characteristic WENO-Z scheme (104, k_char_face), and TVD-RK3 with the CFL time step, on
+// the characteristic WENO-Z scheme (104, k_char_face) and AdaWENO (105, the same kernel with the
+// branches the forward took), and TVD-RK3 with the CFL time step, on
 // grids periodic in x and y (benchmarks 11 and 14) or with extrapolated, mirror and fixed-state
 // sides (benchmarks 1, 2, 3, 4, 5, 9, 13; wall_terms).
 //
@@ -78,6 +79,9 @@ struct AdjParams {
     // rbar[8][face plane] a direction (left cell 0..3, right cell 4..7), xi then eta
     int charac;
     double* rbar;
+    // AdaWENO (105): the smooth branch's surrogate rho + F(normal momentum) adds the density
+    // sensitivities of its stencil cells, planes 40 + s*5 + m of the gathered face array
+    int adapt;
 };
 // Ghost rules of the benchmarks the adjoint covers (boundary_*_general.f90): a periodic copy,
 // the recursive 4/3, -1/3 extrapolation of the two cells next to the side, the mirror of the
@@ -445,6 +449,26 @@ __device__ __forceinline__ void gather_line(const double* __restrict__ T, const 
     }
 }
 
+// AdaWENO: the density sensitivity of cell x of a line (faces as gather_line) from the faces
+// whose surrogate stencils read it, periodic images included.
+__device__ __forceinline__ double gather_rho_line(const double* __restrict__ T, long long ts, long long base,
+                                                  long long stride, int x, int n, bool periodic) {
+    double acc = 0.0;
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+            const int f = s == 0 ? x + 3 - m : x - 2 + m;
+            const double* R = T + (long long)(40 + s * 5 + m) * ts + base;
+            if (f >= 0 && f <= n) acc += R[(long long)f * stride];
+            if (!periodic) continue;
+            if (f >= n) acc += R[(long long)(f - n) * stride];
+            if (f <= 0) acc += R[(long long)(f + n) * stride];
+        }
+    }
+    return acc;
+}
+
 // The ghost cells of a side with a wall rule that the interior cell (i, j) feeds, in direction
 // DIR (0: the left and right sides of row j, 1: the bottom and top of column i): for each such
 // ghost, its state rebuilt from the interior state by the rule, the sensitivities of its F+ and
@@ -578,6 +602,8 @@ __device__ __forceinline__ void wall_terms(const AdjParams& a, const double* __r
                 prb[4] = ab;
                 if (SPL == 1 && (rule == kRuleReflect || dist == 1)) lb += lamb;
             }
+            if (a.adapt)  // the ghost's density in the surrogate stencils that read it
+                prb[0] += gather_rho_line(T, ts, base, stride, side == 0 ? -1 - k : n + k, n, false);
             if (a.charac && k == 0) {
                 // the ghost next to the side is a Roe cell of the boundary face: the left cell of
                 // face 0, the right cell of face n
@@ -662,7 +688,8 @@ __device__ __forceinline__ void fetch_cell(const AdjParams& a, const double* __r
 template <int DIR>
 __global__ void __launch_bounds__(128, 3) k_char_face(AdjParams a, const double* __restrict__ u,
                                                   const double* __restrict__ hb, const double* __restrict__ lamv,
-                                                  const double* __restrict__ tp, double* __restrict__ fbar) {
+                                                  const double* __restrict__ tp, const double* __restrict__ flags,
+                                                  double* __restrict__ fbar) {
     constexpr int FA = DIR == 0 ? 16 : 4;  // faces of a block along the direction
     constexpr int NB = DIR == 0 ? 4 : 16;  // lines of a block
     constexpr int NA = FA + 5;             // cells staged along a line: f0-3 .. f0+FA+1
@@ -699,9 +726,14 @@ __global__ void __launch_bounds__(128, 3) k_char_face(AdjParams a, const double*
     const long long ts = DIR == 0 ? a.xs : a.ys;
     const long long to = DIR == 0 ? (long long)line * (ni + 1) + f : (long long)f * ni + line;
     const double g1 = a.gamma - 1.0, kg = a.gamma / g1;
+    // AdaWENO (flags): the branches the forward took at this face, bit 0 "+" smooth, bit 1 "-"
+    int fbits = 0;
+    if (flags && valid) fbits = (int)flags[(DIR == 0 ? 0 : 5 * a.xs) + to];
+    const bool smooth = (fbits >> sg) & 1, any_char = fbits != 3;
     // this sign's split flux of stencil point m, component cc (F+ of cells f-3..f+1, F- of
-    // cells f+2..f-2)
-    auto F = [&](int m, int cc) { return sC[sg * 4 + cc][bi][fa + (sg ? 5 - m : m)]; };
+    // cells f+2..f-2), and the cell's density
+    auto am = [&](int m) { return fa + (sg ? 5 - m : m); };
+    auto F = [&](int m, int cc) { return sC[sg * 4 + cc][bi][am(m)]; };
     // the eigen quantities' sensitivities (this lane's sign; summed across the pair below)
     double un0b = 0, ut0b = 0, a0b = 0, h0b = 0, uu0b = 0, a0un0b = 0;
     double A0[4] = {0, 0, 0, 0}, A1[4] = {0, 0, 0, 0}, A3[4] = {0, 0, 0, 0}, A20 = 0;  // A[k][cc]
@@ -718,73 +750,116 @@ __global__ void __launch_bounds__(128, 3) k_char_face(AdjParams a, const double*
     double r = 0.5, u0 = 0, v0 = 0, h0 = 0, uu0 = 0, c2 = 1, ia = 1, a0 = 1;
     double ihh = 0, un0 = 0, ut0 = 0;
     if (valid) {
-        r = 1.0 / (sl + sr);
-        u0 = (sr * ur + sl * ul) * r; v0 = (sr * vr + sl * vl) * r; h0 = (sr * hr + sl * hl) * r;
-        uu0 = 0.5 * (u0 * u0 + v0 * v0);
-        c2 = g1 * (h0 - uu0);
-        ia = 1.0 / sqrt(c2); a0 = c2 * ia; ihh = g1 * ia * ia;
-        un0 = DIR == 0 ? u0 : v0; ut0 = DIR == 0 ? v0 : u0;
-        const double a0un0 = a0 * un0;
-        const double hu = 0.5 * uu0 * ihh, nu = 0.5 * un0 * ia, ia5 = 0.5 * ia;
-        const double pn = 0.5 * un0 * ihh, pt = 0.5 * ut0 * ihh, ih = 0.5 * ihh;
-        const double ln0 = -pn - ia5, ln3 = -pn + ia5;
-        // M[cc][k]: the coefficient of split-flux component cc in characteristic field k
-        double M[4][4];
-        M[0][0] = hu + nu; M[3][0] = ih;
-        M[0][3] = hu - nu; M[3][3] = ih;
-        if (DIR == 0) { M[1][0] = ln0; M[2][0] = -pt; M[1][3] = ln3; M[2][3] = -pt; }
-        else          { M[1][0] = -pt; M[2][0] = ln0; M[1][3] = -pt; M[2][3] = ln3; }
-        M[0][1] = 1.0 - uu0 * ihh; M[1][1] = u0 * ihh; M[2][1] = v0 * ihh; M[3][1] = -ihh;
-        M[0][2] = -ut0; M[1][2] = DIR == 1 ? 1.0 : 0.0; M[2][2] = DIR == 0 ? 1.0 : 0.0; M[3][2] = 0.0;
+        double* const FB = fbar + (DIR == 0 ? 0 : a.gnp * a.xs) + to;
         double HB[4];
 #pragma unroll
         for (int v = 0; v < 4; ++v) HB[v] = hb[(DIR == 0 ? 0 : 4 * a.xs) + v * ts + to];
-        const double hn = HB[1 + DIR], ht = HB[2 - DIR];
-        // the back-projection's transpose: each field value's sensitivity
-        const double sb = HB[0] + un0 * hn + ut0 * ht, db = a0 * hn + a0un0 * HB[3];
-        const double cb[4] = {sb - db + h0 * HB[3], sb + uu0 * HB[3], ht + ut0 * HB[3], sb + db + h0 * HB[3]};
+        if (any_char) {  // a face whose signs are both smooth never forms its Roe average
+            r = 1.0 / (sl + sr);
+            u0 = (sr * ur + sl * ul) * r; v0 = (sr * vr + sl * vl) * r; h0 = (sr * hr + sl * hl) * r;
+            uu0 = 0.5 * (u0 * u0 + v0 * v0);
+            c2 = g1 * (h0 - uu0);
+            ia = 1.0 / sqrt(c2); a0 = c2 * ia; ihh = g1 * ia * ia;
+            un0 = DIR == 0 ? u0 : v0; ut0 = DIR == 0 ? v0 : u0;
+        }
+        if (!smooth) {
+            const double a0un0 = a0 * un0;
+            const double hu = 0.5 * uu0 * ihh, nu = 0.5 * un0 * ia, ia5 = 0.5 * ia;
+            const double pn = 0.5 * un0 * ihh, pt = 0.5 * ut0 * ihh, ih = 0.5 * ihh;
+            const double ln0 = -pn - ia5, ln3 = -pn + ia5;
+            // M[cc][k]: the coefficient of split-flux component cc in characteristic field k
+            double M[4][4];
+            M[0][0] = hu + nu; M[3][0] = ih;
+            M[0][3] = hu - nu; M[3][3] = ih;
+            if (DIR == 0) { M[1][0] = ln0; M[2][0] = -pt; M[1][3] = ln3; M[2][3] = -pt; }
+            else          { M[1][0] = -pt; M[2][0] = ln0; M[1][3] = -pt; M[2][3] = ln3; }
+            M[0][1] = 1.0 - uu0 * ihh; M[1][1] = u0 * ihh; M[2][1] = v0 * ihh; M[3][1] = -ihh;
+            M[0][2] = -ut0; M[1][2] = DIR == 1 ? 1.0 : 0.0; M[2][2] = DIR == 0 ? 1.0 : 0.0; M[3][2] = 0.0;
+            const double hn = HB[1 + DIR], ht = HB[2 - DIR];
+            // the back-projection's transpose: each field value's sensitivity
+            const double sb = HB[0] + un0 * hn + ut0 * ht, db = a0 * hn + a0un0 * HB[3];
+            const double cb[4] = {sb - db + h0 * HB[3], sb + uu0 * HB[3], ht + ut0 * HB[3], sb + db + h0 * HB[3]};
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            double lf[5];
+            for (int k = 0; k < 4; ++k) {
+                double lf[5];
 #pragma unroll
-            for (int m = 0; m < 5; ++m)
-                lf[m] = fma(M[0][k], F(m, 0), fma(M[1][k], F(m, 1), fma(M[2][k], F(m, 2), M[3][k] * F(m, 3))));
+                for (int m = 0; m < 5; ++m)
+                    lf[m] = fma(M[0][k], F(m, 0), fma(M[1][k], F(m, 1), fma(M[2][k], F(m, 2), M[3][k] * F(m, 3))));
+                double gd[4], d0, d1, d2;
+                first_differences(lf, gd);
+                betas_g(gd, d0, d1, d2);
+                const double B[3] = {fma(-3.0, gd[1], gd[0]), gd[1] + gd[2], fma(3.0, gd[2], -gd[3])};
+                WenoTerms wt;
+                weno_terms<true>(gd, d0, d1, d2, wt);
+                const double iN = rcp_nr(wt.N), num = weno_num(wt);
+                const double cv = fma(num, iN, lf[2]);
+                double G[5];
+                weno_grad<true>(gd, B, d0, d1, d2, wt, num * iN, iN, G);
+#pragma unroll
+                for (int m = 0; m < 5; ++m) sL[k * 5 + m][tid] = cb[k] * G[m];
+                // the back-projection's own sensitivities, linear in the field values: with
+                // s = cv0 + cv1 + cv3 and d = cv3 - cv0, un0 takes s hn, a0 d hn, ut0 s ht + cv2 h3,
+                // h0 (cv0 + cv3) h3, a0 un0 d h3, uu0 cv1 h3
+                if (k != 2) { un0b = fma(cv, hn, un0b); ut0b = fma(cv, ht, ut0b); }
+                if (k == 0) { a0b = fma(-cv, hn, a0b); h0b = fma(cv, HB[3], h0b); a0un0b = fma(-cv, HB[3], a0un0b); }
+                if (k == 3) { a0b = fma(cv, hn, a0b); h0b = fma(cv, HB[3], h0b); a0un0b = fma(cv, HB[3], a0un0b); }
+                if (k == 1) uu0b = fma(cv, HB[3], uu0b);
+                if (k == 2) ut0b = fma(cv, HB[3], ut0b);
+            }
+            // the split fluxes' sensitivities (the transposed projection) and the projection
+            // coefficients' (sum over the stencil of the projected values' times the split fluxes)
+#pragma unroll
+            for (int m = 0; m < 5; ++m) {
+                const double l0_ = sL[m][tid], l1_ = sL[5 + m][tid], l2_ = sL[10 + m][tid], l3_ = sL[15 + m][tid];
+#pragma unroll
+                for (int cc = 0; cc < 4; ++cc) {
+                    const double Fm = F(m, cc);
+                    FB[(long long)((sg * 5 + m) * 4 + cc) * ts] =
+                        fma(M[cc][0], l0_, fma(M[cc][1], l1_, fma(M[cc][2], l2_, M[cc][3] * l3_)));
+                    A0[cc] = fma(l0_, Fm, A0[cc]);
+                    A1[cc] = fma(l1_, Fm, A1[cc]);
+                    A3[cc] = fma(l3_, Fm, A3[cc]);
+                    if (cc == 0) A20 = fma(l2_, Fm, A20);
+                }
+                if (flags) FB[(long long)(40 + sg * 5 + m) * ts] = 0.0;  // no density share
+            }
+        } else {
+            // AdaWENO's smooth branch (scheme_weno5th_SC.f90:110-124): every component
+            // reconstructed from its own candidates with the WENO-Z weights w_k of the scalar
+            // surrogate sur = rho + F(normal momentum). Its reverse: dh_v/dF_v[m] = sum_k w_k
+            // a_k,m, the same for the four components; the weights' sensitivities Q_k =
+            // sum_v hbar_v q_k(F_v) = q_k(phi), phi[m] = sum_v hbar_v F_v[m], sent through the
+            // surrogate's weights to its five values, and from each to the cell's density and
+            // normal-momentum split flux.
+            double phi[5], sur[5];
+#pragma unroll
+            for (int m = 0; m < 5; ++m) {
+                phi[m] = fma(HB[0], F(m, 0), fma(HB[1], F(m, 1), fma(HB[2], F(m, 2), HB[3] * F(m, 3))));
+                sur[m] = sC[8][bi][am(m)] + F(m, 1 + DIR);
+            }
             double gd[4], d0, d1, d2;
-            first_differences(lf, gd);
+            first_differences(sur, gd);
             betas_g(gd, d0, d1, d2);
             const double B[3] = {fma(-3.0, gd[1], gd[0]), gd[1] + gd[2], fma(3.0, gd[2], -gd[3])};
             WenoTerms wt;
             weno_terms<true>(gd, d0, d1, d2, wt);
-            const double iN = rcp_nr(wt.N), num = weno_num(wt);
-            const double cv = fma(num, iN, lf[2]);
-            double G[5];
-            weno_grad<true>(gd, B, d0, d1, d2, wt, num * iN, iN, G);
+            const double iN = rcp_nr(wt.N);
+            const double w0 = c30 * wt.v[0] * iN, w1 = c31 * wt.v[1] * iN, w2 = c32 * wt.v[2] * iN;
+            const double Q0 = fma(a300, phi[0], fma(a301, phi[1], a302 * phi[2]));
+            const double Q1 = fma(a310, phi[1], fma(a311, phi[2], a312 * phi[3]));
+            const double Q2 = fma(a320, phi[2], fma(a321, phi[3], a322 * phi[4]));
+            const double Wq = fma(w0, Q0, fma(w1, Q1, w2 * Q2));
+            const double E[3] = {c30 * (Q0 - Wq), c31 * (Q1 - Wq), c32 * (Q2 - Wq)};
+            double gw[5];
+            weno_weight_grad<true>(gd, B, d0, d1, d2, wt, E, iN, gw);
+            const double gc[5] = {w0 * a300, fma(w0, a301, w1 * a310), fma(w0, a302, fma(w1, a311, w2 * a320)),
+                                  fma(w1, a312, w2 * a321), w2 * a322};
 #pragma unroll
-            for (int m = 0; m < 5; ++m) sL[k * 5 + m][tid] = cb[k] * G[m];
-            // the back-projection's own sensitivities, linear in the field values: with
-            // s = cv0 + cv1 + cv3 and d = cv3 - cv0, un0 takes s hn, a0 d hn, ut0 s ht + cv2 h3,
-            // h0 (cv0 + cv3) h3, a0 un0 d h3, uu0 cv1 h3
-            if (k != 2) { un0b = fma(cv, hn, un0b); ut0b = fma(cv, ht, ut0b); }
-            if (k == 0) { a0b = fma(-cv, hn, a0b); h0b = fma(cv, HB[3], h0b); a0un0b = fma(-cv, HB[3], a0un0b); }
-            if (k == 3) { a0b = fma(cv, hn, a0b); h0b = fma(cv, HB[3], h0b); a0un0b = fma(cv, HB[3], a0un0b); }
-            if (k == 1) uu0b = fma(cv, HB[3], uu0b);
-            if (k == 2) ut0b = fma(cv, HB[3], ut0b);
-        }
-        // the split fluxes' sensitivities (the transposed projection) and the projection
-        // coefficients' (sum over the stencil of the projected values' times the split fluxes)
-        double* const FB = fbar + (DIR == 0 ? 0 : a.gnp * a.xs) + to;
+            for (int m = 0; m < 5; ++m) {
 #pragma unroll
-        for (int m = 0; m < 5; ++m) {
-            const double l0_ = sL[m][tid], l1_ = sL[5 + m][tid], l2_ = sL[10 + m][tid], l3_ = sL[15 + m][tid];
-#pragma unroll
-            for (int cc = 0; cc < 4; ++cc) {
-                const double Fm = F(m, cc);
-                FB[(long long)((sg * 5 + m) * 4 + cc) * ts] =
-                    fma(M[cc][0], l0_, fma(M[cc][1], l1_, fma(M[cc][2], l2_, M[cc][3] * l3_)));
-                A0[cc] = fma(l0_, Fm, A0[cc]);
-                A1[cc] = fma(l1_, Fm, A1[cc]);
-                A3[cc] = fma(l3_, Fm, A3[cc]);
-                if (cc == 0) A20 = fma(l2_, Fm, A20);
+                for (int cc = 0; cc < 4; ++cc)
+                    FB[(long long)((sg * 5 + m) * 4 + cc) * ts] = cc == 1 + DIR ? fma(HB[cc], gc[m], gw[m]) : HB[cc] * gc[m];
+                FB[(long long)(40 + sg * 5 + m) * ts] = gw[m];
             }
         }
     }
@@ -795,6 +870,12 @@ __global__ void __launch_bounds__(128, 3) k_char_face(AdjParams a, const double*
     for (int cc = 0; cc < 4; ++cc) { pair_sum(A0[cc]); pair_sum(A1[cc]); pair_sum(A3[cc]); }
     pair_sum(A20);
     if (!valid) return;
+    double* const RB = a.rbar + (DIR == 0 ? 0 : 8 * a.xs) + to + (long long)(4 * sg) * ts;
+    if (!any_char) {  // no Roe average at this face
+#pragma unroll
+        for (int v = 0; v < 4; ++v) RB[v * ts] = 0.0;
+        return;
+    }
     // the eigenvector entries' sensitivities back to the Roe quantities
     const double l00b = A0[0], l03b = A3[0];
     const double l10b = A0[1], l13b = A3[1], l20b = A0[2], l23b = A3[2];
@@ -831,7 +912,6 @@ __global__ void __launch_bounds__(128, 3) k_char_face(AdjParams a, const double*
     const double sbar = r * ((us - u0) * u0b + (vs - v0) * v0b + (hs - h0) * h0b);
     const double sr_ = ss * r, kgir = kg * irs;
     const double hbar = sr_ * h0b;
-    double* const RB = a.rbar + (DIR == 0 ? 0 : 8 * a.xs) + to + (long long)(4 * sg) * ts;
     RB[0 * ts] = fma(0.5 * ss * irs, sbar, -(kgir * ps * irs * hbar));  // d sqrt(rho)/d rho = 1/(2 sqrt(rho))
     RB[1 * ts] = fma(us, hbar, sr_ * u0b);
     RB[2 * ts] = fma(vs, hbar, sr_ * v0b);
@@ -898,6 +978,9 @@ __global__ void __launch_bounds__(128) k_rev(AdjParams a, const double* __restri
             }
             prim_pullback_all(U, q, a.gamma, rb[0], rb[1], rb[2], rb[3], 0.0, Ub);
         }
+        if (a.adapt)  // the surrogate stencils' density sensitivities (rho = U[0])
+            Ub[0] += gather_rho_line(tape, a.xs, (long long)j * (ni + 1), 1, i, ni, px) +
+                     gather_rho_line(tape + a.gnp * a.xs, a.ys, i, ni, j, nj, py);
         if (WALLS && (!px || !py)) {  // the ghost cells of wall sides that this cell feeds
             // (a separate instantiation: the periodic kernels keep their registers)
             double pbar[5] = {0, 0, 0, 0, 0};
@@ -1309,8 +1392,9 @@ void vjp(dense_adjoint* a, int stage, const double* u, const double* tape, const
     }
     k_hbar<<<a->gh, dim3(kHX, kHY), 0, s>>>(a->ap, w, tape, a->hb, part);
     if (charac) {
-        k_char_face<0><<<a->gfx, dim3(kCX, kCY), 0, s>>>(a->ap, u, a->hb, a->lamv, tp, a->fbar);
-        k_char_face<1><<<a->gfy, dim3(kCX, kCY), 0, s>>>(a->ap, u, a->hb, a->lamv, tp, a->fbar);
+        const double* flags = a->ap.adapt ? tape : nullptr;  // the branches taken, first plane a direction
+        k_char_face<0><<<a->gfx, dim3(kCX, kCY), 0, s>>>(a->ap, u, a->hb, a->lamv, tp, flags, a->fbar);
+        k_char_face<1><<<a->gfy, dim3(kCX, kCY), 0, s>>>(a->ap, u, a->hb, a->lamv, tp, flags, a->fbar);
         a->launches += 2;
         launch_rev<DENSE_RECON_WENOZ5, 1>(a, stage, u, a->fbar, w, out, dtp, tp, s);
     } else if (glf) launch_rev_recon<1>(a, stage, u, tape, w, out, dtp, tp, s);
@@ -1462,13 +1546,14 @@ void dense_adjoint_destroy(dense_adjoint_t* a) {
 int dense_adjoint_create(const dense_config_t* cfg, int checkpoint_every, dense_adjoint_t** out) {
     if (!out || !cfg) return aerr(nullptr, DENSE_ERR_ARG, "null argument");
     *out = nullptr;
-    const bool charac = cfg->splitting == DENSE_SPLIT_CH;
+    const bool adapt = cfg->splitting == DENSE_SPLIT_SC;
+    const bool charac = cfg->splitting == DENSE_SPLIT_CH || adapt;
     if (cfg->splitting != DENSE_SPLIT_LLF && cfg->splitting != DENSE_SPLIT_GLF && cfg->splitting != DENSE_SPLIT_SW &&
         !charac)
         return aerr(nullptr, DENSE_ERR_ARG,
-                    "the adjoint covers the LLF, GLF and Steger-Warming splittings (101-103) and the characteristic "
-                    "WENO-Z (104); not the adaptive scheme (105)");
-    // the characteristic scheme reconstructs by its own WENO-Z; the recon field is not read
+                    "the adjoint covers the LLF, GLF and Steger-Warming splittings (101-103), the characteristic "
+                    "WENO-Z (104) and AdaWENO (105)");
+    // the characteristic schemes reconstruct by their own WENO-Z; the recon field is not read
     if (!charac && cfg->recon != DENSE_RECON_UPWIND5 && cfg->recon != DENSE_RECON_WENOJS5 &&
         cfg->recon != DENSE_RECON_WENOZ5)
         return aerr(nullptr, DENSE_ERR_ARG, "the adjoint covers reconstructions 251, 253 and 255");
@@ -1530,9 +1615,10 @@ int dense_adjoint_create(const dense_config_t* cfg, int checkpoint_every, dense_
     p.ni = cfg->ni; p.nj = cfg->nj; p.plane = (long long)cfg->ni * cfg->nj;
     p.xs = (long long)cfg->nj * (cfg->ni + 1);
     p.ys = (long long)(cfg->nj + 1) * cfg->ni;
-    p.np = charac ? 4 : dense::tape_planes(cfg->recon);
-    p.gnp = charac ? 40 : p.np;
+    p.np = adapt ? 5 : charac ? 4 : dense::tape_planes(cfg->recon);
+    p.gnp = adapt ? 50 : charac ? 40 : p.np;
     p.charac = charac ? 1 : 0;
+    p.adapt = adapt ? 1 : 0;
     p.gamma = cfg->gamma; p.dx = cfg->dx; p.dy = cfg->dy; p.inv_dx = 1.0 / cfg->dx; p.inv_dy = 1.0 / cfg->dy;
     p.cfl = cfg->cfl;
     for (int k = 0; k < 4; ++k) p.rule[k] = rules[k];
@@ -1561,7 +1647,7 @@ int dense_adjoint_create(const dense_config_t* cfg, int checkpoint_every, dense_
     }
     if (charac) {
         const size_t fp = (size_t)(p.xs + p.ys);
-        struct B2 { double** p; size_t n; } cb[] = {{&a->fbar, 40 * fp}, {&p.rbar, 8 * fp}, {&a->ones, 4 * fp}};
+        struct B2 { double** p; size_t n; } cb[] = {{&a->fbar, (size_t)p.gnp * fp}, {&p.rbar, 8 * fp}, {&a->ones, 4 * fp}};
         for (auto& b : cb) {
             cudaError_t e = cudaMalloc((void**)b.p, b.n * sizeof(double));
             if (e != cudaSuccess) { a->err = std::string("cudaMalloc: ") + cudaGetErrorString(e); return fail(DENSE_ERR_NOMEM); }

@@ -68,7 +68,9 @@ struct Params {
     int periodic_ghosts;
     int count_branches;  // accumulate Scalars::branch_count in the AdaWENO sweeps
     // Tape of the sweeps for the discrete adjoint (flux_tape launches only; for the characteristic
-    // sweeps (104) only the fluxes, 4 planes a direction). The component-wise LLF/GLF/SW sweeps':
+    // sweeps (104) only the fluxes, 4 planes a direction; for AdaWENO (105) the branches taken,
+    // bit 0 "+" smooth and bit 1 "-" smooth, then the fluxes, 5 planes a direction). The
+    // component-wise LLF/GLF/SW sweeps':
     // per direction tape_planes(recon) planes of the direction's face array (xi [nj][ni+1], eta
     // [nj+1][ni], eta after xi): the reconstructions' stencil gradients g[(s*5 + m)*4 + v] (s = 0
     // for F+, 1 for F-; none for upwind5, whose gradient is constant), then the fluxes h[v].

@@ -876,9 +876,10 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
         for (int v = 0; v < 4; ++v) {
             (DIR == 0 ? p.hx : p.he)[fidx<DIR>(p, v, line, f)] = hsum[v];
         }
-        if (p.tape) {  // the adjoint's taping recompute (104): the face fluxes, 4 planes a direction
+        if (p.tape) {  // the adjoint's taping recompute: the face fluxes, the last 4 planes a direction
+            constexpr int NP = ADAPT ? 5 : 4;
             const long long xs = (long long)p.nj * (p.ni + 1), ts = DIR == 0 ? xs : (long long)(p.nj + 1) * p.ni;
-            double* T = p.tape + (DIR == 0 ? 0 : 4 * xs) + fidx<DIR>(p, 0, line, f);
+            double* T = p.tape + (DIR == 0 ? 0 : NP * xs) + (NP - 4) * ts + fidx<DIR>(p, 0, line, f);
 #pragma unroll
             for (int v = 0; v < 4; ++v) T[v * ts] = hsum[v];
         }
@@ -987,6 +988,12 @@ __device__ __forceinline__ void flux_char_block(const Params& p, int irk, int bx
 #endif
         }
         __syncthreads();  // the staged surrogate terms are consumed; the region takes the results next
+        if (p.tape && valid) {
+            // the adjoint's taping recompute: the branches taken (1: "+" smooth, 2: "-" smooth)
+            // in the first of the direction's 5 planes, so that the reverse follows the same ones
+            const long long xs = (long long)p.nj * (p.ni + 1);
+            p.tape[(DIR == 0 ? 0 : 5 * xs) + fidx<DIR>(p, 0, line, f)] = (double)((smooth[0] ? 1 : 0) + (smooth[1] ? 2 : 0));
+        }
         if (p.count_branches) {
             const int ns = valid ? (int)smooth[0] + (int)smooth[1] : 0;
             const int nc = valid ? 2 - ns : 0;
@@ -1808,7 +1815,7 @@ static void launch_flux(const Params& p, int irk, int dir, void* stream) {
 // flux(dir) plus the adjoint tape: LLF/GLF with reconstruction 251, 253 or 255 only
 static void launch_flux_tape(const Params& p, int irk, int dir, void* stream) {
     cudaStream_t s = (cudaStream_t)stream;
-    if (p.splitting == DENSE_SPLIT_CH) {  // the plain sweep, which stores the fluxes on the tape too
+    if (p.splitting == DENSE_SPLIT_CH || p.splitting == DENSE_SPLIT_SC) {  // the plain sweep, which tapes too
         launch_flux(p, irk, dir, stream);
         return;
     }

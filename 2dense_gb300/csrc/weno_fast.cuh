@@ -143,3 +143,43 @@ __device__ __forceinline__ void weno_grad(const double gd[4], const double B[3],
     g[4] = fma(c32 * a322, u[2], fma(k, PA2, -NB2));
     g[2] = 1.0 - ((g[0] + g[1]) + (g[3] + g[4]));
 }
+
+// The weights' share alone of a reconstruction's stencil gradient, for weights computed from one
+// stencil (lf, through gd, B, d_k and its weno_terms t, iN = 1/N) and applied to candidates of
+// other data: AdaWENO's smooth branch reconstructs every component with the WENO-Z weights of
+// its scalar surrogate. With the value sum_k w_k Q_k (Q_k the candidates, already contracted with
+// the components' sensitivities) and E_k = c_k (Q_k - sum_j w_j Q_j), g[m] = d(sum_k w_k Q_k)/dlf[m]
+// -- weno_grad's indicator terms with its candidate terms left out. The weights see differences
+// only, so the five entries sum to zero.
+template <bool Z>
+__device__ __forceinline__ void weno_weight_grad(const double gd[4], const double B[3], double d0, double d1,
+                                                 double d2, const WenoTerms& t, const double E[3], double iN,
+                                                 double g[5]) {
+    const double iD = 4.0 * rcp_nr(t.D);
+    const double id0 = d0 * (t.P[0] * iD), id1 = d1 * (t.P[1] * iD), id2 = d2 * (t.P[2] * iD);  // 1/(ss + beta_k)
+    const double A0 = gd[0] - gd[1], A1 = gd[1] - gd[2], A2 = gd[2] - gd[3];
+    double r0, r1, r2;
+    if (!Z) {
+        r0 = (E[0] * (t.v[0] * iN)) * id0;
+        r1 = (E[1] * (t.v[1] * iN)) * id1;
+        r2 = (E[2] * (t.v[2] * iN)) * id2;
+    } else {
+        const double tau = t.tau;
+        const double s0 = (E[0] * tau) * (t.P[0] * iN);
+        const double s1 = (E[1] * tau) * (t.P[1] * iN);
+        const double s2 = (E[2] * tau) * (t.P[2] * iN);
+        const double st = 4.0 * (s0 + s1 + s2);
+        const double sh = d2 >= d0 ? st : -st;
+        r0 = fma(s0 * tau, id0, sh);
+        r1 = s1 * tau * id1;
+        r2 = fma(s2 * tau, id2, -sh);
+    }
+    const double PA0 = r0 * A0, PA1 = r1 * A1, PA2 = r2 * A2;
+    const double NB0 = r0 * B[0], NB1 = r1 * B[1], NB2 = r2 * B[2];
+    constexpr double k = -13.0 / 3.0;
+    g[0] = fma(k, PA0, -NB0);
+    g[1] = fma(-2.0 * k, PA0, fma(k, PA1, fma(4.0, NB0, -NB1)));
+    g[3] = fma(k, PA1, fma(-2.0 * k, PA2, fma(4.0, NB2, NB1)));
+    g[4] = fma(k, PA2, -NB2);
+    g[2] = -((g[0] + g[1]) + (g[3] + g[4]));
+}

@@ -345,12 +345,13 @@ def run_batched(args, dense, lib):
 
 # the adjoint workload's schemes: (splitting, recon, name, FLOP-count key)
 ADJ_SCHEMES = {"llf-js": (101, 253, "LLF + WENO-JS5", "LLF+WENO-JS5"),
-               "char": (104, 0, "characteristic WENO-Z + GLF (104)", "CH (104)")}
+               "char": (104, 0, "characteristic WENO-Z + GLF (104)", "CH (104)"),
+               "adaweno": (105, 0, "AdaWENO + GLF (105), DELTA 0.5", "AdaWENO (105) smooth vortex")}
 
 
 def run_adjoint(args, dense, lib):
     """Gradient of a vortex run through the discrete adjoint: 256x256 periodic vortex, LLF +
-    WENO-JS5 (or the characteristic scheme 104: --adj-scheme char), CFL 0.4, 400 steps,
+    WENO-JS5 (or the characteristic scheme 104 / AdaWENO 105: --adj-scheme char / adaweno), CFL 0.4, 400 steps,
     checkpoints every 20. Loss 1/2 ||rho(T) - rho_target||^2, the
     target from the unperturbed vortex (eps 5, centre (5,5)); the run starts from that vortex plus
     a seeded Gaussian density perturbation of amplitude 1e-3. Gradients w.r.t. the perturbation
@@ -519,7 +520,8 @@ def main():
                          "phase, or one persistent launch per step (tiles and order tuned either way)")
     ap.add_argument("--adj-steps", type=int, default=400, help="time steps of the adjoint workload's run")
     ap.add_argument("--adj-scheme", default="llf-js", choices=sorted(ADJ_SCHEMES),
-                    help="the adjoint workload's scheme: LLF + WENO-JS5 (101 + 253) or characteristic (104)")
+                    help="the adjoint workload's scheme: LLF + WENO-JS5 (101 + 253), characteristic (104) "
+                         "or AdaWENO (105)")
     args = ap.parse_args()
     if args.steps is None:
         args.steps = 200 if args.workload == "batched" else 100

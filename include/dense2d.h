@@ -371,12 +371,13 @@ int dense_batch_steps_device(dense_batch_t* b, int nsteps, double t_end, int tot
 
 /* No counterpart in the reference (it has no derivatives): the reverse mode of n steps of the
    plain solver, for the LLF, GLF or Steger-Warming splitting (101-103) with upwind5, WENO-JS5
-   or WENO-Z5 (251/253/255), or the characteristic WENO-Z scheme (104; its recon is not read),
+   or WENO-Z5 (251/253/255), or the characteristic schemes (104, AdaWENO 105; recon not read),
    on grids periodic in x and y (benchmarks 11 and 14) or with extrapolated, mirror and
    fixed-state sides (benchmarks 1, 2, 4, 9, Rayleigh-Taylor's 3 and 13 with its body force,
    and the double Mach reflection 5), CFL or constant dt. GLF's global wave speed of each stage
-   (104 splits by GLF) is differentiated like the time step: its gradient goes to the cell where
-   the maximum is attained. States and gradients
+   (104 and 105 split by GLF) is differentiated like the time step: its gradient goes to the cell
+   where the maximum is attained; AdaWENO's branch at each face and sign is the one the forward
+   took (a switch, held fixed like the maxima's cells). States and gradients
    are device arrays of the interior, u[4][nj][ni] (conserved variables, i fastest). The
    forward runs the plain solver's kernels and keeps the state every `checkpoint_every` steps;
    the reverse recomputes each segment from its checkpoint, storing the three stage states of

@@ -30,7 +30,7 @@ def perturbed_state(dense, cfg, seed=0, amp=1e-3):
 
 
 @pytest.mark.parametrize("split,recon", [(101, 251), (101, 253), (101, 255), (102, 251), (102, 253),
-                                         (102, 255), (103, 251), (103, 253), (103, 255), (104, 0)])
+                                         (102, 255), (103, 251), (103, 253), (103, 255), (104, 0), (105, 0)])
 def test_rhs_vjp_matches_autograd(dense, adjoint, split, recon):
     cfg = vortex_cfg(dense, recon, ni=24, nj=20, var_eps=4.0, var_xc=4.6, var_yc=5.3, splitting=split)
     c, U = perturbed_state(dense, cfg)
@@ -38,7 +38,7 @@ def test_rhs_vjp_matches_autograd(dense, adjoint, split, recon):
     with adjoint.Adjoint(c) as adj:
         out, vdotl = adj.rhs_vjp(U, v)
     Ut = U.clone().requires_grad_(True)
-    L = torch_step.rhs(Ut, c.gamma, c.dx, c.dy, recon, split)
+    L = torch_step.rhs(Ut, c.gamma, c.dx, c.dy, recon, split, delta=c.delta)
     (ref,) = torch.autograd.grad(L, Ut, v)
     L = L.detach()
     # two evaluation orders of derivatives whose WENO weights scale like 1/(1e-6 + beta)^3
@@ -48,7 +48,8 @@ def test_rhs_vjp_matches_autograd(dense, adjoint, split, recon):
 
 @pytest.mark.parametrize("split,recon,const_dt", [(101, 253, 0), (101, 255, 0), (101, 251, 0), (101, 253, 1),
                                                   (102, 253, 0), (102, 255, 0), (102, 251, 1),
-                                                  (103, 253, 0), (103, 255, 0), (104, 0, 0), (104, 0, 1)])
+                                                  (103, 253, 0), (103, 255, 0), (104, 0, 0), (104, 0, 1),
+                                                  (105, 0, 0)])
 def test_steps_gradient_matches_autograd(dense, adjoint, split, recon, const_dt):
     """7 steps with checkpoints every 3: two full segments and a partial one."""
     cfg = vortex_cfg(dense, recon, ni=24, nj=20, var_eps=4.0, var_xc=4.6, var_yc=5.3,
@@ -60,7 +61,8 @@ def test_steps_gradient_matches_autograd(dense, adjoint, split, recon, const_dt)
         g0 = adj.backward(gT)
         dts = adj.dts()
     Ut = U.clone().requires_grad_(True)
-    ref_T = torch_step.run(Ut, 7, c.gamma, c.dx, c.dy, recon, c.cfl, c.dt if const_dt else None, split)
+    ref_T = torch_step.run(Ut, 7, c.gamma, c.dx, c.dy, recon, c.cfl, c.dt if const_dt else None, split,
+                           delta=c.delta)
     assert rel(uT, ref_T.detach()) < 1e-12
     (ref,) = torch.autograd.grad(ref_T, Ut, gT)
     assert rel(g0, ref) < 1e-10
@@ -75,7 +77,8 @@ def padded(U):
     return cons
 
 
-@pytest.mark.parametrize("split,recon", [(101, 251), (101, 253), (101, 255), (102, 255), (103, 253), (104, 0)])
+@pytest.mark.parametrize("split,recon", [(101, 251), (101, 253), (101, 255), (102, 255), (103, 253), (104, 0),
+                                         (105, 0)])
 def test_taped_recompute_reproduces_the_forward(dense, adjoint, split, recon):
     """The taping sweeps of the reverse pass recompute each segment bit for bit: after a
     backward the solver holds the state after the first segment, equal to a plain solve, and the
@@ -167,7 +170,8 @@ def rough_state(dense, cfg, seed):
                                                (2, 103, 251), (1, 102, 255), (3, 101, 253), (13, 102, 255),
                                                (13, 103, 253), (5, 101, 253), (5, 102, 255), (5, 103, 253),
                                                (1, 104, 0), (2, 104, 0), (3, 104, 0), (4, 104, 0), (5, 104, 0),
-                                               (9, 104, 0), (13, 104, 0)])
+                                               (9, 104, 0), (13, 104, 0), (1, 105, 0), (2, 105, 0), (3, 105, 0),
+                                               (4, 105, 0), (5, 105, 0), (13, 105, 0)])
 def test_rhs_vjp_with_walls_matches_autograd(dense, adjoint, bench, split, recon):
     """The reference's benchmarks with walls -- extrapolated (1: x; 2: top, right; 4, 9: sides;
     5: right), mirror (2: bottom, left; 4, 9: bottom, top; 13: sides; 5: the bottom from x = 1/6)
@@ -180,7 +184,7 @@ def test_rhs_vjp_with_walls_matches_autograd(dense, adjoint, bench, split, recon
     with adjoint.Adjoint(c) as adj:
         out, vdotl = adj.rhs_vjp(U, v)
     Ut = U.clone().requires_grad_(True)
-    L = torch_step.rhs(Ut, c.gamma, c.dx, c.dy, recon, split, bench)
+    L = torch_step.rhs(Ut, c.gamma, c.dx, c.dy, recon, split, bench, delta=c.delta)
     (ref,) = torch.autograd.grad(L, Ut, v)
     assert rel(out, ref) < 1e-10
     assert abs(vdotl - float((v * L.detach()).sum())) < 1e-12 * float((v * L.detach()).abs().sum())
@@ -189,7 +193,8 @@ def test_rhs_vjp_with_walls_matches_autograd(dense, adjoint, bench, split, recon
 @pytest.mark.parametrize("bench,split,recon", [(4, 101, 253), (2, 102, 255), (1, 103, 253), (3, 101, 253),
                                                (13, 102, 253), (13, 103, 255), (5, 101, 253), (5, 102, 253),
                                                (5, 103, 253), (2, 104, 0), (3, 104, 0), (4, 104, 0),
-                                               (5, 104, 0), (13, 104, 0)])
+                                               (5, 104, 0), (13, 104, 0), (3, 105, 0), (4, 105, 0), (5, 105, 0),
+                                               (13, 105, 0)])
 def test_steps_gradient_with_walls_matches_autograd(dense, adjoint, bench, split, recon):
     """5 steps with checkpoints every 2 on grids with wall sides, CFL time step; on the
     Rayleigh-Taylor grids (3, 13) with the body force of every stage, whose time-step factor
@@ -202,14 +207,14 @@ def test_steps_gradient_with_walls_matches_autograd(dense, adjoint, bench, split
         uT = adj.forward(U, 5)
         g0 = adj.backward(gT)
     Ut = U.clone().requires_grad_(True)
-    ref_T = torch_step.run(Ut, 5, c.gamma, c.dx, c.dy, recon, c.cfl, None, split, bench)
+    ref_T = torch_step.run(Ut, 5, c.gamma, c.dx, c.dy, recon, c.cfl, None, split, bench, delta=c.delta)
     assert rel(uT, ref_T.detach()) < 1e-12
     (ref,) = torch.autograd.grad(ref_T, Ut, gT)
     assert rel(g0, ref) < 1e-10
 
 
 def test_rejects_unsupported_configurations(dense, adjoint):
-    for kw in (dict(recon=0, splitting=105), dict(benchmark=6), dict(ni=6)):
+    for kw in (dict(recon=0, splitting=106), dict(benchmark=6), dict(ni=6)):
         cfg = dense.init_general(vortex_cfg(dense, 253))[0]
         for k, v in kw.items():
             setattr(cfg, k, v)

@@ -41,7 +41,9 @@ def test_torch_step_matches_oracle(dense, orc, split, recon):
                                                (1, 103, 251), (3, 101, 253), (13, 102, 255), (13, 103, 251),
                                                (5, 101, 253), (5, 102, 255), (5, 103, 253), (11, 104, 0),
                                                (3, 104, 0), (13, 104, 0), (4, 104, 0), (1, 104, 0),
-                                               (2, 104, 0), (5, 104, 0), (9, 104, 0)])
+                                               (2, 104, 0), (5, 104, 0), (9, 104, 0), (11, 105, 0), (3, 105, 0),
+                                               (13, 105, 0), (4, 105, 0), (1, 105, 0), (2, 105, 0), (5, 105, 0),
+                                               (9, 105, 0)])
 def test_torch_step_with_walls_matches_oracle(dense, orc, bench, split, recon):
     """The ghost rules of the reference's benchmarks with walls (extrapolation, mirror,
     Rayleigh-Taylor's fixed states with its body force, the double Mach reflection's wall,
@@ -61,7 +63,7 @@ def test_torch_step_with_walls_matches_oracle(dense, orc, bench, split, recon):
     o.steps(3)
     ref = to_state(o.get_state()[0])
     got = torch_step.run(torch.from_numpy(to_state(cons)), 3, c.gamma, c.dx, c.dy, recon, c.cfl,
-                         split=split, bench=bench).numpy()
+                         split=split, bench=bench, delta=c.delta).numpy()
     scale = np.abs(ref).max(axis=(1, 2), keepdims=True)
     assert (np.abs(got - ref) / scale).max() < 1e-12
 

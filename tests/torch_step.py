@@ -158,18 +158,19 @@ def dmr_sides(U, gamma, dx, t):
     return ((wall, post[0]), top[0]), ((wall, post[1]), top[1]), post
 
 
-def rhs(U, gamma, dx, dy, rec, split=101, bench=11, t=0.0):
+def rhs(U, gamma, dx, dy, rec, split=101, bench=11, t=0.0, delta=0.5):
     """L(U) = -(h_{i+1/2} - h_{i-1/2})/dx - (g_{j+1/2} - g_{j-1/2})/dy; t is the step's start
-    time (the double Mach reflection's top ghosts)."""
-    if bench not in (11, 14) or split == 104:
+    time (the double Mach reflection's top ghosts), delta AdaWENO's switch (105)."""
+    if bench not in (11, 14) or split in (104, 105):
         if bench in (3, 13):
             fixed = [fixed_state(gamma, *st) for st in RT_STATES]
             ys = ((fixed[0][0], fixed[1][0]), (fixed[0][1], fixed[1][1]))
-            return _rhs_padded(U, gamma, dx, dy, rec, split, RULES[bench], ys)
+            return _rhs_padded(U, gamma, dx, dy, rec, split, RULES[bench], ys, delta=delta)
         if bench == 5:
             yu, yp, post = dmr_sides(U, gamma, dx, t)
-            return _rhs_padded(U, gamma, dx, dy, rec, split, RULES[bench], (yu, yp), ((post[0], None), (post[1], None)))
-        return _rhs_padded(U, gamma, dx, dy, rec, split, RULES[bench])
+            return _rhs_padded(U, gamma, dx, dy, rec, split, RULES[bench], (yu, yp),
+                               ((post[0], None), (post[1], None)), delta)
+        return _rhs_padded(U, gamma, dx, dy, rec, split, RULES[bench], delta=delta)
     rho, u, v, p, a = primitives(U, gamma)
     out = torch.zeros_like(U)
     for d, (un, h, axis) in enumerate(((u, dx, 2), (v, dy, 1))):
@@ -231,11 +232,29 @@ def roe_eigen(gamma, rl, rr, ul, ur, vl, vr, pl, pr, d):
     return L, R
 
 
-def _char_faces(Fp, Fm, Pg, gamma, axis, n, d):
+def weno5z_weights_theta(f):
+    """WENO-Z weights of a 5-point stencil and the AdaWENO indicator theta = 1/(1 + (sum alpha -
+    1)^2) (weno5z_stencil_omega_theta, weno_mod.f90:82-95)."""
+    f0, f1, f2, f3, f4 = f
+    b0 = 13.0 * (f0 - 2.0 * f1 + f2) ** 2 / 12.0 + (f0 - 4.0 * f1 + 3.0 * f2) ** 2 / 4.0
+    b1 = 13.0 * (f1 - 2.0 * f2 + f3) ** 2 / 12.0 + (f1 - f3) ** 2 / 4.0
+    b2 = 13.0 * (f2 - 2.0 * f3 + f4) ** 2 / 12.0 + (3.0 * f2 - 4.0 * f3 + f4) ** 2 / 4.0
+    tau = (b2 - b0).abs()
+    a0 = C[0] * (1.0 + (tau / (SS + b0)) ** 2)
+    a1 = C[1] * (1.0 + (tau / (SS + b1)) ** 2)
+    a2 = C[2] * (1.0 + (tau / (SS + b2)) ** 2)
+    s = a0 + a1 + a2
+    return (a0 / s, a1 / s, a2 / s), 1.0 / (1.0 + (s - 1.0) ** 2)
+
+
+def _char_faces(Fp, Fm, Pg, gamma, axis, n, d, delta=None):
     """h at the faces 0..n of the characteristic WENO-Z scheme (104, flux_splitting_CH.f90:24-110,
     scheme_weno5th_CH.f90): per face the Roe eigenvectors of its two cells (padded 3 + f and
     4 + f), each sign's five split fluxes projected on them, WENO-Z per characteristic field, and
-    the back-projection."""
+    the back-projection. With delta, AdaWENO (105, flux_splitting_SC.f90:141-237,
+    scheme_weno5th_SC.f90): per face and sign the indicator theta of the scalar surrogate rho +
+    F+-(normal momentum) chooses between the component-wise reconstruction with the surrogate's
+    WENO-Z weights (theta > delta, SC.f90:110-124) and the characteristic one."""
     sl = lambda F, k: F.narrow(axis, k, n + 1)
     sp = lambda F, k: F.narrow(axis - 1, k, n + 1)  # one primitive's plane
     r_, u_, v_, p_, _ = Pg
@@ -248,12 +267,22 @@ def _char_faces(Fp, Fm, Pg, gamma, axis, n, d):
         for k in range(4):
             lf = [L[0][k] * f[0] + L[1][k] * f[1] + L[2][k] * f[2] + L[3][k] * f[3] for f in st]
             cv.append(_recon(lf, 255))
-        h = h + torch.stack([R[0][q] * cv[0] + R[1][q] * cv[1] + R[2][q] * cv[2] + R[3][q] * cv[3]
-                             for q in range(4)])
+        hc = torch.stack([R[0][q] * cv[0] + R[1][q] * cv[1] + R[2][q] * cv[2] + R[3][q] * cv[3]
+                          for q in range(4)])
+        if delta is not None:
+            sur = [sp(r_, k) + f[1 + d] for k, f in zip(ks, st)]
+            (w0, w1, w2), theta = weno5z_weights_theta(sur)
+            f0, f1, f2, f3, f4 = st
+            q0 = 1.0 / 3.0 * f0 - 7.0 / 6.0 * f1 + 11.0 / 6.0 * f2
+            q1 = -1.0 / 6.0 * f1 + 5.0 / 6.0 * f2 + 1.0 / 3.0 * f3
+            q2 = 1.0 / 3.0 * f2 + 5.0 / 6.0 * f3 - 1.0 / 6.0 * f4
+            hs = w0 * q0 + w1 * q1 + w2 * q2
+            hc = torch.where(theta > delta, hs, hc)
+        h = h + hc
     return h
 
 
-def _rhs_padded(U, gamma, dx, dy, rec, split, rules, ys=None, xs=None):
+def _rhs_padded(U, gamma, dx, dy, rec, split, rules, ys=None, xs=None, delta=None):
     """L(U) on a grid with ghost layers filled by the given rules (bottom, top, left, right);
     ys, xs: the states of the y sides (bottom, top) and x sides (left, right) that need them, as
     ((of the conserved variables), (of the primitives))."""
@@ -267,14 +296,14 @@ def _rhs_padded(U, gamma, dx, dy, rec, split, rules, ys=None, xs=None):
         Pg = _pad_axis(Pr, axis, lo, hi, 1 + d, spec[1] if spec else None)
         r_, u_, v_, p_, a_ = Pg
         un = u_ if d == 0 else v_
-        if split == 104:  # GLF split, then the characteristic reconstruction
+        if split in (104, 105):  # GLF split, then the characteristic (or AdaWENO) reconstruction
             lam = ((u if d == 0 else v).abs() + a).max()
             zero = torch.zeros_like(p_)
             P = torch.stack([zero, p_ if d == 0 else zero, p_ if d == 1 else zero, un * p_])
             Fp = 0.5 * ((un + lam) * Ug + P)
             Fm = 0.5 * ((un - lam) * Ug + P)
             n = U.shape[axis]
-            hf = _char_faces(Fp, Fm, Pg, gamma, axis, n, d)
+            hf = _char_faces(Fp, Fm, Pg, gamma, axis, n, d, delta if split == 105 else None)
             out = out - (hf.narrow(axis, 1, n) - hf.narrow(axis, 0, n)) / h
             continue
         if split == 103:
@@ -302,7 +331,8 @@ def body_force(U):
     return torch.stack([zero, zero, U[0], U[2]])
 
 
-def time_step(U, gamma, dx, dy, rec, cfl, dt_const=None, split=101, bench=11, bodyforce=None, t=0.0):
+def time_step(U, gamma, dx, dy, rec, cfl, dt_const=None, split=101, bench=11, bodyforce=None, t=0.0,
+              delta=0.5):
     """One TVD-RK3 step; returns (U_next, dt). The body force (Rayleigh-Taylor, benchmarks 3
     and 13 unless bodyforce says otherwise) is added to each stage after the combine, f_s times
     the source of the stage's input with f_s = dt, dt/4 and 2/3 (single precision) dt
@@ -318,16 +348,16 @@ def time_step(U, gamma, dx, dy, rec, cfl, dt_const=None, split=101, bench=11, bo
     else:
         dt = torch.tensor(dt_const, dtype=U.dtype, device=U.device)
     src = (lambda W, f: f * dt * body_force(W)) if bodyforce else (lambda W, f: 0.0)
-    L = lambda W: rhs(W, gamma, dx, dy, rec, split, bench, t)
+    L = lambda W: rhs(W, gamma, dx, dy, rec, split, bench, t, delta)
     u1 = U + dt * L(U) + src(U, 1.0)
     u2 = 3.0 / 4.0 * U + 1.0 / 4.0 * u1 + 1.0 / 4.0 * dt * L(u1) + src(u1, 0.25)
     u3 = 1.0 / 3.0 * U + 2.0 / 3.0 * u2 + 2.0 / 3.0 * dt * L(u2) + src(u2, TWO_THIRDS_SINGLE)
     return u3, dt
 
 
-def run(U, n, gamma, dx, dy, rec, cfl, dt_const=None, split=101, bench=11, bodyforce=None):
+def run(U, n, gamma, dx, dy, rec, cfl, dt_const=None, split=101, bench=11, bodyforce=None, delta=0.5):
     t = 0.0  # the steps' start times, accumulated as the solver does (general_main.f90:34)
     for _ in range(n):
-        U, dt = time_step(U, gamma, dx, dy, rec, cfl, dt_const, split, bench, bodyforce, t)
+        U, dt = time_step(U, gamma, dx, dy, rec, cfl, dt_const, split, bench, bodyforce, t, delta)
         t = t + float(dt.detach())
     return U
