@@ -343,6 +343,17 @@ def run_batched(args, dense, lib):
     print(json.dumps(line), flush=True)
 
 
+FD_CRITERION = ("Richardson-extrapolated central differences (h = 1e-6, 2e-6) within 1e-6 relative of the "
+                "adjoint in every direction, with the cells of the wave-speed maxima unchanged")
+# AdaWENO switches each (face, sign) between two reconstructions at theta = delta: the discrete
+# loss is smooth only between switches, and over a 400-step run a 1e-6 step in a parameter flips
+# some of its hundreds of millions of decisions, whose jumps dominate a central difference. The
+# adjoint is the derivative with the switches held (like the time step's maxima), checked
+# against autograd with the same switches (tests/test_gpu_adjoint.py); the differences are
+# reported, not judged.
+FD_NOT_A_CRITERION_105 = ("not a criterion for AdaWENO (105): its per-face switch makes the loss piecewise "
+                          "smooth, and a 1e-6 step flips some of the run's switches; the gradient is checked "
+                          "against autograd with the switches held")
 # the adjoint workload's schemes: (splitting, recon, name, FLOP-count key)
 ADJ_SCHEMES = {"llf-js": (101, 253, "LLF + WENO-JS5", "LLF+WENO-JS5"),
                "char": (104, 0, "characteristic WENO-Z + GLF (104)", "CH (104)"),
@@ -476,11 +487,9 @@ def run_adjoint(args, dense, lib):
                         "loss": loss0, "fd_check": fd, "fd_h": h,
                         "max_rel_err_fd_h": max(v["rel_err_fd_h"] for v in fd.values()),
                         "max_rel_err_richardson": max(v["rel_err_richardson"] for v in fd.values()),
-                        "fd_criterion": "Richardson-extrapolated central differences (h = 1e-6, 2e-6) "
-                                        "within 1e-6 relative of the adjoint in every direction, with "
-                                        "the cells of the wave-speed maxima unchanged",
-                        "fd_pass": all(v["rel_err_richardson"] <= 1e-6 and v["max_cells_unchanged"]
-                                       for v in fd.values())},
+                        "fd_criterion": FD_CRITERION if split != 105 else FD_NOT_A_CRITERION_105,
+                        "fd_pass": None if split == 105 else
+                        all(v["rel_err_richardson"] <= 1e-6 and v["max_cells_unchanged"] for v in fd.values())},
             "e2e": {"value": cells * n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": drho_h.numel() * 8,
                     "d2h_bytes_per_step": (g_host[0].numel() + g_host[1].numel()) * 8,
                     "note": "perturbation field from pinned host memory, forward, backward, gradients to host"},
