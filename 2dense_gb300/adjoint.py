@@ -4,7 +4,8 @@
 Steger-Warming splitting with upwind5 / WENO-JS5 / WENO-Z5, the characteristic WENO-Z scheme
 104 or AdaWENO 105, on x- and y-periodic grids or the
 reference's benchmarks with extrapolated, mirror and fixed-state sides (1, 2, 3, 4, 5, 9, 13;
-the Rayleigh-Taylor ones with their body force), TVD-RK3, CFL or constant dt).
+the Rayleigh-Taylor ones with their body force) or the shear layer's time-dependent inflow (6),
+TVD-RK3, CFL or constant dt).
 States are CUDA float64 tensors of the interior, shape (4, nj, ni): conserved variables
 (rho, rho u, rho v, E) with i fastest -- the reference's cons(i, j, v) without ghost layers.
 

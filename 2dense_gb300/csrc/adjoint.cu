@@ -2,8 +2,8 @@
 // splitting (101, 102, 103) with upwind5 / WENO-JS5 / WENO-Z5 reconstruction (251/253/255), or
 // the characteristic WENO-Z scheme (104, k_char_face) and AdaWENO (105, the same kernel with the
 // branches the forward took), and TVD-RK3 with the CFL time step, on
-// grids periodic in x and y (benchmarks 11 and 14) or with extrapolated, mirror and fixed-state
-// sides (benchmarks 1, 2, 3, 4, 5, 9, 13; wall_terms).
+// grids periodic in x and y (benchmarks 11 and 14) or with extrapolated, mirror, fixed-state and
+// time-dependent inflow sides (benchmarks 1, 2, 3, 4, 5, 6, 9, 13; wall_terms).
 //
 // The forward step (time_rk3_general, time_advance_general.f90:9-267) applies per stage
 //     L(u)_c = -(h_{f+1} - h_f)/dx - (g_{f'+1} - g_{f'})/dy,     cell c between faces f, f+1,
@@ -82,6 +82,14 @@ struct AdjParams {
     // AdaWENO (105): the smooth branch's surrogate rho + F(normal momentum) adds the density
     // sensitivities of its stencil cells, planes 40 + s*5 + m of the gathered face array
     int adapt;
+    // the shock / shear layer (6): the rows' cell-centre y (the inflow's profile); the stages'
+    // per-block sums of the inflow ghosts' time sensitivity (tpart[(s - 1) nm + block]); tacc[0]
+    // the running sum, over the steps already reversed, of the loss's sensitivity to their start
+    // times, which every earlier time step moves
+    int ssl;
+    const double* yleft;
+    double* tpart;
+    double* tacc;
 };
 // Ghost rules of the benchmarks the adjoint covers (boundary_*_general.f90): a periodic copy,
 // the recursive 4/3, -1/3 extrapolation of the two cells next to the side, the mirror of the
@@ -92,6 +100,9 @@ constexpr int kRulePeriodic = 0, kRuleExtrap = 1, kRuleReflect = 2, kRuleFixed =
 // the double Mach reflection's bottom: the mirror where the column's centre x >= 1/6, the fixed
 // post-shock state before it (boundary_doublemach_general.f90:14-48)
 constexpr int kRuleDMRBottom = 4;
+// the shock / shear layer's left inflow (boundary_ssl_general.f90:40-66): a state per row that
+// oscillates in the step's start time, which the time steps make a function of the state
+constexpr int kRuleSSLInflow = 5;
 constexpr double kTwoThirdsSingle = (double)(2.0f / 3.0f);  // time_advance_general.f90:242
 
 // get_primary of one cell (get_primary.f90:53-60), with the pressure floor of :58; rs = 1/alpha'
@@ -486,10 +497,31 @@ __device__ __forceinline__ double gather_rho_line(const double* __restrict__ T, 
 // the double Mach reflection's inflow and bottom-before-the-wall post-shock state, and its top,
 // post-shock ahead of the moving shock x < 1/6 + (1 + 20 t)/sqrt(3), pre-shock behind it
 // (boundary_doublemach_general.f90:51-99). Same formulas as the boundary fill's state_from.
+// The shear layer's inflow at row `line` and time t (boundary_ssl_general.f90:40-66: the same
+// formulas as the boundary fill), and dv/dt, the only component that moves with t.
+__device__ __forceinline__ void ssl_inflow(const AdjParams& a, int line, double t, double& rho, double& u, double& v,
+                                           double& pr, double& dv) {
+    const double yy = a.yleft[line];
+    const double pie = 3.141592653589793115997963468544185161590576171875;
+    rho = yy >= 0.0 ? 1.6374 : 0.3626;
+    pr = 0.3327;
+    u = 2.5 + 0.5 * tanh(2.0 * yy);
+    const double e = exp(-(yy * yy) / 10.0), om = 2.0 * pie / (30.0 / 2.68);
+    const double a1 = 2.0 * pie * t / (30.0 / 2.68), a2 = 2.0 * pie * 2.0 * t / (30.0 / 2.68) + pie / 2.0;
+    v = 0.05 * cos(a1) * e + 0.05 * cos(a2) * e;
+    dv = -0.05 * e * (om * sin(a1) + 2.0 * om * sin(a2));
+}
 __device__ __forceinline__ void fixed_state(const AdjParams& a, int dir, int side, int line, double t, double Ug[4],
                                             double* qg = nullptr) {
     double rho, u = 0.0, v = 0.0, pr;
-    if (a.bench == DENSE_BENCH_DMR) {
+    if (a.bench == DENSE_BENCH_SSL) {
+        if (dir == 1) {  // the top: the setup's post-shock state, never refilled
+            rho = 2.1101; u = 2.9709; v = -0.1367; pr = (double)0.4754f;
+        } else {         // the left inflow at time t
+            double dv;
+            ssl_inflow(a, line, t, rho, u, v, pr, dv);
+        }
+    } else if (a.bench == DENSE_BENCH_DMR) {
         const double x = ((double)(line + 1) - 0.5) * a.dx;  // the column's centre (init centres)
         const bool post = !(dir == 1 && side == 1) || x < (1.0 / 6.0 + (1.0 + 20.0 * t) / sqrt(3.0));
         if (post) { rho = 8.0; u = (double)8.25f * sqrt(3.0) * 0.5; v = -(double)8.25f * 0.5; pr = 116.5; }
@@ -508,7 +540,7 @@ template <int DIR, int SPL, int REC>
 __device__ __forceinline__ void wall_terms(const AdjParams& a, const double* __restrict__ u,
                                            const double* __restrict__ tape, const double* __restrict__ hb, int i,
                                            int j, const Prim& q, const double U[4], double lam_g, double t,
-                                           double Ub[4], double pbar[5], double& lb) {
+                                           double Ub[4], double pbar[5], double& lb, double& tl) {
     const int n = DIR == 0 ? a.ni : a.nj, x = DIR == 0 ? i : j;
     const long long ts = DIR == 0 ? a.xs : a.ys;
     const double* T = DIR == 0 ? tape : tape + a.gnp * a.xs;
@@ -524,21 +556,51 @@ __device__ __forceinline__ void wall_terms(const AdjParams& a, const double* __r
         const int line = DIR == 0 ? j : i;
         if (rule == kRuleDMRBottom) rule = ((double)(i + 1) - 0.5) * a.dx >= 1.0 / 6.0 ? kRuleReflect : kRuleFixed;
         const int dist = side == 0 ? x + 1 : n - x;  // 1 = next to the side
-        if (rule == kRuleFixed) {
+        if (rule == kRuleFixed || rule == kRuleSSLInflow) {
             // a fixed ghost state depends on no cell; only GLF's global lambda enters its
             // split, dF+-/dlambda = +-U/2, whose sensitivity the cell next to the side takes for
-            // the line's four ghosts
-            if (SPL != 1 || dist != 1) continue;
-            double Ug[4];
-            fixed_state(a, DIR, side, line, t, Ug);
+            // the line's four ghosts. The shear layer's inflow moves with the step's start time:
+            // the same cell takes its ghosts' time sensitivity, (dL/dghost)^T w . dghost/dt
+            // with only v moving (dU/dt = (0, 0, rho, rho v) v', dprim/dt = (0, 0, v', 0, 0)),
+            // and, for the characteristic schemes, the boundary face's Roe share of ghost 0.
+            const bool moving = rule == kRuleSSLInflow;
+            if (dist != 1 || (SPL != 1 && !moving)) continue;
+            double Ug[4], qg[5];
+            fixed_state(a, DIR, side, line, t, Ug, qg);
+            double dv = 0.0;
+            if (moving) {
+                double r_, u_, v_, p_;
+                ssl_inflow(a, line, t, r_, u_, v_, p_, dv);
+            }
 #pragma unroll 1
             for (int k = 0; k < 4; ++k) {
                 double gp[4] = {0, 0, 0, 0}, gm[4] = {0, 0, 0, 0};
                 gather_line<REC>(T, H, ts, base, stride, side == 0 ? -1 - k : n + k, n, false, gp, gm);
-                double s = 0.0;
+                if (SPL == 1) {
+                    double s = 0.0;
 #pragma unroll
-                for (int c = 0; c < 4; ++c) s = fma(gp[c] - gm[c], Ug[c], s);
-                lb += 0.5 * s;
+                    for (int c = 0; c < 4; ++c) s = fma(gp[c] - gm[c], Ug[c], s);
+                    lb += 0.5 * s;
+                }
+                if (!moving) continue;
+                if (SPL == 2) {
+                    const double pv[4] = {qg[0], qg[1], qg[2], qg[4]};
+                    double pr4[4] = {0, 0, 0, 0};
+                    sw_prim_bar<DIR>(pv, a.gamma, gp, gm, pr4);
+                    tl = fma(pr4[2], dv, tl);
+                } else {
+                    // U of the ghost and its primitives (rho, u, v, p, alpha)
+                    const double g[9] = {Ug[0], Ug[1], Ug[2], Ug[3], qg[0], qg[1], qg[2], qg[3], qg[4]};
+                    double Ubg[4] = {0, 0, 0, 0}, unb, pb, ab;
+                    llf_bar<DIR, SPL == 1>(g, g[5 + DIR], g[7], g[8], gp, gm, lam_g, Ubg, unb, pb, ab);
+                    // the normal velocity (u on the left side) does not move; v does
+                    tl = fma(Ubg[2] * qg[0] + Ubg[3] * (qg[0] * qg[2]), dv, tl);
+                    if (DIR == 1) tl = fma(unb, dv, tl);
+                }
+                if (a.charac && k == 0) {
+                    const double* RB = a.rbar + (DIR == 0 ? 0 : 8 * a.xs) + base + (long long)(side == 0 ? 0 : n) * stride;
+                    tl = fma(RB[(side == 0 ? 2 : 6) * ts], dv, tl);
+                }
             }
             continue;
         }
@@ -938,6 +1000,7 @@ __global__ void __launch_bounds__(128) k_rev(AdjParams a, const double* __restri
     long long i1 = LLONG_MAX, i2 = LLONG_MAX;
     double lbx = 0.0, lby = 0.0;
     double bsum = 0.0, Ub_bf0 = 0.0, Ub_bf2 = 0.0;  // the body force's terms (a.bodyforce)
+    double tsl = 0.0;                                 // the inflow ghosts' time sensitivity (a.ssl)
     if (i < ni && j < nj) {
         const long long o = (long long)j * ni + i;
         double U[4], Ub[4] = {0.0, 0.0, 0.0, 0.0};
@@ -985,8 +1048,8 @@ __global__ void __launch_bounds__(128) k_rev(AdjParams a, const double* __restri
             // (a separate instantiation: the periodic kernels keep their registers)
             double pbar[5] = {0, 0, 0, 0, 0};
             const double t = tp ? *tp : 0.0;  // the step's start time (the moving shock's ghosts)
-            if (!px) wall_terms<0, SPL, REC>(a, u, tape, hb, i, j, q, U, GLF ? lamv[0] : 0.0, t, Ub, pbar, lbx);
-            if (!py) wall_terms<1, SPL, REC>(a, u, tape, hb, i, j, q, U, GLF ? lamv[1] : 0.0, t, Ub, pbar, lby);
+            if (!px) wall_terms<0, SPL, REC>(a, u, tape, hb, i, j, q, U, GLF ? lamv[0] : 0.0, t, Ub, pbar, lbx, tsl);
+            if (!py) wall_terms<1, SPL, REC>(a, u, tape, hb, i, j, q, U, GLF ? lamv[1] : 0.0, t, Ub, pbar, lby, tsl);
             prim_pullback_all(U, q, a.gamma, pbar[0], pbar[1], pbar[2], pbar[3], pbar[4], Ub);
         }
         const double dt = STAGE == 0 ? 0.0 : *dtp;
@@ -1041,12 +1104,14 @@ __global__ void __launch_bounds__(128) k_rev(AdjParams a, const double* __restri
             lp[1] = lby;
         }
     }
-    if (STAGE != 0 && a.bodyforce) {  // uniform over the grid
+    if (STAGE != 0 && (a.bodyforce || a.ssl)) {  // uniform over the grid
         __syncthreads();  // the shared arrays of the reductions above are free again
-        double zero = 0.0;
-        block_sum2(bsum, zero);
-        if (threadIdx.x == 0 && threadIdx.y == 0)
-            a.bpart[(STAGE - 1) * (gridDim.x * gridDim.y) + blockIdx.y * gridDim.x + blockIdx.x] = bsum;
+        block_sum2(bsum, tsl);
+        const int blk = (STAGE - 1) * (gridDim.x * gridDim.y) + blockIdx.y * gridDim.x + blockIdx.x;
+        if (threadIdx.x == 0 && threadIdx.y == 0) {
+            if (a.bodyforce) a.bpart[blk] = bsum;
+            if (a.ssl) a.tpart[blk] = tsl;
+        }
     }
 }
 
@@ -1138,25 +1203,40 @@ __global__ void __launch_bounds__(256) k_dt(AdjParams a, const double* __restric
             const int st = k / nm;
             s += (st == 0 ? 1.0 : st == 1 ? 0.25 : kTwoThirdsSingle) * a.bpart[k];
         }
+    double ts_ = 0.0;  // the shear layer: the stages' time sensitivities, with L's stage factors
+    if (a.ssl)
+        for (int k = t; k < 3 * nm; k += blockDim.x) {
+            const int st = k / nm;
+            ts_ += (st == 0 ? 1.0 : st == 1 ? 0.25 : 2.0 / 3.0) * a.tpart[k];
+        }
     double e1 = -1.0, e2 = -1.0, i1 = 1e300, i2 = 1e300;
     for (int k = t; k < nm; k += blockDim.x) {
         const double* mp = mpart + 4 * k;
         if (mp[0] > e1 || (mp[0] == e1 && mp[1] < i1)) { e1 = mp[0]; i1 = mp[1]; }
         if (mp[2] > e2 || (mp[2] == e2 && mp[3] < i2)) { e2 = mp[2]; i2 = mp[3]; }
     }
-    __shared__ double rs[256], re1[256], re2[256], ri1[256], ri2[256];
-    rs[t] = s; re1[t] = e1; re2[t] = e2; ri1[t] = i1; ri2[t] = i2;
+    __shared__ double rs[256], re1[256], re2[256], ri1[256], ri2[256], rt[256];
+    rs[t] = s; re1[t] = e1; re2[t] = e2; ri1[t] = i1; ri2[t] = i2; rt[t] = ts_;
     __syncthreads();
     for (int h = blockDim.x / 2; h; h >>= 1) {
         if (t < h) {
             rs[t] += rs[t + h];
+            rt[t] += rt[t + h];
             if (re1[t + h] > re1[t] || (re1[t + h] == re1[t] && ri1[t + h] < ri1[t])) { re1[t] = re1[t + h]; ri1[t] = ri1[t + h]; }
             if (re2[t + h] > re2[t] || (re2[t + h] == re2[t] && ri2[t + h] < ri2[t])) { re2[t] = re2[t + h]; ri2[t] = ri2[t + h]; }
         }
         __syncthreads();
     }
     if (t == 0) {
-        const double dt = *dtp, dtbar = rs[0];
+        const double dt = *dtp;
+        double dtbar = rs[0];
+        if (a.ssl) {
+            // this step's dt moves the start time of every later step: it takes the sensitivities
+            // to their start times summed so far; then this step's own joins the sum
+            const double S = a.tacc[0];
+            dtbar += S;
+            a.tacc[0] = fma(dt, rt[0], S);
+        }
         // no cell holds a finite maximum (a NaN state): nothing to differentiate
         if (!(ri1[0] >= 0.0 && ri1[0] < (double)a.plane && ri2[0] >= 0.0 && ri2[0] < (double)a.plane)) return;
         const long long c1 = (long long)ri1[0], c2 = (long long)ri2[0];
@@ -1531,7 +1611,8 @@ void dense_adjoint_destroy(dense_adjoint_t* a) {
     if (!a) return;
     if (a->h) cudaStreamSynchronize(a->h->stream);
     double* bufs[] = {a->ckpt, a->dts, a->rec, a->tape, a->g, a->g1, a->g2, a->acc, a->hb, a->part, a->mpart,
-                      a->lamv, a->lmp, a->lpart, a->seg_dts, a->ap.bpart, a->fbar, a->ones, a->ap.rbar};
+                      a->lamv, a->lmp, a->lpart, a->seg_dts, a->ap.bpart, a->fbar, a->ones, a->ap.rbar,
+                      a->ap.tpart, a->ap.tacc};
     for (double* b : bufs) if (b) cudaFree(b);
     if (a->argmax) cudaFree(a->argmax);
     if (a->seg_argmax) cudaFree(a->seg_argmax);
@@ -1576,10 +1657,12 @@ int dense_adjoint_create(const dense_config_t* cfg, int checkpoint_every, dense_
     case DENSE_BENCH_DMR:  // wall from x = 1/6 on, moving-shock top, inflow left, extrapolated right
         rules[0] = dense::adj::kRuleDMRBottom; rules[1] = rules[2] = dense::adj::kRuleFixed;
         rules[3] = dense::adj::kRuleExtrap; break;
+    case DENSE_BENCH_SSL:  // mirror bottom, the setup's top ghosts, oscillating inflow, extrapolated right
+        rules[0] = dense::adj::kRuleReflect; rules[1] = dense::adj::kRuleFixed;
+        rules[2] = dense::adj::kRuleSSLInflow; rules[3] = dense::adj::kRuleExtrap; break;
     default:
         return aerr(nullptr, DENSE_ERR_ARG,
-                    "the adjoint covers the benchmarks with periodic, extrapolated, mirror or fixed-state sides "
-                    "(1, 2, 3, 4, 5, 9, 11, 13, 14); not the shear layer's oscillating inflow (6)");
+                    "the adjoint covers the benchmarks 1, 2, 3, 4, 5, 6, 9, 11, 13 and 14");
     }
     if (cfg->ni < 8 || cfg->nj < 8) return aerr(nullptr, DENSE_ERR_ARG, "the adjoint needs ni, nj >= 8");
     if (checkpoint_every < 1) return aerr(nullptr, DENSE_ERR_ARG, "checkpoint_every must be >= 1");
@@ -1611,6 +1694,23 @@ int dense_adjoint_create(const dense_config_t* cfg, int checkpoint_every, dense_
             return fail(DENSE_ERR_CUDA);
         }
     }
+    if (cfg->benchmark == DENSE_BENCH_SSL) {
+        // the setup's state once, for what the restarts (interior only) do not write: the top
+        // ghost rows, which the shear layer's rule never refills, and the rows' y of the inflow
+        dense_config_t c2 = *cfg;
+        long long nc = 0, np_ = 0, nxy = 0;
+        if (dense_array_sizes(&c2, &nc, &np_, &nxy) != DENSE_OK) {
+            a->err = "dense_array_sizes failed";
+            return fail(DENSE_ERR_ARG);
+        }
+        std::vector<double> cons((size_t)nc), prim((size_t)np_), xs((size_t)nxy), ys((size_t)nxy);
+        if (dense_init_setup(&c2, cons.data(), prim.data(), xs.data(), ys.data()) != DENSE_OK ||
+            dense_upload(a->h, cons.data(), prim.data(), xs.data(), ys.data()) != DENSE_OK ||
+            cudaStreamSynchronize(a->h->stream) != cudaSuccess) {
+            a->err = std::string("the shear layer's setup state: ") + dense_last_error(a->h);
+            return fail(DENSE_ERR_CUDA);
+        }
+    }
     AdjParams& p = a->ap;
     p.ni = cfg->ni; p.nj = cfg->nj; p.plane = (long long)cfg->ni * cfg->nj;
     p.xs = (long long)cfg->nj * (cfg->ni + 1);
@@ -1626,6 +1726,8 @@ int dense_adjoint_create(const dense_config_t* cfg, int checkpoint_every, dense_
     p.bodyforce = cfg->if_bodyforce &&
                   (cfg->benchmark == DENSE_BENCH_RT || cfg->benchmark == DENSE_BENCH_RT_REFLECT);
     p.bench = cfg->benchmark;
+    p.ssl = cfg->benchmark == DENSE_BENCH_SSL ? 1 : 0;
+    p.yleft = a->h->yleft;
     a->tape_stage = (size_t)p.np * (size_t)(p.xs + p.ys);
     a->gh = dim3((cfg->ni + 1 + kHX - 1) / kHX, (cfg->nj + 1 + kHY - 1) / kHY, 2);
     a->gc = dim3((cfg->ni + kCX - 1) / kCX, (cfg->nj + kCY - 1) / kCY);
@@ -1639,7 +1741,7 @@ int dense_adjoint_create(const dense_config_t* cfg, int checkpoint_every, dense_
         {&a->hb, (size_t)4 * (p.xs + p.ys)}, {&a->part, (size_t)3 * a->npart}, {&a->mpart, (size_t)4 * a->nm},
         {&a->rec, (size_t)3 * a->k * a->state}, {&a->tape, (size_t)3 * a->k * a->tape_stage},
         {&a->lamv, 4}, {&a->lmp, (size_t)4 * a->nm}, {&a->lpart, (size_t)2 * a->nm}, {&a->seg_dts, (size_t)2 * a->k},
-        {&p.bpart, (size_t)3 * a->nm},
+        {&p.bpart, (size_t)3 * a->nm}, {&p.tpart, (size_t)3 * a->nm}, {&p.tacc, 1},
     };
     for (auto& b : bufs) {
         cudaError_t e = cudaMalloc((void**)b.p, b.n * sizeof(double));
@@ -1713,6 +1815,7 @@ int dense_adjoint_backward(dense_adjoint_t* a, const double* gT, double* g0, voi
     if (rc) return rc;
     dense_handle* h = a->h;
     ACK(a, cudaMemcpyAsync(a->g, gT, a->state * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+    if (a->ap.ssl) ACK(a, cudaMemsetAsync(a->ap.tacc, 0, sizeof(double), h->stream));  // no later step yet
     const int nseg = (a->nsteps + a->k - 1) / a->k;
     if (a->nsteps >= a->k) {
         rc = segment_graphs(a);

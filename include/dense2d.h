@@ -374,7 +374,8 @@ int dense_batch_steps_device(dense_batch_t* b, int nsteps, double t_end, int tot
    or WENO-Z5 (251/253/255), or the characteristic schemes (104, AdaWENO 105; recon not read),
    on grids periodic in x and y (benchmarks 11 and 14) or with extrapolated, mirror and
    fixed-state sides (benchmarks 1, 2, 4, 9, Rayleigh-Taylor's 3 and 13 with its body force,
-   and the double Mach reflection 5), CFL or constant dt. GLF's global wave speed of each stage
+   the double Mach reflection 5, and the shear layer 6, whose inflow moves with the start time
+   that the time steps make a function of the state), CFL or constant dt. GLF's global wave speed of each stage
    (104 and 105 split by GLF) is differentiated like the time step: its gradient goes to the cell
    where the maximum is attained; AdaWENO's branch at each face and sign is the one the forward
    took (a switch, held fixed like the maxima's cells). States and gradients

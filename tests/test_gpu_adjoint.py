@@ -171,7 +171,8 @@ def rough_state(dense, cfg, seed):
                                                (13, 103, 253), (5, 101, 253), (5, 102, 255), (5, 103, 253),
                                                (1, 104, 0), (2, 104, 0), (3, 104, 0), (4, 104, 0), (5, 104, 0),
                                                (9, 104, 0), (13, 104, 0), (1, 105, 0), (2, 105, 0), (3, 105, 0),
-                                               (4, 105, 0), (5, 105, 0), (13, 105, 0)])
+                                               (4, 105, 0), (5, 105, 0), (13, 105, 0), (6, 101, 253), (6, 102, 255),
+                                               (6, 103, 253), (6, 104, 0), (6, 105, 0)])
 def test_rhs_vjp_with_walls_matches_autograd(dense, adjoint, bench, split, recon):
     """The reference's benchmarks with walls -- extrapolated (1: x; 2: top, right; 4, 9: sides;
     5: right), mirror (2: bottom, left; 4, 9: bottom, top; 13: sides; 5: the bottom from x = 1/6)
@@ -194,12 +195,14 @@ def test_rhs_vjp_with_walls_matches_autograd(dense, adjoint, bench, split, recon
                                                (13, 102, 253), (13, 103, 255), (5, 101, 253), (5, 102, 253),
                                                (5, 103, 253), (2, 104, 0), (3, 104, 0), (4, 104, 0),
                                                (5, 104, 0), (13, 104, 0), (3, 105, 0), (4, 105, 0), (5, 105, 0),
-                                               (13, 105, 0)])
+                                               (13, 105, 0), (6, 101, 253), (6, 102, 253), (6, 103, 255), (6, 104, 0),
+                                               (6, 105, 0)])
 def test_steps_gradient_with_walls_matches_autograd(dense, adjoint, bench, split, recon):
     """5 steps with checkpoints every 2 on grids with wall sides, CFL time step; on the
     Rayleigh-Taylor grids (3, 13) with the body force of every stage, whose time-step factor
     carries the step's sensitivity to dt as well; on the double Mach reflection's (5) with its
-    top ghosts chosen by each step's start time."""
+    top ghosts chosen by each step's start time; on the shear layer's (6) with its inflow
+    oscillating in the start time, which every earlier time step moves."""
     cfg = dense.config_default(ni=24, nj=20, benchmark=bench, splitting=split, recon=recon, cfl=0.4)
     c, U = rough_state(dense, cfg, seed=7 + bench)
     gT = torch.randn(U.shape, generator=torch.Generator().manual_seed(5), dtype=torch.float64).cuda()
@@ -214,7 +217,7 @@ def test_steps_gradient_with_walls_matches_autograd(dense, adjoint, bench, split
 
 
 def test_rejects_unsupported_configurations(dense, adjoint):
-    for kw in (dict(recon=0, splitting=106), dict(benchmark=6), dict(ni=6)):
+    for kw in (dict(recon=0, splitting=106), dict(benchmark=7), dict(ni=6)):
         cfg = dense.init_general(vortex_cfg(dense, 253))[0]
         for k, v in kw.items():
             setattr(cfg, k, v)

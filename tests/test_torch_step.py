@@ -43,14 +43,15 @@ def test_torch_step_matches_oracle(dense, orc, split, recon):
                                                (3, 104, 0), (13, 104, 0), (4, 104, 0), (1, 104, 0),
                                                (2, 104, 0), (5, 104, 0), (9, 104, 0), (11, 105, 0), (3, 105, 0),
                                                (13, 105, 0), (4, 105, 0), (1, 105, 0), (2, 105, 0), (5, 105, 0),
-                                               (9, 105, 0)])
+                                               (9, 105, 0), (6, 101, 253), (6, 102, 255), (6, 103, 253),
+                                               (6, 104, 0), (6, 105, 0)])
 def test_torch_step_with_walls_matches_oracle(dense, orc, bench, split, recon):
     """The ghost rules of the reference's benchmarks with walls (extrapolation, mirror,
     Rayleigh-Taylor's fixed states with its body force, the double Mach reflection's wall,
-    moving-shock top and inflow) from a rough seeded state: three steps within 1e-12 of the
-    oracle."""
+    moving-shock top and inflow, the shear layer's untouched top and oscillating inflow) from a
+    rough seeded state: three steps within 1e-12 of the oracle."""
     cfg = dense.config_default(ni=24, nj=20, benchmark=bench, splitting=split, recon=recon, cfl=0.4)
-    c, cons, prim, x, y = dense.init_general(cfg)
+    c, cons0, prim, x, y = dense.init_general(cfg)
     rng = np.random.default_rng(bench * 1000 + split + recon)
     shape = (c.ni + 8, c.nj + 8)
     rho, u, v, p = (rng.uniform(0.5, 2.0, shape), rng.uniform(-1, 1, shape), rng.uniform(-1, 1, shape),
@@ -58,6 +59,8 @@ def test_torch_step_with_walls_matches_oracle(dense, orc, bench, split, recon):
     cons = np.zeros(shape + (4,), order="F")
     cons[..., 0], cons[..., 1], cons[..., 2] = rho, rho * u, rho * v
     cons[..., 3] = p / (c.gamma - 1.0) + 0.5 * rho * (u * u + v * v)
+    if bench == 6:  # the shear layer never refills its top ghosts: they keep the setup's state
+        cons[:, c.nj + 4:, :] = cons0[:, c.nj + 4:, :]
     o = orc.OracleSolver(c)
     o.set_state(cons, None)
     o.steps(3)

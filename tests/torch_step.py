@@ -15,6 +15,8 @@ walls from the reference's rules (RULES).
 """
 from __future__ import annotations
 
+import math
+
 import torch
 
 SS = float(torch.tensor(1.0e-6, dtype=torch.float32))  # weno_mod.f90:37, a default-real literal
@@ -86,8 +88,8 @@ def steger_warming(rho, u, v, a, gamma, d):
 # where the column's centre x >= 1/6 and the fixed post-shock state before it, "T" its top, the
 # post-shock state ahead of the moving shock x < 1/6 + (1 + 20 t)/sqrt(3) and the pre-shock
 # state behind it (t the step's start time), "F" its post-shock inflow on the left.
-RULES = {1: "PPEE", 2: "RERE", 3: "FFPP", 4: "RREE", 5: "BTFE", 9: "RREE", 11: "PPPP", 13: "FFRR",
-         14: "PPPP"}
+RULES = {1: "PPEE", 2: "RERE", 3: "FFPP", 4: "RREE", 5: "BTFE", 6: "RFFE", 9: "RREE", 11: "PPPP",
+         13: "FFRR", 14: "PPPP"}
 # the fixed states (rho, u, v, p) of the "F" sides: bottom, top
 RT_STATES = ((2.0, 0.0, 0.0, 1.0), (1.0, 0.0, 0.0, 2.5))
 # the stage-3 body-force factor 2.0/3.0 is a default-real literal (time_advance_general.f90:242)
@@ -144,6 +146,28 @@ def _pad_axis(A, axis, lo, hi, flip, fixed=None):
     return torch.cat(list(reversed(low)) + [A] + high, dim=axis)
 
 
+def ssl_sides(U, gamma, dy, t):
+    """The shock / shear layer's side specifications for _rhs_padded: ((bottom, top) of the
+    conserved variables, (bottom, top) of the primitives) and the same for (left, right). The
+    top ghosts keep the post-shock state the setup gave them (the rule's loop body is empty,
+    boundary_ssl_general.f90:47-52); the left inflow (:40-66) is rho 1.6374 above y = 0 and
+    0.3626 below, p 0.3327, u = 2.5 + 0.5 tanh(2 y) and v oscillating in the step's start time t
+    (a tensor: the time steps make it a function of the state)."""
+    nj = U.shape[1]
+    y = ((torch.arange(nj, dtype=U.dtype, device=U.device) + 1.0) - 0.5) * dy - 20.0
+    post = fixed_state(gamma, 2.1101, 2.9709, -0.1367, float(torch.tensor(0.4754, dtype=torch.float32)))
+    rho = torch.where(y >= 0.0, torch.full_like(y, 1.6374), torch.full_like(y, 0.3626))
+    pr = torch.full_like(y, 0.3327)
+    u = 2.5 + 0.5 * torch.tanh(2.0 * y)
+    pie = math.pi
+    e = torch.exp(-(y * y) / 10.0)
+    v = (0.05 * torch.cos(torch.as_tensor(2.0 * pie * t / (30.0 / 2.68), dtype=U.dtype)) * e
+         + 0.05 * torch.cos(torch.as_tensor(2.0 * pie * 2.0 * t / (30.0 / 2.68) + pie / 2.0, dtype=U.dtype)) * e)
+    cons, prim = fixed_state(gamma, rho, u, v, pr)
+    col = lambda q: torch.stack(list(q)).view(len(q), nj, 1)
+    return ((None, post[0]), (None, post[1])), ((col(cons), None), (col(prim), None))
+
+
 def dmr_sides(U, gamma, dx, t):
     """The double Mach reflection's side specifications for _rhs_padded: ((bottom, top) of the
     conserved variables, (bottom, top) of the primitives, (left) of both)."""
@@ -166,6 +190,9 @@ def rhs(U, gamma, dx, dy, rec, split=101, bench=11, t=0.0, delta=0.5):
             fixed = [fixed_state(gamma, *st) for st in RT_STATES]
             ys = ((fixed[0][0], fixed[1][0]), (fixed[0][1], fixed[1][1]))
             return _rhs_padded(U, gamma, dx, dy, rec, split, RULES[bench], ys, delta=delta)
+        if bench == 6:
+            ys, xs = ssl_sides(U, gamma, dy, t)
+            return _rhs_padded(U, gamma, dx, dy, rec, split, RULES[bench], ys, xs, delta)
         if bench == 5:
             yu, yp, post = dmr_sides(U, gamma, dx, t)
             return _rhs_padded(U, gamma, dx, dy, rec, split, RULES[bench], (yu, yp),
@@ -356,8 +383,10 @@ def time_step(U, gamma, dx, dy, rec, cfl, dt_const=None, split=101, bench=11, bo
 
 
 def run(U, n, gamma, dx, dy, rec, cfl, dt_const=None, split=101, bench=11, bodyforce=None, delta=0.5):
-    t = 0.0  # the steps' start times, accumulated as the solver does (general_main.f90:34)
+    # the steps' start times, accumulated as the solver does (general_main.f90:34); a tensor
+    # carrying the time steps' dependence on the state (the shear layer's inflow reads it)
+    t = 0.0
     for _ in range(n):
         U, dt = time_step(U, gamma, dx, dy, rec, cfl, dt_const, split, bench, bodyforce, t, delta)
-        t = t + float(dt.detach())
+        t = t + dt
     return U
