@@ -73,8 +73,8 @@ struct AdjParams {
     int bodyforce;
     double* bpart;
     int bench;        // the benchmark (its fixed ghost states: fixed_state)
-    // characteristic WENO-Z (104): k_char_face writes each face's split-flux sensitivities (the
-    // gather's "tape", read against unit face weights) and, per face, the sensitivities of the
+    // characteristic WENO-Z (104, 105): k_char_face writes each face's split-flux sensitivities
+    // (what the cell kernel gathers, kRecFaceSens) and, per face, the sensitivities of the
     // primitives (rho, u, v, p) of its left and right cells through the Roe eigenvectors:
     // rbar[8][face plane] a direction (left cell 0..3, right cell 4..7), xi then eta
     int charac;
@@ -423,15 +423,22 @@ __global__ void __launch_bounds__(256) k_hbar(AdjParams a, const double* __restr
 // Sensitivities of the F+ and F- values of cell x of a line (faces 0..n of the line, at offset
 // base + f*stride of their planes): sum over the faces whose "+" stencil reads the cell
 // (face x+3-m reads it as its m-th value) or whose "-" stencil does (face x-2+m), including the
-// faces that read it through a periodic image (x -+ n).
+// faces that read it through a periodic image (x -+ n). REC = kRecFaceSens: T holds the split
+// fluxes' sensitivities themselves (the characteristic schemes' face kernel wrote them with the
+// faces' hbar already applied), and H is not read.
+constexpr int kRecFaceSens = 0;
 template <int REC>
 __device__ __forceinline__ void add_face(const double* __restrict__ T, const double* __restrict__ H, long long ts,
                                          long long off, int s, int m, double acc[4]) {
     constexpr double cu[5] = {2.0 / 60.0, -13.0 / 60.0, 47.0 / 60.0, 27.0 / 60.0, -3.0 / 60.0};
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
-        const double g = REC == DENSE_RECON_UPWIND5 ? cu[m] : T[(long long)((s * 5 + m) * 4 + v) * ts + off];
-        acc[v] = fma(g, H[v * ts + off], acc[v]);
+        if (REC == kRecFaceSens) {
+            acc[v] += T[(long long)((s * 5 + m) * 4 + v) * ts + off];
+        } else {
+            const double g = REC == DENSE_RECON_UPWIND5 ? cu[m] : T[(long long)((s * 5 + m) * 4 + v) * ts + off];
+            acc[v] = fma(g, H[v * ts + off], acc[v]);
+        }
     }
 }
 template <int REC>
@@ -737,7 +744,7 @@ __device__ __forceinline__ void fetch_cell(const AdjParams& a, const double* __r
 // face's hbar: the back-projection's transpose gives each field's value sensitivity, times the
 // field's stencil gradient the sensitivities of the projected values, the transposed
 // projection those of the split fluxes, written per (sign, stencil point, component) as the
-// cell kernel's gather reads them (against unit face weights); and the eigenvectors'
+// cell kernel's gather reads them (kRecFaceSens); and the eigenvectors'
 // sensitivities -- from the projections (sum over the stencil of the projected-value
 // sensitivities times the split fluxes) and the back-projection, the two signs' shares summed
 // across the lane pair -- sent through the eigenvectors' formulas and the Roe average to the
@@ -1301,9 +1308,9 @@ struct dense_adjoint {
     // GLF: the stage's (lambda_x, lambda_y, their cells), block maxima, block sums of lambda's
     // sensitivity
     double *lamv = nullptr, *lmp = nullptr, *lpart = nullptr;
-    // characteristic WENO-Z (104): the faces' split-flux sensitivities (40 planes a direction)
-    // the cell kernel gathers against unit face weights (ones, 4 planes a direction)
-    double *fbar = nullptr, *ones = nullptr;
+    // the characteristic schemes (104, 105): the faces' split-flux sensitivities (40 planes a
+    // direction; 50 with AdaWENO's densities) the cell kernel gathers
+    double* fbar = nullptr;
     dim3 gh, gc, gfx, gfy;
     int nsteps = -1;                              // steps of the last forward
     cudaEvent_t ev_in = nullptr, ev_out = nullptr;
@@ -1429,7 +1436,7 @@ void launch_rev_w(dense_adjoint* a, int stage, const double* u, const double* ta
     const dim3 bc(kCX, kCY);
     double* const lv = a->lamv;
     double* const lp = a->lpart;
-    const double* hb = a->ap.charac ? a->ones : a->hb;
+    const double* hb = a->hb;
     if (stage == 0)
         k_rev<REC, SPL, WALLS><<<a->gc, bc, 0, s>>>(a->ap, u, w, tape, hb, nullptr, out, nullptr, tp, nullptr,
                                                     lv, lp, 0);
@@ -1476,7 +1483,7 @@ void vjp(dense_adjoint* a, int stage, const double* u, const double* tape, const
         k_char_face<0><<<a->gfx, dim3(kCX, kCY), 0, s>>>(a->ap, u, a->hb, a->lamv, tp, flags, a->fbar);
         k_char_face<1><<<a->gfy, dim3(kCX, kCY), 0, s>>>(a->ap, u, a->hb, a->lamv, tp, flags, a->fbar);
         a->launches += 2;
-        launch_rev<DENSE_RECON_WENOZ5, 1>(a, stage, u, a->fbar, w, out, dtp, tp, s);
+        launch_rev<dense::adj::kRecFaceSens, 1>(a, stage, u, a->fbar, w, out, dtp, tp, s);  // the faces' own sensitivities
     } else if (glf) launch_rev_recon<1>(a, stage, u, tape, w, out, dtp, tp, s);
     else if (a->cfg.splitting == DENSE_SPLIT_SW) launch_rev_recon<2>(a, stage, u, tape, w, out, dtp, tp, s);
     else launch_rev_recon<0>(a, stage, u, tape, w, out, dtp, tp, s);
@@ -1611,7 +1618,7 @@ void dense_adjoint_destroy(dense_adjoint_t* a) {
     if (!a) return;
     if (a->h) cudaStreamSynchronize(a->h->stream);
     double* bufs[] = {a->ckpt, a->dts, a->rec, a->tape, a->g, a->g1, a->g2, a->acc, a->hb, a->part, a->mpart,
-                      a->lamv, a->lmp, a->lpart, a->seg_dts, a->ap.bpart, a->fbar, a->ones, a->ap.rbar,
+                      a->lamv, a->lmp, a->lpart, a->seg_dts, a->ap.bpart, a->fbar, a->ap.rbar,
                       a->ap.tpart, a->ap.tacc};
     for (double* b : bufs) if (b) cudaFree(b);
     if (a->argmax) cudaFree(a->argmax);
@@ -1749,15 +1756,10 @@ int dense_adjoint_create(const dense_config_t* cfg, int checkpoint_every, dense_
     }
     if (charac) {
         const size_t fp = (size_t)(p.xs + p.ys);
-        struct B2 { double** p; size_t n; } cb[] = {{&a->fbar, (size_t)p.gnp * fp}, {&p.rbar, 8 * fp}, {&a->ones, 4 * fp}};
+        struct B2 { double** p; size_t n; } cb[] = {{&a->fbar, (size_t)p.gnp * fp}, {&p.rbar, 8 * fp}};
         for (auto& b : cb) {
             cudaError_t e = cudaMalloc((void**)b.p, b.n * sizeof(double));
             if (e != cudaSuccess) { a->err = std::string("cudaMalloc: ") + cudaGetErrorString(e); return fail(DENSE_ERR_NOMEM); }
-        }
-        const std::vector<double> one(4 * fp, 1.0);
-        if (cudaMemcpy(a->ones, one.data(), one.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
-            a->err = "cudaMemcpy of the unit face weights failed";
-            return fail(DENSE_ERR_CUDA);
         }
     }
     if (cudaMalloc((void**)&a->seg_argmax, (size_t)2 * a->k * sizeof(int)) != cudaSuccess) {
