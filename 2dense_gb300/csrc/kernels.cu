@@ -653,9 +653,16 @@ __device__ __forceinline__ void flux_cw_block(const Params& p, int irk, int bx, 
     }
 }
 
+// Programmatic dependent launch: in the plain step graph a kernel may be scheduled while the
+// one before it drains (its edges are programmatic); every such kernel waits here, before it
+// touches memory, until its predecessors have completed and their writes are visible. Launched
+// without a programmatic dependency (eagerly, in the batched graphs) it returns at once.
+__device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // Unknown reconstruction index with a component-wise splitting: the reference leaves h_xi and
 // h_eta untouched (scheme_invs_general.f90:4-27); they start at zero (allocate_block).
 __global__ void k_flux_noop(Params p, int irk) {
+    grid_dependency_wait();
     if (!p.sc->active) return;
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         stage_scalars(p, irk);
@@ -1509,18 +1516,27 @@ __device__ __forceinline__ void bc_block(const Params& p, int bx) {
 constexpr int char_min_blocks(bool adapt) { return adapt ? 3 : 1; }
 template <int DIR, int SPL, int REC, int TX, int TY, bool TAPE = false, int TZ = 1>
 __global__ void __launch_bounds__(TX* TY* TZ) k_flux_cw(Params p, int irk) {
+    grid_dependency_wait();
     flux_cw_block<DIR, SPL, REC, TX, TY, TAPE, TZ>(p, irk, blockIdx.x, blockIdx.y);
 }
 template <int DIR, bool ADAPT, int TX, int TY>
 __global__ void __launch_bounds__(TX* TY, char_min_blocks(ADAPT)) k_flux_char(Params p, int irk) {
+    grid_dependency_wait();
     flux_char_block<DIR, ADAPT, TX, TY>(p, irk, blockIdx.x, blockIdx.y);
 }
-__global__ void k_prim(Params p, int slot) { prim_block(p, slot, blockIdx.x, blockIdx.y); }
+__global__ void k_prim(Params p, int slot) {
+    grid_dependency_wait();
+    prim_block(p, slot, blockIdx.x, blockIdx.y);
+}
 template <int IRK>
 __global__ void k_update(Params p) {
+    grid_dependency_wait();
     update_block<IRK>(p, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y);
 }
-__global__ void k_bc(Params p) { bc_block(p, blockIdx.x); }
+__global__ void k_bc(Params p) {
+    grid_dependency_wait();
+    bc_block(p, blockIdx.x);
+}
 
 // Batched kernels: one launch covers every instance of a batch. Block b works on instance
 // map[b].x at block coordinates (map[b].y, map[b].z) of that instance's own grid, with the
@@ -1582,8 +1598,14 @@ __device__ __forceinline__ void k_step_end_body(Scalars* sc) {
             sc->hold = 1;
     }
 }
-__global__ void k_step_begin(Scalars* sc) { k_step_begin_body(sc); }
-__global__ void k_step_end(Scalars* sc) { k_step_end_body(sc); }
+__global__ void k_step_begin(Scalars* sc) {
+    grid_dependency_wait();
+    k_step_begin_body(sc);
+}
+__global__ void k_step_end(Scalars* sc) {
+    grid_dependency_wait();
+    k_step_end_body(sc);
+}
 
 #define DENSE_PERSIST (FAST && !DENSE_CHECK)
 #if DENSE_PERSIST
