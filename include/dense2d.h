@@ -165,7 +165,10 @@ int dense_stage(dense_handle_t* h, int irk, double current_time, double* dt_inou
 /* The device-resident step loop of general_main.f90:23-38: up to nsteps steps of `stages`
    stages, each taken only while (*t_inout < t_end && *step_inout < total_step), advancing
    time and step on the device; no host synchronisation between steps. On return *t_inout,
-   *step_inout and *dt_out hold the driver's current_time, current_step and dt. */
+   *step_inout and *dt_out hold the driver's current_time, current_step and dt. One CUDA graph
+   runs a step; for AdaWENO (105) grids of 200,000 cells or more its kernel-to-kernel edges are
+   programmatic (each kernel scheduled as the one before it drains), which the environment
+   variable DENSE_PDL=0 or 1 turns off or on for every grid. Results are the same either way. */
 int dense_steps(dense_handle_t* h, int nsteps, double t_end, int total_step,
                 double* t_inout, int* step_inout, double* dt_out);
 
